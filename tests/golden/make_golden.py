@@ -1,0 +1,94 @@
+"""Generates the golden fixtures in this folder from the reference's own CPU MD code.
+
+Run from the repository root after building the oracle harness (needs the reference sources):
+
+    make -C oracle/ref REF=/root/reference && python tests/golden/make_golden.py
+
+Each case is a seeded synthetic system (moltwister_gb300/workloads.py).  The harness
+(oracle/ref/harness.cpp, linked from the unmodified reference sources) builds the
+CMolTwisterState through the reference API and records:
+  static : the 1000-point tables, the bonded lists the reference discovers, the cell list, the
+           full neighbour list and per-atom F/U at the input positions;
+  run    : a trajectory of `steps` steps (r, p, F every `stride` steps plus U, K, T, P, V and the
+           Nose-Hoover chain), with momenta and chain variables injected from the seeded system.
+The inputs are stored next to the outputs so the GPU tests can rebuild the system on a machine
+without the reference.
+"""
+from __future__ import annotations
+
+import dataclasses
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
+sys.path.insert(0, ROOT)
+
+from moltwister_gb300 import workloads as W  # noqa: E402
+from oracle.sysfile import harness_run, harness_static  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def cases():
+    """name -> (system, config, steps, stride)"""
+    out = {}
+    s, c = W.argon(ncell=5, seed=11, jitter=0.05)
+    c.neighshell = 1.0                      # 3 cells per axis
+    out["argon500_nvt"] = (s, c, 100, 25)
+    s, c = W.argon(ncell=5, seed=12, jitter=0.05, T=90.0)
+    c.neighshell = 1.0
+    c.ensemble = "NVE"
+    out["argon500_nve"] = (s, c, 100, 25)
+    s, c = W.argon(ncell=4, seed=13, jitter=0.05)
+    out["argon256_2cells"] = (s, c, 20, 10)   # 2 cells per axis: duplicated neighbours (reference trap)
+    s, c = W.water(n_mol=216, L=W.water_box_length(216), seed=14, rc=6.0)
+    c.neighshell = 0.2
+    out["water648_nvt"] = (s, c, 100, 25)
+    s, c = W.chains(n_chain=27, L=24.0, seed=15, immobile_every=7)
+    out["chains108_nvt"] = (s, c, 100, 25)
+    return out
+
+
+def pack(name, s, c, steps, stride):
+    st = harness_static(s, c)
+    tr = harness_run(s, c, steps, stride)
+    cnt = st["neigh_count"]
+    maxc = int(cnt.max()) if cnt.size else 0
+    terms = {
+        "nonbonded": [dataclasses.asdict(t) for t in s.nonbonded],
+        "bond_terms": [dataclasses.asdict(t) for t in s.bond_terms],
+        "angle_terms": [dataclasses.asdict(t) for t in s.angle_terms],
+        "dihedral_terms": [dataclasses.asdict(t) for t in s.dihedral_terms],
+    }
+    cfg = dataclasses.asdict(c)
+    arrays = dict(
+        in_box=s.box, in_ids=np.array(s.ids), in_r=s.r, in_q=s.q, in_m=s.m, in_mobile=s.mobile.astype(np.int8),
+        in_p=s.p, in_nhT_eta=s.nhT_eta, in_nhT_peta=s.nhT_peta,
+        in_terms=np.array(json.dumps(terms)), in_cfg=np.array(json.dumps(cfg)),
+        steps=np.array(steps), stride=np.array(stride),
+        nb_table=st["nb_table"], nb_count=st["nb_count"], bond_table=st["bond_table"],
+        angle_table=st["angle_table"], dih_table=st["dih_table"],
+        atom_type=st["atom_type"], atom_mol=st["atom_mol"],
+        bonds=st["bonds"], angles=st["angles"], dihedrals=st["dihedrals"],
+        cell_dims=st["cell_dims"], atom_cell=st["atom_cell"], cell_ptr=st["cell_ptr"], cell_list=st["cell_list"],
+        neigh_count=cnt, neigh_list=st["neigh_list"][:, :maxc],
+        F=st["F"], U=st["U"],
+        traj_r=tr["traj_r"], traj_p=tr["traj_p"], traj_F=tr["traj_F"], traj_U=tr["traj_U"],
+        traj_scalars=tr["traj_scalars"], traj_nhT=tr["traj_nhT"],
+    )
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    return path
+
+
+def main():
+    for name, (s, c, steps, stride) in cases().items():
+        p = pack(name, s, c, steps, stride)
+        print(f"{name}: {os.path.getsize(p) / 1024:.0f} KiB")
+
+
+if __name__ == "__main__":
+    main()
