@@ -1,0 +1,303 @@
+"""Benchmark: MD atom-steps/s of the GB300 engine on the flexible-water workload.
+
+Workload: 3,000 flexible SPC/E-like waters (9,000 atoms) in a 44.8 A periodic box, NVT 300 K
+(Nose-Hoover chain M=4, RESPA 4), dt = 0.5 fs, LJ on O-O (cutoff 10 A), cutoff Coulomb at 10 A,
+harmonic O-H bonds and H-O-H angles; molecules on a seeded lattice with random orientations,
+Maxwell-Boltzmann momenta.  Mixed precision (FP32 arithmetic, int64 fixed-point forces).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-resident throughput (CUDA events on the engine's stream
+around the captured step graphs, L2 flushed between timed chunks of 100 steps); `e2e` is the same
+metric through the C ABI with host buffers (state upload, the run with host output every 100
+steps, final download) timed by wall clock.  The reference arm times the CPU oracle's restatement
+of the reference's own MD step (tables, full lists every step, all-pairs Coulomb; 1 thread,
+as the reference is single-threaded) on a bounded sample of the same system.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "water9000_nvt_mixed"
+METRIC = "atom-steps/s"
+CHUNK = 100
+SIGMA_O, EPS_O = 3.166, 0.650
+
+
+def make_system(precision: str = "mixed"):
+    from moltwister_gb300 import workloads as W
+    s, cfg = W.water(n_mol=3000, L=44.8, seed=2, rc=10.0, dt=0.5)
+    cfg.precision = precision
+    cfg.coulomb = "cutoff"
+    cfg.coulombcutoff = 10.0
+    cfg.listskin = 1.0
+    return s, cfg
+
+
+# ------------------------------------------------------------------------------------------------
+# Algorithmic work (per step): FLOP per unordered pair within cutoff -- 23 for 12-6 LJ, +7 when
+# Coulomb is added to an LJ pair, 15 for a Coulomb-only pair -- plus bonds 20 and angles 60.
+# ------------------------------------------------------------------------------------------------
+def count_pairs(r: np.ndarray, box: np.ndarray, rc: float, is_o: np.ndarray, mol: np.ndarray):
+    n = r.shape[0]
+    lj_coul = 0
+    coul = 0
+    for a in range(0, n, 512):
+        d = r[a:a + 512, None, :] - r[None, :, :]
+        d -= box * np.rint(d / box)
+        r2 = (d * d).sum(-1)
+        idx = np.arange(a, min(a + 512, n))
+        upper = np.arange(n)[None, :] > idx[:, None]
+        intra = mol[idx][:, None] == mol[None, :]
+        within = (r2 < rc * rc) & upper & ~intra
+        oo = is_o[idx][:, None] & is_o[None, :]
+        lj_coul += int((within & oo).sum())
+        coul += int((within & ~oo).sum())
+    return lj_coul, coul
+
+
+def algorithmic_flops(s, cfg) -> float:
+    is_o = np.array([i == "Ow" for i in s.ids])
+    ljc, c = count_pairs(s.r, s.box, cfg.cutoffradius, is_o, s.mol_index())
+    return 30.0 * ljc + 15.0 * c + 20.0 * len(s.bonds) + 60.0 * len(s.angles)
+
+
+# ------------------------------------------------------------------------------------------------
+# Clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                parts = [p.strip() for p in out.stdout.strip().split(",")]
+                if len(parts) == 6:
+                    self.samples.append(parts)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def flush_l2():
+    import torch
+    buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    buf.fill_(1.0)
+    torch.cuda.synchronize()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU baseline: the oracle's restatement of the reference step (reference mode), 1 thread
+# ------------------------------------------------------------------------------------------------
+def cpu_baseline(s, cfg, budget_s: float = 20.0, max_steps: int = 3):
+    from oracle import oracle as O
+    from moltwister_gb300.system import MDConfig
+    c = MDConfig(**{k: getattr(cfg, k) for k in cfg.__dataclass_fields__})
+    c.precision = "reference"
+    c.coulomb = "allpairs"        # the reference has no cutoff Coulomb
+    orc = O.Oracle(s, c)
+    t0 = time.perf_counter()
+    orc.run_ref(1, 1)             # one step, to size the sample
+    one = time.perf_counter() - t0
+    steps = int(max(1, min(max_steps, budget_s // max(one, 1e-9))))
+    t0 = time.perf_counter()
+    orc.run_ref(steps, steps)
+    dt = time.perf_counter() - t0
+    return {"value": s.n * steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{steps} MD steps of the 9,000-atom water system after 1 untimed step "
+                      f"(reference arithmetic: tables, cell + neighbour lists every step, all-pairs Coulomb)",
+            "seconds": dt}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    s, cfg = make_system("mixed")
+    base = cpu_baseline(s, cfg, budget_s=min(60.0, 10.0 * max(1, args.steps)), max_steps=max(1, min(args.steps, 5)))
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "impl": "reference", "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "atoms": s.n, "coulomb": "all-pairs minimum image (reference)"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------------
+# Our arm
+# ------------------------------------------------------------------------------------------------
+def timed_device(e, steps: int):
+    """Device ms of exactly `steps` steps, run in chunks of CHUNK with an L2 flush between chunks."""
+    total = 0.0
+    done = 0
+    builds = 0
+    launches = 0
+    while done < steps:
+        n = min(CHUNK, steps - done)
+        e.run(n)
+        st = e.stats()
+        total += st["device_ms"]
+        builds += st["list_builds"]
+        launches += st["kernel_launches"]
+        done += n
+        flush_l2()
+    return total, builds, launches
+
+
+def our_arm(args):
+    import torch
+    from moltwister_gb300.build import build
+    from moltwister_gb300.engine import Engine, device_name
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build()
+    s, cfg = make_system("mixed")
+    n = s.n
+    e = Engine(s, cfg, device=local)
+    # warm-up: graph capture and first list builds
+    e.run(max(args.warmup, 3) * 1)
+    for _ in range(max(args.warmup, 3)):
+        e.run(CHUNK)
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        ms, builds, launches = timed_device(e, args.steps)
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * n * args.steps / (ms / 1e3)
+
+    # per-phase timing (same stream, CUDA events) for the roofline
+    phases = e.profile_phases(200)
+    # e2e: C ABI with host buffers: upload state, run with host output every 100 steps, download
+    r0, p0, th0 = e.get_state()
+    t0 = time.perf_counter()
+    e.set_state(r=r0, p=p0, thermo=th0)
+    recs = e.run(args.steps, out_stride=CHUNK)
+    r1, p1, _ = e.get_state()
+    e2e_s = time.perf_counter() - t0
+    e2e_val = world * n * args.steps / e2e_s
+    h2d = 2 * 3 * 8 * n
+    d2h = (len(recs) + 1) * 2 * 3 * 8 * n
+
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp32+int64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "atoms": n, "molecules": n // 3, "box_A": 44.8, "dt_fs": 0.5,
+                      "precision": "mixed (FP32 pair/bonded arithmetic, int64 fixed-point forces, FP64 positions/"
+                                   "thermostat/reductions)",
+                      "coulomb": "cutoff 10 A (new option; the reference is all-pairs)", "lj_cutoff_A": 10.0,
+                      "list_skin_A": cfg.listskin, "ensemble": "NVT Nose-Hoover M=4 RESPA 4",
+                      "l2": f"flushed (256 MiB write) between timed chunks of {CHUNK} steps",
+                      "parallelism": "replicas only" if world > 1 else "single GPU",
+                      "device": device_name(local)},
+           "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d / args.steps,
+                   "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s},
+           "gpu_launches": int(launches),
+           "list_builds": int(builds),
+           "phase_ms": phases}
+    if rank == 0:
+        pk, kind = peaks()
+        flops = algorithmic_flops(s, cfg)
+        clk_s = clk.summary()
+        sm_max = pk.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        fms = phases["force"]
+        achieved = flops / (fms * 1e-3) / 1e12
+        out["roofline"] = {"bound": "fp32", "kernel": "k_pforce (force gather)", "achieved": achieved,
+                           "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                           "peak_source": f"nominal FP32 SIMT peak 152 SM x 128 lanes x 2 x {sm_max:.0f} MHz "
+                                          f"(sm_max_mhz {kind} in MEASURED_PEAKS.json)",
+                           "algorithmic_flop_per_launch": flops, "traffic": None}
+        # integrator: HBM-bound, 148 B/atom-step algorithmic
+        kd = phases["kick_drift"] + phases["kick_reduce"]
+        out["roofline_integrator"] = {"bound": "hbm", "achieved": 148.0 * n / (kd * 1e-3) / 1e9,
+                                      "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                      "frac": 148.0 * n / (kd * 1e-3) / 1e9 / pk["hbm_gbs"],
+                                      "peak_source": kind}
+        out["clocks"] = clk_s
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(s, cfg)
+        print(json.dumps(out))
+    e.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,257 @@
+/*
+ * mtgpu.h -- C ABI of libmtgpu.so, the GB300-native (sm_103a) molecular-dynamics engine that
+ * replaces the engine behind MolTwister's `moldyn run`.
+ *
+ * What it replaces.  In the reference, `CCmdRun::execute` (Cmd/MolTwisterCmdMolDyn/CmdRun.cpp:84-139)
+ * hands the whole CMolTwisterState to `mtdev::CMDSimulator::run(SMolDynConfigStruct, FILE*,
+ * CSerializer&)` (Simulator/MDSimulator.h:33-43, MDSimulator.cpp:28-47), which builds
+ * CSimulationBox/CMDLoop and runs velocity-Verlet + Nose-Hoover with forces from
+ * CMDFFMatrices + CFunctorCalcForce.  Here the caller describes the system once
+ * (mtg_system_desc: atoms plus the MDFF term tables and parameters) and the run settings
+ * (mtg_config_desc: the SMolDynConfigStruct fields the engine reads), then steps it on the GPU.
+ *
+ * Conventions.
+ *   - Every function returns MTG_OK (0) or a negative MTG_E* code; mtg_last_error() gives a
+ *     message.  No C++ exception crosses this boundary.
+ *   - The caller owns every host array it passes; the library copies what it needs and owns all
+ *     device memory of a context.
+ *   - A context is not re-entrant: call it from one thread at a time.  Distinct contexts may be
+ *     used from distinct threads.
+ *   - Units are the reference's (Integrators/Constants.h:23-40): A, g/mol, kJ/mol, e; momenta
+ *     p = m v with v in A per 100 fs; temperatures in K; times in fs.
+ *   - The periodic box spans [-L/2, L/2) on each axis, as CCellList::updatePBC assumes
+ *     (MDFFMatrices.cpp:67-76).
+ *   - Any wait inside a device kernel is bounded and reports MTG_E_TIMEOUT.
+ */
+#ifndef MTGPU_H
+#define MTGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MTG_ABI_VERSION 1
+
+/* Return codes */
+#define MTG_OK 0
+#define MTG_E_INVALID (-1)    /* bad argument or inconsistent descriptor */
+#define MTG_E_CUDA (-2)       /* CUDA runtime error (message holds cudaGetErrorString) */
+#define MTG_E_NOMEM (-3)      /* device or host allocation failed */
+#define MTG_E_OVERFLOW (-4)   /* a list could not be grown to hold its entries */
+#define MTG_E_TIMEOUT (-5)    /* a bounded device wait gave up */
+#define MTG_E_UNSUPPORTED (-6)/* valid request this build does not implement */
+#define MTG_E_NONFINITE (-7)  /* NaN/Inf in inputs or in the integrated state */
+
+/* Points per tabulated 1D force/potential profile (MDFFMatrices.h:27) and non-bonded terms per
+ * atom-type pair (MDFFMatrices.h:26). */
+#define MTG_NPTS 1000
+#define MTG_MAX_FF_PER_PAIR 5
+#define MTG_MAX_NH_CHAIN 16
+
+/* Term kinds.  Parameters follow the reference classes' parse order (see mtg_term). */
+#define MTG_KIND_NONE 0
+#define MTG_NB_LJ 1           /* p = {epsilon, sigma, alpha}         MolTwisterMDFFNonBonded_LJ.cpp:131-162 */
+#define MTG_NB_LJ1208 2       /* p = {epsilon, sigma, alpha}         MolTwisterMDFFNonBonded_LJ1208.cpp:131-170 */
+#define MTG_NB_BUCK 3         /* p = {A, rho, C}                     MolTwisterMDFFNonBonded_Buck.cpp:116-143 */
+#define MTG_NB_LJBUCK 4       /* table only                          MolTwisterMDFFNonBonded_LJBuck.cpp:181-251 */
+#define MTG_BOND_HARM 11      /* p = {k, r0}, U = k (r - r0)^2       MolTwisterMDFFBond_Harm.cpp:90-110 */
+#define MTG_BOND_MORSE 12     /* p = {D, alpha, r0}                  MolTwisterMDFFBond_Morse.cpp:95-117 */
+#define MTG_BOND_LJC 13       /* table only (zero force)             MolTwisterMDFFBond_LJC.cpp */
+#define MTG_ANGLE_HARM 21     /* p = {k, theta0 [deg], toRad}        MolTwisterMDFFAngle_Harm.cpp:94-130 */
+#define MTG_ANGLE_CLASS2 22   /* table only                          MolTwisterMDFFAngle_Class2.cpp:145-296 */
+#define MTG_DIH_HARM 31       /* p = {K, D, N}, U = K(1 + D cos N phi) MolTwisterMDFFDih_Harm.cpp:96-132 */
+#define MTG_DIH_FOURIER4T 32  /* p = {V1, V2, V3, V4}                MolTwisterMDFFDih_Fourier4t.cpp:98-142 */
+
+/* Precision modes (new key `precision`; the reference has only its own arithmetic). */
+#define MTG_PREC_REFERENCE 0  /* reference semantics: 1000-point FP32 tables, FP64 accumulation,
+                                 cell + neighbour lists rebuilt every step with the reference's
+                                 order, all-pairs minimum-image Coulomb.  The parity mode. */
+#define MTG_PREC_FP64 1       /* analytic terms in FP64, Verlet list with skin */
+#define MTG_PREC_MIXED 2      /* analytic terms in FP32, forces summed as int64 fixed point
+                                 (deterministic), positions as FP32 hi+lo pairs updated in FP64,
+                                 FP64 reductions and thermostat */
+
+/* Coulomb treatment (new key `coulomb`). */
+#define MTG_COULOMB_ALLPAIRS 0 /* the reference: minimum image over all pairs, no cutoff
+                                  (FunctorCalcForce.cpp:258-278,514-535) */
+#define MTG_COULOMB_CUTOFF 1   /* truncated at coulomb_cutoff (new option) */
+
+/* Ensembles (SMolDynConfigStruct::Ensemble, MolDynConfigStruct.h:24) */
+#define MTG_NVT 0
+#define MTG_NPT 1
+#define MTG_NVE 2
+
+/* One MDFF term: the kind code and up to four parameters, in the order listed above. */
+typedef struct mtg_term {
+    int32_t kind;
+    int32_t reserved;
+    double p[4];
+} mtg_term;
+
+/* System description.  Mirrors what CMDFFMatrices::prepareFFMatrices extracts from the state
+ * (MDFFMatrices.cpp:181-536).  Atom types are numbered in first-appearance order of the atom IDs
+ * (MolTwisterState.cpp:459-487).  Tables hold (x, -dU/dx, U) triples as produced by the MDFF
+ * classes' calc1DForceProfile / calc1DPotentialProfile over [0.01, rc] (non-bonded, bonds) or
+ * [0, 2 pi] (angles, dihedrals); pass NULL to have the library generate them from the terms
+ * (the generator covers every kind except LJBuck and Class2, which then require tables). */
+typedef struct mtg_system_desc {
+    int32_t n_atoms;
+    int32_t n_types;
+    const double* r;            /* [n_atoms*3] positions */
+    const double* p;            /* [n_atoms*3] momenta, or NULL for zero */
+    const double* mass;         /* [n_atoms] */
+    const double* charge;       /* [n_atoms] */
+    const int32_t* type;        /* [n_atoms] 0..n_types-1 */
+    const int32_t* mol;         /* [n_atoms] molecule index (-1 = none), or NULL */
+    const uint8_t* mobile;      /* [n_atoms] 0/1, or NULL for all mobile */
+    double box[3];              /* periodic box widths */
+    /* Non-bonded terms per (row, col) type pair; row = type of the atom the force acts on. */
+    const int32_t* nb_count;    /* [n_types*n_types] number of terms (<= MTG_MAX_FF_PER_PAIR) */
+    const mtg_term* nb_terms;   /* [n_types*n_types*MTG_MAX_FF_PER_PAIR] */
+    const float* nb_tables;     /* [n_types*n_types*MTG_MAX_FF_PER_PAIR*MTG_NPTS*3] or NULL */
+    int32_t n_bond_types;
+    const mtg_term* bond_terms; /* [n_bond_types] */
+    const float* bond_tables;   /* [n_bond_types*MTG_NPTS*3] or NULL */
+    int32_t n_angle_types;
+    const mtg_term* angle_terms;
+    const float* angle_tables;
+    int32_t n_dih_types;
+    const mtg_term* dih_terms;
+    const float* dih_tables;
+    /* Topology, as CMolTwisterStateTools::getAllMD{Bonds,Angles,Dihedrals}InSystem returns it
+     * (MolTwisterStateTools.cpp:544-1209).  The order fixes the per-atom list order. */
+    int32_t n_bonds;
+    const int32_t* bonds;       /* [n_bonds*3]: atom i, atom j, bond type (-1 = skipped) */
+    int32_t n_angles;
+    const int32_t* angles;      /* [n_angles*4]: i, j (centre), k, angle type */
+    int32_t n_dihedrals;
+    const int32_t* dihedrals;   /* [n_dihedrals*5]: i, j, k, l, dihedral type */
+} mtg_system_desc;
+
+/* Run settings: the SMolDynConfigStruct fields the MD engine reads
+ * (Config/MolDynConfigStruct.h:24-65, defaults Config/MolDynConfig.cpp:289-328) plus new keys. */
+typedef struct mtg_config_desc {
+    int32_t ensemble;           /* MTG_NVT / MTG_NPT / MTG_NVE */
+    int32_t temperature_nh_len; /* temperaturenhlen (M, <= MTG_MAX_NH_CHAIN) */
+    int32_t temperature_respa;  /* temperaturerespa */
+    int32_t pressure_nh_len;    /* pressurenhlen */
+    int32_t pressure_respa;     /* pressurerespa */
+    int32_t precision;          /* MTG_PREC_* (new) */
+    int32_t coulomb;            /* MTG_COULOMB_* (new) */
+    int32_t clip_forces;        /* apply per-component clipping at cutoff_force (NVT/NVE) */
+    double timestep;            /* fs */
+    double temperature;         /* K */
+    double temperature_relax;   /* fs */
+    double pressure;            /* atm */
+    double pressure_relax;      /* fs */
+    double cutoff_radius;       /* A */
+    double neigh_shell;         /* A, only sizes the cells (MDFFMatrices.cpp:45-58) */
+    double cutoff_force;        /* cutoffforce */
+    double scale12, scale13, scale14, scale1N;
+    double coulomb_cutoff;      /* A, for MTG_COULOMB_CUTOFF (new) */
+    double list_skin;           /* A, Verlet skin of the production neighbour list (new) */
+    double opt_learning_rate;   /* optlearningrate */
+    double opt_accuracy;        /* optaccuracy */
+    int32_t opt_max_steps;      /* optmaxsteps */
+    int32_t device;             /* CUDA device ordinal */
+} mtg_config_desc;
+
+/* Thermostat/barostat state (CNHChain eta_/p_eta_, NHChain.h:55-61; CVelVerlet p_eps_, VelVerlet.h:57-62). */
+typedef struct mtg_thermo_state {
+    int32_t M;
+    int32_t reserved;
+    double eta[MTG_MAX_NH_CHAIN];
+    double p_eta[MTG_MAX_NH_CHAIN];
+    double p_eps;
+    double eps;
+} mtg_thermo_state;
+
+/* Scalars of one output step (the info-line columns of MDLoop.cpp:388-403, in reduced units as
+ * CSimulationBox returns them: T = sum p^2/m / 3N [kJ/mol], P [kJ/mol/A^3], V [A^3]). */
+typedef struct mtg_output {
+    int64_t step;               /* 0-based step index just completed */
+    double T, P, V, U, K, E;
+    const double* r;            /* [n_atoms*3] positions after the step (host, valid during the call) */
+    const double* p;            /* [n_atoms*3] momenta after the step */
+} mtg_output;
+
+/* Output callback: return non-zero to stop the run early. */
+typedef int (*mtg_output_cb)(const mtg_output* out, void* user);
+
+typedef struct mtg_ctx mtg_ctx;
+
+/* Library version (MTG_ABI_VERSION) and device name of ordinal `device`. */
+int mtg_version(void);
+int mtg_device_name(int device, char* buf, int buflen);
+
+/* Tabulates one MDFF term on the host, as the term's calc1DForceProfile / calc1DPotentialProfile
+ * do (MolTwisterMDFFNonBonded.cpp:126-172, MolTwisterMDFFBond.cpp:133-179,
+ * MolTwisterMDFFAngle.cpp:210-257, MolTwisterMDFFDih.cpp:272-320): out[3*i .. 3*i+2] =
+ * (x_i, -dU/dx, U) for x_i = x0 + i (x1 - x0)/(npts - 1).  No GPU is needed.  The reference calls
+ * these with (0.01, rc) for non-bonded and bond terms and (0, 2 pi) for angles and dihedrals. */
+int mtg_term_profile(const mtg_term* term, float x0, float x1, int npts, float* out);
+
+/* Creates a context: validates the descriptors, uploads atoms, tables and topology, builds the
+ * per-atom bonded lists (MDFFMatrices.cpp:384-520) and computes the initial forces.
+ * Replaces CMDSimulator::run's setup half (MDSimulator.cpp:35-47, CSimulationBox ctor). */
+int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx** out);
+void mtg_destroy(mtg_ctx* ctx);
+const char* mtg_last_error(const mtg_ctx* ctx);   /* ctx may be NULL (creation errors) */
+
+/* Sets positions (NULL keeps), momenta (NULL keeps) and thermostat state (NULL keeps) and
+ * recomputes forces.  Used to inject a seeded initial state (the reference draws it from rand(),
+ * SimulationBox.cpp:98-133, NHChain.cpp:126-143). */
+int mtg_set_state(mtg_ctx* ctx, const double* r, const double* p, const mtg_thermo_state* th);
+int mtg_get_state(mtg_ctx* ctx, double* r, double* p, mtg_thermo_state* th);
+
+/* Runs nsteps of the reference step sequence NH_P, NH_T, velocity-Verlet, NH_T, NH_P, pbcWrap
+ * (MDLoop.cpp:128-133).  Every out_stride steps (step % out_stride == 0, as MDLoop.cpp:388) the
+ * callback receives the output scalars and host copies of r and p; cb may be NULL. */
+int mtg_run(mtg_ctx* ctx, int nsteps, int out_stride, mtg_output_cb cb, void* user);
+
+/* Gradient-descent energy minimisation, CMDLoop::runOptimization (MDLoop.cpp:143-173). */
+int mtg_optimize(mtg_ctx* ctx, double accuracy, int max_steps, int out_stride, mtg_output_cb cb, void* user);
+
+/* Parity hooks. */
+/* Forces and per-atom energies at the current positions, F = Fpi (no Ewald); any of the
+ * pointers may be NULL.  U follows the reference bookkeeping (FunctorCalcForce.cpp:498-502,
+ * 523-527, 562-566, 633-634, 700-701). */
+int mtg_compute_forces(mtg_ctx* ctx, double* F, double* Fpi, double* U);
+/* Cell list of the reference mode at the current positions: per-atom (ix,iy,iz), per-cell
+ * first entry / count, and the cell-ordered atom list (FunctorGenCellList.cpp:49-142).  dims
+ * receives the cell counts; ncells is the capacity of cell_first/cell_count. */
+int mtg_get_cells(mtg_ctx* ctx, int32_t* dims, int32_t* ixyz, int32_t* cell_first, int32_t* cell_count,
+                  int32_t ncells, int32_t* cell_list);
+/* Full neighbour list of the reference mode at the current positions, in the reference order
+ * (FunctorGenNeighList.cpp:72-151).  count[n]; list[n*max_neigh] when list != NULL;
+ * *needed receives the largest count. */
+int mtg_get_neighbors(mtg_ctx* ctx, int32_t max_neigh, int32_t* count, int32_t* list, int32_t* needed);
+
+/* Timing/diagnostics of the last mtg_run: device milliseconds of the step loop, steps done,
+ * neighbour-list rebuilds, and kernel launches per step. */
+typedef struct mtg_run_stats {
+    double device_ms;
+    int64_t steps;
+    int64_t list_builds;
+    int64_t kernel_launches;
+    int32_t graph_steps;        /* steps per captured CUDA graph (0 = not captured) */
+    int32_t reserved;
+} mtg_run_stats;
+int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
+
+/* Profiling hook (no counterpart in the reference, which only prints a per-step wall time,
+ * MDLoop.cpp:434-456): runs `steps` un-captured steps with CUDA events around each phase on the
+ * context's stream and returns the mean device milliseconds per step of
+ * phase_ms[0] kick+drift, [1] list build (cell list / Verlet list; the early-exit kernels when no
+ * rebuild is due), [2] force gather, [3] kick + wrap + reductions + thermostat.
+ * The state advances by `steps` steps exactly as mtg_run would advance it. */
+int mtg_profile_phases(mtg_ctx* ctx, int steps, double* phase_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MTGPU_H */

@@ -1,0 +1,976 @@
+// C ABI of libmtgpu.so (include/mtgpu.h): context lifetime, uploads, the step loop and the
+// parity hooks.  Host code; the kernels live in ref_kernels.cu and md_kernels.cu.
+//
+// Step loop.  One MD step is the reference sequence (MDLoop.cpp:128-133) mapped to kernels:
+//   kick+drift (first thermostat half-step folded in as a pending momentum scale)
+//   -> [reference: cell list + neighbour list every step | production: Verlet list if due]
+//   -> force gather -> clip + kick + pbc wrap + KE reduction, whose last block runs the
+//   thermostat's second half-step and the next step's first half-step.
+// Steps are captured into CUDA graphs, one chunk per output interval; the state at the start of
+// a chunk is kept so that a chunk whose neighbour list overflowed is redone after growing it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mtg_internal.h"
+
+using namespace mtg;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DeviceArena {
+    std::vector<void*> ptrs;
+    ~DeviceArena() { release(); }
+    void release() {
+        for(void* p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+}  // namespace
+
+struct mtg_ctx {
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Params P{};
+    DevSys d{};
+    mtg_config_desc cfg{};
+    int ncell_ref = 0, ncell_prod = 0;
+    int nblocks_red = 0;
+    // host mirrors
+    std::vector<double> h_mass;
+    std::vector<int> h_type;
+    // buffers
+    std::vector<void*> bufs;         // owned device allocations
+    void* nbr_buf = nullptr;         // reference neighbour list (growable)
+    void* vlist_buf = nullptr;       // production list (growable)
+    // snapshot for chunk rollback
+    struct Snap {
+        void* dst;
+        const void* src;
+        size_t bytes;
+    };
+    std::vector<Snap> snaps;
+    std::vector<void*> snap_bufs;
+    // graphs keyed by (steps, output_at_end)
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    int generation = 0;
+    bool forces_valid = false;
+    mtg_run_stats stats{};
+    // output staging
+    std::vector<double> h_r, h_p;
+
+    ~mtg_ctx() {
+        for(auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+        for(void* p : bufs) cudaFree(p);
+        for(void* p : snap_bufs) cudaFree(p);
+        if(nbr_buf) cudaFree(nbr_buf);
+        if(vlist_buf) cudaFree(vlist_buf);
+        if(ev0) cudaEventDestroy(ev0);
+        if(ev1) cudaEventDestroy(ev1);
+        if(stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int fail(mtg_ctx* c, int code, const std::string& msg) {
+    if(c) c->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                        \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if(e_ != cudaSuccess) return fail((ctx), MTG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while(0)
+
+template<class T>
+int dalloc(mtg_ctx* c, T** out, size_t count) {
+    void* p = nullptr;
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    cudaMemset(p, 0, bytes);
+    c->bufs.push_back(p);
+    *out = (T*)p;
+    return MTG_OK;
+}
+
+template<class T>
+int upload(mtg_ctx* c, T** out, const T* host, size_t count) {
+    int rc = dalloc(c, out, count);
+    if(rc) return rc;
+    if(count && host) CUDA_TRY(c, cudaMemcpy(*out, host, count * sizeof(T), cudaMemcpyHostToDevice));
+    return MTG_OK;
+}
+
+bool finite_all(const double* a, size_t n) {
+    for(size_t i = 0; i < n; i++)
+        if(!std::isfinite(a[i])) return false;
+    return true;
+}
+
+// Per-atom bonded lists in the reference's order (MDFFMatrices.cpp:384-520).
+struct AtomLists {
+    std::vector<int> bptr, bj, bt, aptr, ai, aj, at, acen, dptr, di, dj, dl, dt, dcen;
+};
+
+AtomLists build_atom_lists(int n, int nb, const int* bonds, int na, const int* angles, int nd, const int* dih) {
+    AtomLists L;
+    std::vector<std::vector<int>> bl(n), al(n), dl(n);
+    for(int j = 0; j < nb; j++) {
+        const int a = bonds[3 * j], b = bonds[3 * j + 1], t = bonds[3 * j + 2];
+        if(t < 0) continue;
+        bl[a].push_back(j);
+        if(b != a) bl[b].push_back(j);
+    }
+    for(int j = 0; j < na; j++) {
+        if(angles[4 * j + 3] < 0) continue;
+        int s[3] = {angles[4 * j], angles[4 * j + 1], angles[4 * j + 2]};
+        std::sort(s, s + 3);
+        for(int q = 0; q < 3; q++)
+            if(q == 0 || s[q] != s[q - 1]) al[s[q]].push_back(j);
+    }
+    for(int j = 0; j < nd; j++) {
+        if(dih[5 * j + 4] < 0) continue;
+        int s[4] = {dih[5 * j], dih[5 * j + 1], dih[5 * j + 2], dih[5 * j + 3]};
+        std::sort(s, s + 4);
+        for(int q = 0; q < 4; q++)
+            if(q == 0 || s[q] != s[q - 1]) dl[s[q]].push_back(j);
+    }
+    L.bptr.assign(n + 1, 0);
+    L.aptr.assign(n + 1, 0);
+    L.dptr.assign(n + 1, 0);
+    for(int k = 0; k < n; k++) {
+        L.bptr[k + 1] = L.bptr[k] + (int)bl[k].size();
+        for(int j : bl[k]) {
+            const int a = bonds[3 * j], b = bonds[3 * j + 1];
+            int to = -1;
+            if(a == k) to = b;
+            if(b == k) to = a;
+            L.bj.push_back(to);
+            L.bt.push_back(bonds[3 * j + 2]);
+        }
+        L.aptr[k + 1] = L.aptr[k] + (int)al[k].size();
+        for(int j : al[k]) {
+            const int a1 = angles[4 * j], a2 = angles[4 * j + 1], a3 = angles[4 * j + 2];
+            int I = -1, J = -1, cen = 0;
+            if(a1 == k) { I = a2; J = a3; }
+            if(a2 == k) { cen = 1; I = a1; J = a3; }
+            if(a3 == k) { I = a2; J = a1; }
+            L.ai.push_back(I);
+            L.aj.push_back(J);
+            L.at.push_back(angles[4 * j + 3]);
+            L.acen.push_back(cen);
+        }
+        L.dptr[k + 1] = L.dptr[k] + (int)dl[k].size();
+        for(int j : dl[k]) {
+            const int a1 = dih[5 * j], a2 = dih[5 * j + 1], a3 = dih[5 * j + 2], a4 = dih[5 * j + 3];
+            int I = -1, J = -1, Lx = -1, cen = 0;
+            if(a1 == k) { I = a2; J = a3; Lx = a4; }
+            if(a2 == k) { cen = 1; I = a1; J = a3; Lx = a4; }
+            if(a3 == k) { cen = 1; I = a4; J = a2; Lx = a1; }
+            if(a4 == k) { I = a3; J = a2; Lx = a1; }
+            L.di.push_back(I);
+            L.dj.push_back(J);
+            L.dl.push_back(Lx);
+            L.dt.push_back(dih[5 * j + 4]);
+            L.dcen.push_back(cen);
+        }
+    }
+    return L;
+}
+
+// Cells per axis as CCellList::init computes them (MDFFMatrices.cpp:45-58).
+int ref_cells(double L, double rc, double shell) {
+    const float R = (float)rc + (float)shell;
+    return (int)std::floor(double((float)L / R));
+}
+
+int grow_neighbors(mtg_ctx* c, int needed) {
+    const int cap = needed + 10;     // the reference grows to need + 10 (MDFFMatrices.cpp:172-176)
+    if(c->nbr_buf) cudaFree(c->nbr_buf);
+    c->nbr_buf = nullptr;
+    void* p;
+    cudaError_t e = cudaMalloc(&p, (size_t)c->P.n * cap * sizeof(int));
+    if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, "neighbour list allocation failed");
+    c->nbr_buf = p;
+    c->d.nbr_list = (int*)p;
+    c->d.nbr_max = cap;
+    c->generation++;
+    return MTG_OK;
+}
+
+int grow_vlist(mtg_ctx* c, int needed) {
+    const int cap = ((needed + needed / 4 + 32) + 31) / 32 * 32;
+    if(c->vlist_buf) cudaFree(c->vlist_buf);
+    c->vlist_buf = nullptr;
+    void* p;
+    cudaError_t e = cudaMalloc(&p, (size_t)c->P.n * cap * sizeof(uint32_t));
+    if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, "Verlet list allocation failed");
+    c->vlist_buf = p;
+    c->d.vlist = (uint32_t*)p;
+    c->d.vmax = cap;
+    c->generation++;
+    return MTG_OK;
+}
+
+StepScalars read_scalars(mtg_ctx* c) {
+    StepScalars s{};
+    cudaMemcpyAsync(&s, c->d.sc, sizeof(s), cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return s;
+}
+
+void clear_overflow(mtg_ctx* c) {
+    // zero overflow, needed, nonfinite (contiguous int32 fields)
+    cudaMemsetAsync(&c->d.sc->overflow, 0, 3 * sizeof(int32_t), c->stream);
+}
+
+bool is_reference(const mtg_ctx* c) { return c->P.precision == MTG_PREC_REFERENCE; }
+bool is_mixed(const mtg_ctx* c) { return c->P.precision == MTG_PREC_MIXED; }
+
+// Forces at the current positions, growing lists as needed.  Host-synchronous.
+int compute_forces_now(mtg_ctx* c, bool energy) {
+    for(int attempt = 0; attempt < 64; attempt++) {
+        clear_overflow(c);
+        if(is_reference(c)) {
+            launch_ref_cells(c->d, c->P, c->stream);
+            launch_ref_neigh(c->d, c->P, c->stream);
+            launch_ref_force(c->d, c->P, c->stream);
+        } else {
+            launch_prod_build(c->d, c->P, true, c->stream);
+            launch_prod_force(c->d, c->P, energy, c->stream);
+        }
+        CUDA_TRY(c, cudaGetLastError());
+        StepScalars s = read_scalars(c);
+        CUDA_TRY(c, cudaGetLastError());
+        if(!s.overflow) {
+            c->forces_valid = true;
+            return MTG_OK;
+        }
+        int rc = is_reference(c) ? grow_neighbors(c, s.needed) : grow_vlist(c, s.needed);
+        if(rc) return rc;
+    }
+    return fail(c, MTG_E_OVERFLOW, "neighbour list did not converge");
+}
+
+void enqueue_step(mtg_ctx* c, bool output) {
+    if(is_reference(c)) {
+        launch_ref_kick_drift(c->d, c->P, c->stream);
+        launch_ref_cells(c->d, c->P, c->stream);
+        launch_ref_neigh(c->d, c->P, c->stream);
+        launch_ref_force(c->d, c->P, c->stream);
+        launch_ref_kick2(c->d, c->P, output, c->stream);
+    } else {
+        launch_prod_kick_drift(c->d, c->P, c->stream);
+        launch_prod_build(c->d, c->P, false, c->stream);
+        launch_prod_force(c->d, c->P, output, c->stream);
+        launch_prod_kick2(c->d, c->P, output, c->stream);
+    }
+}
+
+int kernels_per_step(const mtg_ctx* c) { return is_reference(c) ? 8 : 9; }
+
+int get_graph(mtg_ctx* c, int steps, bool output, cudaGraphExec_t* out) {
+    auto key = std::make_pair(steps, output ? 1 : 0);
+    auto it = c->graphs.find(key);
+    if(it != c->graphs.end()) {
+        *out = it->second;
+        return MTG_OK;
+    }
+    cudaGraph_t g;
+    CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    for(int s = 0; s < steps; s++) enqueue_step(c, output && s == steps - 1);
+    CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
+    cudaGraphExec_t ge;
+    cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if(e != cudaSuccess) return fail(c, MTG_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    c->graphs[key] = ge;
+    *out = ge;
+    return MTG_OK;
+}
+
+void drop_graphs(mtg_ctx* c) {
+    for(auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+    c->graphs.clear();
+}
+
+int add_snap(mtg_ctx* c, const void* src, size_t bytes) {
+    void* p;
+    if(cudaMalloc(&p, std::max<size_t>(bytes, 1)) != cudaSuccess) return fail(c, MTG_E_NOMEM, "snapshot allocation failed");
+    c->snap_bufs.push_back(p);
+    c->snaps.push_back({p, src, bytes});
+    return MTG_OK;
+}
+
+void take_snapshot(mtg_ctx* c) {
+    for(auto& s : c->snaps) cudaMemcpyAsync(s.dst, s.src, s.bytes, cudaMemcpyDeviceToDevice, c->stream);
+}
+
+void restore_snapshot(mtg_ctx* c) {
+    for(auto& s : c->snaps) cudaMemcpyAsync((void*)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice, c->stream);
+}
+
+// Host copies of r and p after a step; p carries the pending scale c2 of the last second
+// thermostat half-step (the kernels apply it lazily at the next kick).
+int fetch_rp(mtg_ctx* c, double c2) {
+    const size_t n3 = (size_t)c->P.n * 3;
+    c->h_r.resize(n3);
+    c->h_p.resize(n3);
+    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_r.data(), c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_p.data(), c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if(c2 != 1.0)
+        for(size_t i = 0; i < n3; i++) c->h_p[i] *= c2;
+    return MTG_OK;
+}
+
+// Applies the pending c2 to the device momenta and rewinds the thermostat to the state after the
+// last completed step (end of a run).
+int settle_state(mtg_ctx* c) {
+    StepScalars s = read_scalars(c);
+    if(s.c2 != 1.0 || s.S != 1.0) {
+        std::vector<double> p((size_t)c->P.n * 3);
+        CUDA_TRY(c, cudaMemcpy(p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for(double& v : p) v *= s.c2;
+        CUDA_TRY(c, cudaMemcpy(c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(c->d.th, c->d.th_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
+        s.c2 = 1.0;
+        s.S = 1.0;
+        CUDA_TRY(c, cudaMemcpy(c->d.sc, &s, sizeof(s), cudaMemcpyHostToDevice));
+    }
+    return MTG_OK;
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+int mtg_version(void) { return MTG_ABI_VERSION; }
+
+int mtg_device_name(int device, char* buf, int buflen) {
+    cudaDeviceProp prop;
+    if(cudaGetDeviceProperties(&prop, device) != cudaSuccess) return MTG_E_CUDA;
+    if(buf && buflen > 0) {
+        std::snprintf(buf, (size_t)buflen, "%s (sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor, prop.multiProcessorCount);
+    }
+    return MTG_OK;
+}
+
+int mtg_term_profile(const mtg_term* term, float x0, float x1, int npts, float* out) {
+    if(!term || !out || npts < 2) return MTG_E_INVALID;
+    const int k = term->kind;
+    if(k >= MTG_NB_LJ && k <= MTG_NB_LJBUCK) return profile_nonbonded(k, term->p, x0, x1, npts, out);
+    if(k >= MTG_BOND_HARM && k <= MTG_BOND_LJC) return profile_bond(k, term->p, x0, x1, npts, out);
+    if(k >= MTG_ANGLE_HARM && k <= MTG_ANGLE_CLASS2) return profile_angle(k, term->p, x0, x1, npts, out);
+    if(k >= MTG_DIH_HARM && k <= MTG_DIH_FOURIER4T) return profile_dihedral(k, term->p, x0, x1, npts, out);
+    return MTG_E_UNSUPPORTED;
+}
+
+const char* mtg_last_error(const mtg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+void mtg_destroy(mtg_ctx* ctx) { delete ctx; }
+
+int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx** out) {
+    g_create_error.clear();
+    if(!sys || !cfg || !out) return fail(nullptr, MTG_E_INVALID, "null argument");
+    *out = nullptr;
+    const int n = sys->n_atoms, T = sys->n_types;
+    if(n <= 0) return fail(nullptr, MTG_E_INVALID, "n_atoms must be positive");
+    if(n > (int)kIdxMask) return fail(nullptr, MTG_E_INVALID, "too many atoms for 29-bit list indices");
+    if(T <= 0 || !sys->type || !sys->r || !sys->mass || !sys->charge || !sys->nb_count)
+        return fail(nullptr, MTG_E_INVALID, "missing atom arrays or non-bonded counts");
+    for(int a = 0; a < 3; a++)
+        if(!(sys->box[a] > 0.0) || !std::isfinite(sys->box[a])) return fail(nullptr, MTG_E_INVALID, "box widths must be positive");
+    if(!finite_all(sys->r, (size_t)3 * n) || (sys->p && !finite_all(sys->p, (size_t)3 * n)) ||
+       !finite_all(sys->mass, n) || !finite_all(sys->charge, n))
+        return fail(nullptr, MTG_E_NONFINITE, "non-finite positions, momenta, masses or charges");
+    for(int i = 0; i < n; i++) {
+        if(sys->type[i] < 0 || sys->type[i] >= T) return fail(nullptr, MTG_E_INVALID, "atom type out of range");
+        if(!(sys->mass[i] > 0.0)) return fail(nullptr, MTG_E_INVALID, "masses must be positive");
+    }
+    if(cfg->precision < MTG_PREC_REFERENCE || cfg->precision > MTG_PREC_MIXED) return fail(nullptr, MTG_E_INVALID, "bad precision");
+    if(cfg->ensemble == MTG_NPT) return fail(nullptr, MTG_E_UNSUPPORTED, "NPT (MTK barostat) is not implemented in this build");
+    if(cfg->ensemble != MTG_NVT && cfg->ensemble != MTG_NVE) return fail(nullptr, MTG_E_INVALID, "bad ensemble");
+    if(cfg->temperature_nh_len < 0 || cfg->temperature_nh_len > kMaxChain) return fail(nullptr, MTG_E_INVALID, "chain length out of range");
+    if(cfg->ensemble == MTG_NVT && (cfg->temperature_nh_len < 1 || cfg->temperature_respa < 1 || !(cfg->temperature > 0.0) || !(cfg->temperature_relax > 0.0)))
+        return fail(nullptr, MTG_E_INVALID, "NVT needs temperature > 0, relaxation > 0, chain length >= 1, RESPA >= 1");
+    if(!(cfg->timestep > 0.0) || !(cfg->cutoff_radius > 0.0)) return fail(nullptr, MTG_E_INVALID, "timestep and cutoff must be positive");
+    for(int q = 0; q < T * T; q++)
+        if(sys->nb_count[q] < 0 || sys->nb_count[q] > kMaxFF) return fail(nullptr, MTG_E_INVALID, "nb_count out of range");
+    if(cfg->precision != MTG_PREC_REFERENCE && cfg->coulomb == MTG_COULOMB_ALLPAIRS) {
+        bool anyq = false;
+        for(int i = 0; i < n; i++) anyq |= (sys->charge[i] != 0.0);
+        if(anyq) return fail(nullptr, MTG_E_UNSUPPORTED, "all-pairs Coulomb is available in the reference precision mode; use cutoff Coulomb with fp64/mixed");
+    }
+    auto check_topo = [&](int cnt, const int* a, int w, int ntypes) -> bool {
+        if(cnt < 0 || (cnt > 0 && !a)) return false;
+        for(int j = 0; j < cnt; j++) {
+            for(int q = 0; q < w - 1; q++)
+                if(a[w * j + q] < 0 || a[w * j + q] >= n) return false;
+            if(a[w * j + w - 1] >= ntypes) return false;
+        }
+        return true;
+    };
+    if(!check_topo(sys->n_bonds, sys->bonds, 3, sys->n_bond_types) || !check_topo(sys->n_angles, sys->angles, 4, sys->n_angle_types) ||
+       !check_topo(sys->n_dihedrals, sys->dihedrals, 5, sys->n_dih_types))
+        return fail(nullptr, MTG_E_INVALID, "bonded topology indices out of range");
+
+    std::unique_ptr<mtg_ctx> c(new mtg_ctx());
+    c->cfg = *cfg;
+    c->device = cfg->device;
+    if(cudaSetDevice(c->device) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "cudaSetDevice failed (no GPU?)");
+    if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "stream creation failed");
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+
+    // ---- parameters ----
+    Params& P = c->P;
+    P.n = n;
+    P.T = T;
+    for(int a = 0; a < 3; a++) {
+        P.box[a] = sys->box[a];
+        P.boxf[a] = (float)sys->box[a];
+    }
+    P.ensemble = cfg->ensemble;
+    P.precision = cfg->precision;
+    P.coulomb = cfg->coulomb;
+    P.clip = cfg->clip_forces;
+    P.dt = cfg->timestep / kConvt;
+    P.kT = cfg->temperature / kConvT;
+    P.tau = cfg->temperature_relax / kConvt;
+    P.M = cfg->ensemble == MTG_NVE ? 0 : cfg->temperature_nh_len;
+    P.nresp = cfg->temperature_respa;
+    P.fcut = cfg->cutoff_force;
+    P.rc = (float)cfg->cutoff_radius;
+    P.shell = (float)cfg->neigh_shell;
+    P.rcoul = (float)(cfg->coulomb_cutoff > 0.0 ? cfg->coulomb_cutoff : cfg->cutoff_radius);
+    P.skin = (float)(cfg->list_skin > 0.0 ? cfg->list_skin : 0.0);
+    P.scale12 = (float)cfg->scale12;
+    P.scale13 = (float)cfg->scale13;
+    P.scale14 = (float)cfg->scale14;
+    P.scale1N = (float)cfg->scale1N;
+    P.scale[0] = 1.0f;
+    P.scale[1] = P.scale12;
+    P.scale[2] = P.scale13;
+    P.scale[3] = P.scale14;
+    P.scale[4] = P.scale1N;
+    P.nx = ref_cells(sys->box[0], cfg->cutoff_radius, cfg->neigh_shell);
+    P.ny = ref_cells(sys->box[1], cfg->cutoff_radius, cfg->neigh_shell);
+    P.nz = ref_cells(sys->box[2], cfg->cutoff_radius, cfg->neigh_shell);
+    if(P.nx < 1 || P.ny < 1 || P.nz < 1) return fail(nullptr, MTG_E_INVALID, "box narrower than cutoff + shell: the reference cell list is empty");
+    {
+        const double rlist = std::max((double)P.rc, P.coulomb == MTG_COULOMB_CUTOFF ? (double)P.rcoul : 0.0) + P.skin;
+        int pn[3];
+        for(int a = 0; a < 3; a++) {
+            pn[a] = (int)std::floor(sys->box[a] / rlist);
+            if(pn[a] < 3) pn[a] = 1;   // small box: scan every atom once (no duplicated images)
+        }
+        // keep the grid modest: at most ~ n/2 cells
+        while((long long)pn[0] * pn[1] * pn[2] > std::max(27, n / 2)) {
+            for(int a = 0; a < 3; a++) pn[a] = std::max(3, pn[a] - 1);
+            if(pn[0] == 3 && pn[1] == 3 && pn[2] == 3) break;
+        }
+        P.pnx = pn[0];
+        P.pny = pn[1];
+        P.pnz = pn[2];
+        if(P.precision != MTG_PREC_REFERENCE) {
+            const double half = 0.5 * std::min(sys->box[0], std::min(sys->box[1], sys->box[2]));
+            if(rlist > half && (pn[0] > 1 || pn[1] > 1 || pn[2] > 1))
+                return fail(nullptr, MTG_E_INVALID, "cutoff + skin exceeds half the box");
+            if(std::max((double)P.rc, (double)P.rcoul) >= half)
+                return fail(nullptr, MTG_E_INVALID, "cutoff must be below half the box (minimum image)");
+        }
+    }
+    c->ncell_ref = P.nx * P.ny * P.nz;
+    c->ncell_prod = P.pnx * P.pny * P.pnz;
+    c->nblocks_red = reduction_blocks(n);
+
+    // ---- tables ----
+    const size_t TT = (size_t)T * T;
+    std::vector<float> nb_tab(TT * kMaxFF * kNpts * 3, 0.0f);
+    std::vector<int> nb_kind(TT * kMaxFF, 0);
+    std::vector<double> nb_coef(TT * kMaxFF * 4, 0.0);
+    std::vector<float> nb_coeff(TT * kMaxFF * 4, 0.0f);
+    const float rcf = (float)cfg->cutoff_radius;
+    for(size_t q = 0; q < TT; q++) {
+        for(int ff = 0; ff < sys->nb_count[q]; ff++) {
+            const size_t idx = q * kMaxFF + ff;
+            const mtg_term& t = sys->nb_terms[idx];
+            nb_kind[idx] = t.kind;
+            if(sys->nb_tables) {
+                std::memcpy(&nb_tab[idx * kNpts * 3], sys->nb_tables + idx * kNpts * 3, sizeof(float) * kNpts * 3);
+            } else if(profile_nonbonded(t.kind, t.p, 0.01f, rcf, kNpts, &nb_tab[idx * kNpts * 3]) != MTG_OK) {
+                return fail(nullptr, MTG_E_UNSUPPORTED, "non-bonded kind needs tables (LJBuck or unknown)");
+            }
+            // analytic coefficients (production modes)
+            double* co = &nb_coef[idx * 4];
+            if(t.kind == MTG_NB_LJ || t.kind == MTG_NB_LJ1208) {
+                const double s2 = t.p[1] * t.p[1], s4 = s2 * s2, s6 = s4 * s2, s8 = s4 * s4, s12 = s6 * s6;
+                co[0] = 4.0 * t.p[0] * s12;
+                co[1] = 4.0 * t.p[0] * t.p[2] * (t.kind == MTG_NB_LJ ? s6 : s8);
+            } else if(t.kind == MTG_NB_BUCK) {
+                co[0] = t.p[0];
+                co[1] = (t.p[1] == 0.0) ? 1E-10 : 1.0 / t.p[1];
+                co[2] = t.p[2];
+            } else {
+                nb_kind[idx] = 99;   // interpolate the table
+            }
+            for(int w = 0; w < 4; w++) nb_coeff[idx * 4 + w] = (float)co[w];
+        }
+    }
+    auto bonded_tables = [&](int ntypes, const mtg_term* terms, const float* given, float x0, float x1,
+                             int (*gen)(int, const double*, float, float, int, float*), std::vector<float>& tab,
+                             std::vector<int>& kinds, std::vector<double>& par) -> int {
+        tab.assign((size_t)std::max(ntypes, 1) * kNpts * 3, 0.0f);
+        kinds.assign(std::max(ntypes, 1), 0);
+        par.assign((size_t)std::max(ntypes, 1) * 4, 0.0);
+        for(int t = 0; t < ntypes; t++) {
+            kinds[t] = terms ? terms[t].kind : 99;
+            if(terms) for(int w = 0; w < 4; w++) par[4 * t + w] = terms[t].p[w];
+            if(given) std::memcpy(&tab[(size_t)t * kNpts * 3], given + (size_t)t * kNpts * 3, sizeof(float) * kNpts * 3);
+            else if(!terms || gen(terms[t].kind, terms[t].p, x0, x1, kNpts, &tab[(size_t)t * kNpts * 3]) != MTG_OK)
+                return MTG_E_UNSUPPORTED;
+        }
+        return MTG_OK;
+    };
+    std::vector<float> btab, atab, dtab;
+    std::vector<int> bkind, akind, dkind;
+    std::vector<double> bpar, apar, dpar;
+    const float two_pi = float(2.0 * M_PI);
+    if(bonded_tables(sys->n_bond_types, sys->bond_terms, sys->bond_tables, 0.01f, rcf, profile_bond, btab, bkind, bpar) ||
+       bonded_tables(sys->n_angle_types, sys->angle_terms, sys->angle_tables, 0.0f, two_pi, profile_angle, atab, akind, apar) ||
+       bonded_tables(sys->n_dih_types, sys->dih_terms, sys->dih_tables, 0.0f, two_pi, profile_dihedral, dtab, dkind, dpar))
+        return fail(nullptr, MTG_E_UNSUPPORTED, "bonded kind needs tables (Class2 or unknown)");
+
+    // ---- per-atom data ----
+    std::vector<float> qf(n);
+    std::vector<int> mol(n), mob(n), type(sys->type, sys->type + n);
+    std::vector<float> invm(n);
+    for(int i = 0; i < n; i++) {
+        qf[i] = (float)sys->charge[i];
+        mol[i] = sys->mol ? sys->mol[i] : -1;
+        mob[i] = sys->mobile ? (sys->mobile[i] != 0) : 1;
+        invm[i] = (float)(1.0 / sys->mass[i]);
+    }
+    c->h_mass.assign(sys->mass, sys->mass + n);
+    c->h_type = type;
+    AtomLists L = build_atom_lists(n, sys->n_bonds, sys->bonds, sys->n_angles, sys->angles, sys->n_dihedrals, sys->dihedrals);
+
+    DevSys& d = c->d;
+    d.n = n;
+    d.T = T;
+    std::vector<double> p0((size_t)3 * n, 0.0);
+    if(sys->p) std::memcpy(p0.data(), sys->p, sizeof(double) * 3 * n);
+    for(int i = 0; i < n; i++)
+        if(!mob[i]) p0[3 * i] = p0[3 * i + 1] = p0[3 * i + 2] = 0.0;   // SimulationBox.cpp:117-122
+    int rc = 0;
+    {
+        mtg_ctx* C = c.get();
+        rc = rc || upload(C, &d.r, sys->r, (size_t)3 * n);
+        rc = rc || upload(C, &d.p, p0.data(), (size_t)3 * n);
+        rc = rc || dalloc(C, &d.F, (size_t)3 * n);
+        rc = rc || dalloc(C, &d.U, (size_t)n);
+        rc = rc || upload(C, &d.m, sys->mass, (size_t)n);
+        rc = rc || upload(C, &d.qd, sys->charge, (size_t)n);
+        rc = rc || upload(C, &d.qf, qf.data(), (size_t)n);
+        rc = rc || upload(C, &d.type, type.data(), (size_t)n);
+        rc = rc || upload(C, &d.mol, mol.data(), (size_t)n);
+        rc = rc || upload(C, &d.mobile, mob.data(), (size_t)n);
+        float* f;
+        int* ip;
+        double* dp;
+        rc = rc || upload(C, &f, nb_tab.data(), nb_tab.size()); d.nb_tab = f;
+        rc = rc || upload(C, &ip, sys->nb_count, TT); d.nb_cnt = ip;
+        rc = rc || upload(C, &f, btab.data(), btab.size()); d.bond_tab = f;
+        rc = rc || upload(C, &f, atab.data(), atab.size()); d.angle_tab = f;
+        rc = rc || upload(C, &f, dtab.data(), dtab.size()); d.dih_tab = f;
+        rc = rc || upload(C, &ip, nb_kind.data(), nb_kind.size()); d.nb_kind = ip;
+        rc = rc || upload(C, &dp, nb_coef.data(), nb_coef.size()); d.nb_par = dp;
+        rc = rc || upload(C, &f, nb_coeff.data(), nb_coeff.size()); d.nb_parf = f;
+        rc = rc || upload(C, &ip, bkind.data(), bkind.size()); d.bond_kind = ip;
+        rc = rc || upload(C, &dp, bpar.data(), bpar.size()); d.bond_par = dp;
+        rc = rc || upload(C, &ip, akind.data(), akind.size()); d.angle_kind = ip;
+        rc = rc || upload(C, &dp, apar.data(), apar.size()); d.angle_par = dp;
+        rc = rc || upload(C, &ip, dkind.data(), dkind.size()); d.dih_kind = ip;
+        rc = rc || upload(C, &dp, dpar.data(), dpar.size()); d.dih_par = dp;
+        auto up = [&](const std::vector<int>& v) -> const int* {
+            int* q = nullptr;
+            rc = rc || upload(C, &q, v.data(), v.size());
+            return q;
+        };
+        d.bptr = up(L.bptr); d.bj = up(L.bj); d.bt = up(L.bt);
+        d.aptr = up(L.aptr); d.ai = up(L.ai); d.aj = up(L.aj); d.at = up(L.at); d.acen = up(L.acen);
+        d.dptr = up(L.dptr); d.di = up(L.di); d.dj = up(L.dj); d.dl = up(L.dl); d.dt = up(L.dt); d.dcen = up(L.dcen);
+        rc = rc || dalloc(C, &d.atom_cell, (size_t)3 * n);
+        rc = rc || dalloc(C, &d.cell_first, (size_t)c->ncell_ref);
+        rc = rc || dalloc(C, &d.cell_count, (size_t)c->ncell_ref);
+        rc = rc || dalloc(C, &d.cell_cursor, (size_t)c->ncell_ref);
+        rc = rc || dalloc(C, &d.cell_list, (size_t)n);
+        rc = rc || dalloc(C, &d.nbr_count, (size_t)n);
+        rc = rc || dalloc(C, &d.pcell_of, (size_t)n);
+        rc = rc || dalloc(C, &d.pcell_first, (size_t)c->ncell_prod);
+        rc = rc || dalloc(C, &d.pcell_count, (size_t)c->ncell_prod);
+        rc = rc || dalloc(C, &d.pcell_cursor, (size_t)c->ncell_prod);
+        rc = rc || dalloc(C, &d.pcell_list, (size_t)n);
+        rc = rc || dalloc(C, &d.vcount, (size_t)n);
+        rc = rc || dalloc(C, &d.r_build, (size_t)3 * n);
+        rc = rc || dalloc(C, &d.rb4, (size_t)n);
+        rc = rc || dalloc(C, &d.hi, (size_t)n);
+        rc = rc || dalloc(C, &d.lo, (size_t)n);
+        rc = rc || dalloc(C, &d.Fx, (size_t)n);
+        rc = rc || dalloc(C, &d.Fy, (size_t)n);
+        rc = rc || dalloc(C, &d.Fz, (size_t)n);
+        rc = rc || upload(C, &d.inv_m, invm.data(), (size_t)n);
+        rc = rc || dalloc(C, &d.partial, (size_t)c->nblocks_red * 4);
+        rc = rc || dalloc(C, &d.sc, 1);
+        rc = rc || dalloc(C, &d.th, 1);
+        rc = rc || dalloc(C, &d.th_saved, 1);
+        rc = rc || dalloc(C, &d.rec, 8);
+    }
+    if(rc) return fail(nullptr, rc, c->err);
+    // thermostat masses (NHChain.cpp:115-124): Q0 = dim N kT tau^2, Qj = kT tau^2
+    {
+        ThermoDev th{};
+        for(int j = 0; j < kMaxChain; j++) th.Q[j] = 1.0;
+        if(P.M > 0) {
+            th.Q[0] = double(3 * n) * P.kT * P.tau * P.tau;
+            for(int j = 1; j < P.M; j++) th.Q[j] = P.kT * P.tau * P.tau;
+        }
+        cudaMemcpy(d.th, &th, sizeof(th), cudaMemcpyHostToDevice);
+        cudaMemcpy(d.th_saved, &th, sizeof(th), cudaMemcpyHostToDevice);
+        StepScalars s{};
+        s.S = 1.0;
+        s.c2 = 1.0;
+        cudaMemcpy(d.sc, &s, sizeof(s), cudaMemcpyHostToDevice);
+    }
+    // list capacities: start from a density estimate, grown on demand
+    {
+        const double V = sys->box[0] * sys->box[1] * sys->box[2];
+        const double rho = n / V;
+        const double rc3 = std::pow(cfg->cutoff_radius, 3.0);
+        int est = (int)(1.3 * rho * 4.18879 * rc3) + 32;
+        rc = grow_neighbors(c.get(), std::min(est, n));
+        if(rc) return fail(nullptr, rc, c->err);
+        double rl = std::max((double)P.rc, P.coulomb == MTG_COULOMB_CUTOFF ? (double)P.rcoul : 0.0) + P.skin;
+        int vest = (int)(1.2 * rho * 4.18879 * rl * rl * rl) + 32;
+        rc = grow_vlist(c.get(), std::min(vest, n));
+        if(rc) return fail(nullptr, rc, c->err);
+    }
+    if(is_mixed(c.get())) launch_prod_sync_positions(d, P, true, c->stream);
+    // snapshot set for chunk rollback
+    {
+        mtg_ctx* C = c.get();
+        rc = rc || add_snap(C, d.r, sizeof(double) * 3 * n);
+        rc = rc || add_snap(C, d.p, sizeof(double) * 3 * n);
+        rc = rc || add_snap(C, d.F, sizeof(double) * 3 * n);
+        rc = rc || add_snap(C, d.U, sizeof(double) * n);
+        rc = rc || add_snap(C, d.th, sizeof(ThermoDev));
+        rc = rc || add_snap(C, d.th_saved, sizeof(ThermoDev));
+        rc = rc || add_snap(C, d.sc, sizeof(StepScalars));
+        if(is_mixed(C)) {
+            rc = rc || add_snap(C, d.hi, sizeof(float4) * n);
+            rc = rc || add_snap(C, d.lo, sizeof(float4) * n);
+            rc = rc || add_snap(C, d.Fx, sizeof(long long) * n);
+            rc = rc || add_snap(C, d.Fy, sizeof(long long) * n);
+            rc = rc || add_snap(C, d.Fz, sizeof(long long) * n);
+        }
+        if(rc) return fail(nullptr, rc, c->err);
+    }
+    rc = compute_forces_now(c.get(), true);
+    if(rc) return fail(nullptr, rc, c->err);
+    if(cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "initial force evaluation failed");
+    *out = c.release();
+    return MTG_OK;
+}
+
+int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo_state* th) {
+    if(!c) return MTG_E_INVALID;
+    const size_t n3 = (size_t)c->P.n * 3;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    if(r) {
+        if(!finite_all(r, n3)) return fail(c, MTG_E_NONFINITE, "non-finite positions");
+        CUDA_TRY(c, cudaMemcpy(c->d.r, r, n3 * sizeof(double), cudaMemcpyHostToDevice));
+        if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, true, c->stream);
+    }
+    if(p) {
+        if(!finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
+        CUDA_TRY(c, cudaMemcpy(c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if(th) {
+        ThermoDev t{};
+        CUDA_TRY(c, cudaMemcpy(&t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
+        const int M = std::min<int>(th->M, kMaxChain);
+        for(int j = 0; j < M; j++) {
+            t.eta[j] = th->eta[j];
+            t.peta[j] = th->p_eta[j];
+        }
+        CUDA_TRY(c, cudaMemcpy(c->d.th, &t, sizeof(t), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(c->d.th_saved, &t, sizeof(t), cudaMemcpyHostToDevice));
+    }
+    if(r) return compute_forces_now(c, true);
+    return MTG_OK;
+}
+
+int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
+    if(!c) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    const size_t n3 = (size_t)c->P.n * 3;
+    if(r) {
+        if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+        CUDA_TRY(c, cudaMemcpyAsync(r, c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    if(p) CUDA_TRY(c, cudaMemcpyAsync(p, c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if(th) {
+        ThermoDev t{};
+        CUDA_TRY(c, cudaMemcpy(&t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
+        std::memset(th, 0, sizeof(*th));
+        th->M = c->P.M;
+        for(int j = 0; j < c->P.M; j++) {
+            th->eta[j] = t.eta[j];
+            th->p_eta[j] = t.peta[j];
+        }
+    }
+    return MTG_OK;
+}
+
+int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user) {
+    if(!c || nsteps < 0) return MTG_E_INVALID;
+    if(nsteps == 0) return MTG_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if(out_stride <= 0) out_stride = nsteps + 1;
+    c->stats = mtg_run_stats{};
+    // thermostat first half-step of step 0 from the current momenta
+    launch_prologue(c->d, c->P, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    float total_ms = 0.0f;
+    int t = 0;
+    int gen_seen = c->generation;
+    while(t < nsteps) {
+        // chunk: up to the next output step (t % out_stride == 0) inclusive
+        int next_out = (t % out_stride == 0) ? t : (t / out_stride + 1) * out_stride;
+        int end = std::min(nsteps - 1, next_out);
+        const bool output = (end % out_stride == 0);
+        const int steps = end - t + 1;
+        int attempt = 0;
+        for(;;) {
+            if(c->generation != gen_seen) {
+                drop_graphs(c);
+                gen_seen = c->generation;
+            }
+            take_snapshot(c);
+            clear_overflow(c);
+            cudaGraphExec_t ge;
+            int rc = get_graph(c, steps, output, &ge);
+            if(rc) return rc;
+            CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+            CUDA_TRY(c, cudaGraphLaunch(ge, c->stream));
+            CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+            StepScalars s = read_scalars(c);
+            CUDA_TRY(c, cudaGetLastError());
+            if(s.overflow) {
+                restore_snapshot(c);
+                if(is_reference(c)) rc = grow_neighbors(c, s.needed);
+                else {
+                    rc = grow_vlist(c, s.needed);
+                    cudaMemsetAsync(&c->d.sc->rebuild, 0xff, sizeof(int32_t), c->stream);
+                }
+                if(rc) return rc;
+                if(++attempt > 32) return fail(c, MTG_E_OVERFLOW, "neighbour list did not converge");
+                continue;
+            }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+            total_ms += ms;
+            if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite momenta during the run");
+            c->stats.list_builds = s.builds;
+            if(output) {
+                double rec[8];
+                CUDA_TRY(c, cudaMemcpy(rec, c->d.rec, sizeof(rec), cudaMemcpyDeviceToHost));
+                if(!std::isfinite(rec[0]) || !std::isfinite(rec[1])) return fail(c, MTG_E_NONFINITE, "non-finite energy during the run");
+                if(cb) {
+                    int frc = fetch_rp(c, s.c2);
+                    if(frc) return frc;
+                    mtg_output o{};
+                    o.step = end;
+                    o.U = rec[0];
+                    o.K = rec[1];
+                    o.T = rec[2];
+                    o.P = rec[3];
+                    o.V = rec[4];
+                    o.E = rec[0] + rec[1];
+                    o.r = c->h_r.data();
+                    o.p = c->h_p.data();
+                    if(cb(&o, user)) {
+                        t = end + 1;
+                        c->stats.steps = t;
+                        c->stats.device_ms = total_ms;
+                        return settle_state(c);
+                    }
+                }
+            }
+            break;
+        }
+        t = end + 1;
+        c->stats.graph_steps = steps;
+    }
+    c->stats.steps = nsteps;
+    c->stats.device_ms = total_ms;
+    c->stats.kernel_launches = (int64_t)nsteps * kernels_per_step(c) + 1;
+    return settle_state(c);
+}
+
+int mtg_compute_forces(mtg_ctx* c, double* F, double* Fpi, double* U) {
+    if(!c) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    rc = compute_forces_now(c, true);
+    if(rc) return rc;
+    if(is_mixed(c)) launch_prod_forces_to_double(c->d, c->P, c->stream);
+    const size_t n3 = (size_t)c->P.n * 3;
+    if(F) CUDA_TRY(c, cudaMemcpyAsync(F, c->d.F, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if(Fpi) CUDA_TRY(c, cudaMemcpyAsync(Fpi, c->d.F, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if(U) CUDA_TRY(c, cudaMemcpyAsync(U, c->d.U, (size_t)c->P.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MTG_OK;
+}
+
+int mtg_get_cells(mtg_ctx* c, int32_t* dims, int32_t* ixyz, int32_t* cell_first, int32_t* cell_count, int32_t ncells,
+                  int32_t* cell_list) {
+    if(!c) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if(dims) {
+        dims[0] = c->P.nx;
+        dims[1] = c->P.ny;
+        dims[2] = c->P.nz;
+    }
+    if((cell_first || cell_count) && ncells < c->ncell_ref) return fail(c, MTG_E_INVALID, "cell arrays too small");
+    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    launch_ref_cells(c->d, c->P, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    const int n = c->P.n;
+    if(ixyz) CUDA_TRY(c, cudaMemcpyAsync(ixyz, c->d.atom_cell, sizeof(int) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    if(cell_first) CUDA_TRY(c, cudaMemcpyAsync(cell_first, c->d.cell_first, sizeof(int) * c->ncell_ref, cudaMemcpyDeviceToHost, c->stream));
+    if(cell_count) CUDA_TRY(c, cudaMemcpyAsync(cell_count, c->d.cell_count, sizeof(int) * c->ncell_ref, cudaMemcpyDeviceToHost, c->stream));
+    if(cell_list) CUDA_TRY(c, cudaMemcpyAsync(cell_list, c->d.cell_list, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MTG_OK;
+}
+
+int mtg_get_neighbors(mtg_ctx* c, int32_t max_neigh, int32_t* count, int32_t* list, int32_t* needed) {
+    if(!c) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    for(int attempt = 0; attempt < 64; attempt++) {
+        clear_overflow(c);
+        launch_ref_cells(c->d, c->P, c->stream);
+        launch_ref_neigh(c->d, c->P, c->stream);
+        CUDA_TRY(c, cudaGetLastError());
+        StepScalars s = read_scalars(c);
+        if(!s.overflow) break;
+        int rc = grow_neighbors(c, s.needed);
+        if(rc) return rc;
+    }
+    const int n = c->P.n;
+    std::vector<int> cnt(n);
+    CUDA_TRY(c, cudaMemcpy(cnt.data(), c->d.nbr_count, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    int mx = 0;
+    for(int v : cnt) mx = std::max(mx, v);
+    if(needed) *needed = mx;
+    if(count) std::memcpy(count, cnt.data(), sizeof(int) * n);
+    if(list) {
+        if(max_neigh < mx) return fail(c, MTG_E_INVALID, "max_neigh smaller than the longest list");
+        std::vector<int> tmp((size_t)n * c->d.nbr_max);
+        CUDA_TRY(c, cudaMemcpy(tmp.data(), c->d.nbr_list, tmp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for(int k = 0; k < n; k++)
+            for(int e = 0; e < max_neigh; e++) list[(size_t)k * max_neigh + e] = e < cnt[k] ? tmp[(size_t)k * c->d.nbr_max + e] : -1;
+    }
+    return MTG_OK;
+}
+
+int mtg_optimize(mtg_ctx* c, double accuracy, int max_steps, int out_stride, mtg_output_cb cb, void* user) {
+    (void)c; (void)accuracy; (void)max_steps; (void)out_stride; (void)cb; (void)user;
+    if(!c) return MTG_E_INVALID;
+    return fail(c, MTG_E_UNSUPPORTED, "gradient-descent optimisation is not implemented in this build");
+}
+
+int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
+    if(!c || steps <= 0 || !phase_ms) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    cudaEvent_t ev[5];
+    for(auto& e : ev) CUDA_TRY(c, cudaEventCreate(&e));
+    double acc[4] = {0, 0, 0, 0};
+    launch_prologue(c->d, c->P, c->stream);
+    take_snapshot(c);
+    clear_overflow(c);
+    for(int s = 0; s < steps; s++) {
+        cudaEventRecord(ev[0], c->stream);
+        if(is_reference(c)) launch_ref_kick_drift(c->d, c->P, c->stream);
+        else launch_prod_kick_drift(c->d, c->P, c->stream);
+        cudaEventRecord(ev[1], c->stream);
+        if(is_reference(c)) {
+            launch_ref_cells(c->d, c->P, c->stream);
+            launch_ref_neigh(c->d, c->P, c->stream);
+        } else {
+            launch_prod_build(c->d, c->P, false, c->stream);
+        }
+        cudaEventRecord(ev[2], c->stream);
+        if(is_reference(c)) launch_ref_force(c->d, c->P, c->stream);
+        else launch_prod_force(c->d, c->P, false, c->stream);
+        cudaEventRecord(ev[3], c->stream);
+        if(is_reference(c)) launch_ref_kick2(c->d, c->P, false, c->stream);
+        else launch_prod_kick2(c->d, c->P, false, c->stream);
+        cudaEventRecord(ev[4], c->stream);
+        CUDA_TRY(c, cudaEventSynchronize(ev[4]));
+        for(int q = 0; q < 4; q++) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+            acc[q] += ms;
+        }
+    }
+    for(auto& e : ev) cudaEventDestroy(e);
+    CUDA_TRY(c, cudaGetLastError());
+    StepScalars sc = read_scalars(c);
+    if(sc.overflow) {
+        restore_snapshot(c);
+        int rc = is_reference(c) ? grow_neighbors(c, sc.needed) : grow_vlist(c, sc.needed);
+        if(rc) return rc;
+        return fail(c, MTG_E_OVERFLOW, "list grew during profiling; state restored, call again");
+    }
+    for(int q = 0; q < 4; q++) phase_ms[q] = acc[q] / steps;
+    return settle_state(c);
+}
+
+int mtg_get_run_stats(mtg_ctx* c, mtg_run_stats* st) {
+    if(!c || !st) return MTG_E_INVALID;
+    *st = c->stats;
+    return MTG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,781 @@
+// Production kernels: analytic force field in FP64 or mixed precision, Verlet neighbour list with
+// a skin, fused integrator kernels, and the reduction/thermostat prologue shared by all modes.
+//
+// Layout in HBM (per atom):
+//   FP64 mode : r double[3] (master), p double[3], F double[3]
+//   mixed     : hi float4 (x,y,z hi, charge), lo float4 (x,y,z lo, type bits) -- the positions,
+//               held as FP32 hi+lo pairs and updated in FP64 -- p double[3], F int64 x3 (SoA,
+//               2^32 units per kJ/mol/A: per-pair contributions are rounded to fixed point and
+//               summed exactly, so the result does not depend on summation order), inv_m float.
+// Neighbour list: [atom][slot] uint32, atom index in the low 29 bits and the exclusion class of
+// the pair (none, 1-2, 1-3, 1-4, same molecule; FunctorCalcForce.cpp:95-157) in the top 3 bits.
+// Pairs whose class scale is exactly 0 are left out of the list.  Rebuilt when an atom has moved
+// more than skin/2 since the last build.
+//
+// The force gather keeps the reference's structure (FunctorCalcForce.cpp:159-281): each atom sums
+// its own bonded terms, its neighbours and (cutoff) Coulomb, using the full list, so no atomics are
+// needed and the energy bookkeeping (pair energy on the lower index, angle energy on the centre,
+// half the dihedral energy on each centre atom) is the reference's.
+#include <float.h>
+#include <stdint.h>
+
+#include "md_device.cuh"
+#include "mtg_internal.h"
+
+namespace mtg {
+
+int reduction_blocks(int n) {
+    int b = (n + 255) / 256;
+    return b < 1 ? 1 : b;
+}
+
+namespace {
+
+constexpr int kWarp = 32;
+
+// ---------------------------------------------------------------------------------------------
+// Prologue: sum p^2/m, then the first thermostat half-step of the coming step.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_prologue(DevSys d, Params P) {
+    __shared__ double smem[32];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if(k < P.n) {
+        const double px = d.p[3 * k], py = d.p[3 * k + 1], pz = d.p[3 * k + 2];
+        v[0] = (px * px + py * py + pz * pz) / d.m[k];
+    }
+    block_sum<1>(v, smem);
+    if(threadIdx.x == 0) d.partial[blockIdx.x * 4] = v[0];
+    if(last_block(&d.sc->done_blocks)) {
+        if(threadIdx.x == 0) {
+            double KE2 = 0.0;
+            for(int b = 0; b < (int)gridDim.x; b++) KE2 += d.partial[b * 4];
+            double c1 = 1.0;
+            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) {
+                ThermoDev t = *d.th;
+                *d.th_saved = t;
+                c1 = nh_chain_half(t, KE2, double(3 * P.n), P.kT, P.dt, P.M, P.nresp);
+                *d.th = t;
+            }
+            d.sc->S = c1;
+            d.sc->c2 = 1.0;
+            d.sc->done_blocks = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Position access
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void load_pos(const DevSys& d, int i, double& x, double& y, double& z, bool mixed) {
+    if(mixed) {
+        const float4 h = d.hi[i], l = d.lo[i];
+        x = double(h.x) + double(l.x);
+        y = double(h.y) + double(l.y);
+        z = double(h.z) + double(l.z);
+    } else {
+        x = d.r[3 * i];
+        y = d.r[3 * i + 1];
+        z = d.r[3 * i + 2];
+    }
+}
+
+__device__ __forceinline__ void store_pos(const DevSys& d, int i, double x, double y, double z, bool mixed) {
+    if(mixed) {
+        const float hx = (float)x, hy = (float)y, hz = (float)z;
+        float4 h = d.hi[i], l = d.lo[i];
+        h.x = hx; h.y = hy; h.z = hz;
+        l.x = (float)(x - double(hx));
+        l.y = (float)(y - double(hy));
+        l.z = (float)(z - double(hz));
+        d.hi[i] = h;
+        d.lo[i] = l;
+    } else {
+        d.r[3 * i] = x;
+        d.r[3 * i + 1] = y;
+        d.r[3 * i + 2] = z;
+    }
+}
+
+__device__ __forceinline__ void load_force(const DevSys& d, int i, double& fx, double& fy, double& fz, bool mixed) {
+    if(mixed) {
+        fx = double(d.Fx[i]) * (1.0 / kFixScale);
+        fy = double(d.Fy[i]) * (1.0 / kFixScale);
+        fz = double(d.Fz[i]) * (1.0 / kFixScale);
+    } else {
+        fx = d.F[3 * i];
+        fy = d.F[3 * i + 1];
+        fz = d.F[3 * i + 2];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Integration
+// ---------------------------------------------------------------------------------------------
+template<bool MIXED>
+__global__ void k_pkick_drift(DevSys d, Params P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= P.n) return;
+    const double S = d.sc->S;
+    const double dt_2 = P.dt / 2.0;
+    const double dm = P.dt / d.m[k];
+    double fx, fy, fz, x, y, z;
+    load_force(d, k, fx, fy, fz, MIXED);
+    load_pos(d, k, x, y, z, MIXED);
+    double px = d.p[3 * k] * S + fx * dt_2;
+    double py = d.p[3 * k + 1] * S + fy * dt_2;
+    double pz = d.p[3 * k + 2] * S + fz * dt_2;
+    d.p[3 * k] = px;
+    d.p[3 * k + 1] = py;
+    d.p[3 * k + 2] = pz;
+    x += px * dm;
+    y += py * dm;
+    z += pz * dm;
+    store_pos(d, k, x, y, z, MIXED);
+    // displacement since the last list build (minimum image: wrapping is not a displacement)
+    const double bx = minimg_d(x - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
+    const double by = minimg_d(y - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
+    const double bz = minimg_d(z - d.r_build[3 * k + 2], P.box[2], 1.0 / P.box[2]);
+    const double h = 0.5 * double(P.skin);
+    if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
+}
+
+__device__ __forceinline__ double wrap_coord(double x, double Lm) {
+    // pbcWrap (SimulationBox.cpp:135-166)
+    const double h = Lm / 2.0;
+    if(x >= h) x -= double((int)((x + h) / Lm)) * Lm;
+    if(x < -h) x -= double((int)((x + (-h)) / Lm)) * Lm;
+    return x;
+}
+
+template<bool MIXED, bool OUTPUT>
+__global__ void k_pkick2(DevSys d, Params P) {
+    __shared__ double smem[32 * 3];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if(k < P.n) {
+        const double dt_2 = P.dt / 2.0;
+        double f[3], r[3];
+        load_force(d, k, f[0], f[1], f[2], MIXED);
+        load_pos(d, k, r[0], r[1], r[2], MIXED);
+        double p2 = 0.0, fr = 0.0;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            if(P.clip && P.fcut > 0.0 && fabs(f[a]) > P.fcut) {
+                f[a] = ((f[a] >= 0.0) ? 1.0 : -1.0) * P.fcut;
+                if(MIXED) {
+                    long long q = (long long)(f[a] * kFixScale);
+                    if(a == 0) d.Fx[k] = q; else if(a == 1) d.Fy[k] = q; else d.Fz[k] = q;
+                } else {
+                    d.F[3 * k + a] = f[a];
+                }
+            }
+            const double p = d.p[3 * k + a] + f[a] * dt_2;
+            d.p[3 * k + a] = p;
+            r[a] = wrap_coord(r[a], P.box[a]);
+            p2 += p * p;
+            fr += f[a] * r[a];
+        }
+        store_pos(d, k, r[0], r[1], r[2], MIXED);
+        v[0] = p2 / d.m[k];
+        if(OUTPUT) {
+            v[1] = fr;
+            v[2] = d.U[k];
+        }
+    }
+    block_sum<3>(v, smem);
+    if(threadIdx.x == 0) {
+        d.partial[blockIdx.x * 4 + 0] = v[0];
+        d.partial[blockIdx.x * 4 + 1] = v[1];
+        d.partial[blockIdx.x * 4 + 2] = v[2];
+    }
+    if(last_block(&d.sc->done_blocks)) {
+        if(threadIdx.x == 0) {
+            double s[3] = {0.0, 0.0, 0.0};
+            for(int b = 0; b < (int)gridDim.x; b++)
+                for(int q = 0; q < 3; q++) s[q] += d.partial[b * 4 + q];
+            end_of_step(P, d.sc, d.th, d.th_saved, s[0], s[2], s[1], OUTPUT, d.rec);
+            d.sc->done_blocks = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Verlet list build: cell grid with edge >= rlist (or one cell for small boxes), counting sort
+// with a per-cell rank pass (deterministic order), then one warp per atom scanning the 27 cells.
+// ---------------------------------------------------------------------------------------------
+template<bool MIXED>
+__global__ void k_pcell_assign(DevSys d, Params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n || !d.sc->rebuild) return;
+    double x, y, z;
+    load_pos(d, i, x, y, z, MIXED);
+    d.r_build[3 * i] = x;
+    d.r_build[3 * i + 1] = y;
+    d.r_build[3 * i + 2] = z;
+    d.rb4[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    int ix = (int)floor((x + 0.5 * P.box[0]) * P.pnx / P.box[0]);
+    int iy = (int)floor((y + 0.5 * P.box[1]) * P.pny / P.box[1]);
+    int iz = (int)floor((z + 0.5 * P.box[2]) * P.pnz / P.box[2]);
+    ix = ix < 0 ? 0 : (ix >= P.pnx ? P.pnx - 1 : ix);
+    iy = iy < 0 ? 0 : (iy >= P.pny ? P.pny - 1 : iy);
+    iz = iz < 0 ? 0 : (iz >= P.pnz ? P.pnz - 1 : iz);
+    const int c = ix + P.pnx * (iy + P.pny * iz);
+    d.pcell_of[i] = c;
+    atomicAdd(&d.pcell_count[c], 1);
+}
+
+__global__ void k_pcell_scan(DevSys d, int ncell) {
+    if(!d.sc->rebuild) return;
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    if(threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for(int base = 0; base < ncell; base += blockDim.x) {
+        const int c = base + threadIdx.x;
+        const int v = (c < ncell) ? d.pcell_count[c] : 0;
+        int x = v;
+        for(int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if(lane >= o) x += y;
+        }
+        if(lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if(warp == 0) {
+            int t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0;
+            for(int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, t, o);
+                if(lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        const int excl = carry + (warp ? warp_tot[warp - 1] : 0) + x - v;
+        if(c < ncell) {
+            d.pcell_first[c] = excl;
+            d.pcell_cursor[c] = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+}
+
+__global__ void k_pcell_scatter(DevSys d, Params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n || !d.sc->rebuild) return;
+    const int c = d.pcell_of[i];
+    const int slot = atomicAdd(&d.pcell_cursor[c], 1);
+    d.vcount[d.pcell_first[c] + slot] = i;   // vcount doubles as scratch until the list kernel
+}
+
+__global__ void k_pcell_rank(DevSys d, int ncell) {
+    if(!d.sc->rebuild) return;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if(warp >= ncell) return;
+    const int cnt = d.pcell_count[warp], first = d.pcell_first[warp];
+    const int* tmp = d.vcount;
+    for(int a = lane; a < cnt; a += 32) {
+        const int v = tmp[first + a];
+        int rank = 0;
+        for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < v);
+        d.pcell_list[first + rank] = v;
+    }
+}
+
+// Exclusion class of the pair (k, i) from k's bonded lists and molecule indices.
+__device__ __forceinline__ int excl_class(const DevSys& d, int k, int i) {
+    for(int e = d.bptr[k]; e < d.bptr[k + 1]; e++) if(d.bj[e] == i) return 1;
+    for(int e = d.aptr[k]; e < d.aptr[k + 1]; e++) if(!d.acen[e] && d.aj[e] == i) return 2;
+    for(int e = d.dptr[k]; e < d.dptr[k + 1]; e++) if(!d.dcen[e] && d.dl[e] == i) return 3;
+    const int mi = d.mol[i], mk = d.mol[k];
+    if(mi >= 0 && mk >= 0 && mi == mk) return 4;
+    return 0;
+}
+
+template<bool MIXED>
+__global__ void k_vlist(DevSys d, Params P, float rlist) {
+    if(!d.sc->rebuild) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if(i >= P.n) return;
+    // FP32 distances: rounding (~1e-6 A) is far inside the skin margin
+    const float4 ri = d.rb4[i];
+    const float rl2 = rlist * rlist;
+    const float Lx = P.boxf[0], Ly = P.boxf[1], Lz = P.boxf[2];
+    const float iLx = 1.0f / Lx, iLy = 1.0f / Ly, iLz = 1.0f / Lz;
+    const int ci = d.pcell_of[i];
+    const int cx = ci % P.pnx, cy = (ci / P.pnx) % P.pny, cz = ci / (P.pnx * P.pny);
+    const int sx = P.pnx >= 3 ? 3 : 1, sy = P.pny >= 3 ? 3 : 1, sz = P.pnz >= 3 ? 3 : 1;
+    uint32_t* out = d.vlist + (size_t)i * d.vmax;
+    int cnt = 0;
+    for(int oz = 0; oz < sz; oz++) {
+        const int z = sz == 1 ? 0 : (cz + oz - 1 + P.pnz) % P.pnz;
+        for(int oy = 0; oy < sy; oy++) {
+            const int y = sy == 1 ? 0 : (cy + oy - 1 + P.pny) % P.pny;
+            for(int ox = 0; ox < sx; ox++) {
+                const int x = sx == 1 ? 0 : (cx + ox - 1 + P.pnx) % P.pnx;
+                const int c = x + P.pnx * (y + P.pny * z);
+                const int first = d.pcell_first[c], n = d.pcell_count[c];
+                for(int base = 0; base < n; base += 32) {
+                    bool take = false;
+                    uint32_t entry = 0;
+                    if(base + lane < n) {
+                        const int j = d.pcell_list[first + base + lane];
+                        if(j != i) {
+                            const float4 rj = d.rb4[j];
+                            const float dx = minimg_f(ri.x - rj.x, Lx, iLx);
+                            const float dy = minimg_f(ri.y - rj.y, Ly, iLy);
+                            const float dz = minimg_f(ri.z - rj.z, Lz, iLz);
+                            if(dx * dx + dy * dy + dz * dz < rl2) {
+                                const int cls = excl_class(d, i, j);
+                                if(P.scale[cls] != 0.0f) {
+                                    take = true;
+                                    entry = (uint32_t)j | ((uint32_t)cls << kClassShift);
+                                }
+                            }
+                        }
+                    }
+                    const unsigned ball = __ballot_sync(0xffffffffu, take);
+                    if(take) {
+                        const int slot = cnt + __popc(ball & ((1u << lane) - 1u));
+                        if(slot < d.vmax) out[slot] = entry;
+                    }
+                    cnt += __popc(ball);
+                }
+            }
+        }
+    }
+    if(lane == 0) {
+        d.vcount[i] = cnt;
+        if(cnt > d.vmax) {
+            d.sc->overflow = 1;
+            atomicMax(&d.sc->needed, cnt);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Force gather
+// ---------------------------------------------------------------------------------------------
+template<class R>
+struct Acc {
+    R x, y, z;
+};
+
+// Fixed-point accumulation of one FP32 contribution (mixed mode).
+__device__ __forceinline__ void addfix(long long& a, float f) { a += __float2ll_rn(f * kFixScaleF); }
+
+// -dU/dr / r (= g) and U of the analytic pair terms for type pair `pair`; table kinds interpolate.
+template<class R>
+__device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R& g, R& u, bool energy) {
+    const int cnt = d.nb_cnt[pair];
+    for(int ff = 0; ff < cnt; ff++) {
+        const int idx = pair * kMaxFF + ff;
+        const int kind = d.nb_kind[idx];
+        if(kind == MTG_NB_LJ || kind == MTG_NB_LJ1208) {
+            R a, b;
+            if(sizeof(R) == 4) { a = (R)d.nb_parf[4 * idx]; b = (R)d.nb_parf[4 * idx + 1]; }
+            else { a = (R)d.nb_par[4 * idx]; b = (R)d.nb_par[4 * idx + 1]; }
+            const R ir2 = R(1) / r2;
+            const R ir6 = ir2 * ir2 * ir2;
+            if(kind == MTG_NB_LJ) {
+                // a = 4 eps sigma^12, b = 4 eps alpha sigma^6
+                const R t12 = a * ir6 * ir6, t6 = b * ir6;
+                g += (R(12) * t12 - R(6) * t6) * ir2;
+                if(energy) u += t12 - t6;
+            } else {
+                const R ir8 = ir6 * ir2;
+                const R t12 = a * ir6 * ir6, t8 = b * ir8;
+                g += (R(12) * t12 - R(8) * t8) * ir2;
+                if(energy) u += t12 - t8;
+            }
+        } else if(kind == MTG_NB_BUCK) {
+            R A, ir, C;
+            if(sizeof(R) == 4) { A = (R)d.nb_parf[4 * idx]; ir = (R)d.nb_parf[4 * idx + 1]; C = (R)d.nb_parf[4 * idx + 2]; }
+            else { A = (R)d.nb_par[4 * idx]; ir = (R)d.nb_par[4 * idx + 1]; C = (R)d.nb_par[4 * idx + 2]; }
+            const R r = sqrt(r2);
+            const R ir2 = R(1) / r2, ir6 = ir2 * ir2 * ir2;
+            const R e = A * exp(-r * ir);
+            g += (e * ir * r - R(6) * C * ir6) * ir2;
+            if(energy) u += e - C * ir6;
+        } else {
+            // tabulated kind: linear interpolation of (x, -dU/dx, U) like the reference
+            const float* tab = d.nb_tab + (size_t)idx * kNpts * 3;
+            const float rr = (float)sqrt(r2);
+            const float delta = (tab[3 * (kNpts - 1)] - tab[0]) / float(kNpts - 1);
+            const float q = (rr - tab[0]) / delta;
+            if(q >= 0.0f && q < float(kNpts - 1)) {
+                const int t = (int)q;
+                const float* p1 = tab + 3 * t;
+                const float* p2 = p1 + 3;
+                const float a = (p1[1] - p2[1]) / (p1[0] - p2[0]);
+                g += R((a * rr + (p1[1] - a * p1[0])) / rr);
+                if(energy) {
+                    const float ae = (p1[2] - p2[2]) / (p1[0] - p2[0]);
+                    u += R(ae * rr + (p1[2] - ae * p1[0]));
+                }
+            }
+        }
+    }
+}
+
+// Relative vector r_i - r_j (minimum image) in the arithmetic precision R.
+template<bool MIXED, class R>
+__device__ __forceinline__ void rel(const DevSys& d, const Params& P, int i, int j, R& dx, R& dy, R& dz) {
+    if(MIXED) {
+        const float4 hi = d.hi[i], li = d.lo[i], hj = d.hi[j], lj = d.lo[j];
+        dx = minimg_f((hi.x - hj.x) + (li.x - lj.x), P.boxf[0], 1.0f / P.boxf[0]);
+        dy = minimg_f((hi.y - hj.y) + (li.y - lj.y), P.boxf[1], 1.0f / P.boxf[1]);
+        dz = minimg_f((hi.z - hj.z) + (li.z - lj.z), P.boxf[2], 1.0f / P.boxf[2]);
+    } else {
+        dx = (R)minimg_d(d.r[3 * i] - d.r[3 * j], P.box[0], 1.0 / P.box[0]);
+        dy = (R)minimg_d(d.r[3 * i + 1] - d.r[3 * j + 1], P.box[1], 1.0 / P.box[1]);
+        dz = (R)minimg_d(d.r[3 * i + 2] - d.r[3 * j + 2], P.box[2], 1.0 / P.box[2]);
+    }
+}
+
+template<class R>
+__device__ __forceinline__ R acos_clamped(R c) {
+    c = c > R(1) ? R(1) : (c < R(-1) ? R(-1) : c);
+    return acos(c);
+}
+
+// Bonded contribution of entry `e` (global bonded-entry index space: bonds, then angles, then
+// dihedrals of atom k) to the force on k, and to k's energy (reference bookkeeping).
+template<bool MIXED, class R>
+__device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& fx, R& fy, R& fz, double& u, bool energy) {
+    const int nb = d.bptr[k + 1] - d.bptr[k];
+    const int na = d.aptr[k + 1] - d.aptr[k];
+    if(e < nb) {
+        const int q = d.bptr[k] + e;
+        const int i = d.bj[q], t = d.bt[q];
+        R dx, dy, dz;
+        rel<MIXED, R>(d, P, k, i, dx, dy, dz);     // r_k - r_i
+        const R r = sqrt(dx * dx + dy * dy + dz * dz);
+        const int kind = d.bond_kind[t];
+        R md = 0, uu = 0;
+        const double* p = d.bond_par + 4 * t;
+        if(kind == MTG_BOND_HARM) {
+            const R dr = r - (R)p[1];
+            md = -R(2) * (R)p[0] * dr;
+            uu = (R)p[0] * dr * dr;
+        } else if(kind == MTG_BOND_MORSE) {
+            const R ex = exp(-(R)p[1] * (r - (R)p[2]));
+            md = -R(2) * (R)p[0] * (R)p[1] * ex * (R(1) - ex);
+            uu = (R)p[0] * (R(1) - ex) * (R(1) - ex);
+        } else {
+            const float* tab = d.bond_tab + (size_t)t * kNpts * 3;
+            const float rr = (float)r;
+            const float delta = (tab[3 * (kNpts - 1)] - tab[0]) / float(kNpts - 1);
+            const float qq = (rr - tab[0]) / delta;
+            if(qq >= 0.0f && qq < float(kNpts - 1)) {
+                const int ti = (int)qq;
+                const float* p1 = tab + 3 * ti;
+                const float* p2 = p1 + 3;
+                const float a = (p1[1] - p2[1]) / (p1[0] - p2[0]);
+                md = R(a * rr + (p1[1] - a * p1[0]));
+                const float ae = (p1[2] - p2[2]) / (p1[0] - p2[0]);
+                uu = R(ae * rr + (p1[2] - ae * p1[0]));
+            }
+        }
+        const R s = md / r;
+        fx += s * dx; fy += s * dy; fz += s * dz;
+        if(energy && i > k) u += (double)uu;
+        return;
+    }
+    e -= nb;
+    if(e < na) {
+        const int q = d.aptr[k] + e;
+        const int t = d.at[q];
+        int c, a1, a3;
+        if(d.acen[q]) { c = k; a1 = d.ai[q]; a3 = d.aj[q]; }
+        else { c = d.ai[q]; a1 = k; a3 = d.aj[q]; }
+        R ux, uy, uz, vx, vy, vz;
+        rel<MIXED, R>(d, P, a1, c, ux, uy, uz);
+        rel<MIXED, R>(d, P, a3, c, vx, vy, vz);
+        const R n1 = sqrt(ux * ux + uy * uy + uz * uz), n3 = sqrt(vx * vx + vy * vy + vz * vz);
+        const R cs = (ux * vx + uy * vy + uz * vz) / (n1 * n3);
+        const R th = acos_clamped(cs);
+        R sn = sqrt(R(1) - cs * cs);
+        sn = sn < R(1e-6) ? R(1e-6) : sn;
+        const double* p = d.angle_par + 4 * t;
+        R dU = 0, uu = 0;
+        if(d.angle_kind[t] == MTG_ANGLE_HARM) {
+            const R dd = th - (R)(p[1] * p[2]);
+            dU = R(2) * (R)p[0] * dd;
+            uu = (R)p[0] * dd * dd;
+        } else {
+            // tabulated: the table holds -dU/dtheta
+            const float* tab = d.angle_tab + (size_t)t * kNpts * 3;
+            const float tt = (float)th;
+            const float delta = (tab[3 * (kNpts - 1)] - tab[0]) / float(kNpts - 1);
+            const float qq = (tt - tab[0]) / delta;
+            if(qq >= 0.0f && qq < float(kNpts - 1)) {
+                const int ti = (int)qq;
+                const float* p1 = tab + 3 * ti;
+                const float* p2 = p1 + 3;
+                const float a = (p1[1] - p2[1]) / (p1[0] - p2[0]);
+                dU = -R(a * tt + (p1[1] - a * p1[0]));
+                const float ae = (p1[2] - p2[2]) / (p1[0] - p2[0]);
+                uu = R(ae * tt + (p1[2] - ae * p1[0]));
+            }
+        }
+        // d theta / d u = -(v/(n1 n3) - cs u / n1^2) / sin, similarly for v
+        const R inv = R(1) / (n1 * n3);
+        const R g1x = -(vx * inv - cs * ux / (n1 * n1)) / sn, g1y = -(vy * inv - cs * uy / (n1 * n1)) / sn,
+                g1z = -(vz * inv - cs * uz / (n1 * n1)) / sn;
+        if(d.acen[q]) {
+            const R g3x = -(ux * inv - cs * vx / (n3 * n3)) / sn, g3y = -(uy * inv - cs * vy / (n3 * n3)) / sn,
+                    g3z = -(uz * inv - cs * vz / (n3 * n3)) / sn;
+            fx += dU * (g1x + g3x); fy += dU * (g1y + g3y); fz += dU * (g1z + g3z);
+            if(energy) u += (double)uu;
+        } else {
+            fx -= dU * g1x; fy -= dU * g1y; fz -= dU * g1z;
+        }
+        return;
+    }
+    e -= na;
+    {
+        const int q = d.dptr[k] + e;
+        const int t = d.dt[q];
+        int a, b, c, dd;
+        if(d.dcen[q]) { a = d.di[q]; b = k; c = d.dj[q]; dd = d.dl[q]; }
+        else { a = k; b = d.di[q]; c = d.dj[q]; dd = d.dl[q]; }
+        R b1x, b1y, b1z, b2x, b2y, b2z, b3x, b3y, b3z;
+        rel<MIXED, R>(d, P, b, a, b1x, b1y, b1z);
+        rel<MIXED, R>(d, P, c, b, b2x, b2y, b2z);
+        rel<MIXED, R>(d, P, dd, c, b3x, b3y, b3z);
+        const R mx = b1y * b2z - b1z * b2y, my = b1z * b2x - b1x * b2z, mz = b1x * b2y - b1y * b2x;
+        const R nx = b2y * b3z - b2z * b3y, ny = b2z * b3x - b2x * b3z, nz = b2x * b3y - b2y * b3x;
+        const R m2 = mx * mx + my * my + mz * mz, n2 = nx * nx + ny * ny + nz * nz;
+        const R lb2 = sqrt(b2x * b2x + b2y * b2y + b2z * b2z);
+        if(!(m2 > R(1e-20) && n2 > R(1e-20))) return;
+        const R cs = (mx * nx + my * ny + mz * nz) / sqrt(m2 * n2);
+        const R phi = acos_clamped(cs);
+        const double* p = d.dih_par + 4 * t;
+        const int kind = d.dih_kind[t];
+        R dV = 0, V = 0;
+        if(kind == MTG_DIH_HARM) {
+            const R K = (R)p[0];
+            const int D = (int)p[1], N = (int)p[2];
+            dV = -K * R(D * N) * sin(R(N) * phi);
+            V = K * (R(1) + R(D) * cos(R(N) * phi));
+        } else if(kind == MTG_DIH_FOURIER4T) {
+            dV = R(-0.5) * (R)p[0] * sin(phi) + (R)p[1] * sin(R(2) * phi) + R(-1.5) * (R)p[2] * sin(R(3) * phi) +
+                 R(2) * (R)p[3] * sin(R(4) * phi);
+            V = R(0.5) * ((R)p[0] * (R(1) + cos(phi)) + (R)p[1] * (R(1) - cos(R(2) * phi)) +
+                          (R)p[2] * (R(1) + cos(R(3) * phi)) + (R)p[3] * (R(1) - cos(R(4) * phi)));
+        }
+        // gradient of the signed dihedral; |psi| = phi, sign = sign(b1 . n)
+        const R sgn = (b1x * nx + b1y * ny + b1z * nz) >= R(0) ? R(1) : R(-1);
+        const R ga = -lb2 / m2, gd = lb2 / n2;
+        R gx, gy, gz;
+        if(d.dcen[q]) {
+            const R f1 = (b1x * b2x + b1y * b2y + b1z * b2z) / (lb2 * lb2);
+            const R f3 = (b3x * b2x + b3y * b2y + b3z * b2z) / (lb2 * lb2);
+            gx = -(R(1) + f1) * ga * mx + f3 * gd * nx;
+            gy = -(R(1) + f1) * ga * my + f3 * gd * ny;
+            gz = -(R(1) + f1) * ga * mz + f3 * gd * nz;
+            if(energy) u += 0.5 * (double)V;
+        } else {
+            gx = ga * mx; gy = ga * my; gz = ga * mz;
+        }
+        fx -= dV * sgn * gx; fy -= dV * sgn * gy; fz -= dV * sgn * gz;
+    }
+}
+
+template<bool MIXED, bool ENERGY>
+__global__ void __launch_bounds__(256) k_pforce(DevSys d, Params P) {
+    using R = typename std::conditional<MIXED, float, double>::type;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if(i >= P.n) return;
+    const bool mob = d.mobile[i] != 0;
+    long long ax = 0, ay = 0, az = 0;       // mixed: fixed point
+    double bx = 0, by = 0, bz = 0;          // fp64
+    double uacc = 0.0;
+    if(mob) {
+        const R rc2 = (R)P.rc * (R)P.rc;
+        const R rq2 = (R)P.rcoul * (R)P.rcoul;
+        const int T = P.T;
+        const int ti = MIXED ? __float_as_int(d.lo[i].w) : d.type[i];
+        const R qi = MIXED ? (R)d.hi[i].w : (R)d.qd[i];
+        const R kq = MIXED ? (R)kCoulombKf : (R)1389.32;
+        const int cnt = min(d.vcount[i], d.vmax);   // an overflowed build is redone; stay in the row
+        const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
+        for(int e = lane; e < cnt; e += kWarp) {
+            const uint32_t ent = lst[e];
+            const int j = (int)(ent & kIdxMask);
+            const int cls = (int)(ent >> kClassShift);
+            R dx, dy, dz;
+            rel<MIXED, R>(d, P, i, j, dx, dy, dz);
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            R g = 0, u = 0;
+            if(r2 < rc2 && r2 >= R(1e-6)) {
+                const int tj = MIXED ? __float_as_int(d.lo[j].w) : d.type[j];
+                pair_terms<R>(d, ti * T + tj, r2, g, u, ENERGY);
+            }
+            if(P.coulomb == MTG_COULOMB_CUTOFF && r2 < rq2) {
+                const R qj = MIXED ? (R)d.hi[j].w : (R)d.qd[j];
+                const R qq = kq * qi * qj;
+                if(qq != R(0)) {
+                    const R ir = R(1) / sqrt(r2);
+                    g += qq * ir * ir * ir;
+                    if(ENERGY) u += qq * ir;
+                }
+            }
+            if(cls) {
+                const R sc = (R)P.scale[cls];
+                g *= sc;
+                u *= sc;
+            }
+            if(MIXED) {
+                addfix(ax, (float)(g * dx));
+                addfix(ay, (float)(g * dy));
+                addfix(az, (float)(g * dz));
+            } else {
+                bx += (double)(g * dx);
+                by += (double)(g * dy);
+                bz += (double)(g * dz);
+            }
+            if(ENERGY && j > i) uacc += (double)u;
+        }
+        // bonded terms of atom i, one entry per lane
+        const int nbd = (d.bptr[i + 1] - d.bptr[i]) + (d.aptr[i + 1] - d.aptr[i]) + (d.dptr[i + 1] - d.dptr[i]);
+        for(int e = lane; e < nbd; e += kWarp) {
+            R fx = 0, fy = 0, fz = 0;
+            bonded_entry<MIXED, R>(d, P, i, e, fx, fy, fz, uacc, ENERGY);
+            if(MIXED) {
+                addfix(ax, (float)fx);
+                addfix(ay, (float)fy);
+                addfix(az, (float)fz);
+            } else {
+                bx += (double)fx;
+                by += (double)fy;
+                bz += (double)fz;
+            }
+        }
+    }
+    // warp reduction (integer: exact; FP64: fixed tree)
+    for(int o = 16; o > 0; o >>= 1) {
+        if(MIXED) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+            az += __shfl_xor_sync(0xffffffffu, az, o);
+        } else {
+            bx += __shfl_xor_sync(0xffffffffu, bx, o);
+            by += __shfl_xor_sync(0xffffffffu, by, o);
+            bz += __shfl_xor_sync(0xffffffffu, bz, o);
+        }
+        if(ENERGY) uacc += __shfl_xor_sync(0xffffffffu, uacc, o);
+    }
+    if(lane == 0) {
+        if(MIXED) {
+            d.Fx[i] = ax;
+            d.Fy[i] = ay;
+            d.Fz[i] = az;
+        } else {
+            d.F[3 * i] = bx;
+            d.F[3 * i + 1] = by;
+            d.F[3 * i + 2] = bz;
+        }
+        if(ENERGY) d.U[i] = uacc;
+    }
+}
+
+// Conversions between the mixed-mode position/force formats and the FP64 host-facing arrays.
+__global__ void k_sync_pos(DevSys d, Params P, int to_master) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n) return;
+    if(to_master) {
+        // d.r -> hi/lo (set_state)
+        store_pos(d, i, d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2], true);
+        float4 h = d.hi[i], l = d.lo[i];
+        h.w = d.qf[i];
+        l.w = __int_as_float(d.type[i]);
+        d.hi[i] = h;
+        d.lo[i] = l;
+    } else {
+        double x, y, z;
+        load_pos(d, i, x, y, z, true);
+        d.r[3 * i] = x;
+        d.r[3 * i + 1] = y;
+        d.r[3 * i + 2] = z;
+    }
+}
+
+__global__ void k_forces_to_double(DevSys d, Params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n) return;
+    d.F[3 * i] = double(d.Fx[i]) * (1.0 / kFixScale);
+    d.F[3 * i + 1] = double(d.Fy[i]) * (1.0 / kFixScale);
+    d.F[3 * i + 2] = double(d.Fz[i]) * (1.0 / kFixScale);
+}
+
+__global__ void k_clear_rebuild(DevSys d) {
+    if(threadIdx.x == 0 && blockIdx.x == 0 && d.sc->rebuild) {
+        d.sc->rebuild = 0;
+        d.sc->builds += 1;
+    }
+}
+
+}  // namespace
+
+static inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
+    k_prologue<<<reduction_blocks(P.n), 256, 0, s>>>(d, P);
+}
+
+void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s) {
+    if(P.precision == MTG_PREC_MIXED) k_pkick_drift<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    else k_pkick_drift<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+}
+
+void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
+    const int ncell = P.pnx * P.pny * P.pnz;
+    if(force) cudaMemsetAsync(&d.sc->rebuild, 0xff, sizeof(int32_t), s);
+    // counts are cleared unconditionally; the kernels below return early when no rebuild is due
+    cudaMemsetAsync(d.pcell_count, 0, sizeof(int) * ncell, s);
+    if(P.precision == MTG_PREC_MIXED) k_pcell_assign<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    k_pcell_scan<<<1, 1024, 0, s>>>(d, ncell);
+    k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell);
+    const float rlist = fmaxf(P.rc, P.coulomb == MTG_COULOMB_CUTOFF ? P.rcoul : 0.0f) + P.skin;
+    if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, rlist);
+    else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, rlist);
+    k_clear_rebuild<<<1, 32, 0, s>>>(d);
+}
+
+void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s) {
+    const int nb = nblk(P.n * 32, 256);
+    if(P.precision == MTG_PREC_MIXED) {
+        if(energy) k_pforce<true, true><<<nb, 256, 0, s>>>(d, P);
+        else k_pforce<true, false><<<nb, 256, 0, s>>>(d, P);
+    } else {
+        if(energy) k_pforce<false, true><<<nb, 256, 0, s>>>(d, P);
+        else k_pforce<false, false><<<nb, 256, 0, s>>>(d, P);
+    }
+}
+
+void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
+    const int nb = reduction_blocks(P.n);
+    if(P.precision == MTG_PREC_MIXED) {
+        if(output) k_pkick2<true, true><<<nb, 256, 0, s>>>(d, P);
+        else k_pkick2<true, false><<<nb, 256, 0, s>>>(d, P);
+    } else {
+        if(output) k_pkick2<false, true><<<nb, 256, 0, s>>>(d, P);
+        else k_pkick2<false, false><<<nb, 256, 0, s>>>(d, P);
+    }
+}
+
+void launch_prod_sync_positions(const DevSys& d, const Params& P, bool to_master, cudaStream_t s) {
+    k_sync_pos<<<nblk(P.n, 256), 256, 0, s>>>(d, P, to_master ? 1 : 0);
+}
+
+void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s) {
+    k_forces_to_double<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+}
+
+}  // namespace mtg

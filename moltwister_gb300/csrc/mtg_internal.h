@@ -1,0 +1,164 @@
+// Internal declarations shared by the translation units of libmtgpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mtgpu.h"
+
+namespace mtg {
+
+constexpr int kNpts = MTG_NPTS;
+constexpr int kMaxFF = MTG_MAX_FF_PER_PAIR;
+constexpr int kMaxChain = MTG_MAX_NH_CHAIN;
+constexpr float kCoulombKf = 1389.32f;     // Integrators/Constants.h:40 (float literal)
+constexpr double kConvT = 120.272;         // Constants.h Conv_T
+constexpr double kConvt = 1.0E2;           // Constants.h Conv_t
+constexpr double kConvPress = 16388.2461;  // Constants.h Conv_press
+// Fixed-point scale of the mixed-precision force accumulators: 2^32 units per kJ/(mol A).
+constexpr double kFixScale = 4294967296.0;
+constexpr float kFixScaleF = 4294967296.0f;
+// Neighbour-list entry: atom index in the low 29 bits, exclusion class in the top 3 bits.
+constexpr uint32_t kIdxMask = 0x1FFFFFFFu;
+constexpr int kClassShift = 29;
+// Exclusion classes (FunctorCalcForce.cpp:95-157): 0 none, 1 1-2, 2 1-3, 3 1-4, 4 same molecule.
+
+// Device-side thermostat state.  `th` is the live chain; `saved` is the chain right after the
+// second half-step of the last completed step (what the reference holds between steps).
+struct ThermoDev {
+    double eta[kMaxChain];
+    double peta[kMaxChain];
+    double Q[kMaxChain];
+};
+
+// Scalars the step kernels exchange through device memory.
+struct StepScalars {
+    double S;             // pending momentum scale: c2(previous step) * c1(this step)
+    double c2;            // scale of the last second half-step (applied on output / at run end)
+    double KE2;           // sum p^2/m after the last second half-step (p scaled by c2)
+    double U;             // total potential energy (output steps)
+    double virial;        // sum F.r with wrapped r (output steps)
+    int32_t rebuild;      // production list: 1 = rebuild before the next force evaluation
+    int32_t overflow;     // list capacity exceeded (entries needed in `needed`)
+    int32_t needed;
+    int32_t nonfinite;
+    uint32_t done_blocks; // last-block counter of the reduction kernels
+    int32_t builds;       // neighbour-list rebuilds performed
+    double max_disp2;
+};
+
+struct Params {
+    int n, T;
+    double box[3];
+    float boxf[3];
+    int ensemble, precision, coulomb, clip;
+    double dt;            // reduced time step
+    double kT;            // reduced temperature
+    double tau;
+    int M, nresp;
+    double fcut;
+    float rc, shell;
+    float rcoul;          // Coulomb cutoff (production, cutoff mode)
+    float skin;
+    float scale[5];       // by exclusion class: 1, s12, s13, s14, s1N
+    float scale12, scale13, scale14, scale1N;
+    int nx, ny, nz;       // reference cell counts (from the input box, MDFFMatrices.cpp:56-58)
+    int pnx, pny, pnz;    // production cell counts (cell edge >= rlist), 1 = all-pairs build
+};
+
+// Everything a force/integration kernel reads, as raw device pointers.
+struct DevSys {
+    int n, T;
+    // reference & fp64 masters
+    double* r;            // [3n]
+    double* p;            // [3n]
+    double* F;            // [3n]  FP64 forces (reference, fp64)
+    double* U;            // [n]   per-atom energies
+    double* m;            // [n]
+    double* qd;           // [n]   charges (double)
+    float* qf;            // [n]   charges as float (CMDFFMatrices::CAtom::q_)
+    int* type;
+    int* mol;
+    int* mobile;
+    // tables (x, -dU/dx, U); nb layout [((row*T + col)*5 + ff)*1000 + pt]
+    const float* nb_tab;
+    const int* nb_cnt;
+    const float* bond_tab;
+    const float* angle_tab;
+    const float* dih_tab;
+    const int* nb_kind;
+    const double* nb_par;     // [pair*5+ff][4]
+    const float* nb_parf;     // [pair*5+ff][4] (FP32 copy)
+    const int* bond_kind;
+    const double* bond_par;
+    const int* angle_kind;
+    const double* angle_par;
+    const int* dih_kind;
+    const double* dih_par;
+    // per-atom bonded lists (CSR)
+    const int *bptr, *bj, *bt;
+    const int *aptr, *ai, *aj, *at, *acen;
+    const int *dptr, *di, *dj, *dl, *dt, *dcen;
+    // reference cell & neighbour lists
+    int* atom_cell;       // [3n]
+    int* cell_first;      // [ncell]
+    int* cell_count;      // [ncell]
+    int* cell_cursor;     // [ncell]
+    int* cell_list;       // [n]
+    int* nbr_count;       // [n]
+    int* nbr_list;        // [n * nbr_max]
+    int nbr_max;
+    // production (Verlet) list
+    int* pcell_of;        // [n] production cell of each atom
+    int* pcell_first;     // [pncell]
+    int* pcell_count;     // [pncell]
+    int* pcell_cursor;    // [pncell]
+    int* pcell_list;      // [n]
+    uint32_t* vlist;      // [n * vmax]
+    int* vcount;          // [n]
+    int vmax;
+    double* r_build;      // [3n] positions at the last build (displacement check)
+    float4* rb4;          // [n]  the same in FP32 (list distances)
+    // mixed
+    float4* hi;           // [n] x,y,z hi, charge
+    float4* lo;           // [n] x,y,z lo, type bits
+    long long* Fx;        // [n] fixed-point forces (SoA)
+    long long* Fy;
+    long long* Fz;
+    float* inv_m;         // [n]
+    // reductions
+    double* partial;      // [nblocks * 4]
+    StepScalars* sc;
+    ThermoDev* th;
+    ThermoDev* th_saved;
+    double* rec;          // output record ring [8]
+};
+
+// Kernel launchers (defined in ref_kernels.cu and md_kernels.cu).
+// Reference mode
+void launch_ref_cells(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_ref_neigh(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_ref_kick_drift(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_ref_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s);
+// Shared
+void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s);
+// Production modes
+void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s);
+void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s);
+void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s);
+void launch_prod_sync_positions(const DevSys& d, const Params& P, bool to_master, cudaStream_t s);
+void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s);
+int reduction_blocks(int n);
+
+// Host-side table generation (tables.cpp): out[npts*3] = (x, -dU/dx, U)
+int profile_nonbonded(int kind, const double* p, float r0, float r1, int npts, float* out);
+int profile_bond(int kind, const double* p, float r0, float r1, int npts, float* out);
+int profile_angle(int kind, const double* p, float t0, float t1, int npts, float* out);
+int profile_dihedral(int kind, const double* p, float t0, float t1, int npts, float* out);
+
+}  // namespace mtg

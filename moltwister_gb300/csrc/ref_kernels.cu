@@ -1,0 +1,578 @@
+// Reference-mode kernels: MolTwister's MD arithmetic reproduced on the GPU.
+//
+// These kernels replace the Thrust functors and serial kernels of the reference
+// (FunctorGenCellList.cpp:49-142, FunctorGenNeighList.cpp:72-191, FunctorCalcForce.cpp:95-709) and the
+// host loops of VelVerlet.cpp:74-122 / SimulationBox.cpp:135-166 in the parity mode.  The cell
+// assignment, neighbour order and per-atom summation order are the reference's, and this file is
+// compiled with -fmad=false so no multiply-add is fused: cell lists and neighbour lists are
+// bit-identical to the reference and per-atom forces agree to the last few ulps (libm acos may
+// differ in the last bit).
+//
+// Parallel structure: one thread per atom for the gather kernels (the reference's per-atom order
+// is sequential), a counting sort with a per-cell rank pass for the cell list (the reference's
+// serial kernelAssembleList order is ascending atom index within each cell), and grid-wide
+// deterministic reductions for the kinetic energy with the thermostat in the last block.
+#include <float.h>
+#include <stdint.h>
+
+#include "md_device.cuh"
+#include "mtg_internal.h"
+
+namespace mtg {
+namespace {
+
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ D3 d3(double x, double y, double z) { return {x, y, z}; }
+__device__ __forceinline__ D3 sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 scl(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ double dotp(D3 a, D3 b) { return (a.x * b.x) + (a.y * b.y) + (a.z * b.z); }
+__device__ __forceinline__ double nrm(D3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ D3 crs(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ D3 load3(const double* r, int i) { return {r[3 * i], r[3 * i + 1], r[3 * i + 2]}; }
+
+// C3DVector::moveToSameSideOfPBCAsThis (Utilities/3DVector.cpp:133-165)
+__device__ __forceinline__ void same_side(D3 c, D3& v, const double* w) {
+    double dX = c.x - v.x, dY = c.y - v.y, dZ = c.z - v.z;
+    dX = (dX < 0.0) ? -dX : dX;
+    dY = (dY < 0.0) ? -dY : dY;
+    dZ = (dZ < 0.0) ? -dZ : dZ;
+    if(dX > (w[0] / 2.0)) { if(c.x > v.x) v.x += w[0]; else v.x -= w[0]; }
+    if(dY > (w[1] / 2.0)) { if(c.y > v.y) v.y += w[1]; else v.y -= w[1]; }
+    if(dZ > (w[2] / 2.0)) { if(c.z > v.z) v.z += w[2]; else v.z -= w[2]; }
+}
+
+__device__ D3 coeff12(D3 r1, D3 r2) {
+    D3 r12 = sub(r2, r1);
+    double R = nrm(r12);
+    return scl(r12, (R == 0.0) ? 1.0 / 1E-10 : 1.0 / R);
+}
+
+__device__ D3 coeff_ang13(D3 r1, D3 r2, D3 r3) {
+    D3 r12 = sub(r1, r2);
+    double R = nrm(r12);
+    D3 K = scl(r12, (R == 0.0) ? 1.0 / 1E-10 : 1.0 / R);
+    D3 r32 = sub(r3, r2);
+    double A = K.x * r32.x + K.y * r32.y + K.z * r32.z;
+    double B = r32.x * r32.x + r32.y * r32.y + r32.z * r32.z;
+    double sB = sqrt(B);
+    double sB3 = (B == 0.0) ? sqrt(1E-30) : sB * sB * sB;
+    double gx = (K.x * B - r32.x * A) / sB3, gy = (K.y * B - r32.y * A) / sB3, gz = (K.z * B - r32.z * A) / sB3;
+    double W = (sB == 0.0) ? A / 10E-3 : A / sB;
+    double den = sqrt(1.0 - W * W);
+    double f = (den == 0.0) ? -1.0 / 1E-10 : -1.0 / den;
+    return {f * gx, f * gy, f * gz};
+}
+
+__device__ D3 coeff_ang2(D3 r1, D3 r2, D3 r3) {
+    D3 r12 = sub(r1, r2), r32 = sub(r3, r2);
+    double A = r12.x * r12.x + r12.y * r12.y + r12.z * r12.z;
+    double B = r32.x * r32.x + r32.y * r32.y + r32.z * r32.z;
+    double C = r12.x * r32.x + r12.y * r32.y + r12.z * r32.z;
+    double AB = A * B;
+    double sAB = sqrt(AB);
+    double sAB3 = (AB == 0.0) ? sqrt(1E-30) : sAB * sAB * sAB;
+    double gx = ((2.0 * r2.x - r1.x - r3.x) * AB + (r32.x * A + r12.x * B) * C) / sAB3;
+    double gy = ((2.0 * r2.y - r1.y - r3.y) * AB + (r32.y * A + r12.y * B) * C) / sAB3;
+    double gz = ((2.0 * r2.z - r1.z - r3.z) * AB + (r32.z * A + r12.z * B) * C) / sAB3;
+    double W = (sAB == 0.0) ? A / 10E-3 : C / sAB;
+    double den = sqrt(1.0 - W * W);
+    double f = (den == 0.0) ? -1.0 / 1E-10 : -1.0 / den;
+    return {f * gx, f * gy, f * gz};
+}
+
+__device__ D3 coeff_dih14(D3 r1, D3 r2, D3 r3, D3 r4) {
+    D3 r21 = sub(r1, r2), r23 = sub(r3, r2);
+    D3 r32 = scl(r23, -1.0);
+    D3 r34 = sub(r4, r3);
+    D3 n1 = crs(r23, r21);
+    double n1n = nrm(n1);
+    D3 K = scl(n1, (n1n == 0.0) ? 1.0 / 1E-10 : 1.0 / n1n);
+    double a = r32.y * r34.z - r32.z * r34.y;
+    double b = r32.z * r34.x - r32.x * r34.z;
+    double c = r32.x * r34.y - r32.y * r34.x;
+    double A = K.x * a + K.y * b + K.z * c;
+    double B = a * a + b * b + c * c;
+    double sBi = (B == 0.0) ? 1.0 / 1E-20 : 1.0 / sqrt(B);
+    double sBi3 = sBi * sBi * sBi;
+    double W = A * sBi;
+    double gx = ((K.y * r32.z - K.z * r32.y) * B - (r32.z * (r32.z * r34.x - r32.x * r34.z) - r32.y * (r32.x * r34.y - r32.y * r34.x)) * A) * sBi3;
+    double gy = ((K.z * r32.x - K.x * r32.z) * B - (r32.x * (r32.x * r34.y - r32.y * r34.x) - r32.z * (r32.y * r34.z - r32.z * r34.y)) * A) * sBi3;
+    double gz = ((K.x * r32.y - K.y * r32.x) * B - (r32.y * (r32.y * r34.z - r32.z * r34.y) - r32.x * (r32.z * r34.x - r32.x * r34.z)) * A) * sBi3;
+    double den = sqrt(1.0 - W * W);
+    double f = (den == 0.0) ? 1.0 / 1E-10 : 1.0 / den;
+    return scl(d3(f * gx, f * gy, f * gz), -1.0);
+}
+
+__device__ D3 coeff_dih23(D3 r1, D3 r2, D3 r3, D3 r4) {
+    D3 r21 = sub(r1, r2), r23 = sub(r3, r2);
+    D3 r32 = scl(r23, -1.0);
+    D3 r34 = sub(r4, r3);
+    double K1 = r32.z * r34.x - r32.x * r34.z, K2 = r34.z - r32.z, K3 = r23.z * r21.x - r23.x * r21.z;
+    double K4 = r32.x * r34.y - r32.y * r34.x, K5 = r32.y - r34.y, K6 = r23.x * r21.y - r23.y * r21.x;
+    double L1 = r32.y * r34.z - r32.z * r34.y, L2 = -K2, L3 = r23.y * r21.z - r23.z * r21.y;
+    double L4 = K4, L5 = r34.x - r32.x, L6 = K6;
+    double M1 = L1, M2 = -K5, M3 = L3, M4 = K1, M5 = -L5, M6 = K3;
+    double A = L3 * L3 + K3 * K3 + K6 * K6;
+    double B = L1 * L1 + K1 * K1 + K4 * K4;
+    double C = L3 * L1 + K3 * K1 + K6 * K4;
+    double AB = A * B;
+    double sABi = (AB == 0.0) ? 1.0 / 1E-20 : 1.0 / sqrt(AB);
+    double sABi3 = sABi * sABi * sABi;
+    double W = C * sABi;
+    double dCx = K2 * K3 + r21.y * K4 + K5 * K6 - r21.z * K1;
+    double dCy = L2 * L3 - r21.x * L4 + L5 * L6 + r21.z * L1;
+    double dCz = M2 * M3 + r21.x * M4 + M5 * M6 - r21.y * M1;
+    double gx = (dCx * AB - C * ((r21.y * K6 - r21.z * K3) * B + (K1 * K2 + K4 * K5) * A)) * sABi3;
+    double gy = (dCy * AB - C * ((r21.z * L3 - r21.x * L6) * B + (L1 * L2 + L4 * L5) * A)) * sABi3;
+    double gz = (dCz * AB - C * ((r21.x * M6 - r21.y * M3) * B + (M1 * M2 + M4 * M5) * A)) * sABi3;
+    double den = sqrt(1.0 - W * W);
+    double f = (den == 0.0) ? 1.0 / 1E-10 : 1.0 / den;
+    return scl(d3(f * gx, f * gy, f * gz), -1.0);
+}
+
+// (int) of a float with x86-64 semantics (NaN / out of range -> INT_MIN), so an invalid table
+// index is rejected the way the reference's x86-64 build rejects it.
+__device__ __forceinline__ int f2i_x86(float x) {
+    if(!(x > -2147483648.0f && x < 2147483648.0f)) return INT32_MIN;
+    return (int)x;
+}
+
+// calcIndexOfLowerPointOfInterpolationLine (FunctorCalcForce.cpp:426-430)
+__device__ __forceinline__ int tindex(float x, const float* tab) {
+    float delta = (tab[3 * (kNpts - 1)] - tab[0]) / float(kNpts - 1);
+    return f2i_x86((x - tab[0]) / delta);
+}
+
+// interpolateLinear (FunctorCalcForce.cpp:457-465)
+__device__ __forceinline__ float interp(float r, float x1, float y1, float x2, float y2) {
+    float denom = x1 - x2;
+    if(denom == 0.0f) denom = 3.0f * FLT_MIN;
+    float a = (y1 - y2) / denom;
+    float b = y1 - a * x1;
+    return (a * r + b);
+}
+
+__device__ float calc_angle(D3 rk, D3 ri, D3 rj) {
+    D3 rik = sub(rk, ri), rij = sub(rj, ri);
+    float dp = (float)dotp(rik, rij);
+    float RR = (float)nrm(rik) * (float)nrm(rij);
+    float c = (RR != 0.0f) ? dp / RR : 1.0f;
+    return (float)acos((double)c);
+}
+
+__device__ float calc_dihedral(D3 rk, D3 ri, D3 rj, D3 rl) {
+    D3 rik = sub(rk, ri), rij = sub(rj, ri), rjl = sub(rl, rj);
+    D3 n1 = crs(rik, rij), n2 = crs(rij, rjl);
+    float dp = (float)dotp(n1, n2);
+    float nn = (float)nrm(n1) * (float)nrm(n2);
+    float c = (nn != 0.0f) ? dp / nn : 1.0f;
+    if(c < -1.0f) c = -1.0f;
+    if(c > 1.0f) c = 1.0f;
+    return (float)acos((double)c);
+}
+
+// scaleForcesAndPotentials (FunctorCalcForce.cpp:95-157) as a (applies, factor) pair.
+__device__ __forceinline__ bool exclusion(const DevSys& d, const Params& P, int k, int i, float& f) {
+    for(int e = d.bptr[k]; e < d.bptr[k + 1]; e++) if(d.bj[e] == i) { f = P.scale12; return true; }
+    for(int e = d.aptr[k]; e < d.aptr[k + 1]; e++) if(!d.acen[e] && d.aj[e] == i) { f = P.scale13; return true; }
+    for(int e = d.dptr[k]; e < d.dptr[k + 1]; e++) if(!d.dcen[e] && d.dl[e] == i) { f = P.scale14; return true; }
+    const int mi = d.mol[i], mk = d.mol[k];
+    if(mi >= 0 && mk >= 0 && mi == mk) { f = P.scale1N; return true; }
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Cell list (CFunctorGenCellList::operator() and kernelAssembleList)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_cell_assign(DevSys d, Params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n) return;
+    const float wx = P.boxf[0], wy = P.boxf[1], wz = P.boxf[2];
+    const float lx = -wx / 2.0f, ly = -wy / 2.0f, lz = -wz / 2.0f;
+    const int Nx = P.nx, Ny = P.ny, Nz = P.nz;
+    int ix = (int)floor((d.r[3 * i] - double(lx)) * double(Nx) / double(wx));
+    int iy = (int)floor((d.r[3 * i + 1] - double(ly)) * double(Ny) / double(wy));
+    int iz = (int)floor((d.r[3 * i + 2] - double(lz)) * double(Nz) / double(wz));
+    ix = (ix < 0) ? 0 : ((ix >= Nx) ? Nx - 1 : ix);
+    iy = (iy < 0) ? 0 : ((iy >= Ny) ? Ny - 1 : iy);
+    iz = (iz < 0) ? 0 : ((iz >= Nz) ? Nz - 1 : iz);
+    d.atom_cell[3 * i] = ix;
+    d.atom_cell[3 * i + 1] = iy;
+    d.atom_cell[3 * i + 2] = iz;
+    atomicAdd(&d.cell_count[ix + Nx * (iy + iz * Ny)], 1);
+}
+
+// Exclusive scan of the cell counts in one block; empty cells get first = -1 (CListPointer default).
+__global__ void k_cell_scan(DevSys d, int ncell) {
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    if(threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for(int base = 0; base < ncell; base += blockDim.x) {
+        const int c = base + threadIdx.x;
+        const int v = (c < ncell) ? d.cell_count[c] : 0;
+        int x = v;
+        for(int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if(lane >= o) x += y;
+        }
+        if(lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if(warp == 0) {
+            int t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0;
+            for(int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, t, o);
+                if(lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        const int excl = carry + (warp ? warp_tot[warp - 1] : 0) + x - v;
+        if(c < ncell) {
+            d.cell_first[c] = (v != 0) ? excl : -1;
+            d.cell_cursor[c] = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+}
+
+__global__ void k_cell_scatter(DevSys d, Params P, int* tmp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n) return;
+    const int c = d.atom_cell[3 * i] + P.nx * (d.atom_cell[3 * i + 1] + d.atom_cell[3 * i + 2] * P.ny);
+    const int slot = atomicAdd(&d.cell_cursor[c], 1);
+    tmp[d.cell_first[c] + slot] = i;
+}
+
+// One warp per cell: place each atom at its rank (number of smaller indices in the cell), which
+// is the reference's serial order (ascending atom index within a cell).
+__global__ void k_cell_rank(DevSys d, int ncell, const int* tmp) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if(warp >= ncell) return;
+    const int cnt = d.cell_count[warp], first = d.cell_first[warp];
+    for(int a = lane; a < cnt; a += 32) {
+        const int v = tmp[first + a];
+        int rank = 0;
+        for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < v);
+        d.cell_list[first + rank] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Full neighbour list in the reference order (CFunctorGenNeighList::operator())
+// ---------------------------------------------------------------------------------------------
+__global__ void k_neigh(DevSys d, Params P, float rc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= P.n) return;
+    float rc2f = rc;
+    rc2f *= rc2f;
+    const double rc2 = (double)rc2f;
+    const float lx = -P.boxf[0] / 2.0f, ly = -P.boxf[1] / 2.0f, lz = -P.boxf[2] / 2.0f;
+    const double w[3] = {double(lx + P.boxf[0]) - double(lx), double(ly + P.boxf[1]) - double(ly),
+                         double(lz + P.boxf[2]) - double(lz)};
+    const int Nx = P.nx, Ny = P.ny, Nz = P.nz;
+    const double x0 = d.r[3 * k], y0 = d.r[3 * k + 1], z0 = d.r[3 * k + 2];
+    const int cx = d.atom_cell[3 * k], cy = d.atom_cell[3 * k + 1], cz = d.atom_cell[3 * k + 2];
+    int c = 0;
+    int* out = d.nbr_list + (size_t)k * d.nbr_max;
+    for(int ix = cx - 1; ix <= cx + 1; ix++) {
+        const int Ix = (ix >= 0) ? ((ix < Nx) ? ix : 0) : Nx - 1;
+        for(int iy = cy - 1; iy <= cy + 1; iy++) {
+            const int Iy = (iy >= 0) ? ((iy < Ny) ? iy : 0) : Ny - 1;
+            for(int iz = cz - 1; iz <= cz + 1; iz++) {
+                const int Iz = (iz >= 0) ? ((iz < Nz) ? iz : 0) : Nz - 1;
+                const int cell = Ix + Nx * (Iy + Iz * Ny);
+                const int cnt = d.cell_count[cell], first = d.cell_first[cell];
+                for(int e = 0; e < cnt; e++) {
+                    const int j = d.cell_list[first + e];
+                    double dX = x0 - d.r[3 * j], dY = y0 - d.r[3 * j + 1], dZ = z0 - d.r[3 * j + 2];
+                    dX = (dX < 0.0) ? -dX : dX;
+                    dY = (dY < 0.0) ? -dY : dY;
+                    dZ = (dZ < 0.0) ? -dZ : dZ;
+                    if(dX > (w[0] / 2.0)) dX = w[0] - dX;
+                    if(dY > (w[1] / 2.0)) dY = w[1] - dY;
+                    if(dZ > (w[2] / 2.0)) dZ = w[2] - dZ;
+                    const double d2 = dX * dX + dY * dY + dZ * dZ;
+                    if(d2 < rc2 && j != k) {
+                        if(c < d.nbr_max) out[c] = j;
+                        c++;
+                    }
+                }
+            }
+        }
+    }
+    d.nbr_count[k] = c;
+    if(c > d.nbr_max) {
+        d.sc->overflow = 1;
+        atomicMax(&d.sc->needed, c);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Per-atom force/energy gather, table mode (CFunctorCalcForce::operator())
+// ---------------------------------------------------------------------------------------------
+__global__ void k_force(DevSys d, Params P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= P.n) return;
+    const float Lf[3] = {P.boxf[0], P.boxf[1], P.boxf[2]};
+    const double w[3] = {double(Lf[0]) / 2.0 - (-double(Lf[0]) / 2.0), double(Lf[1]) / 2.0 - (-double(Lf[1]) / 2.0),
+                         double(Lf[2]) / 2.0 - (-double(Lf[2]) / 2.0)};
+    if(d.sc->overflow) return;   // neighbour list incomplete: the step is redone after growing it
+    double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+    float Uk = 0.0f;
+    if(!d.mobile[k]) {
+        d.F[3 * k] = d.F[3 * k + 1] = d.F[3 * k + 2] = 0.0;
+        d.U[k] = 0.0;
+        return;
+    }
+    const D3 rk = load3(d.r, k);
+    // bonds
+    for(int e = d.bptr[k]; e < d.bptr[k + 1]; e++) {
+        const int i = d.bj[e];
+        D3 ri = load3(d.r, i);
+        same_side(rk, ri, w);
+        const float* tab = d.bond_tab + (size_t)d.bt[e] * kNpts * 3;
+        const float rr = (float)nrm(sub(rk, ri));
+        const int idx = tindex(rr, tab);
+        float md = 0.0f;
+        if(idx >= 0 && idx < kNpts - 1) {
+            const float* p1 = tab + 3 * idx;
+            const float* p2 = p1 + 3;
+            md += interp(rr, p1[0], p1[1], p2[0], p2[1]);
+            if(i > k) Uk += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+        }
+        const D3 f = scl(coeff12(ri, rk), (double)md);
+        Fx += f.x; Fy += f.y; Fz += f.z;
+    }
+    // angles
+    for(int e = d.aptr[k]; e < d.aptr[k + 1]; e++) {
+        D3 ri = load3(d.r, d.ai[e]), rj = load3(d.r, d.aj[e]);
+        same_side(rk, ri, w);
+        same_side(rk, rj, w);
+        const float* tab = d.angle_tab + (size_t)d.at[e] * kNpts * 3;
+        D3 f;
+        if(d.acen[e]) {
+            const float th = calc_angle(ri, rk, rj);
+            const int idx = tindex(th, tab);
+            float md = 0.0f;
+            if(idx >= 0 && idx < kNpts - 1) {
+                const float* p1 = tab + 3 * idx;
+                const float* p2 = p1 + 3;
+                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+                Uk += interp(th, p1[0], p1[2], p2[0], p2[2]);
+            }
+            f = scl(coeff_ang2(rj, rk, ri), (double)md);
+        } else {
+            const float th = calc_angle(rk, ri, rj);
+            const int idx = tindex(th, tab);
+            float md = 0.0f;
+            if(idx >= 0 && idx < kNpts - 1) {
+                const float* p1 = tab + 3 * idx;
+                const float* p2 = p1 + 3;
+                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+            }
+            f = scl(coeff_ang13(rj, ri, rk), (double)md);
+        }
+        Fx += f.x; Fy += f.y; Fz += f.z;
+    }
+    // dihedrals
+    for(int e = d.dptr[k]; e < d.dptr[k + 1]; e++) {
+        D3 ri = load3(d.r, d.di[e]), rj = load3(d.r, d.dj[e]), rl = load3(d.r, d.dl[e]);
+        same_side(rk, ri, w);
+        same_side(rk, rj, w);
+        same_side(rk, rl, w);
+        const float* tab = d.dih_tab + (size_t)d.dt[e] * kNpts * 3;
+        D3 f;
+        if(d.dcen[e]) {
+            const float th = calc_dihedral(ri, rk, rj, rl);
+            const int idx = tindex(th, tab);
+            float md = 0.0f;
+            if(idx >= 0 && idx < kNpts - 1) {
+                const float* p1 = tab + 3 * idx;
+                const float* p2 = p1 + 3;
+                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+                Uk += 0.5f * interp(th, p1[0], p1[2], p2[0], p2[2]);
+            }
+            f = scl(coeff_dih23(rl, rj, rk, ri), (double)md);
+        } else {
+            const float th = calc_dihedral(rk, ri, rj, rl);
+            const int idx = tindex(th, tab);
+            float md = 0.0f;
+            if(idx >= 0 && idx < kNpts - 1) {
+                const float* p1 = tab + 3 * idx;
+                const float* p2 = p1 + 3;
+                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+            }
+            f = scl(coeff_dih14(rl, rj, ri, rk), (double)md);
+        }
+        Fx += f.x; Fy += f.y; Fz += f.z;
+    }
+    // short range, neighbour-list order
+    const int T = P.T;
+    const int nn = min(d.nbr_count[k], d.nbr_max);
+    const int* nl = d.nbr_list + (size_t)k * d.nbr_max;
+    for(int e = 0; e < nn; e++) {
+        const int i = nl[e];
+        float u = 0.0f;
+        D3 ri = load3(d.r, i);
+        same_side(rk, ri, w);
+        D3 f = d3(0, 0, 0);
+        const float rr = (float)nrm(sub(rk, ri));
+        if(!(rr < 1E-3f)) {
+            float sum = 0.0f;
+            const int pair = d.type[k] * T + d.type[i];
+            const int cnt = d.nb_cnt[pair];
+            for(int ff = 0; ff < cnt; ff++) {
+                const float* tab = d.nb_tab + ((size_t)pair * kMaxFF + ff) * kNpts * 3;
+                const int idx = tindex(rr, tab);
+                if(idx >= 0 && idx < kNpts - 1) {
+                    const float* p1 = tab + 3 * idx;
+                    const float* p2 = p1 + 3;
+                    sum += interp(rr, p1[0], p1[1], p2[0], p2[1]);
+                    if(i > k) u += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+                }
+            }
+            f = scl(coeff12(ri, rk), (double)sum);
+        }
+        float sc;
+        if(exclusion(d, P, k, i, sc)) { f = scl(f, (double)sc); u *= sc; }
+        Fx += f.x; Fy += f.y; Fz += f.z;
+        Uk += u;
+    }
+    // Coulomb over all atoms, minimum image, no cutoff (FunctorCalcForce.cpp:258-278, 514-535)
+    const float qk = d.qf[k];
+    for(int i = 0; i < P.n; i++) {
+        float u = 0.0f;
+        D3 ri = load3(d.r, i);
+        same_side(rk, ri, w);
+        const D3 rv = sub(rk, ri);
+        const float qi = d.qf[i];
+        const float R = (float)nrm(rv);
+        const double R3 = double(R * R * R);
+        const double K = double(kCoulombKf * qk * qi);
+        if((i > k) && (R != 0.0f)) u += float(K) / R;
+        D3 f = (R3 != 0.0) ? scl(rv, K / R3) : d3(0, 0, 0);
+        float sc;
+        if(exclusion(d, P, k, i, sc)) { f = scl(f, (double)sc); u *= sc; }
+        Fx += f.x; Fy += f.y; Fz += f.z;
+        Uk += u;
+    }
+    d.F[3 * k] = Fx;
+    d.F[3 * k + 1] = Fy;
+    d.F[3 * k + 2] = Fz;
+    d.U[k] = (double)Uk;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Integration (VelVerlet.cpp:74-93 NVT/NVE branch, cutForces :96-122, pbcWrap SimulationBox.cpp:135-166)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_kick_drift(DevSys d, Params P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= P.n) return;
+    const double S = d.sc->S;
+    const double dt_2 = P.dt / 2.0;
+    const double dm = P.dt / d.m[k];
+#pragma unroll
+    for(int a = 0; a < 3; a++) {
+        double p = d.p[3 * k + a] * S;
+        p = p + d.F[3 * k + a] * dt_2;
+        d.p[3 * k + a] = p;
+        d.r[3 * k + a] = d.r[3 * k + a] + p * dm;
+    }
+}
+
+__device__ __forceinline__ double wrap_coord(double x, double Lm) {
+    const double h = Lm / 2.0;
+    if(x >= h) x -= double((int)((x + h) / Lm)) * Lm;
+    if(x < -h) x -= double((int)((x + (-h)) / Lm)) * Lm;
+    return x;
+}
+
+template<bool OUTPUT>
+__global__ void k_kick2(DevSys d, Params P) {
+    __shared__ double smem[32 * 3];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};   // sum p^2/m, sum F.r, sum U
+    if(k < P.n) {
+        const double dt_2 = P.dt / 2.0;
+        double p2 = 0.0, fr = 0.0;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            double f = d.F[3 * k + a];
+            if(P.clip && P.fcut > 0.0 && fabs(f) > P.fcut) {
+                f = ((f >= 0.0) ? 1.0 : -1.0) * P.fcut;
+                d.F[3 * k + a] = f;
+            }
+            const double p = d.p[3 * k + a] + f * dt_2;
+            d.p[3 * k + a] = p;
+            const double x = wrap_coord(d.r[3 * k + a], P.box[a]);
+            d.r[3 * k + a] = x;
+            p2 += p * p;
+            fr += f * x;
+        }
+        v[0] = p2 / d.m[k];
+        if(OUTPUT) {
+            v[1] = fr;
+            v[2] = d.U[k];
+        }
+    }
+    block_sum<3>(v, smem);
+    if(threadIdx.x == 0) {
+        d.partial[blockIdx.x * 4 + 0] = v[0];
+        d.partial[blockIdx.x * 4 + 1] = v[1];
+        d.partial[blockIdx.x * 4 + 2] = v[2];
+    }
+    if(last_block(&d.sc->done_blocks)) {
+        if(threadIdx.x == 0) {
+            double s[3] = {0.0, 0.0, 0.0};
+            for(int b = 0; b < (int)gridDim.x; b++)
+                for(int q = 0; q < 3; q++) s[q] += d.partial[b * 4 + q];
+            // the virial uses momenta after the thermostat: sum (c2 p)^2/m = c2^2 sum p^2/m,
+            // folded in by end_of_step through KE2
+            end_of_step(P, d.sc, d.th, d.th_saved, s[0], s[2], s[1], OUTPUT, d.rec);
+            d.sc->done_blocks = 0;
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------------------
+static inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+void launch_ref_cells(const DevSys& d, const Params& P, cudaStream_t s) {
+    const int ncell = P.nx * P.ny * P.nz;
+    cudaMemsetAsync(d.cell_count, 0, sizeof(int) * ncell, s);
+    k_cell_assign<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    k_cell_scan<<<1, 1024, 0, s>>>(d, ncell);
+    // the scatter target doubles as scratch: nbr_count is rewritten by the neighbour kernel
+    k_cell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P, d.nbr_count);
+    k_cell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell, d.nbr_count);
+}
+
+void launch_ref_neigh(const DevSys& d, const Params& P, cudaStream_t s) {
+    k_neigh<<<nblk(P.n, 128), 128, 0, s>>>(d, P, P.rc);
+}
+
+void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s) {
+    k_force<<<nblk(P.n, 64), 64, 0, s>>>(d, P);
+}
+
+void launch_ref_kick_drift(const DevSys& d, const Params& P, cudaStream_t s) {
+    k_kick_drift<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+}
+
+void launch_ref_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
+    const int nb = reduction_blocks(P.n);
+    if(output) k_kick2<true><<<nb, 256, 0, s>>>(d, P);
+    else k_kick2<false><<<nb, 256, 0, s>>>(d, P);
+}
+
+}  // namespace mtg

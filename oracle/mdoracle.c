@@ -476,6 +476,7 @@ typedef struct orc_sys {
     const int* dih_kind; const double* dih_par;
     int coulomb_mode;         /* 0 all pairs minimum image (reference), 1 truncated at coulomb_rc */
     double coulomb_rc;
+    const double* qd;         /* n charges in FP64 (analytic mode) */
 } orc_sys;
 
 /* FunctorCalcForce::scaleForcesAndPotentials (FunctorCalcForce.cpp:95-157) as a factor */
@@ -796,7 +797,7 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
             if(s->dcen[e]) uk += 0.5 * V;
         }
         /* non-bonded + Coulomb over all atoms (within cutoffs), in index order */
-        const double qk = (double)s->q[k];
+        const double qk = s->qd[k];
         for(int i = 0; i < s->n; i++) {
             if(i == k) continue;
             v3 d = minimg(sub(rk, mk(s->r[3 * i], s->r[3 * i + 1], s->r[3 * i + 2])), L);
@@ -810,7 +811,7 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
                     md += m1; u += u1;
                 }
             }
-            double qi = (double)s->q[i];
+            double qi = s->qd[i];
             if(qk != 0.0 && qi != 0.0 && (s->coulomb_mode == 0 || R2 < crc2)) {
                 double Kc = 1389.32 * qk * qi;
                 md += Kc / R2;

@@ -80,7 +80,7 @@ class OrcSys(C.Structure):
                 ("bond_kind", C.c_void_p), ("bond_par", C.c_void_p),
                 ("angle_kind", C.c_void_p), ("angle_par", C.c_void_p),
                 ("dih_kind", C.c_void_p), ("dih_par", C.c_void_p),
-                ("coulomb_mode", C.c_int), ("coulomb_rc", C.c_double)]
+                ("coulomb_mode", C.c_int), ("coulomb_rc", C.c_double), ("qd", C.c_void_p)]
 
 
 class OrcRun(C.Structure):
@@ -133,6 +133,7 @@ class Oracle:
         n = s.n
         self.r = np.ascontiguousarray(s.r, np.float64).copy()
         self.q = np.ascontiguousarray(s.q, np.float32)          # reference keeps q as float
+        self.qd = np.ascontiguousarray(s.q, np.float64)
         self.m = np.ascontiguousarray(s.m, np.float64)
         self.type = s.type_index().astype(np.int32)
         self.mol = np.ascontiguousarray(s.mol_index() if mol is None else mol, np.int32)
@@ -161,7 +162,7 @@ class Oracle:
         s, cfg, L = self.s, self.cfg, self.lists
         o = OrcSys()
         o.n, o.ntypes = self.s.n, len(self.s.type_names())
-        arrays = dict(r=self.r, q=self.q, m=self.m, type=self.type, mol=self.mol, mobile=self.mobile,
+        arrays = dict(r=self.r, q=self.q, qd=self.qd, m=self.m, type=self.type, mol=self.mol, mobile=self.mobile,
                       nb_tab=self.nb_tab, nb_cnt=self.nb_cnt, bond_tab=self.bond_tab,
                       angle_tab=self.angle_tab, dih_tab=self.dih_tab,
                       nb_kind=self.nb_kind, nb_par=self.nb_par,

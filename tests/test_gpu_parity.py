@@ -1,0 +1,157 @@
+"""GPU parity: libmtgpu.so through its C ABI against the reference's own outputs (tests/golden/)
+and against the CPU oracle.
+
+Tolerances (stated per test):
+  - cell assignment and neighbour lists: bit-exact;
+  - reference-mode forces: 1e-12 relative to the largest force (FP64 with the reference's order;
+    only libm acos on the angle/dihedral paths may differ in the last bit); per-atom energies
+    (FP32 sums) 1e-5 relative;
+  - reference-mode 100-step trajectories: positions and momenta within 1e-8 relative to their
+    scale, energies within 1e-8 relative (the thermostat's kinetic sum is reduced in a different
+    order on the GPU, so the trajectories agree to rounding, not bit for bit);
+  - analytic FP64 mode vs the FP64 oracle: 1e-10 relative RMS;
+  - mixed mode (FP32 arithmetic, int64 fixed-point sums) vs the FP64 oracle: 1e-5 relative RMS
+    force error, the target the mixed mode is specified to.
+"""
+import numpy as np
+import pytest
+
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+CASES = G.names()
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from moltwister_gb300.build import build
+    build()
+
+
+def engine(s, cfg, **kw):
+    from moltwister_gb300.engine import Engine
+    return Engine(s, cfg, **kw)
+
+
+def golden_tables(s, d):
+    from oracle.oracle import reference_nb_layout
+    T = len(s.type_names())
+    return {"nb": reference_nb_layout(d["nb_table"], T), "bond": d["bond_table"].reshape(-1, 1000, 3),
+            "angle": d["angle_table"].reshape(-1, 1000, 3), "dih": d["dih_table"].reshape(-1, 1000, 3)}
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_cells_bit_exact(name):
+    s, cfg, d = G.load(name)
+    e = engine(s, cfg, tables=golden_tables(s, d))
+    dims, ixyz, first, count, lst = e.cells()
+    assert tuple(dims) == tuple(d["cell_dims"])
+    assert np.array_equal(ixyz, d["atom_cell"])
+    assert np.array_equal(first, d["cell_ptr"][:, 0])
+    assert np.array_equal(count, d["cell_ptr"][:, 1])
+    assert np.array_equal(lst, d["cell_list"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_neighbours_bit_exact(name):
+    s, cfg, d = G.load(name)
+    e = engine(s, cfg, tables=golden_tables(s, d))
+    cnt, lst = e.neighbors()
+    assert np.array_equal(cnt, d["neigh_count"])
+    for k in range(s.n):
+        assert np.array_equal(lst[k, :cnt[k]], d["neigh_list"][k, :cnt[k]])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_forces(name):
+    s, cfg, d = G.load(name)
+    e = engine(s, cfg, tables=golden_tables(s, d))
+    F, U = e.forces()
+    scale = np.abs(d["F"]).max()
+    assert np.abs(F - d["F"]).max() <= 1e-12 * scale
+    assert np.allclose(U, d["U"].astype(np.float64), rtol=1e-5, atol=1e-5 * np.abs(d["U"]).max())
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_trajectory(name):
+    s, cfg, d = G.load(name)
+    e = engine(s, cfg, tables=golden_tables(s, d))
+    stride, steps = int(d["stride"]), int(d["steps"])
+    r_scale = float(np.abs(d["traj_r"]).max())
+    p_scale = float(np.abs(d["traj_p"]).max())
+    for rec in range(1, d["traj_r"].shape[0]):
+        n = stride if rec * stride <= steps else steps - (rec - 1) * stride
+        out = e.run(n, out_stride=n - 1 if n > 1 else 1)
+        r, p, _ = e.get_state()
+        assert np.abs(r - d["traj_r"][rec]).max() <= 1e-8 * r_scale, rec
+        assert np.abs(p - d["traj_p"][rec]).max() <= 1e-8 * p_scale, rec
+        last = out[-1]
+        U, K, T, P, V = d["traj_scalars"][rec, 1:6]
+        assert abs(last.U - U) <= 1e-8 * max(1.0, abs(U))
+        assert abs(last.K - K) <= 1e-8 * max(1.0, abs(K))
+        assert abs(last.T - T) <= 1e-8 * max(1.0, abs(T))
+        assert abs(last.V - V) <= 1e-12 * V
+
+
+def analytic_case():
+    """Water in a >=3-cell box with cutoff Coulomb; a jittered copy of the golden input."""
+    s, cfg, d = G.load("water648_nvt")
+    s.r = s.r + np.random.default_rng(7).uniform(-0.02, 0.02, s.r.shape)
+    cfg.coulomb = "cutoff"
+    cfg.coulombcutoff = cfg.cutoffradius
+    return s, cfg
+
+
+def test_fp64_mode_matches_fp64_oracle():
+    from oracle import oracle as O
+    s, cfg = analytic_case()
+    cfg.precision = "fp64"
+    F, U = engine(s, cfg).forces()
+    Fo, Uo = O.Oracle(s, cfg).forces_fp64()
+    rel = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
+    assert rel < 1e-10, rel
+    assert abs(U.sum() - Uo.sum()) < 1e-9 * abs(Uo.sum())
+
+
+def test_mixed_mode_force_error():
+    from oracle import oracle as O
+    s, cfg = analytic_case()
+    cfg.precision = "mixed"
+    F, U = engine(s, cfg).forces()
+    Fo, Uo = O.Oracle(s, cfg).forces_fp64()
+    rel = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
+    assert rel < 1e-5, rel
+    assert abs(U.sum() - Uo.sum()) < 1e-5 * abs(Uo.sum())
+
+
+def test_mixed_mode_bit_reproducible():
+    """Fixed-point accumulation: two evaluations, and a run repeated from the same state, agree
+    bit for bit."""
+    s, cfg = analytic_case()
+    cfg.precision = "mixed"
+    e1 = engine(s, cfg)
+    F1, _ = e1.forces()
+    F2, _ = e1.forces()
+    assert np.array_equal(F1, F2)
+    e1.run(50)
+    r1, p1, _ = e1.get_state()
+    e2 = engine(s, cfg)
+    e2.run(50)
+    r2, p2, _ = e2.get_state()
+    assert np.array_equal(r1, r2) and np.array_equal(p1, p2)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_production_chain_terms(prec):
+    """Bonds (Harm, Morse), angles, dihedrals (Harm), Buckingham + LJ, immobile atoms."""
+    from oracle import oracle as O
+    s, cfg, d = G.load("chains108_nvt")
+    s.r = s.r + np.random.default_rng(3).uniform(-0.03, 0.03, s.r.shape)
+    cfg.precision = prec
+    cfg.coulomb = "cutoff"
+    cfg.coulombcutoff = cfg.cutoffradius
+    F, U = engine(s, cfg).forces()
+    Fo, Uo = O.Oracle(s, cfg).forces_fp64()
+    rel = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
+    assert rel < (1e-10 if prec == "fp64" else 2e-5), rel
