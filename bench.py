@@ -1,9 +1,11 @@
 """Benchmark: MD atom-steps/s of the GB300 engine on the flexible-water workload.
 
 Workload: 3,000 flexible SPC/E-like waters (9,000 atoms) in a 44.8 A periodic box, NVT 300 K
-(Nose-Hoover chain M=4, RESPA 4), dt = 0.5 fs, LJ on O-O (cutoff 10 A), cutoff Coulomb at 10 A,
+(Nose-Hoover chain M=4, RESPA 4), dt = 0.5 fs, LJ on O-O (cutoff 10 A), Coulomb within 10 A,
 harmonic O-H bonds and H-O-H angles; molecules on a seeded lattice with random orientations,
-Maxwell-Boltzmann momenta.  Mixed precision (FP32 arithmetic, int64 fixed-point forces).
+Maxwell-Boltzmann momenta, relaxed by 400 untimed gradient-descent steps.  Coulomb uses the
+shifted-force form at 10 A (a new option: the reference has only all-pairs Coulomb, and plain
+truncation destabilises this start).  Mixed precision (FP32 arithmetic, int64 fixed-point forces).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -39,9 +41,10 @@ def make_system(precision: str = "mixed"):
     from moltwister_gb300 import workloads as W
     s, cfg = W.water(n_mol=3000, L=44.8, seed=2, rc=10.0, dt=0.5)
     cfg.precision = precision
-    cfg.coulomb = "cutoff"
+    cfg.coulomb = "shifted"
     cfg.coulombcutoff = 10.0
     cfg.listskin = 1.0
+    cfg.optlearningrate = 2e-5
     return s, cfg
 
 
@@ -208,6 +211,9 @@ def our_arm(args):
     s, cfg = make_system("mixed")
     n = s.n
     e = Engine(s, cfg, device=local)
+    # untimed preparation: relax the lattice start by gradient descent (the reference's
+    # `moldyn optimizeenergy`), as the Nose-Hoover chain cannot absorb the start's energy release
+    e.optimize(400)
     # warm-up: graph capture and first list builds
     e.run(max(args.warmup, 3) * 1)
     for _ in range(max(args.warmup, 3)):
@@ -246,7 +252,8 @@ def our_arm(args):
            "config": {"workload": WORKLOAD, "atoms": n, "molecules": n // 3, "box_A": 44.8, "dt_fs": 0.5,
                       "precision": "mixed (FP32 pair/bonded arithmetic, int64 fixed-point forces, FP64 positions/"
                                    "thermostat/reductions)",
-                      "coulomb": "cutoff 10 A (new option; the reference is all-pairs)", "lj_cutoff_A": 10.0,
+                      "coulomb": "shifted-force cutoff 10 A (new option; the reference is all-pairs)",
+                      "lj_cutoff_A": 10.0, "prep": "400 gradient-descent steps (lr 2e-5), untimed",
                       "list_skin_A": cfg.listskin, "ensemble": "NVT Nose-Hoover M=4 RESPA 4",
                       "l2": f"flushed (256 MiB write) between timed chunks of {CHUNK} steps",
                       "parallelism": "replicas only" if world > 1 else "single GPU",

@@ -78,6 +78,8 @@ extern "C" {
 #define MTG_COULOMB_ALLPAIRS 0 /* the reference: minimum image over all pairs, no cutoff
                                   (FunctorCalcForce.cpp:258-278,514-535) */
 #define MTG_COULOMB_CUTOFF 1   /* truncated at coulomb_cutoff (new option) */
+#define MTG_COULOMB_SHIFTED 2  /* shifted force, zero force and energy at coulomb_cutoff (new option):
+                                  F = K qi qj (1/r^2 - 1/rc^2), U = K qi qj (1/r - 1/rc + (r - rc)/rc^2) */
 
 /* Ensembles (SMolDynConfigStruct::Ensemble, MolDynConfigStruct.h:24) */
 #define MTG_NVT 0

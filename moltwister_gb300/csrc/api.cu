@@ -42,6 +42,7 @@ struct mtg_ctx {
     std::string err;
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // captures the bodies of conditional graph nodes
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Params P{};
     DevSys d{};
@@ -80,6 +81,7 @@ struct mtg_ctx {
         if(vlist_buf) cudaFree(vlist_buf);
         if(ev0) cudaEventDestroy(ev0);
         if(ev1) cudaEventDestroy(ev1);
+        if(stream2) cudaStreamDestroy(stream2);
         if(stream) cudaStreamDestroy(stream);
     }
 };
@@ -269,7 +271,31 @@ int compute_forces_now(mtg_ctx* c, bool energy) {
     return fail(c, MTG_E_OVERFLOW, "neighbour list did not converge");
 }
 
-void enqueue_step(mtg_ctx* c, bool output) {
+// Appends a production-mode list build wrapped in a graph IF node to the capture on c->stream;
+// its condition is set on the device by the preceding kick+drift kernel.
+int capture_conditional_build(mtg_ctx* c, cudaGraphConditionalHandle cond) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    CUDA_TRY(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CUDA_TRY(c, cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    launch_prod_build(c->d, c->P, false, c->stream2);
+    cudaGraph_t body_out;
+    CUDA_TRY(c, cudaStreamEndCapture(c->stream2, &body_out));
+    CUDA_TRY(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return MTG_OK;
+}
+
+int enqueue_step(mtg_ctx* c, bool output, cudaGraphConditionalHandle cond) {
     if(is_reference(c)) {
         launch_ref_kick_drift(c->d, c->P, c->stream);
         launch_ref_cells(c->d, c->P, c->stream);
@@ -277,14 +303,21 @@ void enqueue_step(mtg_ctx* c, bool output) {
         launch_ref_force(c->d, c->P, c->stream);
         launch_ref_kick2(c->d, c->P, output, c->stream);
     } else {
-        launch_prod_kick_drift(c->d, c->P, c->stream);
-        launch_prod_build(c->d, c->P, false, c->stream);
+        launch_prod_kick_drift(c->d, c->P, c->stream, cond);
+        if(cond) {
+            int rc = capture_conditional_build(c, cond);
+            if(rc) return rc;
+        } else {
+            launch_prod_build(c->d, c->P, false, c->stream);
+        }
         launch_prod_force(c->d, c->P, output, c->stream);
         launch_prod_kick2(c->d, c->P, output, c->stream);
     }
+    return MTG_OK;
 }
 
-int kernels_per_step(const mtg_ctx* c) { return is_reference(c) ? 8 : 9; }
+// Kernels per step when no list rebuild is due (reference mode rebuilds every step).
+int kernels_per_step(const mtg_ctx* c) { return is_reference(c) ? 8 : 3; }
 
 int get_graph(mtg_ctx* c, int steps, bool output, cudaGraphExec_t* out) {
     auto key = std::make_pair(steps, output ? 1 : 0);
@@ -294,8 +327,18 @@ int get_graph(mtg_ctx* c, int steps, bool output, cudaGraphExec_t* out) {
         return MTG_OK;
     }
     cudaGraph_t g;
-    CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    for(int s = 0; s < steps; s++) enqueue_step(c, output && s == steps - 1);
+    CUDA_TRY(c, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond = 0;
+    if(!is_reference(c)) CUDA_TRY(c, cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault));
+    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    for(int s = 0; s < steps; s++) {
+        int rc = enqueue_step(c, output && s == steps - 1, cond);
+        if(rc) {
+            cudaStreamEndCapture(c->stream, &g);
+            cudaGraphDestroy(g);
+            return rc;
+        }
+    }
     CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
     cudaGraphExec_t ge;
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
@@ -410,6 +453,9 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         if(!(sys->mass[i] > 0.0)) return fail(nullptr, MTG_E_INVALID, "masses must be positive");
     }
     if(cfg->precision < MTG_PREC_REFERENCE || cfg->precision > MTG_PREC_MIXED) return fail(nullptr, MTG_E_INVALID, "bad precision");
+    if(cfg->coulomb < MTG_COULOMB_ALLPAIRS || cfg->coulomb > MTG_COULOMB_SHIFTED) return fail(nullptr, MTG_E_INVALID, "bad coulomb mode");
+    if(cfg->precision == MTG_PREC_REFERENCE && cfg->coulomb != MTG_COULOMB_ALLPAIRS)
+        return fail(nullptr, MTG_E_INVALID, "the reference precision mode has all-pairs Coulomb only");
     if(cfg->ensemble == MTG_NPT) return fail(nullptr, MTG_E_UNSUPPORTED, "NPT (MTK barostat) is not implemented in this build");
     if(cfg->ensemble != MTG_NVT && cfg->ensemble != MTG_NVE) return fail(nullptr, MTG_E_INVALID, "bad ensemble");
     if(cfg->temperature_nh_len < 0 || cfg->temperature_nh_len > kMaxChain) return fail(nullptr, MTG_E_INVALID, "chain length out of range");
@@ -440,7 +486,9 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     c->cfg = *cfg;
     c->device = cfg->device;
     if(cudaSetDevice(c->device) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "cudaSetDevice failed (no GPU?)");
-    if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "stream creation failed");
+    if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(nullptr, MTG_E_CUDA, "stream creation failed");
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
 
@@ -480,7 +528,7 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     P.nz = ref_cells(sys->box[2], cfg->cutoff_radius, cfg->neigh_shell);
     if(P.nx < 1 || P.ny < 1 || P.nz < 1) return fail(nullptr, MTG_E_INVALID, "box narrower than cutoff + shell: the reference cell list is empty");
     {
-        const double rlist = std::max((double)P.rc, P.coulomb == MTG_COULOMB_CUTOFF ? (double)P.rcoul : 0.0) + P.skin;
+        const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
         int pn[3];
         for(int a = 0; a < 3; a++) {
             pn[a] = (int)std::floor(sys->box[a] / rlist);
@@ -608,12 +656,18 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         rc = rc || upload(C, &ip, nb_kind.data(), nb_kind.size()); d.nb_kind = ip;
         rc = rc || upload(C, &dp, nb_coef.data(), nb_coef.size()); d.nb_par = dp;
         rc = rc || upload(C, &f, nb_coeff.data(), nb_coeff.size()); d.nb_parf = f;
+        // angle parameters on the device: (k, theta0 in radians, toRad, 0)
+        for(size_t t = 0; t < akind.size(); t++) apar[4 * t + 1] = apar[4 * t + 1] * apar[4 * t + 2];
+        std::vector<float> bparf(bpar.begin(), bpar.end()), aparf(apar.begin(), apar.end()), dparf(dpar.begin(), dpar.end());
         rc = rc || upload(C, &ip, bkind.data(), bkind.size()); d.bond_kind = ip;
         rc = rc || upload(C, &dp, bpar.data(), bpar.size()); d.bond_par = dp;
+        rc = rc || upload(C, &f, bparf.data(), bparf.size()); d.bond_parf = f;
         rc = rc || upload(C, &ip, akind.data(), akind.size()); d.angle_kind = ip;
         rc = rc || upload(C, &dp, apar.data(), apar.size()); d.angle_par = dp;
+        rc = rc || upload(C, &f, aparf.data(), aparf.size()); d.angle_parf = f;
         rc = rc || upload(C, &ip, dkind.data(), dkind.size()); d.dih_kind = ip;
         rc = rc || upload(C, &dp, dpar.data(), dpar.size()); d.dih_par = dp;
+        rc = rc || upload(C, &f, dparf.data(), dparf.size()); d.dih_parf = f;
         auto up = [&](const std::vector<int>& v) -> const int* {
             int* q = nullptr;
             rc = rc || upload(C, &q, v.data(), v.size());
@@ -657,6 +711,7 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
             th.Q[0] = double(3 * n) * P.kT * P.tau * P.tau;
             for(int j = 1; j < P.M; j++) th.Q[j] = P.kT * P.tau * P.tau;
         }
+        for(int j = 0; j < kMaxChain; j++) th.iQ[j] = 1.0 / th.Q[j];
         cudaMemcpy(d.th, &th, sizeof(th), cudaMemcpyHostToDevice);
         cudaMemcpy(d.th_saved, &th, sizeof(th), cudaMemcpyHostToDevice);
         StepScalars s{};
@@ -672,7 +727,7 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         int est = (int)(1.3 * rho * 4.18879 * rc3) + 32;
         rc = grow_neighbors(c.get(), std::min(est, n));
         if(rc) return fail(nullptr, rc, c->err);
-        double rl = std::max((double)P.rc, P.coulomb == MTG_COULOMB_CUTOFF ? (double)P.rcoul : 0.0) + P.skin;
+        double rl = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
         int vest = (int)(1.2 * rho * 4.18879 * rl * rl * rl) + 32;
         rc = grow_vlist(c.get(), std::min(vest, n));
         if(rc) return fail(nullptr, rc, c->err);
@@ -765,6 +820,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     CUDA_TRY(c, cudaSetDevice(c->device));
     if(out_stride <= 0) out_stride = nsteps + 1;
     c->stats = mtg_run_stats{};
+    const int builds0 = read_scalars(c).builds;
     // thermostat first half-step of step 0 from the current momenta
     launch_prologue(c->d, c->P, c->stream);
     CUDA_TRY(c, cudaGetLastError());
@@ -808,7 +864,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             total_ms += ms;
             if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite momenta during the run");
-            c->stats.list_builds = s.builds;
+            c->stats.list_builds = s.builds - builds0;
             if(output) {
                 double rec[8];
                 CUDA_TRY(c, cudaMemcpy(rec, c->d.rec, sizeof(rec), cudaMemcpyDeviceToHost));
@@ -841,7 +897,8 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     }
     c->stats.steps = nsteps;
     c->stats.device_ms = total_ms;
-    c->stats.kernel_launches = (int64_t)nsteps * kernels_per_step(c) + 1;
+    // prologue + per-step kernels + the six build kernels of every production rebuild
+    c->stats.kernel_launches = (int64_t)nsteps * kernels_per_step(c) + 1 + (is_reference(c) ? 0 : 6 * c->stats.list_builds);
     return settle_state(c);
 }
 
@@ -915,9 +972,72 @@ int mtg_get_neighbors(mtg_ctx* c, int32_t max_neigh, int32_t* count, int32_t* li
 }
 
 int mtg_optimize(mtg_ctx* c, double accuracy, int max_steps, int out_stride, mtg_output_cb cb, void* user) {
-    (void)c; (void)accuracy; (void)max_steps; (void)out_stride; (void)cb; (void)user;
-    if(!c) return MTG_E_INVALID;
-    return fail(c, MTG_E_UNSUPPORTED, "gradient-descent optimisation is not implemented in this build");
+    // CMDLoop::runOptimization (MDLoop.cpp:143-173): F at the current positions, r += lr F,
+    // U_{n+1} = U(F's positions), stop when |U_{n+1} - U_n| < accuracy after more than out_stride steps.
+    if(!c || max_steps < 0) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    if(out_stride <= 0) out_stride = max_steps + 1;
+    const double lr = c->cfg.opt_learning_rate;
+    double U_n = 0.0;
+    {
+        rc = compute_forces_now(c, true);
+        if(rc) return rc;
+        std::vector<double> U(c->P.n);
+        CUDA_TRY(c, cudaMemcpy(U.data(), c->d.U, sizeof(double) * c->P.n, cudaMemcpyDeviceToHost));
+        for(double u : U) U_n += u;
+    }
+    c->stats = mtg_run_stats{};
+    for(int i = 0; i < max_steps; i++) {
+        // forces at the current positions (reference: lists rebuilt; production: rebuilt when due)
+        for(int attempt = 0;; attempt++) {
+            clear_overflow(c);
+            if(is_reference(c)) {
+                launch_ref_cells(c->d, c->P, c->stream);
+                launch_ref_neigh(c->d, c->P, c->stream);
+                launch_ref_force(c->d, c->P, c->stream);
+            } else {
+                launch_prod_build(c->d, c->P, false, c->stream);
+                launch_prod_force(c->d, c->P, true, c->stream);
+            }
+            StepScalars s = read_scalars(c);
+            CUDA_TRY(c, cudaGetLastError());
+            if(!s.overflow) break;
+            rc = is_reference(c) ? grow_neighbors(c, s.needed) : grow_vlist(c, s.needed);
+            if(rc) return rc;
+            if(!is_reference(c)) cudaMemsetAsync(&c->d.sc->rebuild, 0xff, sizeof(int32_t), c->stream);
+            if(attempt > 32) return fail(c, MTG_E_OVERFLOW, "neighbour list did not converge");
+        }
+        launch_gd_step(c->d, c->P, lr, c->stream);
+        double rec[8];
+        CUDA_TRY(c, cudaMemcpyAsync(rec, c->d.rec, sizeof(rec), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if(!std::isfinite(rec[0])) return fail(c, MTG_E_NONFINITE, "non-finite energy during optimisation");
+        const double U_np1 = rec[0];
+        const double Udiff = std::fabs(U_np1 - U_n);
+        U_n = U_np1;
+        c->stats.steps = i + 1;
+        if(cb && (i % out_stride) == 0) {
+            rc = fetch_rp(c, 1.0);
+            if(rc) return rc;
+            mtg_output o{};
+            o.step = i;
+            o.U = rec[0];
+            o.K = rec[1];
+            o.T = rec[2];
+            o.P = rec[3];
+            o.V = rec[4];
+            o.E = rec[0] + rec[1];
+            o.r = c->h_r.data();
+            o.p = c->h_p.data();
+            if(cb(&o, user)) break;
+        }
+        if((Udiff < accuracy) && (i > out_stride)) break;
+    }
+    // forces at the final positions for the next run
+    rc = compute_forces_now(c, true);
+    return rc;
 }
 
 int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {

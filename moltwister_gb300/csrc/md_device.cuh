@@ -8,66 +8,121 @@
 
 namespace mtg {
 
+// exp(x) for the thermostat.  Small arguments, which are the normal case (|x| = Dt/8 p_eta/Q is of
+// order 1e-2), use the Taylor series of e^x with the remainder below 1e-17 relative (degree 8 for
+// |x| <= 2^-5, degree 11 for |x| <= 2^-3); larger ones call exp().  On this GPU every FP64
+// instruction costs about as much as thirty FP32 ones, so the instruction count is what matters.
+__device__ __forceinline__ double nh_exp(double x) {
+    const double ax = fabs(x);
+    if(ax <= 0.03125) {
+        double p = 1.0 / 40320.0;
+        p = fma(p, x, 1.0 / 5040.0);
+        p = fma(p, x, 1.0 / 720.0);
+        p = fma(p, x, 1.0 / 120.0);
+        p = fma(p, x, 1.0 / 24.0);
+        p = fma(p, x, 1.0 / 6.0);
+        p = fma(p, x, 0.5);
+        p = fma(p, x, 1.0);
+        return fma(p, x, 1.0);
+    }
+    if(ax <= 0.125) {
+        double p = 1.0 / 39916800.0;
+        p = fma(p, x, 1.0 / 3628800.0);
+        p = fma(p, x, 1.0 / 362880.0);
+        p = fma(p, x, 1.0 / 40320.0);
+        p = fma(p, x, 1.0 / 5040.0);
+        p = fma(p, x, 1.0 / 720.0);
+        p = fma(p, x, 1.0 / 120.0);
+        p = fma(p, x, 1.0 / 24.0);
+        p = fma(p, x, 1.0 / 6.0);
+        p = fma(p, x, 0.5);
+        p = fma(p, x, 1.0);
+        return fma(p, x, 1.0);
+    }
+    return exp(x);
+}
+
 // CMt::exp (Integrators/Math.cpp:29-38): linear above x = 1.
-__device__ __forceinline__ double cmt_exp(double x) { return (x > 1.0) ? 2.71828 * x : exp(x); }
+__device__ __forceinline__ double cmt_exp(double x) { return (x > 1.0) ? 2.71828 * x : nh_exp(x); }
 
 // One call of CNHChain::propagator with the thermostat functor CFctT (NHChain.cpp:54-113,
-// MDLoop.cpp:29-60), single thread.  The particles enter only through G(0) = sum p^2/m - g kT and
-// through the momentum scalings; since a scaling by c multiplies sum p^2/m by c^2, the kinetic
-// term is carried as the scalar `KE2` (= sum p^2/m) and the scalings are returned as one product.
-// Suzuki-Yoshida weights as the reference sets them: w0 = 1/(1 - 2^(1/3)) (NHChain.cpp:45-52).
+// MDLoop.cpp:29-60), executed by all 32 lanes of one warp.  The particles enter only through
+// G(0) = sum p^2/m - g kT and through the momentum scalings; since a scaling by c multiplies
+// sum p^2/m by c^2, the kinetic term is carried as the scalar `KE2` and the scalings are returned
+// as one product.  Every lane carries the whole chain (the serial recurrences run redundantly);
+// work that is independent across chain elements -- the exponentials of step 1.2 and the eta
+// updates of step 1.3 -- is spread over lanes, so it costs one instruction stream, not M.
+// The two identical exponentials of each update (NHChain.cpp:72-78, 92-98) are evaluated once, and
+// 1/Q_j comes precomputed in th.iQ.  Suzuki-Yoshida weights as the reference sets them:
+// w0 = 1/(1 - 2^(1/3)) (NHChain.cpp:45-52).  Lane j writes eta[j] and peta[j] back.
 __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, double kT, double dt, int M, int nresp) {
-    const double w0 = 1.0 / (1.0 - pow(2.0, 1.0 / 3.0));
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double w0 = 1.0 / (1.0 - cbrt(2.0));
     const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
-    const double beta = 1.0 / kT;
     double scale = 1.0;
     if(M <= 0) return scale;
-    if(th.peta[0] > 15.0) th.peta[0] = 10.0;
-    double* pe = th.peta;
-    const double* Q = th.Q;
+    double pe[kMaxChain], iQ[kMaxChain];
+    for(int j = 0; j < M; j++) {
+        pe[j] = th.peta[j];
+        iQ[j] = th.iQ[j];
+    }
+    double eta_mine = (lane < M) ? th.eta[lane] : 0.0;
+    const double gkT = g * kT;
+    if(pe[0] > 15.0) pe[0] = 10.0;
     for(int mu = 0; mu < 3; mu++) {
         const double Dt = w[mu] * dt / double(nresp);
+        const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
         for(int it = 0; it < nresp; it++) {
             // 1.1
-            {
-                const int j = M - 1;
-                const double G = (j == 0) ? KE2 - (g / beta) : (pe[j - 1] * pe[j - 1] / Q[j - 1]) - (1.0 / beta);
-                pe[j] += (Dt / 4.0) * G;
+            pe[M - 1] += d4 * ((M - 1 == 0) ? KE2 - gkT : pe[M - 2] * pe[M - 2] * iQ[M - 2] - kT);
+            // 1.2: the exponentials use the chain as it stands (pe[M-1] just updated)
+            double cl = 1.0;
+            if(lane < M - 1) {
+                double v = 0.0, q = 0.0;
+                for(int j = 0; j < M - 1; j++)
+                    if(j == lane) { v = pe[j + 1]; q = iQ[j + 1]; }
+                cl = cmt_exp(d8 * (v * q));
             }
-            // 1.2
+            double c_last = 1.0;
             for(int j = 0; j < M - 1; j++) {
-                double c = cmt_exp(-(Dt / 8.0) * (pe[j + 1] / Q[j + 1]));
-                pe[j] *= c;
-                const double G = (j == 0) ? KE2 - (g / beta) : (pe[j - 1] * pe[j - 1] / Q[j - 1]) - (1.0 / beta);
-                pe[j] += (Dt / 4.0) * G;
-                c = cmt_exp(-(Dt / 8.0) * (pe[j + 1] / Q[j + 1]));
-                pe[j] *= c;
+                const double c = __shfl_sync(full, cl, j);
+                const double G = (j == 0) ? KE2 - gkT : pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
+                pe[j] = (pe[j] * c + d4 * G) * c;
+                c_last = c;
             }
             // 1.3
-            for(int j = 0; j < M; j++) th.eta[j] += (Dt / 2.0) * (pe[j] / Q[j]);
-            // 1.4: scale momenta
             {
-                const double c = cmt_exp(-((Dt / 2.0) * (pe[0] / Q[0])));
+                double v = 0.0, q = 0.0;
+                for(int j = 0; j < M; j++)
+                    if(j == lane) { v = pe[j]; q = iQ[j]; }
+                if(lane < M) eta_mine += d2 * (v * q);
+            }
+            // 1.4
+            {
+                const double c = cmt_exp(-(d2 * (pe[0] * iQ[0])));
                 scale *= c;
                 KE2 *= c * c;
             }
-            // 1.5
+            // 1.5 (the first update reuses the exponential of pe[M-1], unchanged since 1.2)
             for(int j = M - 2; j >= 0; j--) {
-                double c = cmt_exp(-(Dt / 8.0) * (pe[j + 1] / Q[j + 1]));
-                pe[j] *= c;
-                const double G = (j == 0) ? KE2 - (g / beta) : (pe[j - 1] * pe[j - 1] / Q[j - 1]) - (1.0 / beta);
-                pe[j] += (Dt / 4.0) * G;
-                c = cmt_exp(-(Dt / 8.0) * (pe[j + 1] / Q[j + 1]));
-                pe[j] *= c;
+                const double c = (j == M - 2) ? c_last : cmt_exp(d8 * (pe[j + 1] * iQ[j + 1]));
+                const double G = (j == 0) ? KE2 - gkT : pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
+                pe[j] = (pe[j] * c + d4 * G) * c;
             }
             // 1.6
-            {
-                const int j = M - 1;
-                const double G = (j == 0) ? KE2 - (g / beta) : (pe[j - 1] * pe[j - 1] / Q[j - 1]) - (1.0 / beta);
-                pe[j] += (Dt / 4.0) * G;
-            }
+            pe[M - 1] += d4 * ((M - 1 == 0) ? KE2 - gkT : pe[M - 2] * pe[M - 2] * iQ[M - 2] - kT);
         }
     }
+    __syncwarp(full);
+    if(lane < M) {
+        double v = 0.0;
+        for(int j = 0; j < M; j++)
+            if(j == lane) v = pe[j];
+        th.peta[lane] = v;
+        th.eta[lane] = eta_mine;
+    }
+    __syncwarp(full);
     return scale;
 }
 
@@ -108,33 +163,41 @@ __device__ inline bool last_block(unsigned int* counter) {
     return is_last;
 }
 
-// End-of-step scalar work of the last block: the second thermostat half-step of this step and
-// the first half-step of the next one (MDLoop.cpp:129-132); record output scalars when asked.
+// End-of-step scalar work of the last block, run by its warp 0 (all lanes): the second
+// thermostat half-step of this step and the first half-step of the next one (MDLoop.cpp:129-132);
+// record output scalars when asked.  The chain state is shared through `th` in global memory;
+// lanes read it, each lane j writes element j back.
 __device__ inline void end_of_step(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
                                    double KE2, double U, double vir, bool output, double* rec) {
+    const int lane = threadIdx.x & 31;
     const double g = double(3 * P.n);
     double c2 = 1.0, c1 = 1.0;
     if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) {
-        ThermoDev t = *th;
-        c2 = nh_chain_half(t, KE2, g, P.kT, P.dt, P.M, P.nresp);
-        *th_saved = t;
+        c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, P.M, P.nresp);
+        __threadfence_block();
+        if(lane < P.M) {
+            th_saved->eta[lane] = th->eta[lane];
+            th_saved->peta[lane] = th->peta[lane];
+        }
+        __syncwarp();
         double KEn = KE2;
-        c1 = nh_chain_half(t, KEn, g, P.kT, P.dt, P.M, P.nresp);
-        *th = t;
+        c1 = nh_chain_half(*th, KEn, g, P.kT, P.dt, P.M, P.nresp);
     }
-    sc->c2 = c2;
-    sc->S = c2 * c1;
-    sc->KE2 = KE2;
-    if(output) {
-        const double V = P.box[0] * P.box[1] * P.box[2];
-        // MDLoop.cpp:388-403 / SimulationBox.cpp:168-195: T = sum p^2/m / 3N, P = (sum p^2/m + sum F.r)/3V
-        rec[0] = U;
-        rec[1] = 0.5 * KE2;
-        rec[2] = KE2 / (3.0 * double(P.n));
-        rec[3] = (1.0 / (3.0 * V)) * (KE2 + vir);
-        rec[4] = V;
-        sc->U = U;
-        sc->virial = vir;
+    if(lane == 0) {
+        sc->c2 = c2;
+        sc->S = c2 * c1;
+        sc->KE2 = KE2;
+        if(output) {
+            const double V = P.box[0] * P.box[1] * P.box[2];
+            // MDLoop.cpp:388-403 / SimulationBox.cpp:168-195: T = sum p^2/m / 3N, P = (sum p^2/m + sum F.r)/3V
+            rec[0] = U;
+            rec[1] = 0.5 * KE2;
+            rec[2] = KE2 / (3.0 * double(P.n));
+            rec[3] = (1.0 / (3.0 * V)) * (KE2 + vir);
+            rec[4] = V;
+            sc->U = U;
+            sc->virial = vir;
+        }
     }
 }
 

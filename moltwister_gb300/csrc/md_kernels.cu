@@ -19,6 +19,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <cuda_device_runtime_api.h>
+
 #include "md_device.cuh"
 #include "mtg_internal.h"
 
@@ -47,19 +49,29 @@ __global__ void k_prologue(DevSys d, Params P) {
     block_sum<1>(v, smem);
     if(threadIdx.x == 0) d.partial[blockIdx.x * 4] = v[0];
     if(last_block(&d.sc->done_blocks)) {
+        __shared__ double tot;
         if(threadIdx.x == 0) {
             double KE2 = 0.0;
             for(int b = 0; b < (int)gridDim.x; b++) KE2 += d.partial[b * 4];
+            tot = KE2;
+            d.sc->done_blocks = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x < 32) {
+            double KE2 = tot;
             double c1 = 1.0;
             if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) {
-                ThermoDev t = *d.th;
-                *d.th_saved = t;
-                c1 = nh_chain_half(t, KE2, double(3 * P.n), P.kT, P.dt, P.M, P.nresp);
-                *d.th = t;
+                if(threadIdx.x < P.M) {
+                    d.th_saved->eta[threadIdx.x] = d.th->eta[threadIdx.x];
+                    d.th_saved->peta[threadIdx.x] = d.th->peta[threadIdx.x];
+                }
+                __syncwarp();
+                c1 = nh_chain_half(*d.th, KE2, double(3 * P.n), P.kT, P.dt, P.M, P.nresp);
             }
-            d.sc->S = c1;
-            d.sc->c2 = 1.0;
-            d.sc->done_blocks = 0;
+            if(threadIdx.x == 0) {
+                d.sc->S = c1;
+                d.sc->c2 = 1.0;
+            }
         }
     }
 }
@@ -113,9 +125,32 @@ __device__ __forceinline__ void load_force(const DevSys& d, int i, double& fx, d
 // Integration
 // ---------------------------------------------------------------------------------------------
 template<bool MIXED>
-__global__ void k_pkick_drift(DevSys d, Params P) {
+__device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, int k, int* any);
+
+template<bool MIXED>
+__global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(cond) {
+        // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
+        // graph's IF node that wraps the list build
+        __shared__ int any;
+        if(threadIdx.x == 0) any = 0;
+        __syncthreads();
+        if(k < P.n) kick_drift_atom<MIXED>(d, P, k, &any);
+        if(last_block(&d.sc->done_blocks)) {
+            if(threadIdx.x == 0) {
+                d.sc->done_blocks = 0;
+                cudaGraphSetConditional(cond, d.sc->rebuild ? 1u : 0u);
+            }
+        }
+        return;
+    }
     if(k >= P.n) return;
+    kick_drift_atom<MIXED>(d, P, k, nullptr);
+}
+
+template<bool MIXED>
+__device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, int k, int* any) {
     const double S = d.sc->S;
     const double dt_2 = P.dt / 2.0;
     const double dm = P.dt / d.m[k];
@@ -138,6 +173,7 @@ __global__ void k_pkick_drift(DevSys d, Params P) {
     const double bz = minimg_d(z - d.r_build[3 * k + 2], P.box[2], 1.0 / P.box[2]);
     const double h = 0.5 * double(P.skin);
     if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
+    (void)any;
 }
 
 __device__ __forceinline__ double wrap_coord(double x, double Lm) {
@@ -190,12 +226,17 @@ __global__ void k_pkick2(DevSys d, Params P) {
         d.partial[blockIdx.x * 4 + 2] = v[2];
     }
     if(last_block(&d.sc->done_blocks)) {
+        __shared__ double tot[3];
         if(threadIdx.x == 0) {
             double s[3] = {0.0, 0.0, 0.0};
             for(int b = 0; b < (int)gridDim.x; b++)
                 for(int q = 0; q < 3; q++) s[q] += d.partial[b * 4 + q];
-            end_of_step(P, d.sc, d.th, d.th_saved, s[0], s[2], s[1], OUTPUT, d.rec);
+            for(int q = 0; q < 3; q++) tot[q] = s[q];
             d.sc->done_blocks = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x < 32) {
+            end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
         }
     }
 }
@@ -363,54 +404,73 @@ struct Acc {
     R x, y, z;
 };
 
-// Fixed-point accumulation of one FP32 contribution (mixed mode).
-__device__ __forceinline__ void addfix(long long& a, float f) { a += __float2ll_rn(f * kFixScaleF); }
+// Fixed-point accumulation of FP32 contributions (mixed mode) without the FP64 unit.
+// A contribution f becomes round(f * 2^26) exactly, split over two int32 accumulators:
+//   h += round(f * 2^4)                  (adding 1.5 * 2^23 rounds a float of magnitude < 2^22 to an
+//   l += round((f * 2^4 - h_i) * 2^22)    integer held in the low mantissa bits)
+// and the lane's total is h * 2^22 + l in units of 2^-26 kJ/(mol A).  Every step is exact in FP32,
+// so the fixed-point value of each contribution, and hence every sum of them, is independent of
+// the order of summation.  |f| is clamped to 2^18 (no physical pair force comes near it).
+struct Fix {
+    int h, l;
+};
+__device__ __forceinline__ void fix_add(Fix& a, float f) {
+    const float M = 12582912.0f;                 // 1.5 * 2^23
+    f = fminf(fmaxf(f, -262143.0f), 262143.0f);
+    const float x = __fmul_rn(f, 16.0f);
+    const float tx = __fadd_rn(x, M);
+    const float rx = __fsub_rn(x, __fsub_rn(tx, M));
+    a.h += __float_as_int(tx) - __float_as_int(M);
+    const float ty = __fadd_rn(__fmul_rn(rx, 4194304.0f), M);
+    a.l += __float_as_int(ty) - __float_as_int(M);
+}
+__device__ __forceinline__ long long fix_total(const Fix& a) { return ((long long)a.h << 22) + (long long)a.l; }
 
 // -dU/dr / r (= g) and U of the analytic pair terms for type pair `pair`; table kinds interpolate.
+// ir2 = 1/r^2 and ir = 1/r are passed in (rsqrt in FP32).
 template<class R>
-__device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R& g, R& u, bool energy) {
+__device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir, R ir2, R& g, R& u, bool energy) {
     const int cnt = d.nb_cnt[pair];
     for(int ff = 0; ff < cnt; ff++) {
         const int idx = pair * kMaxFF + ff;
         const int kind = d.nb_kind[idx];
-        if(kind == MTG_NB_LJ || kind == MTG_NB_LJ1208) {
-            R a, b;
-            if(sizeof(R) == 4) { a = (R)d.nb_parf[4 * idx]; b = (R)d.nb_parf[4 * idx + 1]; }
-            else { a = (R)d.nb_par[4 * idx]; b = (R)d.nb_par[4 * idx + 1]; }
-            const R ir2 = R(1) / r2;
+        R a, b, c;
+        if(sizeof(R) == 4) {
+            const float4 q = reinterpret_cast<const float4*>(d.nb_parf)[idx];
+            a = (R)q.x; b = (R)q.y; c = (R)q.z;
+        } else {
+            a = (R)d.nb_par[4 * idx]; b = (R)d.nb_par[4 * idx + 1]; c = (R)d.nb_par[4 * idx + 2];
+        }
+        if(kind == MTG_NB_LJ) {
+            // a = 4 eps sigma^12, b = 4 eps alpha sigma^6
             const R ir6 = ir2 * ir2 * ir2;
-            if(kind == MTG_NB_LJ) {
-                // a = 4 eps sigma^12, b = 4 eps alpha sigma^6
-                const R t12 = a * ir6 * ir6, t6 = b * ir6;
-                g += (R(12) * t12 - R(6) * t6) * ir2;
-                if(energy) u += t12 - t6;
-            } else {
-                const R ir8 = ir6 * ir2;
-                const R t12 = a * ir6 * ir6, t8 = b * ir8;
-                g += (R(12) * t12 - R(8) * t8) * ir2;
-                if(energy) u += t12 - t8;
-            }
+            const R t12 = a * ir6 * ir6, t6 = b * ir6;
+            g += (R(12) * t12 - R(6) * t6) * ir2;
+            if(energy) u += t12 - t6;
+        } else if(kind == MTG_NB_LJ1208) {
+            const R ir4 = ir2 * ir2, ir8 = ir4 * ir4;
+            const R t12 = a * ir8 * ir4, t8 = b * ir8;
+            g += (R(12) * t12 - R(8) * t8) * ir2;
+            if(energy) u += t12 - t8;
         } else if(kind == MTG_NB_BUCK) {
-            R A, ir, C;
-            if(sizeof(R) == 4) { A = (R)d.nb_parf[4 * idx]; ir = (R)d.nb_parf[4 * idx + 1]; C = (R)d.nb_parf[4 * idx + 2]; }
-            else { A = (R)d.nb_par[4 * idx]; ir = (R)d.nb_par[4 * idx + 1]; C = (R)d.nb_par[4 * idx + 2]; }
-            const R r = sqrt(r2);
-            const R ir2 = R(1) / r2, ir6 = ir2 * ir2 * ir2;
-            const R e = A * exp(-r * ir);
-            g += (e * ir * r - R(6) * C * ir6) * ir2;
-            if(energy) u += e - C * ir6;
+            // a = A, b = 1/rho, c = C
+            const R r = r2 * ir;
+            const R ir6 = ir2 * ir2 * ir2;
+            const R e = a * exp(-r * b);
+            g += e * b * ir - R(6) * c * ir6 * ir2;
+            if(energy) u += e - c * ir6;
         } else {
             // tabulated kind: linear interpolation of (x, -dU/dx, U) like the reference
             const float* tab = d.nb_tab + (size_t)idx * kNpts * 3;
-            const float rr = (float)sqrt(r2);
+            const float rr = (float)(r2 * ir);
             const float delta = (tab[3 * (kNpts - 1)] - tab[0]) / float(kNpts - 1);
             const float q = (rr - tab[0]) / delta;
             if(q >= 0.0f && q < float(kNpts - 1)) {
                 const int t = (int)q;
                 const float* p1 = tab + 3 * t;
                 const float* p2 = p1 + 3;
-                const float a = (p1[1] - p2[1]) / (p1[0] - p2[0]);
-                g += R((a * rr + (p1[1] - a * p1[0])) / rr);
+                const float sl = (p1[1] - p2[1]) / (p1[0] - p2[0]);
+                g += R((sl * rr + (p1[1] - sl * p1[0])) / rr);
                 if(energy) {
                     const float ae = (p1[2] - p2[2]) / (p1[0] - p2[0]);
                     u += R(ae * rr + (p1[2] - ae * p1[0]));
@@ -441,10 +501,20 @@ __device__ __forceinline__ R acos_clamped(R c) {
     return acos(c);
 }
 
+template<class R>
+__device__ __forceinline__ void load_par(const double* pd, const float* pf, int t, R (&p)[4]) {
+    if(sizeof(R) == 4) {
+        const float4 q = reinterpret_cast<const float4*>(pf)[t];
+        p[0] = (R)q.x; p[1] = (R)q.y; p[2] = (R)q.z; p[3] = (R)q.w;
+    } else {
+        for(int w = 0; w < 4; w++) p[w] = (R)pd[4 * t + w];
+    }
+}
+
 // Bonded contribution of entry `e` (global bonded-entry index space: bonds, then angles, then
 // dihedrals of atom k) to the force on k, and to k's energy (reference bookkeeping).
 template<bool MIXED, class R>
-__device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& fx, R& fy, R& fz, double& u, bool energy) {
+__device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& fx, R& fy, R& fz, R& u, bool energy) {
     const int nb = d.bptr[k + 1] - d.bptr[k];
     const int na = d.aptr[k + 1] - d.aptr[k];
     if(e < nb) {
@@ -455,7 +525,8 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
         const R r = sqrt(dx * dx + dy * dy + dz * dz);
         const int kind = d.bond_kind[t];
         R md = 0, uu = 0;
-        const double* p = d.bond_par + 4 * t;
+        R p[4];
+        load_par<R>(d.bond_par, d.bond_parf, t, p);
         if(kind == MTG_BOND_HARM) {
             const R dr = r - (R)p[1];
             md = -R(2) * (R)p[0] * dr;
@@ -481,7 +552,7 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
         }
         const R s = md / r;
         fx += s * dx; fy += s * dy; fz += s * dz;
-        if(energy && i > k) u += (double)uu;
+        if(energy && i > k) u += uu;
         return;
     }
     e -= nb;
@@ -499,10 +570,11 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
         const R th = acos_clamped(cs);
         R sn = sqrt(R(1) - cs * cs);
         sn = sn < R(1e-6) ? R(1e-6) : sn;
-        const double* p = d.angle_par + 4 * t;
+        R p[4];
+        load_par<R>(d.angle_par, d.angle_parf, t, p);   // (k, theta0 [rad], toRad, 0)
         R dU = 0, uu = 0;
         if(d.angle_kind[t] == MTG_ANGLE_HARM) {
-            const R dd = th - (R)(p[1] * p[2]);
+            const R dd = th - p[1];
             dU = R(2) * (R)p[0] * dd;
             uu = (R)p[0] * dd * dd;
         } else {
@@ -529,7 +601,7 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
             const R g3x = -(ux * inv - cs * vx / (n3 * n3)) / sn, g3y = -(uy * inv - cs * vy / (n3 * n3)) / sn,
                     g3z = -(uz * inv - cs * vz / (n3 * n3)) / sn;
             fx += dU * (g1x + g3x); fy += dU * (g1y + g3y); fz += dU * (g1z + g3z);
-            if(energy) u += (double)uu;
+            if(energy) u += uu;
         } else {
             fx -= dU * g1x; fy -= dU * g1y; fz -= dU * g1z;
         }
@@ -553,7 +625,8 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
         if(!(m2 > R(1e-20) && n2 > R(1e-20))) return;
         const R cs = (mx * nx + my * ny + mz * nz) / sqrt(m2 * n2);
         const R phi = acos_clamped(cs);
-        const double* p = d.dih_par + 4 * t;
+        R p[4];
+        load_par<R>(d.dih_par, d.dih_parf, t, p);
         const int kind = d.dih_kind[t];
         R dV = 0, V = 0;
         if(kind == MTG_DIH_HARM) {
@@ -577,7 +650,7 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
             gx = -(R(1) + f1) * ga * mx + f3 * gd * nx;
             gy = -(R(1) + f1) * ga * my + f3 * gd * ny;
             gz = -(R(1) + f1) * ga * mz + f3 * gd * nz;
-            if(energy) u += 0.5 * (double)V;
+            if(energy) u += R(0.5) * V;
         } else {
             gx = ga * mx; gy = ga * my; gz = ga * mz;
         }
@@ -591,12 +664,12 @@ __global__ void __launch_bounds__(256) k_pforce(DevSys d, Params P) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(i >= P.n) return;
     const bool mob = d.mobile[i] != 0;
-    long long ax = 0, ay = 0, az = 0;       // mixed: fixed point
-    double bx = 0, by = 0, bz = 0;          // fp64
-    double uacc = 0.0;
+    Fix fx{0, 0}, fy{0, 0}, fz{0, 0}, fu{0, 0};   // mixed: exact fixed point
+    double bx = 0, by = 0, bz = 0, bu = 0;        // fp64
     if(mob) {
         const R rc2 = (R)P.rc * (R)P.rc;
         const R rq2 = (R)P.rcoul * (R)P.rcoul;
+        const R irc = R(1) / (R)P.rcoul;
         const int T = P.T;
         const int ti = MIXED ? __float_as_int(d.lo[i].w) : d.type[i];
         const R qi = MIXED ? (R)d.hi[i].w : (R)d.qd[i];
@@ -604,23 +677,29 @@ __global__ void __launch_bounds__(256) k_pforce(DevSys d, Params P) {
         const int cnt = min(d.vcount[i], d.vmax);   // an overflowed build is redone; stay in the row
         const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
         for(int e = lane; e < cnt; e += kWarp) {
-            const uint32_t ent = lst[e];
+            const uint32_t ent = __ldg(lst + e);
             const int j = (int)(ent & kIdxMask);
             const int cls = (int)(ent >> kClassShift);
             R dx, dy, dz;
             rel<MIXED, R>(d, P, i, j, dx, dy, dz);
             const R r2 = dx * dx + dy * dy + dz * dz;
+            R ir;
+            if(MIXED) ir = (R)rsqrtf((float)r2);
+            else ir = R(1) / sqrt(r2);
+            const R ir2 = ir * ir;
             R g = 0, u = 0;
             if(r2 < rc2 && r2 >= R(1e-6)) {
                 const int tj = MIXED ? __float_as_int(d.lo[j].w) : d.type[j];
-                pair_terms<R>(d, ti * T + tj, r2, g, u, ENERGY);
+                pair_terms<R>(d, ti * T + tj, r2, ir, ir2, g, u, ENERGY);
             }
-            if(P.coulomb == MTG_COULOMB_CUTOFF && r2 < rq2) {
+            if(P.coulomb != MTG_COULOMB_ALLPAIRS && r2 < rq2) {
                 const R qj = MIXED ? (R)d.hi[j].w : (R)d.qd[j];
                 const R qq = kq * qi * qj;
-                if(qq != R(0)) {
-                    const R ir = R(1) / sqrt(r2);
-                    g += qq * ir * ir * ir;
+                if(P.coulomb == MTG_COULOMB_SHIFTED) {
+                    g += qq * (ir2 - irc * irc) * ir;
+                    if(ENERGY) u += qq * (ir - irc + (r2 * ir - (R)P.rcoul) * irc * irc);
+                } else {
+                    g += qq * ir2 * ir;
                     if(ENERGY) u += qq * ir;
                 }
             }
@@ -630,56 +709,63 @@ __global__ void __launch_bounds__(256) k_pforce(DevSys d, Params P) {
                 u *= sc;
             }
             if(MIXED) {
-                addfix(ax, (float)(g * dx));
-                addfix(ay, (float)(g * dy));
-                addfix(az, (float)(g * dz));
+                fix_add(fx, (float)(g * dx));
+                fix_add(fy, (float)(g * dy));
+                fix_add(fz, (float)(g * dz));
+                if(ENERGY && j > i) fix_add(fu, (float)u);
             } else {
                 bx += (double)(g * dx);
                 by += (double)(g * dy);
                 bz += (double)(g * dz);
+                if(ENERGY && j > i) bu += (double)u;
             }
-            if(ENERGY && j > i) uacc += (double)u;
         }
         // bonded terms of atom i, one entry per lane
         const int nbd = (d.bptr[i + 1] - d.bptr[i]) + (d.aptr[i + 1] - d.aptr[i]) + (d.dptr[i + 1] - d.dptr[i]);
         for(int e = lane; e < nbd; e += kWarp) {
-            R fx = 0, fy = 0, fz = 0;
-            bonded_entry<MIXED, R>(d, P, i, e, fx, fy, fz, uacc, ENERGY);
+            R gx = 0, gy = 0, gz = 0, gu = 0;
+            bonded_entry<MIXED, R>(d, P, i, e, gx, gy, gz, gu, ENERGY);
             if(MIXED) {
-                addfix(ax, (float)fx);
-                addfix(ay, (float)fy);
-                addfix(az, (float)fz);
+                fix_add(fx, (float)gx);
+                fix_add(fy, (float)gy);
+                fix_add(fz, (float)gz);
+                if(ENERGY) fix_add(fu, (float)gu);
             } else {
-                bx += (double)fx;
-                by += (double)fy;
-                bz += (double)fz;
+                bx += (double)gx;
+                by += (double)gy;
+                bz += (double)gz;
+                if(ENERGY) bu += (double)gu;
             }
         }
     }
     // warp reduction (integer: exact; FP64: fixed tree)
-    for(int o = 16; o > 0; o >>= 1) {
-        if(MIXED) {
+    if(MIXED) {
+        long long ax = fix_total(fx), ay = fix_total(fy), az = fix_total(fz), au = ENERGY ? fix_total(fu) : 0;
+        for(int o = 16; o > 0; o >>= 1) {
             ax += __shfl_xor_sync(0xffffffffu, ax, o);
             ay += __shfl_xor_sync(0xffffffffu, ay, o);
             az += __shfl_xor_sync(0xffffffffu, az, o);
-        } else {
-            bx += __shfl_xor_sync(0xffffffffu, bx, o);
-            by += __shfl_xor_sync(0xffffffffu, by, o);
-            bz += __shfl_xor_sync(0xffffffffu, bz, o);
+            if(ENERGY) au += __shfl_xor_sync(0xffffffffu, au, o);
         }
-        if(ENERGY) uacc += __shfl_xor_sync(0xffffffffu, uacc, o);
-    }
-    if(lane == 0) {
-        if(MIXED) {
+        if(lane == 0) {
             d.Fx[i] = ax;
             d.Fy[i] = ay;
             d.Fz[i] = az;
-        } else {
+            if(ENERGY) d.U[i] = double(au) * (1.0 / kFixScale);
+        }
+    } else {
+        for(int o = 16; o > 0; o >>= 1) {
+            bx += __shfl_xor_sync(0xffffffffu, bx, o);
+            by += __shfl_xor_sync(0xffffffffu, by, o);
+            bz += __shfl_xor_sync(0xffffffffu, bz, o);
+            if(ENERGY) bu += __shfl_xor_sync(0xffffffffu, bu, o);
+        }
+        if(lane == 0) {
             d.F[3 * i] = bx;
             d.F[3 * i + 1] = by;
             d.F[3 * i + 2] = bz;
+            if(ENERGY) d.U[i] = bu;
         }
-        if(ENERGY) d.U[i] = uacc;
     }
 }
 
@@ -719,17 +805,74 @@ __global__ void k_clear_rebuild(DevSys d) {
     }
 }
 
+// Gradient-descent step of CSimulationBox::gradientDescentStep (SimulationBox.cpp:197-208):
+// r += lr F, no clipping, no wrapping.  Also sums U, p^2/m and F.r (after the move) for the
+// output line, and flags a production list rebuild when an atom moved beyond skin/2.
+__global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
+    __shared__ double smem[32 * 3];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if(k < P.n) {
+        const bool mixed = (mode == MTG_PREC_MIXED);
+        double f[3], r[3];
+        load_force(d, k, f[0], f[1], f[2], mixed);
+        load_pos(d, k, r[0], r[1], r[2], mixed);
+        double fr = 0.0, p2 = 0.0;
+        for(int a = 0; a < 3; a++) {
+            r[a] = r[a] + f[a] * lr;
+            fr += f[a] * r[a];
+            p2 += d.p[3 * k + a] * d.p[3 * k + a];
+        }
+        store_pos(d, k, r[0], r[1], r[2], mixed);
+        if(mode != MTG_PREC_REFERENCE) {
+            const double bx = minimg_d(r[0] - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
+            const double by = minimg_d(r[1] - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
+            const double bz = minimg_d(r[2] - d.r_build[3 * k + 2], P.box[2], 1.0 / P.box[2]);
+            const double h = 0.5 * double(P.skin);
+            if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
+        }
+        v[0] = d.U[k];
+        v[1] = p2 / d.m[k];
+        v[2] = fr;
+    }
+    block_sum<3>(v, smem);
+    if(threadIdx.x == 0) {
+        d.partial[blockIdx.x * 4 + 0] = v[0];
+        d.partial[blockIdx.x * 4 + 1] = v[1];
+        d.partial[blockIdx.x * 4 + 2] = v[2];
+    }
+    if(last_block(&d.sc->done_blocks)) {
+        if(threadIdx.x == 0) {
+            double sum[3] = {0.0, 0.0, 0.0};
+            for(int b = 0; b < (int)gridDim.x; b++)
+                for(int q = 0; q < 3; q++) sum[q] += d.partial[b * 4 + q];
+            const double V = P.box[0] * P.box[1] * P.box[2];
+            d.rec[0] = sum[0];
+            d.rec[1] = 0.5 * sum[1];
+            d.rec[2] = sum[1] / (3.0 * double(P.n));
+            d.rec[3] = (1.0 / (3.0 * V)) * (sum[1] + sum[2]);
+            d.rec[4] = V;
+            d.sc->U = sum[0];
+            d.sc->done_blocks = 0;
+        }
+    }
+}
+
 }  // namespace
 
 static inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s) {
+    k_gd_step<<<reduction_blocks(P.n), 256, 0, s>>>(d, P, lr, P.precision);
+}
 
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
     k_prologue<<<reduction_blocks(P.n), 256, 0, s>>>(d, P);
 }
 
-void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s) {
-    if(P.precision == MTG_PREC_MIXED) k_pkick_drift<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    else k_pkick_drift<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {
+    if(P.precision == MTG_PREC_MIXED) k_pkick_drift<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P, cond);
+    else k_pkick_drift<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P, cond);
 }
 
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
@@ -742,7 +885,7 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     k_pcell_scan<<<1, 1024, 0, s>>>(d, ncell);
     k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell);
-    const float rlist = fmaxf(P.rc, P.coulomb == MTG_COULOMB_CUTOFF ? P.rcoul : 0.0f) + P.skin;
+    const float rlist = fmaxf(P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? P.rcoul : 0.0f) + P.skin;
     if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, rlist);
     else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, rlist);
     k_clear_rebuild<<<1, 32, 0, s>>>(d);

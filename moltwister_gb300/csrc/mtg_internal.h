@@ -18,9 +18,9 @@ constexpr float kCoulombKf = 1389.32f;     // Integrators/Constants.h:40 (float 
 constexpr double kConvT = 120.272;         // Constants.h Conv_T
 constexpr double kConvt = 1.0E2;           // Constants.h Conv_t
 constexpr double kConvPress = 16388.2461;  // Constants.h Conv_press
-// Fixed-point scale of the mixed-precision force accumulators: 2^32 units per kJ/(mol A).
-constexpr double kFixScale = 4294967296.0;
-constexpr float kFixScaleF = 4294967296.0f;
+// Fixed-point scale of the mixed-precision force and energy accumulators: 2^26 units per kJ/mol(/A).
+constexpr double kFixScale = 67108864.0;   // 2^26
+constexpr float kFixScaleF = 67108864.0f;
 // Neighbour-list entry: atom index in the low 29 bits, exclusion class in the top 3 bits.
 constexpr uint32_t kIdxMask = 0x1FFFFFFFu;
 constexpr int kClassShift = 29;
@@ -32,6 +32,7 @@ struct ThermoDev {
     double eta[kMaxChain];
     double peta[kMaxChain];
     double Q[kMaxChain];
+    double iQ[kMaxChain];   // 1/Q
 };
 
 // Scalars the step kernels exchange through device memory.
@@ -93,11 +94,14 @@ struct DevSys {
     const double* nb_par;     // [pair*5+ff][4]
     const float* nb_parf;     // [pair*5+ff][4] (FP32 copy)
     const int* bond_kind;
-    const double* bond_par;
+    const double* bond_par;   // [type][4]; angles hold (k, theta0 [rad], toRad, 0)
+    const float* bond_parf;   // FP32 copies for the mixed kernels
     const int* angle_kind;
     const double* angle_par;
+    const float* angle_parf;
     const int* dih_kind;
     const double* dih_par;
+    const float* dih_parf;
     // per-atom bonded lists (CSR)
     const int *bptr, *bj, *bt;
     const int *aptr, *ai, *aj, *at, *acen;
@@ -147,12 +151,13 @@ void launch_ref_kick2(const DevSys& d, const Params& P, bool output, cudaStream_
 // Shared
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s);
 // Production modes
-void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond = 0);
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s);
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s);
 void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s);
 void launch_prod_sync_positions(const DevSys& d, const Params& P, bool to_master, cudaStream_t s);
 void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s);
+void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s);
 int reduction_blocks(int n);
 
 // Host-side table generation (tables.cpp): out[npts*3] = (x, -dU/dx, U)

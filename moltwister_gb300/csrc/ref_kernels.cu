@@ -528,14 +528,19 @@ __global__ void k_kick2(DevSys d, Params P) {
         d.partial[blockIdx.x * 4 + 2] = v[2];
     }
     if(last_block(&d.sc->done_blocks)) {
+        __shared__ double tot[3];
         if(threadIdx.x == 0) {
             double s[3] = {0.0, 0.0, 0.0};
             for(int b = 0; b < (int)gridDim.x; b++)
                 for(int q = 0; q < 3; q++) s[q] += d.partial[b * 4 + q];
+            for(int q = 0; q < 3; q++) tot[q] = s[q];
+            d.sc->done_blocks = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x < 32) {
             // the virial uses momenta after the thermostat: sum (c2 p)^2/m = c2^2 sum p^2/m,
             // folded in by end_of_step through KE2
-            end_of_step(P, d.sc, d.th, d.th_saved, s[0], s[2], s[1], OUTPUT, d.rec);
-            d.sc->done_blocks = 0;
+            end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
         }
     }
 }

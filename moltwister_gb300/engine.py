@@ -24,7 +24,7 @@ MAXFF = 5
 MAXCHAIN = 16
 
 PREC = {"reference": 0, "fp64": 1, "mixed": 2}
-COULOMB = {"allpairs": 0, "cutoff": 1}
+COULOMB = {"allpairs": 0, "cutoff": 1, "shifted": 2}
 
 MTG_OK = 0
 ERRORS = {-1: "invalid", -2: "cuda", -3: "nomem", -4: "overflow", -5: "timeout", -6: "unsupported", -7: "nonfinite"}
@@ -301,6 +301,21 @@ class Engine:
 
         cb = OUTPUT_CB(_cb) if out_stride > 0 else OUTPUT_CB()
         self._check(self.lib.mtg_run(self.h, int(nsteps), int(out_stride), cb, None))
+        return records
+
+    def optimize(self, max_steps: int, accuracy: float = 0.0, out_stride: int = 0,
+                 callback: Optional[Callable[[OutputRecord], bool]] = None) -> List[OutputRecord]:
+        """Gradient-descent minimisation with the config's learning rate (C ABI mtg_optimize)."""
+        records: List[OutputRecord] = []
+
+        def _cb(op, user):
+            o = op.contents
+            rec = OutputRecord(int(o.step), o.T, o.P, o.V, o.U, o.K, o.E)
+            records.append(rec)
+            return 1 if (callback is not None and callback(rec)) else 0
+
+        cb = OUTPUT_CB(_cb) if out_stride > 0 else OUTPUT_CB()
+        self._check(self.lib.mtg_optimize(self.h, float(accuracy), int(max_steps), int(out_stride), cb, None))
         return records
 
     def stats(self) -> dict:

@@ -118,7 +118,8 @@ class MDConfig:
     New keys (no counterpart in the reference):
       precision     : "reference" (tables, reference arithmetic; the parity mode),
                       "fp64" (analytic FP64), "mixed" (FP32 arithmetic, int64 fixed-point forces).
-      coulomb       : "allpairs" (the reference: minimum image, no cutoff) or "cutoff".
+      coulomb       : "allpairs" (the reference: minimum image, no cutoff), "cutoff" (truncated at
+                      coulombcutoff) or "shifted" (shifted force, smooth at coulombcutoff).
       coulombcutoff : cutoff radius for "cutoff" Coulomb [A] (defaults to cutoffradius).
       listskin      : Verlet skin of the production neighbour list [A].
       clipforces    : apply the reference's per-component force clipping (NVT/NVE only).

@@ -108,9 +108,10 @@ def random_rotation(rng: np.random.Generator) -> np.ndarray:
 
 def water(n_mol: int = 3000, L: float = 44.8, seed: int = 2, T: float = 300.0,
           r0: float = 1.0, theta0: float = 109.47, lattice: Optional[int] = None,
-          rc: float = 10.0, dt: float = 0.5) -> Tuple[MDSystem, MDConfig]:
+          rc: float = 10.0, dt: float = 0.5, min_contact: float = 1.8) -> Tuple[MDSystem, MDConfig]:
     """Config 2: flexible SPC/E-like water.  Molecules on a seeded cubic lattice (lattice^3 sites,
-    the first n_mol of a seeded permutation), uniform random orientations.  Harmonic O-H bonds
+    the first n_mol of a seeded permutation), random orientations redrawn until no atom lies within
+    min_contact of a neighbouring molecule (hydrogens carry no repulsive core).  Harmonic O-H bonds
     (r0=1.0 A, k=4637), harmonic H-O-H angle (theta0=109.47 deg, k=383) in the reference convention
     U = k (x - x0)^2, LJ on O-O only (sigma=3.166 A, eps=0.650), qO=-0.8476, qH=+0.4238."""
     rng = np.random.default_rng(seed)
@@ -118,8 +119,9 @@ def water(n_mol: int = 3000, L: float = 44.8, seed: int = 2, T: float = 300.0,
         lattice = int(math.ceil(n_mol ** (1.0 / 3.0) - 1e-9))
     spacing = L / lattice
     g = np.arange(lattice)
-    sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) * spacing - L / 2.0 + spacing / 2.0
-    sites = sites[rng.permutation(sites.shape[0])[:n_mol]]
+    grid = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    grid = grid[rng.permutation(grid.shape[0])[:n_mol]]
+    sites = grid * spacing - L / 2.0 + spacing / 2.0
     th = math.radians(theta0) / 2.0
     h1 = np.array([r0 * math.sin(th), r0 * math.cos(th), 0.0])
     h2 = np.array([-r0 * math.sin(th), r0 * math.cos(th), 0.0])
@@ -127,12 +129,32 @@ def water(n_mol: int = 3000, L: float = 44.8, seed: int = 2, T: float = 300.0,
     r = np.zeros((N, 3))
     ids, q, m = [], np.zeros(N), np.zeros(N)
     bonds, angles = [], []
+    placed = {}
+    offsets = [(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1) if (a, b, c) != (0, 0, 0)]
     for i in range(n_mol):
-        R = random_rotation(rng)
         o = sites[i]
-        r[3 * i] = o
-        r[3 * i + 1] = o + R @ h1
-        r[3 * i + 2] = o + R @ h2
+        key = tuple(int(v) for v in grid[i])
+        near = [placed[k2] for k2 in (tuple((key[a] + off[a]) % lattice for a in range(3)) for off in offsets)
+                if k2 in placed]
+        near = np.concatenate(near) if near else np.zeros((0, 3))
+        # random orientation, redrawn (at most 60 times) until no atom comes within min_contact of
+        # an already placed molecule; the best draw is kept otherwise
+        best, best_d = None, -1.0
+        for _ in range(60):
+            R = random_rotation(rng)
+            mol3 = np.stack([o, o + R @ h1, o + R @ h2])
+            if near.shape[0] == 0:
+                best = mol3
+                break
+            dd = mol3[:, None, :] - near[None, :, :]
+            dd -= L * np.rint(dd / L)
+            dmin = float(np.sqrt((dd * dd).sum(-1).min()))
+            if dmin > best_d:
+                best, best_d = mol3, dmin
+            if dmin >= min_contact:
+                break
+        r[3 * i:3 * i + 3] = best
+        placed[key] = best
         ids += ["Ow", "Hw", "Hw"]
         q[3 * i:3 * i + 3] = (Q_O, Q_H, Q_H)
         m[3 * i:3 * i + 3] = (M_O, M_H, M_H)

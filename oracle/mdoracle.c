@@ -474,7 +474,7 @@ typedef struct orc_sys {
     const int* bond_kind; const double* bond_par;
     const int* angle_kind; const double* angle_par;
     const int* dih_kind; const double* dih_par;
-    int coulomb_mode;         /* 0 all pairs minimum image (reference), 1 truncated at coulomb_rc */
+    int coulomb_mode;         /* 0 all pairs minimum image (reference), 1 truncated, 2 shifted force at coulomb_rc */
     double coulomb_rc;
     const double* qd;         /* n charges in FP64 (analytic mode) */
 } orc_sys;
@@ -814,8 +814,14 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
             double qi = s->qd[i];
             if(qk != 0.0 && qi != 0.0 && (s->coulomb_mode == 0 || R2 < crc2)) {
                 double Kc = 1389.32 * qk * qi;
-                md += Kc / R2;
-                u += Kc / R;
+                if(s->coulomb_mode == 2) {       /* shifted force */
+                    const double rq = s->coulomb_rc;
+                    md += Kc * (1.0 / R2 - 1.0 / (rq * rq));
+                    u += Kc * (1.0 / R - 1.0 / rq + (R - rq) / (rq * rq));
+                } else {
+                    md += Kc / R2;
+                    u += Kc / R;
+                }
             }
             if(md == 0.0 && u == 0.0) continue;
             int ap;

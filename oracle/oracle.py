@@ -180,7 +180,7 @@ class Oracle:
             o.box[a] = float(s.box[a])
         o.rc, o.shell, o.fcut = cfg.cutoffradius, cfg.neighshell, cfg.cutoffforce
         o.scale12, o.scale13, o.scale14, o.scale1N = cfg.scale12, cfg.scale13, cfg.scale14, cfg.scale1N
-        o.coulomb_mode = 0 if cfg.coulomb == "allpairs" else 1
+        o.coulomb_mode = {"allpairs": 0, "cutoff": 1, "shifted": 2}[cfg.coulomb]
         o.coulomb_rc = cfg.coulombcutoff if cfg.coulombcutoff is not None else cfg.cutoffradius
         return o
 

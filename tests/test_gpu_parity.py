@@ -94,18 +94,19 @@ def test_reference_trajectory(name):
         assert abs(last.V - V) <= 1e-12 * V
 
 
-def analytic_case():
+def analytic_case(coulomb="cutoff"):
     """Water in a >=3-cell box with cutoff Coulomb; a jittered copy of the golden input."""
     s, cfg, d = G.load("water648_nvt")
     s.r = s.r + np.random.default_rng(7).uniform(-0.02, 0.02, s.r.shape)
-    cfg.coulomb = "cutoff"
+    cfg.coulomb = coulomb
     cfg.coulombcutoff = cfg.cutoffradius
     return s, cfg
 
 
-def test_fp64_mode_matches_fp64_oracle():
+@pytest.mark.parametrize("coulomb", ["cutoff", "shifted"])
+def test_fp64_mode_matches_fp64_oracle(coulomb):
     from oracle import oracle as O
-    s, cfg = analytic_case()
+    s, cfg = analytic_case(coulomb)
     cfg.precision = "fp64"
     F, U = engine(s, cfg).forces()
     Fo, Uo = O.Oracle(s, cfg).forces_fp64()
@@ -114,9 +115,10 @@ def test_fp64_mode_matches_fp64_oracle():
     assert abs(U.sum() - Uo.sum()) < 1e-9 * abs(Uo.sum())
 
 
-def test_mixed_mode_force_error():
+@pytest.mark.parametrize("coulomb", ["cutoff", "shifted"])
+def test_mixed_mode_force_error(coulomb):
     from oracle import oracle as O
-    s, cfg = analytic_case()
+    s, cfg = analytic_case(coulomb)
     cfg.precision = "mixed"
     F, U = engine(s, cfg).forces()
     Fo, Uo = O.Oracle(s, cfg).forces_fp64()
@@ -155,3 +157,35 @@ def test_production_chain_terms(prec):
     Fo, Uo = O.Oracle(s, cfg).forces_fp64()
     rel = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
     assert rel < (1e-10 if prec == "fp64" else 2e-5), rel
+
+
+def test_optimize_reference_matches_oracle():
+    """Gradient descent in reference mode (CMDLoop::runOptimization, SimulationBox.cpp:197-208)
+    follows the reference's own energy sequence, which is not monotonic on this input."""
+    from oracle import oracle as O
+    s, cfg, d = G.load("water648_nvt")
+    cfg.optlearningrate = 1e-5
+    e = engine(s, cfg)
+    recs = e.optimize(8, out_stride=1)
+    orc = O.Oracle(s, cfg)
+    r = orc.r.copy()
+    ref = []
+    for _ in range(8):
+        orc.set_positions(r)
+        F, u = orc.forces_ref()
+        ref.append(u.astype(np.float64).sum())
+        r = r + F * cfg.optlearningrate
+    got = np.array([x.U for x in recs])
+    assert np.allclose(got, ref, rtol=1e-9, atol=1e-6), (got, ref)
+
+
+def test_optimize_mixed_lowers_energy():
+    s, cfg, d = G.load("water648_nvt")
+    cfg.precision = "mixed"
+    cfg.coulomb = "shifted"
+    cfg.coulombcutoff = cfg.cutoffradius
+    cfg.optlearningrate = 1e-5
+    recs = engine(s, cfg).optimize(30, out_stride=1)
+    U = [r.U for r in recs]
+    assert len(U) == 30
+    assert all(np.diff(U) < 0), U[:5]
