@@ -240,7 +240,7 @@ typedef struct mtg_run_stats {
     int64_t list_builds;
     int64_t kernel_launches;
     int32_t graph_steps;        /* steps per captured CUDA graph (0 = not captured) */
-    int32_t reserved;
+    int32_t force_team;         /* lanes per atom chosen by the force-kernel autotuner */
 } mtg_run_stats;
 int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
 

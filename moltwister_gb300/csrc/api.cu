@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <string>
 #include <vector>
@@ -42,7 +43,6 @@ struct mtg_ctx {
     std::string err;
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t stream2 = nullptr;   // captures the bodies of conditional graph nodes
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Params P{};
     DevSys d{};
@@ -68,6 +68,7 @@ struct mtg_ctx {
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
     int generation = 0;
     bool forces_valid = false;
+    bool conditional = true;          // production list builds sit under graph IF nodes
     mtg_run_stats stats{};
     // output staging
     std::vector<double> h_r, h_p;
@@ -81,7 +82,6 @@ struct mtg_ctx {
         if(vlist_buf) cudaFree(vlist_buf);
         if(ev0) cudaEventDestroy(ev0);
         if(ev1) cudaEventDestroy(ev1);
-        if(stream2) cudaStreamDestroy(stream2);
         if(stream) cudaStreamDestroy(stream);
     }
 };
@@ -97,7 +97,10 @@ int fail(mtg_ctx* c, int code, const std::string& msg) {
 #define CUDA_TRY(ctx, call)                                                                        \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
-        if(e_ != cudaSuccess) return fail((ctx), MTG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        if(e_ != cudaSuccess) {                                                                    \
+            (void)cudaGetLastError(); /* do not leave a stale error for the next caller */         \
+            return fail((ctx), MTG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+        }                                                                                          \
     } while(0)
 
 template<class T>
@@ -271,31 +274,53 @@ int compute_forces_now(mtg_ctx* c, bool energy) {
     return fail(c, MTG_E_OVERFLOW, "neighbour list did not converge");
 }
 
-// Appends a production-mode list build wrapped in a graph IF node to the capture on c->stream;
-// its condition is set on the device by the preceding kick+drift kernel.
-int capture_conditional_build(mtg_ctx* c, cudaGraphConditionalHandle cond) {
-    cudaStreamCaptureStatus st;
-    cudaGraph_t g;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t ndeps = 0;
-    CUDA_TRY(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &ndeps));
-    cudaGraphNodeParams np{};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = cond;
-    np.conditional.type = cudaGraphCondTypeIf;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    CUDA_TRY(c, cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    launch_prod_build(c->d, c->P, false, c->stream2);
-    cudaGraph_t body_out;
-    CUDA_TRY(c, cudaStreamEndCapture(c->stream2, &body_out));
-    CUDA_TRY(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+// Autotuner for the production force gather: times each team size (lanes per atom) on this
+// system with CUDA events on the context's stream and keeps the fastest.  Choices are cached per
+// (precision, atom-count bucket, list radius, density bucket) for the process.
+struct TuneKey {
+    int precision, nbucket, rlist10, rho100;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(precision, nbucket, rlist10, rho100) < std::tie(o.precision, o.nbucket, o.rlist10, o.rho100);
+    }
+};
+std::map<TuneKey, int> g_tuned;
+
+int autotune_force(mtg_ctx* c) {
+    const Params& P = c->P;
+    const double V = P.box[0] * P.box[1] * P.box[2];
+    const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
+    TuneKey key{P.precision, (int)std::floor(std::log2((double)P.n)), (int)std::lround(rlist * 10.0), (int)std::lround(100.0 * P.n / V)};
+    auto it = g_tuned.find(key);
+    if(it != g_tuned.end()) {
+        c->P.team = it->second;
+        return MTG_OK;
+    }
+    const int teams[3] = {8, 16, 32};
+    float best = 1e30f;
+    int best_team = 32;
+    for(int t : teams) {
+        c->P.team = t;
+        launch_prod_force(c->d, c->P, false, c->stream);
+        CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+        for(int r = 0; r < 5; r++) launch_prod_force(c->d, c->P, false, c->stream);
+        CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+        CUDA_TRY(c, cudaEventSynchronize(c->ev1));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if(ms < best) {
+            best = ms;
+            best_team = t;
+        }
+    }
+    c->P.team = best_team;
+    g_tuned[key] = best_team;
+    // leave the forces of the chosen variant in place
+    launch_prod_force(c->d, c->P, true, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
     return MTG_OK;
 }
 
-int enqueue_step(mtg_ctx* c, bool output, cudaGraphConditionalHandle cond) {
+int enqueue_step(mtg_ctx* c, bool output) {
     if(is_reference(c)) {
         launch_ref_kick_drift(c->d, c->P, c->stream);
         launch_ref_cells(c->d, c->P, c->stream);
@@ -303,13 +328,8 @@ int enqueue_step(mtg_ctx* c, bool output, cudaGraphConditionalHandle cond) {
         launch_ref_force(c->d, c->P, c->stream);
         launch_ref_kick2(c->d, c->P, output, c->stream);
     } else {
-        launch_prod_kick_drift(c->d, c->P, c->stream, cond);
-        if(cond) {
-            int rc = capture_conditional_build(c, cond);
-            if(rc) return rc;
-        } else {
-            launch_prod_build(c->d, c->P, false, c->stream);
-        }
+        launch_prod_kick_drift(c->d, c->P, c->stream);
+        launch_prod_build(c->d, c->P, false, c->stream);
         launch_prod_force(c->d, c->P, output, c->stream);
         launch_prod_kick2(c->d, c->P, output, c->stream);
     }
@@ -317,7 +337,77 @@ int enqueue_step(mtg_ctx* c, bool output, cudaGraphConditionalHandle cond) {
 }
 
 // Kernels per step when no list rebuild is due (reference mode rebuilds every step).
-int kernels_per_step(const mtg_ctx* c) { return is_reference(c) ? 8 : 3; }
+int kernels_per_step(const mtg_ctx* c) { return (is_reference(c) || !c->conditional) ? 9 : 3; }
+
+template<class F>
+int capture_segment(mtg_ctx* c, cudaGraph_t* out, F&& body) {
+    CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaError_t e = cudaStreamEndCapture(c->stream, out);
+    if(e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(c, MTG_E_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    }
+    return MTG_OK;
+}
+
+// Production step graph with the list build under an IF node: each step is
+//   child(kick+drift, sets the condition) -> IF(rebuild){ child(list build) } -> child(force, kick+reduce)
+// assembled explicitly from captured segments.  Returns non-zero if the driver refuses.
+int build_conditional_graph(mtg_ctx* c, int steps, bool output, cudaGraph_t* out) {
+    cudaGraph_t G = nullptr, gA = nullptr, gB = nullptr, gC = nullptr, gCo = nullptr;
+    int rc = MTG_OK;
+    auto cleanup = [&]() {
+        for(cudaGraph_t x : {gA, gB, gC, gCo}) if(x) cudaGraphDestroy(x);
+    };
+    CUDA_TRY(c, cudaGraphCreate(&G, 0));
+    cudaGraphConditionalHandle cond;
+    if(cudaGraphConditionalHandleCreate(&cond, G, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphDestroy(G);
+        return fail(c, MTG_E_UNSUPPORTED, "conditional graph handles unavailable");
+    }
+    rc = rc || capture_segment(c, &gA, [&] { launch_prod_kick_drift(c->d, c->P, c->stream, cond); });
+    rc = rc || capture_segment(c, &gB, [&] { launch_prod_build(c->d, c->P, false, c->stream); });
+    rc = rc || capture_segment(c, &gC, [&] {
+        launch_prod_force(c->d, c->P, false, c->stream);
+        launch_prod_kick2(c->d, c->P, false, c->stream);
+    });
+    rc = rc || capture_segment(c, &gCo, [&] {
+        launch_prod_force(c->d, c->P, true, c->stream);
+        launch_prod_kick2(c->d, c->P, true, c->stream);
+    });
+    if(rc) {
+        cleanup();
+        cudaGraphDestroy(G);
+        return rc;
+    }
+    cudaGraphNode_t prev = nullptr;
+    for(int s = 0; s < steps && !rc; s++) {
+        cudaGraphNode_t nA, nB, nC, nBody;
+        cudaError_t e = cudaGraphAddChildGraphNode(&nA, G, prev ? &prev : nullptr, prev ? 1 : 0, gA);
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        if(e == cudaSuccess) e = cudaGraphAddNode(&nB, G, &nA, nullptr, 1, &np);
+        if(e == cudaSuccess) e = cudaGraphAddChildGraphNode(&nBody, np.conditional.phGraph_out[0], nullptr, 0, gB);
+        if(e == cudaSuccess) e = cudaGraphAddChildGraphNode(&nC, G, &nB, 1, (output && s == steps - 1) ? gCo : gC);
+        if(e != cudaSuccess) {
+            (void)cudaGetLastError();
+            rc = fail(c, MTG_E_UNSUPPORTED, std::string("conditional step graph: ") + cudaGetErrorString(e));
+        }
+        prev = nC;
+    }
+    cleanup();
+    if(rc) {
+        cudaGraphDestroy(G);
+        return rc;
+    }
+    *out = G;
+    return MTG_OK;
+}
 
 int get_graph(mtg_ctx* c, int steps, bool output, cudaGraphExec_t* out) {
     auto key = std::make_pair(steps, output ? 1 : 0);
@@ -326,20 +416,17 @@ int get_graph(mtg_ctx* c, int steps, bool output, cudaGraphExec_t* out) {
         *out = it->second;
         return MTG_OK;
     }
-    cudaGraph_t g;
-    CUDA_TRY(c, cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle cond = 0;
-    if(!is_reference(c)) CUDA_TRY(c, cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault));
-    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    for(int s = 0; s < steps; s++) {
-        int rc = enqueue_step(c, output && s == steps - 1, cond);
-        if(rc) {
-            cudaStreamEndCapture(c->stream, &g);
-            cudaGraphDestroy(g);
-            return rc;
-        }
+    cudaGraph_t g = nullptr;
+    bool built = false;
+    if(!is_reference(c) && c->conditional) {
+        if(build_conditional_graph(c, steps, output, &g) == MTG_OK) built = true;
+        else c->conditional = false;   // this driver refuses IF nodes: plain capture from now on
     }
-    CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
+    if(!built) {
+        CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for(int s = 0; s < steps; s++) enqueue_step(c, output && s == steps - 1);
+        CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
+    }
     cudaGraphExec_t ge;
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
@@ -436,6 +523,7 @@ void mtg_destroy(mtg_ctx* ctx) { delete ctx; }
 
 int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx** out) {
     g_create_error.clear();
+    (void)cudaGetLastError();
     if(!sys || !cfg || !out) return fail(nullptr, MTG_E_INVALID, "null argument");
     *out = nullptr;
     const int n = sys->n_atoms, T = sys->n_types;
@@ -486,8 +574,7 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     c->cfg = *cfg;
     c->device = cfg->device;
     if(cudaSetDevice(c->device) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "cudaSetDevice failed (no GPU?)");
-    if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-       cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess)
+    if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(nullptr, MTG_E_CUDA, "stream creation failed");
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
@@ -752,8 +839,13 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         }
         if(rc) return fail(nullptr, rc, c->err);
     }
+    P.team = 32;
     rc = compute_forces_now(c.get(), true);
     if(rc) return fail(nullptr, rc, c->err);
+    if(!is_reference(c.get())) {
+        rc = autotune_force(c.get());
+        if(rc) return fail(nullptr, rc, c->err);
+    }
     if(cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(nullptr, MTG_E_CUDA, "initial force evaluation failed");
     *out = c.release();
     return MTG_OK;
@@ -864,6 +956,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             total_ms += ms;
             if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite momenta during the run");
+            if(s.timeout) return fail(c, MTG_E_TIMEOUT, "a bounded wait in the thermostat gave up");
             c->stats.list_builds = s.builds - builds0;
             if(output) {
                 double rec[8];
@@ -899,6 +992,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     c->stats.device_ms = total_ms;
     // prologue + per-step kernels + the six build kernels of every production rebuild
     c->stats.kernel_launches = (int64_t)nsteps * kernels_per_step(c) + 1 + (is_reference(c) ? 0 : 6 * c->stats.list_builds);
+    c->stats.force_team = c->P.team;
     return settle_state(c);
 }
 

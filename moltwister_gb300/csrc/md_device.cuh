@@ -126,6 +126,225 @@ __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, dou
     return scale;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Thermostat chain on three warps.  The FP64 units of this GPU serve one sub-partition each at
+// about 30 ns per dependent instruction, so the chain's time is its critical path.  The critical
+// recurrence (steps 1.2 and 1.5 for p_eta[0..M-2]) runs on warp 0; warp 1 computes the step-1.4
+// momentum scaling from p_eta[0] and carries the kinetic term; warp 2 owns p_eta[M-1] (steps 1.1
+// and 1.6) and its exponential.  Values move through shared memory behind monotonically
+// increasing sequence flags; every wait is bounded (on expiry the chain sets `timeout` and
+// finishes with the values it has, so the kernel always terminates).
+// Exact reuse: within one Suzuki-Yoshida stage the step-1.2 exponential of p_eta[j+1] equals the
+// step-1.5 exponential of the previous substep (same argument), so it is not recomputed.  The
+// step-1.5 exponentials are obtained from the step-1.2 ones by a fourth-order correction when the
+// argument moved by less than 2^-10 (remainder below 1e-17), else evaluated afresh.
+// ---------------------------------------------------------------------------------------------
+struct NhExchange {
+    double pe[kMaxChain];
+    double eta[kMaxChain];
+    double iQ[kMaxChain];
+    double KE2, scale;
+    double pe0, ke, pe_m2, etop;            // slots
+    volatile int f_pe0, f_ke, f_pe_m2, f_etop;
+    int timeout;
+};
+
+__device__ __forceinline__ void nh_wait(volatile int* flag, int seq, int* timeout) {
+    for(int it = 0; it < (1 << 22); it++) {
+        if(*flag >= seq) {
+            __threadfence_block();
+            return;
+        }
+        __nanosleep(32);
+    }
+    *timeout = 1;
+}
+
+__device__ __forceinline__ void nh_post(volatile int* flag, int seq) {
+    __threadfence_block();
+    __syncwarp();
+    if((threadIdx.x & 31) == 0) *flag = seq;
+}
+
+// e^x for |x| <= 2^-10 by its Taylor series to order 4 (remainder below 1e-17)
+__device__ __forceinline__ double exp_tiny(double x) {
+    double p = fma(x, 1.0 / 24.0, 1.0 / 6.0);
+    p = fma(p, x, 0.5);
+    p = fma(p, x, 1.0);
+    return fma(p, x, 1.0);
+}
+
+// CMt::exp with branch tests on the bit pattern (x > 1) instead of FP64 comparisons
+__device__ __forceinline__ double cmt_exp_bits(double x) {
+    if(__double_as_longlong(x) > 0x3ff0000000000000LL) return 2.71828 * x;
+    return nh_exp(x);
+}
+
+// One thermostat half-step on warps 0..2; M >= 2.  X holds the chain on entry and exit; the flags
+// continue from `seq` (a counter shared by successive calls so flags only grow).  Returns the new
+// counter value.
+template<int MM>
+__device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, double dt, int M_rt, int nresp, int seq) {
+    constexpr int CAP = MM > 0 ? MM : kMaxChain;   // register arrays when the length is known
+    const int M = MM > 0 ? MM : M_rt;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double w0 = 1.0 / (1.0 - cbrt(2.0));
+    const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
+    const double gkT = g * kT;
+    const int top = M - 1;
+    const int nsub = 3 * nresp;
+    int* tmo = &X.timeout;
+    const long long half_bits = 0x3fe0000000000000LL;       // 0.5
+    const long long tiny_bits = 0x3f50000000000000LL;       // 2^-10
+    if(warp == 0) {
+        // ---------------- main: p_eta[0..M-2], steps 1.2 and 1.5 ----------------
+        double pe[CAP], iQ[CAP], cprev[CAP], xprev[CAP];
+        #pragma unroll
+        for(int j = 0; j < M; j++) {
+            pe[j] = X.pe[j];
+            iQ[j] = X.iQ[j];
+        }
+        double KE2 = X.KE2;
+        double eta_mine = (lane < top) ? X.eta[lane] : 0.0;
+        if(pe[0] > 15.0) pe[0] = 10.0;
+        int s = 0;
+        for(int mu = 0; mu < 3; mu++) {
+            const double Dt = w[mu] * dt / double(nresp);
+            const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
+            for(int it = 0; it < nresp; it++, s++) {
+                nh_wait(&X.f_etop, seq + s + 1, tmo);      // exponential of p_eta[M-1] (warp 2)
+                const double etop = X.etop;
+                double c12[CAP], x12[CAP];
+                // 1.2
+#pragma unroll
+                for(int j = 0; j < top; j++) {
+                    double c, x;
+                    if(j == top - 1) {
+                        c = etop;
+                        x = 0.0;
+                    } else if(it > 0) {
+                        c = cprev[j];                       // same argument as step 1.5 before
+                        x = xprev[j];
+                    } else {
+                        x = d8 * (pe[j + 1] * iQ[j + 1]);
+                        c = cmt_exp_bits(x);
+                    }
+                    c12[j] = c;
+                    x12[j] = x;
+                    const double G = (j == 0) ? KE2 - gkT : pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
+                    pe[j] = (pe[j] * c + d4 * G) * c;
+                    if(j == 0) {
+                        if(lane == 0) X.pe0 = pe[0];
+                        nh_post(&X.f_pe0, seq + s + 1);
+                    }
+                }
+                // 1.3 (this warp's elements)
+                {
+                    double v = 0.0, q = 0.0;
+#pragma unroll
+                    for(int j = 0; j < top; j++)
+                        if(j == lane) { v = pe[j]; q = iQ[j]; }
+                    if(lane < top) eta_mine += d2 * (v * q);
+                }
+                // 1.5
+#pragma unroll
+                for(int j = top - 1; j >= 0; j--) {
+                    double c;
+                    if(j == top - 1) {
+                        c = etop;                           // p_eta[M-1] has not changed since 1.2
+                    } else {
+                        const double xn = d8 * (pe[j + 1] * iQ[j + 1]);
+                        const double dx = xn - x12[j];
+                        if((__double_as_longlong(dx) & 0x7fffffffffffffffLL) <= tiny_bits &&
+                           __double_as_longlong(xn) <= half_bits && __double_as_longlong(x12[j]) <= half_bits)
+                            c = c12[j] * exp_tiny(dx);
+                        else
+                            c = cmt_exp_bits(xn);
+                        cprev[j] = c;
+                        xprev[j] = xn;
+                    }
+                    double G;
+                    if(j == 0) {
+                        nh_wait(&X.f_ke, seq + s + 1, tmo);    // kinetic term after step 1.4 (warp 1)
+                        KE2 = X.ke;
+                        G = KE2 - gkT;
+                    } else {
+                        G = pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
+                    }
+                    pe[j] = (pe[j] * c + d4 * G) * c;
+                    if(j == top - 1) {
+                        if(lane == 0) X.pe_m2 = pe[top - 1];
+                        nh_post(&X.f_pe_m2, seq + s + 1);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if(lane < top) {
+            double v = 0.0;
+#pragma unroll
+            for(int j = 0; j < top; j++)
+                if(j == lane) v = pe[j];
+            X.pe[lane] = v;
+            X.eta[lane] = eta_mine;
+        }
+    } else if(warp == 1) {
+        // ---------------- warp 1: step 1.4, kinetic term, momentum scale ----------------
+        const double iQ0 = X.iQ[0];
+        double KE2 = X.KE2, scale = 1.0;
+        int s = 0;
+        for(int mu = 0; mu < 3; mu++) {
+            const double d2 = (w[mu] * dt / double(nresp)) / 2.0;
+            for(int it = 0; it < nresp; it++, s++) {
+                nh_wait(&X.f_pe0, seq + s + 1, tmo);
+                const double c = cmt_exp_bits(-(d2 * (X.pe0 * iQ0)));
+                scale *= c;
+                KE2 *= c * c;
+                if(lane == 0) X.ke = KE2;
+                nh_post(&X.f_ke, seq + s + 1);
+            }
+        }
+        if(lane == 0) {
+            X.KE2 = KE2;
+            X.scale = scale;
+        }
+    } else if(warp == 2) {
+        // ---------------- warp 2: p_eta[M-1] (steps 1.1, 1.6), its exponential, eta[M-1] ----------------
+        const double iQm = X.iQ[top - 1], iQt = X.iQ[top];
+        double pt = X.pe[top];
+        double eta_t = X.eta[top];
+        double pm = X.pe[top - 1];
+        if(top - 1 == 0 && pm > 15.0) pm = 10.0;    // the guard on p_eta[0] (NHChain.cpp:61-65)
+        int s = 0;
+        for(int mu = 0; mu < 3; mu++) {
+            const double Dt = w[mu] * dt / double(nresp);
+            const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
+            for(int it = 0; it < nresp; it++, s++) {
+                if(s > 0) {
+                    // 1.6 of the previous substep, with that substep's Dt
+                    nh_wait(&X.f_pe_m2, seq + s, tmo);
+                    pm = X.pe_m2;
+                    const double d4p = (w[(s - 1) / nresp] * dt / double(nresp)) / 4.0;
+                    pt += d4p * (pm * pm * iQm - kT);
+                }
+                pt += d4 * (pm * pm * iQm - kT);          // 1.1
+                const double c = cmt_exp_bits(d8 * (pt * iQt));
+                if(lane == 0) X.etop = c;
+                nh_post(&X.f_etop, seq + s + 1);
+                eta_t += d2 * (pt * iQt);                   // 1.3 for the top element
+            }
+        }
+        nh_wait(&X.f_pe_m2, seq + nsub, tmo);             // 1.6 of the last substep
+        pm = X.pe_m2;
+        pt += ((w[2] * dt / double(nresp)) / 4.0) * (pm * pm * iQm - kT);
+        if(lane == 0) {
+            X.pe[top] = pt;
+            X.eta[top] = eta_t;
+        }
+    }
+    return seq + nsub;
+}
+
 // Deterministic block sum of NV doubles (fixed shuffle tree, then fixed order over warps).
 template<int NV>
 __device__ inline void block_sum(double (&v)[NV], double* smem /* [32*NV] */) {
@@ -163,27 +382,99 @@ __device__ inline bool last_block(unsigned int* counter) {
     return is_last;
 }
 
-// End-of-step scalar work of the last block, run by its warp 0 (all lanes): the second
-// thermostat half-step of this step and the first half-step of the next one (MDLoop.cpp:129-132);
-// record output scalars when asked.  The chain state is shared through `th` in global memory;
-// lanes read it, each lane j writes element j back.
-__device__ inline void end_of_step(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
-                                   double KE2, double U, double vir, bool output, double* rec) {
-    const int lane = threadIdx.x & 31;
+__device__ inline int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq) {
+    switch(M) {
+    case 2: return nh_chain_half_3w_t<2>(X, g, kT, dt, M, nresp, seq);
+    case 3: return nh_chain_half_3w_t<3>(X, g, kT, dt, M, nresp, seq);
+    case 4: return nh_chain_half_3w_t<4>(X, g, kT, dt, M, nresp, seq);
+    case 5: return nh_chain_half_3w_t<5>(X, g, kT, dt, M, nresp, seq);
+    case 6: return nh_chain_half_3w_t<6>(X, g, kT, dt, M, nresp, seq);
+    case 8: return nh_chain_half_3w_t<8>(X, g, kT, dt, M, nresp, seq);
+    default: return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq);
+    }
+}
+
+__device__ __forceinline__ void bar96() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
+
+// Thermostat half-steps for the end of a step (second half of this step, then first half of the
+// next: MDLoop.cpp:129-132) or for the prologue of a run (first half only), run by warps 0..2 of
+// one block (threadIdx.x < 96).  th_saved receives the chain after the second half-step (the
+// state the reference holds between steps).  Returns (via *c2, *c1) the momentum scales.
+__device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
+                                  double& KE2, bool second_half, double* c2_out, double* c1_out) {
+    __shared__ NhExchange X;
+    const int tid = threadIdx.x;
     const double g = double(3 * P.n);
     double c2 = 1.0, c1 = 1.0;
-    if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) {
-        c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, P.M, P.nresp);
-        __threadfence_block();
-        if(lane < P.M) {
-            th_saved->eta[lane] = th->eta[lane];
-            th_saved->peta[lane] = th->peta[lane];
+    if(P.M >= 2) {
+        if(tid < kMaxChain) {
+            X.pe[tid] = th->peta[tid];
+            X.eta[tid] = th->eta[tid];
+            X.iQ[tid] = th->iQ[tid];
+        }
+        if(tid == 0) {
+            X.KE2 = KE2;
+            X.scale = 1.0;
+            X.f_pe0 = X.f_ke = X.f_pe_m2 = X.f_etop = 0;
+            X.timeout = 0;
+        }
+        bar96();
+        int seq = 0;
+        if(second_half) {
+            seq = nh_chain_half_3w(X, g, P.kT, P.dt, P.M, P.nresp, seq);
+            bar96();
+            c2 = X.scale;
+            if(tid < P.M) {
+                th_saved->peta[tid] = X.pe[tid];
+                th_saved->eta[tid] = X.eta[tid];
+            }
+            bar96();
+            if(tid == 0) X.scale = 1.0;
+            bar96();
+        } else {
+            if(tid < P.M) {
+                th_saved->peta[tid] = X.pe[tid];
+                th_saved->eta[tid] = X.eta[tid];
+            }
+        }
+        const double KE_after2 = X.KE2;
+        bar96();
+        seq = nh_chain_half_3w(X, g, P.kT, P.dt, P.M, P.nresp, seq);
+        bar96();
+        c1 = X.scale;
+        KE2 = KE_after2;
+        if(tid < P.M) {
+            th->peta[tid] = X.pe[tid];
+            th->eta[tid] = X.eta[tid];
+        }
+        if(tid == 0 && X.timeout) sc->timeout = 1;
+    } else if(P.M == 1 && tid < 32) {
+        if(second_half) {
+            c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, P.M, P.nresp);
+            __threadfence_block();
+            if(tid == 0) {
+                th_saved->eta[0] = th->eta[0];
+                th_saved->peta[0] = th->peta[0];
+            }
+        } else if(tid == 0) {
+            th_saved->eta[0] = th->eta[0];
+            th_saved->peta[0] = th->peta[0];
         }
         __syncwarp();
         double KEn = KE2;
         c1 = nh_chain_half(*th, KEn, g, P.kT, P.dt, P.M, P.nresp);
     }
-    if(lane == 0) {
+    *c2_out = c2;
+    *c1_out = c1;
+}
+
+// End-of-step scalar work of the last block, run by its warps 0..2 (threadIdx.x < 96): the
+// thermostat half-steps and the output scalars.
+__device__ inline void end_of_step(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
+                                   double KE2, double U, double vir, bool output, double* rec) {
+    double c2 = 1.0, c1 = 1.0;
+    if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat(P, sc, th, th_saved, KE2, true, &c2, &c1);
+    if(threadIdx.x == 0) {
         sc->c2 = c2;
         sc->S = c2 * c1;
         sc->KE2 = KE2;

@@ -57,17 +57,10 @@ __global__ void k_prologue(DevSys d, Params P) {
             d.sc->done_blocks = 0;
         }
         __syncthreads();
-        if(threadIdx.x < 32) {
+        if(threadIdx.x < 96) {
             double KE2 = tot;
-            double c1 = 1.0;
-            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) {
-                if(threadIdx.x < P.M) {
-                    d.th_saved->eta[threadIdx.x] = d.th->eta[threadIdx.x];
-                    d.th_saved->peta[threadIdx.x] = d.th->peta[threadIdx.x];
-                }
-                __syncwarp();
-                c1 = nh_chain_half(*d.th, KE2, double(3 * P.n), P.kT, P.dt, P.M, P.nresp);
-            }
+            double c2 = 1.0, c1 = 1.0;
+            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat(P, d.sc, d.th, d.th_saved, KE2, false, &c2, &c1);
             if(threadIdx.x == 0) {
                 d.sc->S = c1;
                 d.sc->c2 = 1.0;
@@ -235,7 +228,7 @@ __global__ void k_pkick2(DevSys d, Params P) {
             d.sc->done_blocks = 0;
         }
         __syncthreads();
-        if(threadIdx.x < 32) {
+        if(threadIdx.x < 96) {
             end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
         }
     }
@@ -416,7 +409,6 @@ struct Fix {
 };
 __device__ __forceinline__ void fix_add(Fix& a, float f) {
     const float M = 12582912.0f;                 // 1.5 * 2^23
-    f = fminf(fmaxf(f, -262143.0f), 262143.0f);
     const float x = __fmul_rn(f, 16.0f);
     const float tx = __fadd_rn(x, M);
     const float rx = __fsub_rn(x, __fsub_rn(tx, M));
@@ -424,6 +416,7 @@ __device__ __forceinline__ void fix_add(Fix& a, float f) {
     const float ty = __fadd_rn(__fmul_rn(rx, 4194304.0f), M);
     a.l += __float_as_int(ty) - __float_as_int(M);
 }
+__device__ __forceinline__ void fix_add_clamped(Fix& a, float f) { fix_add(a, fminf(fmaxf(f, -262143.0f), 262143.0f)); }
 __device__ __forceinline__ long long fix_total(const Fix& a) { return ((long long)a.h << 22) + (long long)a.l; }
 
 // -dU/dr / r (= g) and U of the analytic pair terms for type pair `pair`; table kinds interpolate.
@@ -658,109 +651,179 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
     }
 }
 
-template<bool MIXED, bool ENERGY>
-__global__ void __launch_bounds__(256) k_pforce(DevSys d, Params P) {
+// One neighbour-list entry of atom i: force factor g (F_i += g * d) and pair energy u.
+// Per type pair, staged in shared memory by the force kernel: mode 0 = no term, 1 = one 12-6 LJ
+// term with coefficients (a, b), 2 = anything else (evaluated by pair_terms from global memory).
+struct PairCoef {
+    float a, b;
+    int mode, pad;
+};
+constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
+
+template<bool MIXED, bool ENERGY, class R>
+__device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, R qi,
+                                           R rc2, R rq2, R irc, R kq, const PairCoef* pc,
+                                           R& dx, R& dy, R& dz, R& g, R& u) {
+    const int j = (int)(ent & kIdxMask);
+    const int cls = (int)(ent >> kClassShift);
+    rel<MIXED, R>(d, P, i, j, dx, dy, dz);
+    const R r2 = dx * dx + dy * dy + dz * dz;
+    R ir;
+    if(MIXED) ir = (R)rsqrtf((float)r2);
+    else ir = R(1) / sqrt(r2);
+    const R ir2 = ir * ir;
+    g = 0;
+    u = 0;
+    if(r2 < rc2 && r2 >= R(1e-6)) {
+        const int tj = MIXED ? __float_as_int(d.lo[j].w) : d.type[j];
+        const int pr = ti * P.T + tj;
+        if(MIXED && pc && pr < kSmemPairs) {
+            const PairCoef c = pc[pr];
+            if(c.mode == 1) {
+                const R ir6 = ir2 * ir2 * ir2;
+                const R t12 = (R)c.a * ir6 * ir6, t6 = (R)c.b * ir6;
+                g = (R(12) * t12 - R(6) * t6) * ir2;
+                if(ENERGY) u = t12 - t6;
+            } else if(c.mode == 2) {
+                pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY);
+            }
+        } else {
+            pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY);
+        }
+    }
+    if(P.coulomb != MTG_COULOMB_ALLPAIRS && r2 < rq2) {
+        const R qj = MIXED ? (R)d.hi[j].w : (R)d.qd[j];
+        const R qq = kq * qi * qj;
+        if(P.coulomb == MTG_COULOMB_SHIFTED) {
+            g += qq * (ir2 - irc * irc) * ir;
+            if(ENERGY) u += qq * (ir - irc + (r2 * ir - (R)P.rcoul) * irc * irc);
+        } else {
+            g += qq * ir2 * ir;
+            if(ENERGY) u += qq * ir;
+        }
+    }
+    if(cls) {
+        const R sc = (R)P.scale[cls];
+        g *= sc;
+        u *= sc;
+    }
+    if(!(ENERGY && j > i)) u = 0;
+}
+
+// Force gather: TEAM lanes per atom (8, 16 or 32; chosen per system by the autotuner), each lane
+// walking its share of the atom's neighbour-list row four entries at a time so that four gathers
+// are in flight per lane.  Bonded terms of the atom are spread over the team's lanes.
+template<bool MIXED, bool ENERGY, int TEAM>
+__global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     using R = typename std::conditional<MIXED, float, double>::type;
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if(i >= P.n) return;
-    const bool mob = d.mobile[i] != 0;
+    __shared__ PairCoef pc_s[kSmemPairs];
+    const PairCoef* pc = nullptr;
+    if(MIXED && P.T * P.T <= kSmemPairs) {
+        for(int q = threadIdx.x; q < P.T * P.T; q += blockDim.x) {
+            PairCoef c{0.0f, 0.0f, 0, 0};
+            const int cnt = d.nb_cnt[q];
+            if(cnt == 1 && d.nb_kind[q * kMaxFF] == MTG_NB_LJ) {
+                c.mode = 1;
+                c.a = d.nb_parf[4 * (q * kMaxFF)];
+                c.b = d.nb_parf[4 * (q * kMaxFF) + 1];
+            } else if(cnt > 0) {
+                c.mode = 2;
+            }
+            pc_s[q] = c;
+        }
+        __syncthreads();
+        pc = pc_s;
+    }
+    const R gmax = R(262143.0) / ((R)P.rc + (R)P.rcoul + (R)P.skin);   // keeps |g d| < 2^18
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gt / TEAM, lane = gt % TEAM;
+    const bool active = i < P.n;
+    const bool mob = active && d.mobile[i] != 0;
     Fix fx{0, 0}, fy{0, 0}, fz{0, 0}, fu{0, 0};   // mixed: exact fixed point
     double bx = 0, by = 0, bz = 0, bu = 0;        // fp64
     if(mob) {
         const R rc2 = (R)P.rc * (R)P.rc;
         const R rq2 = (R)P.rcoul * (R)P.rcoul;
         const R irc = R(1) / (R)P.rcoul;
-        const int T = P.T;
         const int ti = MIXED ? __float_as_int(d.lo[i].w) : d.type[i];
         const R qi = MIXED ? (R)d.hi[i].w : (R)d.qd[i];
         const R kq = MIXED ? (R)kCoulombKf : (R)1389.32;
         const int cnt = min(d.vcount[i], d.vmax);   // an overflowed build is redone; stay in the row
         const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
-        for(int e = lane; e < cnt; e += kWarp) {
-            const uint32_t ent = __ldg(lst + e);
-            const int j = (int)(ent & kIdxMask);
-            const int cls = (int)(ent >> kClassShift);
-            R dx, dy, dz;
-            rel<MIXED, R>(d, P, i, j, dx, dy, dz);
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            R ir;
-            if(MIXED) ir = (R)rsqrtf((float)r2);
-            else ir = R(1) / sqrt(r2);
-            const R ir2 = ir * ir;
-            R g = 0, u = 0;
-            if(r2 < rc2 && r2 >= R(1e-6)) {
-                const int tj = MIXED ? __float_as_int(d.lo[j].w) : d.type[j];
-                pair_terms<R>(d, ti * T + tj, r2, ir, ir2, g, u, ENERGY);
-            }
-            if(P.coulomb != MTG_COULOMB_ALLPAIRS && r2 < rq2) {
-                const R qj = MIXED ? (R)d.hi[j].w : (R)d.qd[j];
-                const R qq = kq * qi * qj;
-                if(P.coulomb == MTG_COULOMB_SHIFTED) {
-                    g += qq * (ir2 - irc * irc) * ir;
-                    if(ENERGY) u += qq * (ir - irc + (r2 * ir - (R)P.rcoul) * irc * irc);
+        int e = lane;
+        for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
+            uint32_t ent[4];
+#pragma unroll
+            for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
+#pragma unroll
+            for(int q = 0; q < 4; q++) {
+                R dx, dy, dz, g, u;
+                pair_entry<MIXED, ENERGY, R>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, kq, pc, dx, dy, dz, g, u);
+                if(MIXED) {
+                    g = fminf(fmaxf(g, -gmax), gmax);
+                    fix_add(fx, (float)(g * dx));
+                    fix_add(fy, (float)(g * dy));
+                    fix_add(fz, (float)(g * dz));
+                    if(ENERGY) fix_add_clamped(fu, (float)u);
                 } else {
-                    g += qq * ir2 * ir;
-                    if(ENERGY) u += qq * ir;
+                    bx += (double)(g * dx); by += (double)(g * dy); bz += (double)(g * dz);
+                    if(ENERGY) bu += (double)u;
                 }
             }
-            if(cls) {
-                const R sc = (R)P.scale[cls];
-                g *= sc;
-                u *= sc;
-            }
+        }
+        for(; e < cnt; e += TEAM) {
+            R dx, dy, dz, g, u;
+            pair_entry<MIXED, ENERGY, R>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, kq, pc, dx, dy, dz, g, u);
             if(MIXED) {
+                g = fminf(fmaxf(g, -gmax), gmax);
                 fix_add(fx, (float)(g * dx));
                 fix_add(fy, (float)(g * dy));
                 fix_add(fz, (float)(g * dz));
-                if(ENERGY && j > i) fix_add(fu, (float)u);
+                if(ENERGY) fix_add_clamped(fu, (float)u);
             } else {
-                bx += (double)(g * dx);
-                by += (double)(g * dy);
-                bz += (double)(g * dz);
-                if(ENERGY && j > i) bu += (double)u;
+                bx += (double)(g * dx); by += (double)(g * dy); bz += (double)(g * dz);
+                if(ENERGY) bu += (double)u;
             }
         }
         // bonded terms of atom i, one entry per lane
         const int nbd = (d.bptr[i + 1] - d.bptr[i]) + (d.aptr[i + 1] - d.aptr[i]) + (d.dptr[i + 1] - d.dptr[i]);
-        for(int e = lane; e < nbd; e += kWarp) {
+        for(int b = lane; b < nbd; b += TEAM) {
             R gx = 0, gy = 0, gz = 0, gu = 0;
-            bonded_entry<MIXED, R>(d, P, i, e, gx, gy, gz, gu, ENERGY);
+            bonded_entry<MIXED, R>(d, P, i, b, gx, gy, gz, gu, ENERGY);
             if(MIXED) {
-                fix_add(fx, (float)gx);
-                fix_add(fy, (float)gy);
-                fix_add(fz, (float)gz);
-                if(ENERGY) fix_add(fu, (float)gu);
+                fix_add_clamped(fx, (float)gx);
+                fix_add_clamped(fy, (float)gy);
+                fix_add_clamped(fz, (float)gz);
+                if(ENERGY) fix_add_clamped(fu, (float)gu);
             } else {
-                bx += (double)gx;
-                by += (double)gy;
-                bz += (double)gz;
+                bx += (double)gx; by += (double)gy; bz += (double)gz;
                 if(ENERGY) bu += (double)gu;
             }
         }
     }
-    // warp reduction (integer: exact; FP64: fixed tree)
+    // team reduction (integer: exact; FP64: fixed tree); teams are aligned within the warp
     if(MIXED) {
         long long ax = fix_total(fx), ay = fix_total(fy), az = fix_total(fz), au = ENERGY ? fix_total(fu) : 0;
-        for(int o = 16; o > 0; o >>= 1) {
+        for(int o = TEAM / 2; o > 0; o >>= 1) {
             ax += __shfl_xor_sync(0xffffffffu, ax, o);
             ay += __shfl_xor_sync(0xffffffffu, ay, o);
             az += __shfl_xor_sync(0xffffffffu, az, o);
             if(ENERGY) au += __shfl_xor_sync(0xffffffffu, au, o);
         }
-        if(lane == 0) {
+        if(active && lane == 0) {
             d.Fx[i] = ax;
             d.Fy[i] = ay;
             d.Fz[i] = az;
             if(ENERGY) d.U[i] = double(au) * (1.0 / kFixScale);
         }
     } else {
-        for(int o = 16; o > 0; o >>= 1) {
+        for(int o = TEAM / 2; o > 0; o >>= 1) {
             bx += __shfl_xor_sync(0xffffffffu, bx, o);
             by += __shfl_xor_sync(0xffffffffu, by, o);
             bz += __shfl_xor_sync(0xffffffffu, bz, o);
             if(ENERGY) bu += __shfl_xor_sync(0xffffffffu, bu, o);
         }
-        if(lane == 0) {
+        if(active && lane == 0) {
             d.F[3 * i] = bx;
             d.F[3 * i + 1] = by;
             d.F[3 * i + 2] = bz;
@@ -891,14 +954,22 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     k_clear_rebuild<<<1, 32, 0, s>>>(d);
 }
 
+template<bool MIXED, bool ENERGY>
+static void force_team(const DevSys& d, const Params& P, cudaStream_t s) {
+    const int team = P.team;
+    const int nb = nblk(P.n * team, 256);
+    if(team == 8) k_pforce<MIXED, ENERGY, 8><<<nb, 256, 0, s>>>(d, P);
+    else if(team == 16) k_pforce<MIXED, ENERGY, 16><<<nb, 256, 0, s>>>(d, P);
+    else k_pforce<MIXED, ENERGY, 32><<<nb, 256, 0, s>>>(d, P);
+}
+
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s) {
-    const int nb = nblk(P.n * 32, 256);
     if(P.precision == MTG_PREC_MIXED) {
-        if(energy) k_pforce<true, true><<<nb, 256, 0, s>>>(d, P);
-        else k_pforce<true, false><<<nb, 256, 0, s>>>(d, P);
+        if(energy) force_team<true, true>(d, P, s);
+        else force_team<true, false>(d, P, s);
     } else {
-        if(energy) k_pforce<false, true><<<nb, 256, 0, s>>>(d, P);
-        else k_pforce<false, false><<<nb, 256, 0, s>>>(d, P);
+        if(energy) force_team<false, true>(d, P, s);
+        else force_team<false, false>(d, P, s);
     }
 }
 

@@ -48,7 +48,8 @@ struct StepScalars {
     int32_t nonfinite;
     uint32_t done_blocks; // last-block counter of the reduction kernels
     int32_t builds;       // neighbour-list rebuilds performed
-    double max_disp2;
+    int32_t timeout;      // a bounded device wait gave up
+    int32_t pad;
 };
 
 struct Params {
@@ -68,6 +69,7 @@ struct Params {
     float scale12, scale13, scale14, scale1N;
     int nx, ny, nz;       // reference cell counts (from the input box, MDFFMatrices.cpp:56-58)
     int pnx, pny, pnz;    // production cell counts (cell edge >= rlist), 1 = all-pairs build
+    int team;             // lanes per atom in the production force gather (8, 16, 32)
 };
 
 // Everything a force/integration kernel reads, as raw device pointers.

@@ -80,7 +80,7 @@ class Output(C.Structure):
 
 class RunStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("steps", C.c_int64), ("list_builds", C.c_int64),
-                ("kernel_launches", C.c_int64), ("graph_steps", C.c_int32), ("reserved", C.c_int32)]
+                ("kernel_launches", C.c_int64), ("graph_steps", C.c_int32), ("force_team", C.c_int32)]
 
 
 OUTPUT_CB = C.CFUNCTYPE(C.c_int, C.POINTER(Output), C.c_void_p)
@@ -322,7 +322,8 @@ class Engine:
         st = RunStats()
         self._check(self.lib.mtg_get_run_stats(self.h, C.byref(st)))
         return {"device_ms": st.device_ms, "steps": st.steps, "list_builds": st.list_builds,
-                "kernel_launches": st.kernel_launches, "graph_steps": st.graph_steps}
+                "kernel_launches": st.kernel_launches, "graph_steps": st.graph_steps,
+                "force_team": st.force_team}
 
     def profile_phases(self, steps: int) -> dict:
         """Mean device ms per step of each phase (C ABI mtg_profile_phases)."""
