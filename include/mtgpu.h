@@ -252,6 +252,46 @@ int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
  * The state advances by `steps` steps exactly as mtg_run would advance it. */
 int mtg_profile_phases(mtg_ctx* ctx, int steps, double* phase_ms);
 
+/* ---- No-allocation neighbour list (no counterpart in the reference) ----
+ *
+ * The reference has no such entry point: its neighbour list is built inside CMDFFMatrices, which
+ * owns its device vectors (MDFFMatrices.cpp:163-178).  This one serves callers that hold atom
+ * positions in device memory they manage themselves and must not allocate: an analysis pass
+ * (pair correlation, clustering) running next to a live simulation, where cudaMalloc/cudaFree
+ * would synchronise the device and stall the simulation's streams, or a host framework whose
+ * caching allocator already holds the GPU's memory.  mtg_create allocates, so those callers use
+ * this instead.
+ *
+ * It computes the same reference-order cell assignment and full neighbour list as
+ * mtg_get_neighbors (FunctorGenCellList.cpp:49-142, FunctorGenNeighList.cpp:72-151) for the
+ * positions d_r[3n] (FP64, device memory of the current device) in a box centred at the origin,
+ * with cells floor(float(L)/(cutoff + shell)) per axis (MDFFMatrices.cpp:56-58).  Outputs, in
+ * device memory the caller owns: d_count[n] (full neighbour count of each atom, also when it
+ * exceeds max_neigh) and d_list[n * max_neigh] (the first max_neigh neighbours of each atom; may
+ * be NULL when max_neigh is 0).
+ *
+ * Working memory is one file-scope device array of MTG_NOALLOC_SCRATCH_BYTES per device; the call
+ * needs 16 bytes per atom plus 12 bytes per cell (each part rounded up to 256 bytes) plus 256
+ * bytes, and returns MTG_E_INVALID without launching anything when that exceeds the array
+ * (about a million atoms in a million cells; larger systems use mtg_create).  It performs no
+ * device allocation and calls no allocating library function.
+ *
+ * `stream` is a cudaStream_t (NULL = the legacy default stream).  With needed == NULL the call
+ * only enqueues work and returns; with needed != NULL it waits for the stream and stores in
+ * *needed the largest neighbour count when some atom has more than max_neigh neighbours (its list
+ * in d_list is truncated; d_count still holds the full counts), or 0 when every list fits.
+ *
+ * Limits the caller must respect: the scratch array is shared by every call on a device, so calls
+ * whose work overlaps in time (other streams, other host threads, or a second call enqueued on
+ * another stream before the first finished) race on it and must be serialised by the caller;
+ * calls enqueued one after another on the same stream are safe.  The first call on each device
+ * looks up the array's address (cudaGetSymbolAddress, which may load the module), so make that
+ * first call before any stream capture begins on that device.  Errors are reported through
+ * mtg_last_error(NULL) of the calling thread. */
+#define MTG_NOALLOC_SCRATCH_BYTES (32u << 20)
+int mtg_neighbors_noalloc(const double* d_r, int32_t n, const double box[3], double cutoff, double shell,
+                          int32_t max_neigh, int32_t* d_count, int32_t* d_list, int32_t* needed, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,7 @@
 #include <map>
 #include <tuple>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1188,3 +1189,145 @@ int mtg_get_run_stats(mtg_ctx* c, mtg_run_stats* st) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// No-allocation neighbour list: the reference-order cell list and neighbour list kernels run on
+// caller-owned positions and outputs, with their working arrays carved out of one file-scope
+// device array instead of cudaMalloc'ed buffers.
+// ---------------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MTG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Address of g_noalloc_scratch on `dev` (the current device), looked up once per device.
+cudaError_t noalloc_scratch(int dev, void** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if(!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if(e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+
+// True when p is device (or managed) memory usable by device `dev`.
+bool on_device(const void* p, int dev) {
+    cudaPointerAttributes a{};
+    if(cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    if(a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
+}  // namespace
+
+extern "C" int mtg_neighbors_noalloc(const double* d_r, int32_t n, const double box[3], double cutoff, double shell,
+                                     int32_t max_neigh, int32_t* d_count, int32_t* d_list, int32_t* needed,
+                                     void* stream) {
+    g_create_error.clear();
+    if(!d_r || !box || !d_count || n <= 0 || max_neigh < 0 || (max_neigh > 0 && !d_list))
+        return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: null pointer or non-positive size");
+    if(n > (int32_t)kIdxMask) return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: too many atoms");
+    if(!(cutoff > 0.0) || !(shell >= 0.0) || !std::isfinite(cutoff) || !std::isfinite(shell))
+        return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: cutoff must be positive and shell non-negative");
+    int cells[3];
+    long long ncell = 1;
+    for(int a = 0; a < 3; a++) {
+        if(!(box[a] > 0.0) || !std::isfinite(box[a])) return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: box edges must be positive");
+        const double nc = std::floor(double((float)box[a] / ((float)cutoff + (float)shell)));
+        if(nc < 1.0) return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: box narrower than cutoff + shell");
+        if(nc > 1048576.0) return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: too many cells for the scratch array");
+        cells[a] = (int)nc;
+        ncell *= (long long)nc;
+    }
+    const size_t b_sc = round256(sizeof(StepScalars));
+    const size_t b_atom_cell = round256(sizeof(int) * 3 * (size_t)n);
+    const size_t b_cell = round256(sizeof(int) * (size_t)ncell);
+    const size_t b_list = round256(sizeof(int) * (size_t)n);
+    const size_t need_bytes = b_sc + b_atom_cell + 3 * b_cell + b_list;
+    if(ncell > (1LL << 30) || need_bytes > (size_t)MTG_NOALLOC_SCRATCH_BYTES) {
+        char msg[256];
+        std::snprintf(msg, sizeof msg,
+                      "mtg_neighbors_noalloc: %d atoms in %lld cells need %zu bytes of scratch, the array holds %u; "
+                      "use mtg_create/mtg_get_neighbors for this system",
+                      n, ncell, need_bytes, (unsigned)MTG_NOALLOC_SCRATCH_BYTES);
+        return fail(nullptr, MTG_E_INVALID, msg);
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if(e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        (void)cudaGetLastError();
+        return fail(nullptr, MTG_E_CUDA, "mtg_neighbors_noalloc: no current CUDA device");
+    }
+    if(!on_device(d_r, dev) || !on_device(d_count, dev) || (d_list && !on_device(d_list, dev)))
+        return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: d_r, d_count and d_list must be device memory of the current device");
+    void* base = nullptr;
+    e = noalloc_scratch(dev, &base);
+    if(e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(nullptr, MTG_E_CUDA, std::string("mtg_neighbors_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    }
+    unsigned char* p = static_cast<unsigned char*>(base);
+    DevSys d{};
+    d.n = n;
+    d.r = const_cast<double*>(d_r);
+    d.sc = reinterpret_cast<StepScalars*>(p);
+    p += b_sc;
+    d.atom_cell = reinterpret_cast<int*>(p);
+    p += b_atom_cell;
+    d.cell_first = reinterpret_cast<int*>(p);
+    p += b_cell;
+    d.cell_count = reinterpret_cast<int*>(p);
+    p += b_cell;
+    d.cell_cursor = reinterpret_cast<int*>(p);
+    p += b_cell;
+    d.cell_list = reinterpret_cast<int*>(p);
+    d.nbr_count = d_count;     // also the cell scatter's temporary, rewritten by the list kernel
+    d.nbr_list = d_list;
+    d.nbr_max = max_neigh;
+    Params P{};
+    P.n = n;
+    for(int a = 0; a < 3; a++) {
+        P.box[a] = box[a];
+        P.boxf[a] = (float)box[a];
+    }
+    P.nx = cells[0];
+    P.ny = cells[1];
+    P.nz = cells[2];
+    P.rc = (float)cutoff;
+    P.shell = (float)shell;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Only the list kernel's overflow flag and maximum start at zero; the cell counts are cleared
+    // by the cell-list launch itself, every other array is written before it is read.
+    e = cudaMemsetAsync(d.sc, 0, sizeof(StepScalars), s);
+    if(e == cudaSuccess) {
+        launch_ref_cells(d, P, s);
+        launch_ref_neigh(d, P, s);
+        e = cudaGetLastError();
+    }
+    if(e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(nullptr, MTG_E_CUDA, std::string("mtg_neighbors_noalloc: ") + cudaGetErrorString(e));
+    }
+    if(needed) {
+        int32_t mx[2] = {0, 0};   // StepScalars::overflow, StepScalars::needed
+        e = cudaMemcpyAsync(mx, &d.sc->overflow, sizeof mx, cudaMemcpyDeviceToHost, s);
+        if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if(e != cudaSuccess) {
+            (void)cudaGetLastError();
+            return fail(nullptr, MTG_E_CUDA, std::string("mtg_neighbors_noalloc: ") + cudaGetErrorString(e));
+        }
+        *needed = mx[0] ? mx[1] : 0;
+    }
+    return MTG_OK;
+}

@@ -27,6 +27,7 @@ PREC = {"reference": 0, "fp64": 1, "mixed": 2}
 COULOMB = {"allpairs": 0, "cutoff": 1, "shifted": 2}
 
 MTG_OK = 0
+MTG_E_INVALID = -1
 ERRORS = {-1: "invalid", -2: "cuda", -3: "nomem", -4: "overflow", -5: "timeout", -6: "unsupported", -7: "nonfinite"}
 
 
@@ -114,6 +115,7 @@ def load_library(path: str = LIB_PATH):
         "mtg_get_neighbors": ([P, C.c_int32, P, P, P], C.c_int),
         "mtg_get_run_stats": ([P, C.POINTER(RunStats)], C.c_int),
         "mtg_profile_phases": ([P, C.c_int, P], C.c_int),
+        "mtg_neighbors_noalloc": ([P, C.c_int32, P, C.c_double, C.c_double, C.c_int32, P, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -357,6 +359,24 @@ class Engine:
         lst = np.zeros((self.n, m), np.int32)
         self._check(self.lib.mtg_get_neighbors(self.h, m, _ptr(count), _ptr(lst), _ptr(need)))
         return count, lst
+
+
+def neighbors_noalloc(r_ptr: int, n: int, box, cutoff: float, shell: float, max_neigh: int,
+                      count_ptr: int, list_ptr: int, stream: int = 0, wait: bool = True):
+    """Reference-order neighbour list of device-resident positions through
+    mtg_neighbors_noalloc (no context, no device allocation).  Pointers are device addresses of
+    the current device (e.g. a CUDA tensor's data_ptr()); `stream` a cudaStream_t handle.
+    Returns the largest count when some list was truncated to max_neigh, 0 when all fit, or
+    None when wait is False (the call then only enqueues work)."""
+    lib = load_library()
+    b = (C.c_double * 3)(*[float(x) for x in box])
+    need = C.c_int32(0)
+    rc = lib.mtg_neighbors_noalloc(C.c_void_p(r_ptr), int(n), b, float(cutoff), float(shell), int(max_neigh),
+                                   C.c_void_p(count_ptr), C.c_void_p(list_ptr) if list_ptr else None,
+                                   C.byref(need) if wait else None, C.c_void_p(stream) if stream else None)
+    if rc != MTG_OK:
+        raise MTGError(rc, lib.mtg_last_error(None).decode())
+    return int(need.value) if wait else None
 
 
 def device_name(device: int = 0) -> str:
