@@ -189,6 +189,10 @@ class MDSystem:
     p: Optional[np.ndarray] = None        # (N,3) momenta [g/mol * A / (100 fs)]
     nhT_eta: Optional[np.ndarray] = None
     nhT_peta: Optional[np.ndarray] = None
+    # NPT: barostat momentum p_eps (CVelVerlet::p_eps_) and the barostat's chain (NH_P_)
+    p_eps: Optional[float] = None
+    nhP_eta: Optional[np.ndarray] = None
+    nhP_peta: Optional[np.ndarray] = None
 
     @property
     def n(self) -> int:
@@ -218,7 +222,9 @@ class MDSystem:
             mol=None if self.mol is None else self.mol.copy(),
             p=None if self.p is None else self.p.copy(),
             nhT_eta=None if self.nhT_eta is None else self.nhT_eta.copy(),
-            nhT_peta=None if self.nhT_peta is None else self.nhT_peta.copy())
+            nhT_peta=None if self.nhT_peta is None else self.nhT_peta.copy(),
+            nhP_eta=None if self.nhP_eta is None else self.nhP_eta.copy(),
+            nhP_peta=None if self.nhP_peta is None else self.nhP_peta.copy())
 
     def nonbonded_pair_terms(self, max_per_pair: int = 5) -> Tuple[np.ndarray, List[List[NonBondedTerm]]]:
         """Per (row, col) type pair, the MDFF non-bonded entries that apply, in list order.

@@ -56,6 +56,28 @@ def nh_initial(M: int, N: int, T: float, tau_fs: float, rng: np.random.Generator
     return eta, peta
 
 
+def npt_initial(M: int, T: float, tauP_fs: float, rng: np.random.Generator):
+    """Seeded barostat state: p_eps ~ N(0, W kT) with W = kT tauP^2 (SimulationBox.cpp:73), and the
+    barostat chain as nh_initial with Q_0 = kT tauP^2 (prepareArrays(1, 1), SimulationBox.cpp:88)."""
+    kT = T / CONV_T
+    tau = tauP_fs / 100.0
+    W = kT * tau * tau
+    p_eps = float(rng.standard_normal() * np.sqrt(W * kT))
+    Q = np.array([kT * tau * tau] * M)
+    eta = rng.random(M)
+    peta = rng.standard_normal(M) * np.sqrt(Q * kT)
+    return p_eps, eta, peta
+
+
+def make_npt(sys_: "MDSystem", cfg: "MDConfig", pressure_atm: float, seed: int):
+    """Switches a seeded system to NPT at `pressure_atm` with a seeded barostat state."""
+    cfg.ensemble = "NPT"
+    cfg.pressure = pressure_atm
+    rng = np.random.default_rng(seed)
+    sys_.p_eps, sys_.nhP_eta, sys_.nhP_peta = npt_initial(cfg.pressurenhlen, cfg.temperature, cfg.pressurerelax, rng)
+    return sys_, cfg
+
+
 # ------------------------------------------------------------------------------------------------
 # Config 1: LJ argon, FCC lattice, reduced density 0.8
 # ------------------------------------------------------------------------------------------------

@@ -840,13 +840,17 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
 /* Reference-mode MD loop: MDLoop.cpp:128-133 with NVT (NH chain) or NVE, force clipping       */
 /* ------------------------------------------------------------------------------------------ */
 typedef struct orc_run {
-    int ensemble;             /* 0 NVT, 2 NVE */
+    int ensemble;             /* 0 NVT, 1 NPT, 2 NVE */
     double dt;                /* reduced (fs / 100) */
     double kT;                /* NH_T_.T_ = T / Conv_T */
     double tau;               /* reduced */
     int M, nresp;             /* chain length, RESPA steps */
     double fcut;              /* cutoffforce; <= 0 disables clipping */
     int nx, ny, nz;           /* cell counts */
+    /* NPT (SimulationBox.cpp:58-76): barostat chain NH_P_ and CVelVerlet W_, P_ */
+    int MP, nrespP;           /* pressurenhlen, pressurerespa */
+    double tauP;              /* reduced */
+    double Pext;              /* pressure / Conv_press */
 } orc_run;
 
 static double cmt_exp(double x) { return (x > 1.0) ? 2.71828 * x : exp(x); }   /* Math.cpp:29-38 */
@@ -896,6 +900,90 @@ static void nh_propagate(const orc_sys* s, const orc_run* c, double* p, double* 
 #undef GJ
 }
 
+/* CMt::sinhXoverX (Math.cpp:40-54): the first six terms of the Taylor series of sinh(x)/x. */
+static double sinhx_over_x(double x) {
+    const double a[6] = {1.0, 1.0 / 6.0, 1.0 / 120.0, 1.0 / 5040.0, 1.0 / 362880.0, 1.0 / 39916800.0};
+    double sum = 0.0, xn = 1.0;
+    for(int k = 0; k < 6; k++) {
+        sum += a[k] * xn;
+        xn *= (x * x);
+    }
+    return sum;
+}
+
+/* CNHChain::propagator with CFctP (NHChain.cpp:54-113, MDLoop.cpp:62-83): the barostat's chain,
+ * G_0 = p_eps^2/W - kT, scaling p_eps. */
+static void nhp_propagate(const orc_run* c, double* p_eps, double W, double* eta, double* peta, const double* Q) {
+    const double w0 = 1.0 / (1.0 - pow(2.0, 1.0 / 3.0));
+    const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
+    const double beta = 1.0 / c->kT;
+    const int M = c->MP;
+    if(M > 0 && peta[0] > 15.0) peta[0] = 10.0;
+#define GP(j) ((j) == 0 ? (*p_eps) * (*p_eps) / W - (1.0 / beta) : (peta[(j) - 1] * peta[(j) - 1] / Q[(j) - 1]) - (1.0 / beta))
+    for(int mu = 0; mu < 3; mu++) {
+        double Dt = w[mu] * c->dt / (double)c->nrespP;
+        for(int it = 0; it < c->nrespP; it++) {
+            peta[M - 1] += (Dt / 4.0) * GP(M - 1);
+            for(int j = 0; j < M - 1; j++) {
+                double co = cmt_exp(-(Dt / 8.0) * (peta[j + 1] / Q[j + 1]));
+                peta[j] *= co;
+                peta[j] += (Dt / 4.0) * GP(j);
+                co = cmt_exp(-(Dt / 8.0) * (peta[j + 1] / Q[j + 1]));
+                peta[j] *= co;
+            }
+            for(int j = 0; j < M; j++) eta[j] += (Dt / 2.0) * (peta[j] / Q[j]);
+            double co = cmt_exp(-((Dt / 2.0) * (peta[0] / Q[0])));
+            *p_eps *= co;
+            for(int j = M - 2; j >= 0; j--) {
+                double co2 = cmt_exp(-(Dt / 8.0) * (peta[j + 1] / Q[j + 1]));
+                peta[j] *= co2;
+                peta[j] += (Dt / 4.0) * GP(j);
+                co2 = cmt_exp(-(Dt / 8.0) * (peta[j + 1] / Q[j + 1]));
+                peta[j] *= co2;
+            }
+            peta[M - 1] += (Dt / 4.0) * GP(M - 1);
+        }
+    }
+#undef GP
+}
+
+/* CVelVerlet::G_eps (VelVerlet.cpp:160-174) */
+static double g_eps(const orc_sys* s, const double* p, const double* F, const double* r, double V, double Pext) {
+    double sum_p = 0.0, sum_f = 0.0;
+    for(int k = 0; k < s->n; k++) {
+        double p2 = p[3 * k] * p[3 * k] + p[3 * k + 1] * p[3 * k + 1] + p[3 * k + 2] * p[3 * k + 2];
+        sum_p += (p2 / s->m[k]);
+        sum_f += (F[3 * k] * r[3 * k] + F[3 * k + 1] * r[3 * k + 1] + F[3 * k + 2] * r[3 * k + 2]);
+    }
+    return (1.0 + 1.0 / (double)s->n) * sum_p + sum_f - 3.0 * Pext * V;
+}
+
+/* CVelVerlet::prop_p (VelVerlet.cpp:124-136) */
+static void prop_p(const orc_sys* s, double dt, double p_eps, double W, double* p, const double* F) {
+    double u_eps = p_eps / W;
+    double alpha = (1.0 + 1.0 / (double)s->n);
+    double parm = alpha * u_eps * dt / 4.0;
+    double coeff = cmt_exp(-parm);
+    double coeff2 = coeff * coeff;
+    double coeff3 = sinhx_over_x(parm);
+    double b = (dt / 2.0) * coeff * coeff3;
+    for(int k = 0; k < 3 * s->n; k++) p[k] = p[k] * coeff2 + F[k] * b;
+}
+
+/* CVelVerlet::prop_r (VelVerlet.cpp:138-150) */
+static void prop_r(const orc_sys* s, double dt, double p_eps, double W, double* r, const double* p) {
+    double u_eps = p_eps / W;
+    double parm = u_eps * dt / 2.0;
+    double coeff = cmt_exp(parm);
+    double coeff2 = coeff * coeff;
+    double coeff3 = sinhx_over_x(parm) * coeff;
+    double b = dt * coeff3;
+    for(int k = 0; k < s->n; k++) {
+        double im = 1.0 / s->m[k];
+        for(int a = 0; a < 3; a++) r[3 * k + a] = r[3 * k + a] * coeff2 + (p[3 * k + a] * im) * b;
+    }
+}
+
 typedef struct orc_lists {
     int* atom_cell; int* cell_ptr; int* cell_list; int* count; int* list; int maxn;
 } orc_lists;
@@ -916,10 +1004,11 @@ static int ref_forces(orc_sys* s, const orc_run* c, orc_lists* ls, double* F, fl
     return orc_forces_ref(s, ls->count, ls->list, ls->maxn, F, U);
 }
 
-/* Runs nsteps.  r, p (n*3), eta, peta (M) are updated in place.  Every `stride` steps (and at the
+/* Runs nsteps.  r, p (n*3), eta, peta (M) are updated in place, and for NPT also
+ * baro = [p_eps, eps, eta_P[MP], p_eta_P[MP]] (the box follows eps, VelVerlet.cpp:198-211).  Every `stride` steps (and at the
  * start) it records r, p, F into rec_* ([nrec][n][3]) and U, K, T, P, V into rec_scal ([nrec][5]).
  * Returns the number of records or a negative error. */
-int orc_run_ref(orc_sys* s, const orc_run* c, double* r, double* p, double* eta, double* peta,
+int orc_run_ref(orc_sys* s, const orc_run* c, double* r, double* p, double* eta, double* peta, double* baro,
                 int nsteps, int stride, double* rec_r, double* rec_p, double* rec_F, double* rec_scal) {
     const int n = s->n;
     double* F = (double*)calloc((size_t)3 * n, sizeof(double));
@@ -935,12 +1024,58 @@ int orc_run_ref(orc_sys* s, const orc_run* c, double* r, double* p, double* eta,
     s->r = r;
     Q[0] = (double)(3 * n) * c->kT * c->tau * c->tau;
     for(int j = 1; j < c->M; j++) Q[j] = c->kT * c->tau * c->tau;
-    const double V = s->box[0] * s->box[1] * s->box[2];
+    double V = s->box[0] * s->box[1] * s->box[2];
+    /* NPT state: baro = [p_eps, eps, eta_P[MP], p_eta_P[MP]] (VelVerlet.h:57-62, NH_P_) */
+    const int npt = (c->ensemble == 1);
+    const double Lmax[3] = {s->box[0], s->box[1], s->box[2]};
+    const double V0 = Lmax[0] * Lmax[1] * Lmax[2];
+    const double W = c->kT * c->tauP * c->tauP;
+    double QP[64];
+    if(npt) {
+        if(c->MP < 1 || c->MP > 64) return -2;
+        QP[0] = 1.0 * c->kT * c->tauP * c->tauP;    /* prepareArrays(1, 1): dim*N = 1 */
+        for(int j = 1; j < c->MP; j++) QP[j] = c->kT * c->tauP * c->tauP;
+    }
     int nrec = 0;
     int rc_ = ref_forces(s, c, &ls, F, U);
     if(rc_ < 0) return rc_;
     for(int t = -1; t < nsteps; t++) {
-        if(t >= 0) {
+        if(t >= 0 && npt) {
+            /* MDLoop.cpp:128-133 with VelVerlet.cpp:57-71 (no force clipping in this branch) */
+            double* p_eps = &baro[0];
+            double* eps = &baro[1];
+            double* etaP = baro + 2;
+            double* petaP = baro + 2 + c->MP;
+            nhp_propagate(c, p_eps, W, etaP, petaP, QP);
+            nh_propagate(s, c, p, eta, peta, Q);
+            V = V0 * exp(3.0 * (*eps));
+            *p_eps += ((c->dt / 2.0) * g_eps(s, p, F, r, V, c->Pext));     /* 3.1 */
+            prop_p(s, c->dt, *p_eps, W, p, F);                             /* 3.2 */
+            prop_r(s, c->dt, *p_eps, W, r, p);                             /* 3.3 */
+            *eps += (c->dt * (*p_eps) / W);                                /* 3.4 */
+            {
+                /* getSimBox (VelVerlet.cpp:198-211) */
+                double Vmax = Lmax[0] * Lmax[1] * Lmax[2];
+                double etaCube = (V0 * exp(3.0 * (*eps))) / Vmax;
+                etaCube = pow(etaCube, 1.0 / 3.0);
+                for(int a = 0; a < 3; a++) s->box[a] = etaCube * Lmax[a];
+            }
+            rc_ = ref_forces(s, c, &ls, F, U);
+            if(rc_ < 0) return rc_;
+            prop_p(s, c->dt, *p_eps, W, p, F);                             /* 3.5 */
+            V = V0 * exp(3.0 * (*eps));
+            *p_eps += ((c->dt / 2.0) * g_eps(s, p, F, r, V, c->Pext));     /* 3.6 */
+            nh_propagate(s, c, p, eta, peta, Q);
+            nhp_propagate(c, p_eps, W, etaP, petaP, QP);
+            for(int k = 0; k < n; k++) {
+                for(int a = 0; a < 3; a++) {
+                    double Lm = s->box[a], h = Lm / 2.0;
+                    double* x = &r[3 * k + a];
+                    if(*x >= h) *x -= (double)((int)((*x + h) / Lm)) * Lm;
+                    if(*x < -h) *x -= (double)((int)((*x + (-h)) / Lm)) * Lm;
+                }
+            }
+        } else if(t >= 0) {
             if(c->ensemble == 0) nh_propagate(s, c, p, eta, peta, Q);
             double dt_2 = c->dt / 2.0;
             for(int k = 0; k < n; k++) {
@@ -987,6 +1122,7 @@ int orc_run_ref(orc_sys* s, const orc_run* c, double* r, double* p, double* eta,
             nrec++;
         }
     }
+    if(npt) for(int a = 0; a < 3; a++) s->box[a] = Lmax[a];
     free(F); free(U); free(Q);
     free(ls.atom_cell); free(ls.cell_ptr); free(ls.cell_list); free(ls.count); free(ls.list);
     return nrec;

@@ -21,6 +21,7 @@ LIB = os.path.join(BUILD, "libmdoracle.so")
 NPTS = 1000
 MAXFF = 5
 CONV_T = 120.272
+CONV_PRESS = 16388.2461
 
 
 def build(force: bool = False) -> str:
@@ -54,7 +55,7 @@ def lib():
         _lib.orc_neigh_list.restype = C.c_int
         _lib.orc_forces_ref.argtypes = [P, P, P, C.c_int, P, P]
         _lib.orc_forces_fp64.argtypes = [P, C.c_double, P, P]
-        _lib.orc_run_ref.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P]
+        _lib.orc_run_ref.argtypes = [P, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P]
         _lib.orc_run_ref.restype = C.c_int
     return _lib
 
@@ -86,7 +87,8 @@ class OrcSys(C.Structure):
 class OrcRun(C.Structure):
     _fields_ = [("ensemble", C.c_int), ("dt", C.c_double), ("kT", C.c_double), ("tau", C.c_double),
                 ("M", C.c_int), ("nresp", C.c_int), ("fcut", C.c_double),
-                ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)]
+                ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("MP", C.c_int), ("nrespP", C.c_int), ("tauP", C.c_double), ("Pext", C.c_double)]
 
 
 def profile(kind_group: str, kind: int, params, x0: float, x1: float, npts: int = NPTS) -> np.ndarray:
@@ -240,8 +242,18 @@ class Oracle:
         M = cfg.temperaturenhlen
         eta = np.ascontiguousarray(s.nhT_eta if s.nhT_eta is not None else np.zeros(M), np.float64).copy()
         peta = np.ascontiguousarray(s.nhT_peta if s.nhT_peta is not None else np.zeros(M), np.float64).copy()
+        MP = cfg.pressurenhlen
+        baro = np.zeros(2 + 2 * MP)
+        baro[0] = s.p_eps if s.p_eps is not None else 0.0
+        if s.nhP_eta is not None:
+            baro[2:2 + MP] = s.nhP_eta
+        if s.nhP_peta is not None:
+            baro[2 + MP:] = s.nhP_peta
         rc = OrcRun()
-        rc.ensemble = {"NVT": 0, "NVE": 2}[cfg.ensemble]
+        rc.ensemble = {"NVT": 0, "NPT": 1, "NVE": 2}[cfg.ensemble]
+        rc.MP, rc.nrespP = MP, cfg.pressurerespa
+        rc.tauP = cfg.pressurerelax / 100.0
+        rc.Pext = cfg.pressure / CONV_PRESS
         rc.dt = cfg.timestep / 100.0
         rc.kT = cfg.temperature / CONV_T
         rc.tau = cfg.temperaturerelax / 100.0
@@ -250,8 +262,9 @@ class Oracle:
         rc.nx, rc.ny, rc.nz = self.cells
         nrec = 2 + nsteps // stride
         rr = np.zeros((nrec, n, 3)); rp = np.zeros((nrec, n, 3)); rF = np.zeros((nrec, n, 3)); rs = np.zeros((nrec, 5))
-        got = lib().orc_run_ref(C.byref(self.st), C.byref(rc), _p(r), _p(p), _p(eta), _p(peta),
+        got = lib().orc_run_ref(C.byref(self.st), C.byref(rc), _p(r), _p(p), _p(eta), _p(peta), _p(baro),
                                 nsteps, stride, _p(rr), _p(rp), _p(rF), _p(rs))
         if got < 0:
             raise RuntimeError("oracle run failed")
-        return {"r": rr[:got], "p": rp[:got], "F": rF[:got], "scal": rs[:got], "eta": eta, "peta": peta}
+        return {"r": rr[:got], "p": rp[:got], "F": rF[:got], "scal": rs[:got], "eta": eta, "peta": peta,
+                "p_eps": baro[0], "eps": baro[1], "etaP": baro[2:2 + MP], "petaP": baro[2 + MP:]}

@@ -319,7 +319,7 @@ int cmdRun(const SysIn& s, const std::string& out, int nsteps, int stride) {
     CFctP fctP(&sb.velVerlet_);
     C3DVector boxOut;
     const int N = sb.N_;
-    std::vector<double> R, Pm, Fo, scal, nh;
+    std::vector<double> R, Pm, Fo, scal, nh, nhp, baro;
     std::vector<float> Uo;
     std::vector<CMDFFMatrices::CForces> F = sb.calcParticleForces();
     auto record = [&](int t) {
@@ -338,6 +338,9 @@ int cmdRun(const SysIn& s, const std::string& out, int nsteps, int stride) {
         scal.push_back(sb.calcV());
         for(int j = 0; j < sb.NH_T_.M_; j++) nh.push_back(sb.NH_T_.eta_[j]);
         for(int j = 0; j < sb.NH_T_.M_; j++) nh.push_back(sb.NH_T_.p_eta_[j]);
+        for(int j = 0; j < sb.NH_P_.M_; j++) nhp.push_back(sb.NH_P_.eta_[j]);
+        for(int j = 0; j < sb.NH_P_.M_; j++) nhp.push_back(sb.NH_P_.p_eta_[j]);
+        baro.push_back(sb.velVerlet_.p_eps_);
     };
     record(-1);
     int nrec = 1;
@@ -357,6 +360,8 @@ int cmdRun(const SysIn& s, const std::string& out, int nsteps, int stride) {
     w.f("traj_U", Uo, {(uint64_t)nrec, (uint64_t)N});
     w.d("traj_scalars", scal, {(uint64_t)nrec, 6});
     w.d("traj_nhT", nh, {(uint64_t)nrec, 2, (uint64_t)sb.NH_T_.M_});
+    w.d("traj_nhP", nhp, {(uint64_t)nrec, 2, (uint64_t)sb.NH_P_.M_});
+    w.d("traj_peps", baro, {(uint64_t)nrec});
     fclose(devnull);
     return 0;
 }

@@ -46,6 +46,12 @@ def write_sysfile(path: str, s: MDSystem, cfg: MDConfig, with_state: bool = True
             lines.append("nhT_eta " + " ".join(_f(v) for v in s.nhT_eta))
         if s.nhT_peta is not None:
             lines.append("nhT_peta " + " ".join(_f(v) for v in s.nhT_peta))
+        if s.nhP_eta is not None:
+            lines.append("nhP_eta " + " ".join(_f(v) for v in s.nhP_eta))
+        if s.nhP_peta is not None:
+            lines.append("nhP_peta " + " ".join(_f(v) for v in s.nhP_peta))
+        if s.p_eps is not None:
+            lines.append(f"p_eps {_f(s.p_eps)}")
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + "\n")
 

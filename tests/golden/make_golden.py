@@ -2,7 +2,7 @@
 
 Run from the repository root after building the oracle harness (needs the reference sources):
 
-    make -C oracle/ref REF=/root/reference && python tests/golden/make_golden.py
+    make -C oracle/ref REF=/root/reference && python tests/golden/make_golden.py [case ...]
 
 Each case is a seeded synthetic system (moltwister_gb300/workloads.py).  The harness
 (oracle/ref/harness.cpp, linked from the unmodified reference sources) builds the
@@ -49,6 +49,19 @@ def cases():
     out["water648_nvt"] = (s, c, 100, 25)
     s, c = W.chains(n_chain=27, L=24.0, seed=15, immobile_every=7)
     out["chains108_nvt"] = (s, c, 100, 25)
+    # NPT (VelVerlet.cpp:57-71).  The reference's barostat is driven by sum F.r over wrapped
+    # positions (VelVerlet.cpp:160-174), not the pair virial, so the default 5 ps relaxation time
+    # collapses or explodes these boxes within ~100 steps; slow barostats keep 100 steps finite.
+    s, c = W.argon(ncell=5, seed=11, jitter=0.05)
+    c.neighshell = 1.0
+    c.pressurerelax = 100000.0
+    W.make_npt(s, c, 500.0, 21)
+    out["argon500_npt"] = (s, c, 100, 25)
+    s, c = W.water(n_mol=216, L=W.water_box_length(216), seed=14, rc=6.0)
+    c.neighshell = 0.2
+    c.pressurerelax = 20000.0
+    W.make_npt(s, c, 1.0, 22)
+    out["water648_npt"] = (s, c, 100, 25)
     return out
 
 
@@ -67,6 +80,9 @@ def pack(name, s, c, steps, stride):
     arrays = dict(
         in_box=s.box, in_ids=np.array(s.ids), in_r=s.r, in_q=s.q, in_m=s.m, in_mobile=s.mobile.astype(np.int8),
         in_p=s.p, in_nhT_eta=s.nhT_eta, in_nhT_peta=s.nhT_peta,
+        in_p_eps=np.array(np.nan if s.p_eps is None else s.p_eps),
+        in_nhP_eta=np.zeros(0) if s.nhP_eta is None else s.nhP_eta,
+        in_nhP_peta=np.zeros(0) if s.nhP_peta is None else s.nhP_peta,
         in_terms=np.array(json.dumps(terms)), in_cfg=np.array(json.dumps(cfg)),
         steps=np.array(steps), stride=np.array(stride),
         nb_table=st["nb_table"], nb_count=st["nb_count"], bond_table=st["bond_table"],
@@ -78,17 +94,20 @@ def pack(name, s, c, steps, stride):
         F=st["F"], U=st["U"],
         traj_r=tr["traj_r"], traj_p=tr["traj_p"], traj_F=tr["traj_F"], traj_U=tr["traj_U"],
         traj_scalars=tr["traj_scalars"], traj_nhT=tr["traj_nhT"],
+        traj_nhP=tr["traj_nhP"], traj_peps=tr["traj_peps"],
     )
     path = os.path.join(OUT, name + ".npz")
     np.savez_compressed(path, **arrays)
     return path
 
 
-def main():
+def main(only=()):
     for name, (s, c, steps, stride) in cases().items():
+        if only and name not in only:
+            continue
         p = pack(name, s, c, steps, stride)
         print(f"{name}: {os.path.getsize(p) / 1024:.0f} KiB")
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

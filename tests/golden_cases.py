@@ -39,4 +39,8 @@ def load(name: str) -> Tuple[MDSystem, MDConfig, Dict[str, np.ndarray]]:
     s.p = d["in_p"]
     s.nhT_eta = d["in_nhT_eta"]
     s.nhT_peta = d["in_nhT_peta"]
+    if "in_p_eps" in d and np.isfinite(d["in_p_eps"]):
+        s.p_eps = float(d["in_p_eps"])
+        s.nhP_eta = d["in_nhP_eta"]
+        s.nhP_peta = d["in_nhP_peta"]
     return s, cfg, d

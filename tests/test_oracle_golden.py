@@ -56,9 +56,22 @@ def test_trajectory_bit_exact(name):
     assert np.array_equal(o["F"], d["traj_F"])
     assert np.array_equal(o["scal"], d["traj_scalars"][:, 1:6])
     M = cfg.temperaturenhlen
-    if cfg.ensemble == "NVT":
+    if cfg.ensemble in ("NVT", "NPT"):
         assert np.array_equal(o["eta"], d["traj_nhT"][-1, 0, :M])
         assert np.array_equal(o["peta"], d["traj_nhT"][-1, 1, :M])
+    if cfg.ensemble == "NPT":
+        MP = cfg.pressurenhlen
+        assert o["p_eps"] == d["traj_peps"][-1]
+        assert np.array_equal(o["etaP"], d["traj_nhP"][-1, 0, :MP])
+        assert np.array_equal(o["petaP"], d["traj_nhP"][-1, 1, :MP])
+
+
+def test_npt_volume_changes():
+    """The NPT golden cases really move the box (VelVerlet.cpp:57-71, getSimBox :198-211)."""
+    for name in ("argon500_npt", "water648_npt"):
+        s, cfg, d = G.load(name)
+        V = d["traj_scalars"][:, 5]
+        assert np.all(np.isfinite(V)) and abs(V[-1] - V[0]) > 1e-3 * V[0], (name, V)
 
 
 def test_two_cells_duplicate_neighbours():
