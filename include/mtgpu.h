@@ -161,7 +161,10 @@ typedef struct mtg_config_desc {
     int32_t device;             /* CUDA device ordinal */
 } mtg_config_desc;
 
-/* Thermostat/barostat state (CNHChain eta_/p_eta_, NHChain.h:55-61; CVelVerlet p_eps_, VelVerlet.h:57-62). */
+/* Thermostat/barostat state (CNHChain eta_/p_eta_, NHChain.h:55-61; CVelVerlet p_eps_, eps_,
+ * VelVerlet.h:57-62).  Under NPT, mtg_set_state also sets the barostat momentum p_eps, the strain
+ * eps (the box becomes (e^{3 eps})^{1/3} times the initial box) and the barostat chain NH_P_
+ * (etaP/p_etaP, MP entries); box is output only (the current box). */
 typedef struct mtg_thermo_state {
     int32_t M;
     int32_t reserved;
@@ -169,6 +172,11 @@ typedef struct mtg_thermo_state {
     double p_eta[MTG_MAX_NH_CHAIN];
     double p_eps;
     double eps;
+    int32_t MP;
+    int32_t reserved2;
+    double etaP[MTG_MAX_NH_CHAIN];
+    double p_etaP[MTG_MAX_NH_CHAIN];
+    double box[3];
 } mtg_thermo_state;
 
 /* Scalars of one output step (the info-line columns of MDLoop.cpp:388-403, in reduced units as

@@ -473,9 +473,38 @@ int fetch_rp(mtg_ctx* c, double c2) {
     return MTG_OK;
 }
 
-// Applies the pending c2 to the device momenta and rewinds the thermostat to the state after the
-// last completed step (end of a run).
+// Barostat state with momentum p_eps and strain eps: box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax
+// (VelVerlet.cpp:192-211); the saved copy equals the live one (no step pending).
+BaroDev baro_at(const Params& P, double p_eps, double eps) {
+    BaroDev b{};
+    b.p_eps = b.p_eps_saved = p_eps;
+    b.eps = b.eps_saved = eps;
+    const double Vmax = P.box[0] * P.box[1] * P.box[2];
+    double ec = (P.V0 * std::exp(3.0 * eps)) / Vmax;
+    ec = std::pow(ec, 1.0 / 3.0);
+    for(int a = 0; a < 3; a++) {
+        b.L[a] = b.L_saved[a] = (eps == 0.0) ? P.box[a] : ec * P.box[a];
+        b.Lf[a] = (float)b.L[a];
+    }
+    b.ap = b.ar = 1.0;
+    return b;
+}
+
+// Applies the pending c2 to the device momenta and rewinds the thermostat (and, under NPT, the
+// barostat) to the state after the last completed step (end of a run).
 int settle_state(mtg_ctx* c) {
+    if(c->P.ensemble == MTG_NPT) {
+        BaroDev b{};
+        CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+        b.p_eps = b.p_eps_saved;
+        b.eps = b.eps_saved;
+        for(int a = 0; a < 3; a++) {
+            b.L[a] = b.L_saved[a];
+            b.Lf[a] = (float)b.L[a];
+        }
+        CUDA_TRY(c, cudaMemcpy(c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(c->d.thp, c->d.thp_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
+    }
     StepScalars s = read_scalars(c);
     if(s.c2 != 1.0 || s.S != 1.0) {
         std::vector<double> p((size_t)c->P.n * 3);
@@ -545,8 +574,12 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     if(cfg->coulomb < MTG_COULOMB_ALLPAIRS || cfg->coulomb > MTG_COULOMB_SHIFTED) return fail(nullptr, MTG_E_INVALID, "bad coulomb mode");
     if(cfg->precision == MTG_PREC_REFERENCE && cfg->coulomb != MTG_COULOMB_ALLPAIRS)
         return fail(nullptr, MTG_E_INVALID, "the reference precision mode has all-pairs Coulomb only");
-    if(cfg->ensemble == MTG_NPT) return fail(nullptr, MTG_E_UNSUPPORTED, "NPT (MTK barostat) is not implemented in this build");
-    if(cfg->ensemble != MTG_NVT && cfg->ensemble != MTG_NVE) return fail(nullptr, MTG_E_INVALID, "bad ensemble");
+    if(cfg->ensemble == MTG_NPT && cfg->precision != MTG_PREC_REFERENCE)
+        return fail(nullptr, MTG_E_UNSUPPORTED, "NPT (MTK barostat) is available in the reference precision mode");
+    if(cfg->ensemble == MTG_NPT && (cfg->pressure_nh_len < 1 || cfg->pressure_nh_len > MTG_MAX_NH_CHAIN ||
+                                    cfg->pressure_respa < 1 || !(cfg->pressure_relax > 0.0)))
+        return fail(nullptr, MTG_E_INVALID, "NPT needs 1 <= pressure_nh_len <= MTG_MAX_NH_CHAIN, pressure_respa >= 1, pressure_relax > 0");
+    if(cfg->ensemble != MTG_NVT && cfg->ensemble != MTG_NVE && cfg->ensemble != MTG_NPT) return fail(nullptr, MTG_E_INVALID, "bad ensemble");
     if(cfg->temperature_nh_len < 0 || cfg->temperature_nh_len > kMaxChain) return fail(nullptr, MTG_E_INVALID, "chain length out of range");
     if(cfg->ensemble == MTG_NVT && (cfg->temperature_nh_len < 1 || cfg->temperature_respa < 1 || !(cfg->temperature > 0.0) || !(cfg->temperature_relax > 0.0)))
         return fail(nullptr, MTG_E_INVALID, "NVT needs temperature > 0, relaxation > 0, chain length >= 1, RESPA >= 1");
@@ -598,6 +631,16 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     P.M = cfg->ensemble == MTG_NVE ? 0 : cfg->temperature_nh_len;
     P.nresp = cfg->temperature_respa;
     P.fcut = cfg->cutoff_force;
+    if(P.ensemble == MTG_NPT) {
+        // SimulationBox.cpp:58-76: NH_P_ shares T; W = kT tauP^2, P_ = pressure / Conv_press, V0 = Lx Ly Lz
+        const double tauP = cfg->pressure_relax / kConvt;
+        P.MP = cfg->pressure_nh_len;
+        P.nrespP = cfg->pressure_respa;
+        P.Pext = cfg->pressure / kConvPress;
+        P.W = P.kT * tauP * tauP;
+        P.V0 = sys->box[0] * sys->box[1] * sys->box[2];
+        P.clip = 0;   // the NPT branch does not clip forces (VelVerlet.cpp:57-71)
+    }
     P.rc = (float)cfg->cutoff_radius;
     P.shell = (float)cfg->neigh_shell;
     P.rcoul = (float)(cfg->coulomb_cutoff > 0.0 ? cfg->coulomb_cutoff : cfg->cutoff_radius);
@@ -789,6 +832,9 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         rc = rc || dalloc(C, &d.th, 1);
         rc = rc || dalloc(C, &d.th_saved, 1);
         rc = rc || dalloc(C, &d.rec, 8);
+        rc = rc || dalloc(C, &d.baro, 1);
+        rc = rc || dalloc(C, &d.thp, 1);
+        rc = rc || dalloc(C, &d.thp_saved, 1);
     }
     if(rc) return fail(nullptr, rc, c->err);
     // thermostat masses (NHChain.cpp:115-124): Q0 = dim N kT tau^2, Qj = kT tau^2
@@ -806,6 +852,16 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         s.S = 1.0;
         s.c2 = 1.0;
         cudaMemcpy(d.sc, &s, sizeof(s), cudaMemcpyHostToDevice);
+        // barostat chain: prepareArrays(1, 1) gives Q0 = kT tauP^2 as well (NHChain.cpp:115-124)
+        ThermoDev tp{};
+        for(int j = 0; j < kMaxChain; j++) tp.Q[j] = 1.0;
+        if(P.ensemble == MTG_NPT)
+            for(int j = 0; j < P.MP; j++) tp.Q[j] = P.W;
+        for(int j = 0; j < kMaxChain; j++) tp.iQ[j] = 1.0 / tp.Q[j];
+        cudaMemcpy(d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice);
+        cudaMemcpy(d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice);
+        BaroDev b = baro_at(P, 0.0, 0.0);
+        cudaMemcpy(d.baro, &b, sizeof(b), cudaMemcpyHostToDevice);
     }
     // list capacities: start from a density estimate, grown on demand
     {
@@ -831,6 +887,11 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         rc = rc || add_snap(C, d.th, sizeof(ThermoDev));
         rc = rc || add_snap(C, d.th_saved, sizeof(ThermoDev));
         rc = rc || add_snap(C, d.sc, sizeof(StepScalars));
+        if(P.ensemble == MTG_NPT) {
+            rc = rc || add_snap(C, d.baro, sizeof(BaroDev));
+            rc = rc || add_snap(C, d.thp, sizeof(ThermoDev));
+            rc = rc || add_snap(C, d.thp_saved, sizeof(ThermoDev));
+        }
         if(is_mixed(C)) {
             rc = rc || add_snap(C, d.hi, sizeof(float4) * n);
             rc = rc || add_snap(C, d.lo, sizeof(float4) * n);
@@ -877,6 +938,21 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
         }
         CUDA_TRY(c, cudaMemcpy(c->d.th, &t, sizeof(t), cudaMemcpyHostToDevice));
         CUDA_TRY(c, cudaMemcpy(c->d.th_saved, &t, sizeof(t), cudaMemcpyHostToDevice));
+        if(c->P.ensemble == MTG_NPT) {
+            if(!std::isfinite(th->p_eps) || !std::isfinite(th->eps)) return fail(c, MTG_E_NONFINITE, "non-finite barostat state");
+            ThermoDev tp{};
+            CUDA_TRY(c, cudaMemcpy(&tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
+            const int MP = std::min<int>(th->MP, kMaxChain);
+            for(int j = 0; j < MP; j++) {
+                tp.eta[j] = th->etaP[j];
+                tp.peta[j] = th->p_etaP[j];
+            }
+            CUDA_TRY(c, cudaMemcpy(c->d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, cudaMemcpy(c->d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice));
+            BaroDev b = baro_at(c->P, th->p_eps, th->eps);
+            CUDA_TRY(c, cudaMemcpy(c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
+            if(!r) return compute_forces_now(c, true);   // the box may have changed
+        }
     }
     if(r) return compute_forces_now(c, true);
     return MTG_OK;
@@ -902,6 +978,21 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
         for(int j = 0; j < c->P.M; j++) {
             th->eta[j] = t.eta[j];
             th->p_eta[j] = t.peta[j];
+        }
+        for(int a = 0; a < 3; a++) th->box[a] = c->P.box[a];
+        if(c->P.ensemble == MTG_NPT) {
+            ThermoDev tp{};
+            BaroDev b{};
+            CUDA_TRY(c, cudaMemcpy(&tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
+            CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+            th->MP = c->P.MP;
+            for(int j = 0; j < c->P.MP; j++) {
+                th->etaP[j] = tp.eta[j];
+                th->p_etaP[j] = tp.peta[j];
+            }
+            th->p_eps = b.p_eps;
+            th->eps = b.eps;
+            for(int a = 0; a < 3; a++) th->box[a] = b.L[a];
         }
     }
     return MTG_OK;

@@ -396,17 +396,21 @@ __device__ inline int nh_chain_half_3w(NhExchange& X, double g, double kT, doubl
 
 __device__ __forceinline__ void bar96() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
 
-// Thermostat half-steps for the end of a step (second half of this step, then first half of the
+// Chain half-steps for the end of a step (second half of this step, then first half of the
 // next: MDLoop.cpp:129-132) or for the prologue of a run (first half only), run by warps 0..2 of
 // one block (threadIdx.x < 96).  th_saved receives the chain after the second half-step (the
-// state the reference holds between steps).  Returns (via *c2, *c1) the momentum scales.
-__device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
-                                  double& KE2, bool second_half, double* c2_out, double* c1_out) {
+// state the reference holds between steps).  Returns (via *c2, *c1) the scales of the driven
+// momentum, KE2 after the second half-step and, in *KE_full, after both.  The particle chain has
+// g = 3N (CFctT, MDLoop.cpp:29-60); the barostat's chain g = 1 with KE2 = p_eps^2/W (CFctP,
+// MDLoop.cpp:62-83).
+__device__ inline void thermostat_chain(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
+                                        double& KE2, bool second_half, double* c2_out, double* c1_out,
+                                        double g, int M, int nresp, double* KE_full) {
     __shared__ NhExchange X;
     const int tid = threadIdx.x;
-    const double g = double(3 * P.n);
     double c2 = 1.0, c1 = 1.0;
-    if(P.M >= 2) {
+    double KEf = KE2;
+    if(M >= 2) {
         if(tid < kMaxChain) {
             X.pe[tid] = th->peta[tid];
             X.eta[tid] = th->eta[tid];
@@ -421,10 +425,10 @@ __device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* t
         bar96();
         int seq = 0;
         if(second_half) {
-            seq = nh_chain_half_3w(X, g, P.kT, P.dt, P.M, P.nresp, seq);
+            seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq);
             bar96();
             c2 = X.scale;
-            if(tid < P.M) {
+            if(tid < M) {
                 th_saved->peta[tid] = X.pe[tid];
                 th_saved->eta[tid] = X.eta[tid];
             }
@@ -432,25 +436,27 @@ __device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* t
             if(tid == 0) X.scale = 1.0;
             bar96();
         } else {
-            if(tid < P.M) {
+            if(tid < M) {
                 th_saved->peta[tid] = X.pe[tid];
                 th_saved->eta[tid] = X.eta[tid];
             }
         }
         const double KE_after2 = X.KE2;
         bar96();
-        seq = nh_chain_half_3w(X, g, P.kT, P.dt, P.M, P.nresp, seq);
+        seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq);
         bar96();
         c1 = X.scale;
+        KEf = X.KE2;
         KE2 = KE_after2;
-        if(tid < P.M) {
+        if(tid < M) {
             th->peta[tid] = X.pe[tid];
             th->eta[tid] = X.eta[tid];
         }
         if(tid == 0 && X.timeout) sc->timeout = 1;
-    } else if(P.M == 1 && tid < 32) {
+        bar96();   // X is reused by the next chain of this block
+    } else if(M == 1 && tid < 32) {
         if(second_half) {
-            c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, P.M, P.nresp);
+            c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, M, nresp);
             __threadfence_block();
             if(tid == 0) {
                 th_saved->eta[0] = th->eta[0];
@@ -462,10 +468,17 @@ __device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* t
         }
         __syncwarp();
         double KEn = KE2;
-        c1 = nh_chain_half(*th, KEn, g, P.kT, P.dt, P.M, P.nresp);
+        c1 = nh_chain_half(*th, KEn, g, P.kT, P.dt, M, nresp);
+        KEf = KEn;
     }
     *c2_out = c2;
     *c1_out = c1;
+    if(KE_full) *KE_full = KEf;
+}
+
+__device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
+                                  double& KE2, bool second_half, double* c2_out, double* c1_out) {
+    thermostat_chain(P, sc, th, th_saved, KE2, second_half, c2_out, c1_out, double(3 * P.n), P.M, P.nresp, nullptr);
 }
 
 // End-of-step scalar work of the last block, run by its warps 0..2 (threadIdx.x < 96): the
@@ -488,6 +501,89 @@ __device__ inline void end_of_step(const Params& P, StepScalars* sc, ThermoDev* 
             rec[4] = V;
             sc->U = U;
             sc->virial = vir;
+        }
+    }
+}
+
+// CMt::sinhXoverX (Math.cpp:40-54): the first six terms of the Taylor series of sinh(x)/x.
+__device__ inline double sinhx_over_x(double x) {
+    const double a[6] = {1.0, 1.0 / 6.0, 1.0 / 120.0, 1.0 / 5040.0, 1.0 / 362880.0, 1.0 / 39916800.0};
+    double sum = 0.0, xn = 1.0;
+#pragma unroll
+    for(int k = 0; k < 6; k++) {
+        sum += a[k] * xn;
+        xn *= (x * x);
+    }
+    return sum;
+}
+
+// NPT scalar work (MDLoop.cpp:128-133 with VelVerlet.cpp:57-71), run by warps 0..2 of the last
+// block of a step (second_half) or of a run's prologue.  In order:
+//   3.6  p_eps += dt/2 G_eps(p after 3.5, F, unwrapped r)           (end of a step only)
+//   NH_T second half + next first half; NH_P second half + next first half (the chains act on
+//        disjoint variables, so running NH_T's pair before NH_P's equals the reference order)
+//   output record of the completed step (V = V0 exp(3 eps))
+//   3.1  p_eps += dt/2 G_eps(p after NH_T, F, wrapped r) of the next step
+//   prop_p / prop_r coefficients, 3.4 eps += dt p_eps / W, and the next box getSimBox().
+// G_eps = (1 + 1/N) sum p^2/m + sum F.r - 3 P V (VelVerlet.cpp:160-174).
+__device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2, double vir_unw, double vir_wr,
+                                   double U, bool second_half, bool output) {
+    __shared__ double sh_kep;
+    const int tid = threadIdx.x;
+    BaroDev* b = d.baro;
+    const double dt = P.dt;
+    const double alpha = (1.0 + 1.0 / double(P.n));
+    if(second_half && tid == 0) {
+        const double V = P.V0 * exp(3.0 * b->eps);
+        b->p_eps += ((dt / 2.0) * (alpha * KE2 + vir_unw - 3.0 * P.Pext * V));
+    }
+    bar96();
+    double c2 = 1.0, c1 = 1.0, KEf = KE2;
+    thermostat_chain(P, d.sc, d.th, d.th_saved, KE2, second_half, &c2, &c1, double(3 * P.n), P.M, P.nresp, &KEf);
+    bar96();
+    if(tid == 0) sh_kep = b->p_eps * b->p_eps / P.W;
+    bar96();
+    double KEp = sh_kep, c2p = 1.0, c1p = 1.0;
+    thermostat_chain(P, d.sc, d.thp, d.thp_saved, KEp, second_half, &c2p, &c1p, 1.0, P.MP, P.nrespP, nullptr);
+    bar96();
+    if(tid == 0) {
+        StepScalars* sc = d.sc;
+        double pe = b->p_eps * c2p;            // after NH_P's second half: the completed step
+        b->p_eps_saved = pe;
+        b->eps_saved = b->eps;
+        for(int a = 0; a < 3; a++) b->L_saved[a] = b->L[a];
+        sc->c2 = c2;
+        sc->S = c2 * c1;
+        sc->KE2 = KE2;
+        double V = P.V0 * exp(3.0 * b->eps);
+        if(output) {
+            d.rec[0] = U;
+            d.rec[1] = 0.5 * KE2;
+            d.rec[2] = KE2 / (3.0 * double(P.n));
+            d.rec[3] = (1.0 / (3.0 * V)) * (KE2 + vir_wr);
+            d.rec[4] = V;
+            sc->U = U;
+            sc->virial = vir_wr;
+        }
+        pe *= c1p;
+        pe += ((dt / 2.0) * (alpha * KEf + vir_wr - 3.0 * P.Pext * V));   // 3.1
+        b->p_eps = pe;
+        const double u = pe / P.W;
+        double parm = alpha * u * dt / 4.0;
+        double co = cmt_exp(-parm);
+        b->ap = co * co;
+        b->bp = (dt / 2.0) * co * sinhx_over_x(parm);
+        parm = u * dt / 2.0;
+        co = cmt_exp(parm);
+        b->ar = co * co;
+        b->br = dt * (sinhx_over_x(parm) * co);
+        b->eps += (dt * pe / P.W);                                          // 3.4
+        const double Vmax = P.box[0] * P.box[1] * P.box[2];
+        double ec = (P.V0 * exp(3.0 * b->eps)) / Vmax;
+        ec = pow(ec, 1.0 / 3.0);
+        for(int a = 0; a < 3; a++) {
+            b->L[a] = ec * P.box[a];
+            b->Lf[a] = (float)b->L[a];
         }
     }
 }

@@ -39,24 +39,38 @@ constexpr int kWarp = 32;
 // Prologue: sum p^2/m, then the first thermostat half-step of the coming step.
 // ---------------------------------------------------------------------------------------------
 __global__ void k_prologue(DevSys d, Params P) {
-    __shared__ double smem[32];
+    __shared__ double smem[32 * 2];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[1] = {0.0};
+    double v[2] = {0.0, 0.0};   // sum p^2/m, sum F.r (NPT: G_eps of the first step, VelVerlet.cpp:60)
     if(k < P.n) {
         const double px = d.p[3 * k], py = d.p[3 * k + 1], pz = d.p[3 * k + 2];
         v[0] = (px * px + py * py + pz * pz) / d.m[k];
+        if(P.ensemble == MTG_NPT)
+            v[1] = d.F[3 * k] * d.r[3 * k] + d.F[3 * k + 1] * d.r[3 * k + 1] + d.F[3 * k + 2] * d.r[3 * k + 2];
     }
-    block_sum<1>(v, smem);
-    if(threadIdx.x == 0) d.partial[blockIdx.x * 4] = v[0];
+    block_sum<2>(v, smem);
+    if(threadIdx.x == 0) {
+        d.partial[blockIdx.x * 4] = v[0];
+        d.partial[blockIdx.x * 4 + 1] = v[1];
+    }
     if(last_block(&d.sc->done_blocks)) {
-        __shared__ double tot;
+        __shared__ double tot, tot_fr;
         if(threadIdx.x == 0) {
-            double KE2 = 0.0;
-            for(int b = 0; b < (int)gridDim.x; b++) KE2 += d.partial[b * 4];
+            double KE2 = 0.0, fr = 0.0;
+            for(int b = 0; b < (int)gridDim.x; b++) {
+                KE2 += d.partial[b * 4];
+                fr += d.partial[b * 4 + 1];
+            }
             tot = KE2;
+            tot_fr = fr;
             d.sc->done_blocks = 0;
         }
         __syncthreads();
+        if(P.ensemble == MTG_NPT) {
+            if(threadIdx.x < 96) npt_scalars(P, d, tot, 0.0, tot_fr, 0.0, false, false);
+            if(threadIdx.x == 0) d.sc->c2 = 1.0;
+            return;
+        }
         if(threadIdx.x < 96) {
             double KE2 = tot;
             double c2 = 1.0, c1 = 1.0;

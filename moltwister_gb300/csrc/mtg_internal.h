@@ -35,6 +35,21 @@ struct ThermoDev {
     double iQ[kMaxChain];   // 1/Q
 };
 
+// Barostat state of the NPT ensemble (CVelVerlet p_eps_, eps_, W_, V0_, P_: VelVerlet.h:57-62,
+// SimulationBox.cpp:73-76) and the per-step coefficients derived from it.  `saved` fields hold the
+// state after the last completed step; the live fields run one half-step ahead (the next step's
+// barostat kick, strain update and box are computed at the end of the previous step).
+struct BaroDev {
+    double p_eps, eps;
+    double L[3];          // current box getSimBox() (VelVerlet.cpp:198-211)
+    float Lf[3];          // (float) L, what the list and force kernels use
+    float pad0;
+    double ap, bp;        // prop_p: p = p ap + F bp (VelVerlet.cpp:124-136)
+    double ar, br;        // prop_r: r = r ar + (p (1/m)) br (VelVerlet.cpp:138-150)
+    double p_eps_saved, eps_saved;
+    double L_saved[3];
+};
+
 // Scalars the step kernels exchange through device memory.
 struct StepScalars {
     double S;             // pending momentum scale: c2(previous step) * c1(this step)
@@ -70,7 +85,14 @@ struct Params {
     int nx, ny, nz;       // reference cell counts (from the input box, MDFFMatrices.cpp:56-58)
     int pnx, pny, pnz;    // production cell counts (cell edge >= rlist), 1 = all-pairs build
     int team;             // lanes per atom in the production force gather (8, 16, 32)
+    // NPT
+    int MP, nrespP;       // barostat chain length and RESPA steps
+    double Pext;          // pressure / Conv_press
+    double W;             // barostat mass kT tauP^2
+    double V0;            // LmaxX LmaxY LmaxZ
 };
+
+
 
 // Everything a force/integration kernel reads, as raw device pointers.
 struct DevSys {
@@ -141,7 +163,20 @@ struct DevSys {
     ThermoDev* th;
     ThermoDev* th_saved;
     double* rec;          // output record ring [8]
+    // NPT
+    BaroDev* baro;
+    ThermoDev* thp;       // barostat chain (NH_P_)
+    ThermoDev* thp_saved;
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float box_f(const DevSys& d, const Params& P, int a) {
+    return P.ensemble == MTG_NPT ? d.baro->Lf[a] : P.boxf[a];
+}
+__device__ __forceinline__ double box_d(const DevSys& d, const Params& P, int a) {
+    return P.ensemble == MTG_NPT ? d.baro->L[a] : P.box[a];
+}
+#endif
 
 // Kernel launchers (defined in ref_kernels.cu and md_kernels.cu).
 // Reference mode

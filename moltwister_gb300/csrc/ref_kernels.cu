@@ -189,7 +189,7 @@ __device__ __forceinline__ bool exclusion(const DevSys& d, const Params& P, int 
 __global__ void k_cell_assign(DevSys d, Params P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= P.n) return;
-    const float wx = P.boxf[0], wy = P.boxf[1], wz = P.boxf[2];
+    const float wx = box_f(d, P, 0), wy = box_f(d, P, 1), wz = box_f(d, P, 2);
     const float lx = -wx / 2.0f, ly = -wy / 2.0f, lz = -wz / 2.0f;
     const int Nx = P.nx, Ny = P.ny, Nz = P.nz;
     int ix = (int)floor((d.r[3 * i] - double(lx)) * double(Nx) / double(wx));
@@ -272,9 +272,9 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
     float rc2f = rc;
     rc2f *= rc2f;
     const double rc2 = (double)rc2f;
-    const float lx = -P.boxf[0] / 2.0f, ly = -P.boxf[1] / 2.0f, lz = -P.boxf[2] / 2.0f;
-    const double w[3] = {double(lx + P.boxf[0]) - double(lx), double(ly + P.boxf[1]) - double(ly),
-                         double(lz + P.boxf[2]) - double(lz)};
+    const float Bx = box_f(d, P, 0), By = box_f(d, P, 1), Bz = box_f(d, P, 2);
+    const float lx = -Bx / 2.0f, ly = -By / 2.0f, lz = -Bz / 2.0f;
+    const double w[3] = {double(lx + Bx) - double(lx), double(ly + By) - double(ly), double(lz + Bz) - double(lz)};
     const int Nx = P.nx, Ny = P.ny, Nz = P.nz;
     const double x0 = d.r[3 * k], y0 = d.r[3 * k + 1], z0 = d.r[3 * k + 2];
     const int cx = d.atom_cell[3 * k], cy = d.atom_cell[3 * k + 1], cz = d.atom_cell[3 * k + 2];
@@ -319,7 +319,7 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
 __global__ void k_force(DevSys d, Params P) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if(k >= P.n) return;
-    const float Lf[3] = {P.boxf[0], P.boxf[1], P.boxf[2]};
+    const float Lf[3] = {box_f(d, P, 0), box_f(d, P, 1), box_f(d, P, 2)};
     const double w[3] = {double(Lf[0]) / 2.0 - (-double(Lf[0]) / 2.0), double(Lf[1]) / 2.0 - (-double(Lf[1]) / 2.0),
                          double(Lf[2]) / 2.0 - (-double(Lf[2]) / 2.0)};
     if(d.sc->overflow) return;   // neighbour list incomplete: the step is redone after growing it
@@ -545,6 +545,71 @@ __global__ void k_kick2(DevSys d, Params P) {
     }
 }
 
+// NPT branch (VelVerlet.cpp:57-71): steps 3.2 prop_p and 3.3 prop_r with the coefficients the
+// previous step's last block derived from p_eps (3.1); momenta carry the pending thermostat scale.
+__global__ void k_kick_drift_npt(DevSys d, Params P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= P.n) return;
+    const double S = d.sc->S;
+    const BaroDev* b = d.baro;
+    const double ap = b->ap, bp = b->bp, ar = b->ar, br = b->br;
+    const double im = 1.0 / d.m[k];
+#pragma unroll
+    for(int a = 0; a < 3; a++) {
+        double p = d.p[3 * k + a] * S;
+        p = p * ap + d.F[3 * k + a] * bp;
+        d.p[3 * k + a] = p;
+        d.r[3 * k + a] = d.r[3 * k + a] * ar + (p * im) * br;
+    }
+}
+
+// NPT: 3.5 prop_p with the new forces (no clipping in this branch), pbcWrap in the current box,
+// and the sums sum p^2/m, sum F.r (unwrapped, for 3.6), sum F.r (wrapped, for 3.1 and P), sum U.
+template<bool OUTPUT>
+__global__ void k_kick2_npt(DevSys d, Params P) {
+    __shared__ double smem[32 * 4];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    if(k < P.n) {
+        const BaroDev* b = d.baro;
+        const double ap = b->ap, bp = b->bp;
+        double p2 = 0.0, fu = 0.0, fw = 0.0;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            const double f = d.F[3 * k + a];
+            const double p = d.p[3 * k + a] * ap + f * bp;
+            d.p[3 * k + a] = p;
+            const double x0 = d.r[3 * k + a];
+            const double x = wrap_coord(x0, b->L[a]);
+            d.r[3 * k + a] = x;
+            p2 += p * p;
+            fu += f * x0;
+            fw += f * x;
+        }
+        v[0] = p2 / d.m[k];
+        v[1] = fu;
+        v[2] = fw;
+        if(OUTPUT) v[3] = d.U[k];
+    }
+    block_sum<4>(v, smem);
+    if(threadIdx.x == 0) {
+#pragma unroll
+        for(int q = 0; q < 4; q++) d.partial[blockIdx.x * 4 + q] = v[q];
+    }
+    if(last_block(&d.sc->done_blocks)) {
+        __shared__ double tot[4];
+        if(threadIdx.x == 0) {
+            double s[4] = {0.0, 0.0, 0.0, 0.0};
+            for(int bk = 0; bk < (int)gridDim.x; bk++)
+                for(int q = 0; q < 4; q++) s[q] += d.partial[bk * 4 + q];
+            for(int q = 0; q < 4; q++) tot[q] = s[q];
+            d.sc->done_blocks = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x < 96) npt_scalars(P, d, tot[0], tot[1], tot[2], tot[3], true, OUTPUT);
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -571,11 +636,17 @@ void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s) {
 }
 
 void launch_ref_kick_drift(const DevSys& d, const Params& P, cudaStream_t s) {
-    k_kick_drift<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    if(P.ensemble == MTG_NPT) k_kick_drift_npt<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    else k_kick_drift<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
 }
 
 void launch_ref_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
     const int nb = reduction_blocks(P.n);
+    if(P.ensemble == MTG_NPT) {
+        if(output) k_kick2_npt<true><<<nb, 256, 0, s>>>(d, P);
+        else k_kick2_npt<false><<<nb, 256, 0, s>>>(d, P);
+        return;
+    }
     if(output) k_kick2<true><<<nb, 256, 0, s>>>(d, P);
     else k_kick2<false><<<nb, 256, 0, s>>>(d, P);
 }

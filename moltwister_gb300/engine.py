@@ -10,7 +10,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 from dataclasses import dataclass
-from typing import Callable, List, Optional
+from typing import NamedTuple, Callable, List, Optional
 
 import numpy as np
 
@@ -70,7 +70,21 @@ class ConfigDesc(C.Structure):
 
 class ThermoState(C.Structure):
     _fields_ = [("M", C.c_int32), ("reserved", C.c_int32), ("eta", C.c_double * MAXCHAIN),
-                ("p_eta", C.c_double * MAXCHAIN), ("p_eps", C.c_double), ("eps", C.c_double)]
+                ("p_eta", C.c_double * MAXCHAIN), ("p_eps", C.c_double), ("eps", C.c_double),
+                ("MP", C.c_int32), ("reserved2", C.c_int32), ("etaP", C.c_double * MAXCHAIN),
+                ("p_etaP", C.c_double * MAXCHAIN), ("box", C.c_double * 3)]
+
+
+class Thermo(NamedTuple):
+    """Thermostat chain (eta, peta) and, under NPT, the barostat: p_eps, strain eps, its chain
+    (etaP, petaP) and the current box (output only)."""
+    eta: np.ndarray
+    peta: np.ndarray
+    p_eps: float = 0.0
+    eps: float = 0.0
+    etaP: Optional[np.ndarray] = None
+    petaP: Optional[np.ndarray] = None
+    box: Optional[np.ndarray] = None
 
 
 class Output(C.Structure):
@@ -243,7 +257,12 @@ class Engine:
             raise MTGError(rc, self.lib.mtg_last_error(None).decode())
         self.h = h
         self.n = n
-        if s.nhT_eta is not None and c.ensemble != "NVE":
+        if c.ensemble == "NPT" and s.p_eps is not None:
+            M = c.temperaturenhlen
+            self.set_state(thermo=Thermo(s.nhT_eta if s.nhT_eta is not None else np.zeros(M),
+                                         s.nhT_peta if s.nhT_peta is not None else np.zeros(M),
+                                         float(s.p_eps), 0.0, s.nhP_eta, s.nhP_peta))
+        elif s.nhT_eta is not None and c.ensemble != "NVE":
             self.set_state(thermo=(s.nhT_eta, s.nhT_peta))
 
     # -- lifetime ----------------------------------------------------------------------------------
@@ -268,20 +287,29 @@ class Engine:
         pp = None if p is None else np.ascontiguousarray(p, np.float64)
         th = None
         if thermo is not None:
-            eta, peta = thermo
+            if not isinstance(thermo, Thermo):
+                thermo = Thermo(*thermo)
             th = ThermoState()
-            th.M = len(eta)
-            for j in range(len(eta)):
-                th.eta[j] = float(eta[j])
-                th.p_eta[j] = float(peta[j])
+            th.M = len(thermo.eta)
+            for j in range(len(thermo.eta)):
+                th.eta[j] = float(thermo.eta[j])
+                th.p_eta[j] = float(thermo.peta[j])
+            th.p_eps, th.eps = float(thermo.p_eps), float(thermo.eps)
+            if thermo.etaP is not None:
+                th.MP = len(thermo.etaP)
+                for j in range(th.MP):
+                    th.etaP[j] = float(thermo.etaP[j])
+                    th.p_etaP[j] = float(thermo.petaP[j])
         self._check(self.lib.mtg_set_state(self.h, _ptr(rr), _ptr(pp), C.byref(th) if th is not None else None))
 
     def get_state(self):
+        """(r, p, Thermo) after the last completed step."""
         r = np.zeros((self.n, 3))
         p = np.zeros((self.n, 3))
         th = ThermoState()
         self._check(self.lib.mtg_get_state(self.h, _ptr(r), _ptr(p), C.byref(th)))
-        return r, p, (np.array(th.eta[:th.M]), np.array(th.p_eta[:th.M]))
+        return r, p, Thermo(np.array(th.eta[:th.M]), np.array(th.p_eta[:th.M]), th.p_eps, th.eps,
+                            np.array(th.etaP[:th.MP]), np.array(th.p_etaP[:th.MP]), np.array(th.box[:]))
 
     # -- dynamics ------------------------------------------------------------------------------------
     def run(self, nsteps: int, out_stride: int = 0, callback: Optional[Callable[[OutputRecord], bool]] = None,
