@@ -35,6 +35,9 @@ WORKLOAD = "water9000_nvt_mixed"
 METRIC = "atom-steps/s"
 CHUNK = 100
 SIGMA_O, EPS_O = 3.166, 0.650
+# DRAM bytes (read + write) of one k_pforce launch on this workload, from the ncu capture
+# summarised in profiles/k_pforce_water9000_mixed.md (cold L2: ncu flushes caches per pass)
+FORCE_DRAM_BYTES_PER_LAUNCH = 21.36e6
 
 
 def make_system(precision: str = "mixed"):
@@ -275,7 +278,9 @@ def our_arm(args):
                            "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                            "peak_source": f"nominal FP32 SIMT peak 152 SM x 128 lanes x 2 x {sm_max:.0f} MHz "
                                           f"(sm_max_mhz {kind} in MEASURED_PEAKS.json)",
-                           "algorithmic_flop_per_launch": flops, "traffic": None}
+                           "algorithmic_flop_per_launch": flops, "traffic": FORCE_DRAM_BYTES_PER_LAUNCH,
+                           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, cold L2 "
+                                             "(profiles/k_pforce_water9000_mixed.md)"}
         # integrator: HBM-bound, 148 B/atom-step algorithmic
         kd = phases["kick_drift"] + phases["kick_reduce"]
         out["roofline_integrator"] = {"bound": "hbm", "achieved": 148.0 * n / (kd * 1e-3) / 1e9,
