@@ -149,13 +149,16 @@ struct NhExchange {
     int timeout;
 };
 
+// Bounded wait for a flag of another warp of the block: spins on shared memory for the first
+// 4096 polls (the partner is normally a few hundred cycles away), then backs off; gives up after
+// 2^22 polls and records a timeout.
 __device__ __forceinline__ void nh_wait(volatile int* flag, int seq, int* timeout) {
     for(int it = 0; it < (1 << 22); it++) {
         if(*flag >= seq) {
             __threadfence_block();
             return;
         }
-        __nanosleep(32);
+        if(it >= 4096) __nanosleep(32);
     }
     *timeout = 1;
 }
@@ -211,28 +214,42 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         for(int mu = 0; mu < 3; mu++) {
             const double Dt = w[mu] * dt / double(nresp);
             const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
+            // per-stage coefficients: d4 G_j = pe[j-1]^2 A_j - B (j >= 1), d4 G_0 = KE2 d4 - B0,
+            // exponent of c_j = pe[j+1] D_j, eta step d2 pe/Q = pe E
+            double A[CAP], D[CAP];
+#pragma unroll
+            for(int j = 0; j < top; j++) {
+                A[j] = (j > 0) ? d4 * iQ[j - 1] : 0.0;
+                D[j] = d8 * iQ[j + 1];
+            }
+            const double B = d4 * kT, B0 = d4 * gkT;
+            double E = 0.0;
+#pragma unroll
+            for(int j = 0; j < top; j++)
+                if(j == lane) E = d2 * iQ[j];
             for(int it = 0; it < nresp; it++, s++) {
-                nh_wait(&X.f_etop, seq + s + 1, tmo);      // exponential of p_eta[M-1] (warp 2)
-                const double etop = X.etop;
+                double etop = 0.0;
                 double c12[CAP], x12[CAP];
                 // 1.2
 #pragma unroll
                 for(int j = 0; j < top; j++) {
                     double c, x;
                     if(j == top - 1) {
+                        nh_wait(&X.f_etop, seq + s + 1, tmo);      // exponential of p_eta[M-1] (warp 2)
+                        etop = X.etop;
                         c = etop;
                         x = 0.0;
                     } else if(it > 0) {
                         c = cprev[j];                       // same argument as step 1.5 before
                         x = xprev[j];
                     } else {
-                        x = d8 * (pe[j + 1] * iQ[j + 1]);
+                        x = pe[j + 1] * D[j];
                         c = cmt_exp_bits(x);
                     }
                     c12[j] = c;
                     x12[j] = x;
-                    const double G = (j == 0) ? KE2 - gkT : pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
-                    pe[j] = (pe[j] * c + d4 * G) * c;
+                    const double t = (j == 0) ? fma(KE2, d4, -B0) : fma(pe[j - 1] * pe[j - 1], A[j], -B);
+                    pe[j] = fma(pe[j], c, t) * c;
                     if(j == 0) {
                         if(lane == 0) X.pe0 = pe[0];
                         nh_post(&X.f_pe0, seq + s + 1);
@@ -240,11 +257,11 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                 }
                 // 1.3 (this warp's elements)
                 {
-                    double v = 0.0, q = 0.0;
+                    double v = 0.0;
 #pragma unroll
                     for(int j = 0; j < top; j++)
-                        if(j == lane) { v = pe[j]; q = iQ[j]; }
-                    if(lane < top) eta_mine += d2 * (v * q);
+                        if(j == lane) v = pe[j];
+                    if(lane < top) eta_mine = fma(v, E, eta_mine);
                 }
                 // 1.5
 #pragma unroll
@@ -253,7 +270,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                     if(j == top - 1) {
                         c = etop;                           // p_eta[M-1] has not changed since 1.2
                     } else {
-                        const double xn = d8 * (pe[j + 1] * iQ[j + 1]);
+                        const double xn = pe[j + 1] * D[j];
                         const double dx = xn - x12[j];
                         if((__double_as_longlong(dx) & 0x7fffffffffffffffLL) <= tiny_bits &&
                            __double_as_longlong(xn) <= half_bits && __double_as_longlong(x12[j]) <= half_bits)
@@ -263,15 +280,15 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                         cprev[j] = c;
                         xprev[j] = xn;
                     }
-                    double G;
+                    double t;
                     if(j == 0) {
                         nh_wait(&X.f_ke, seq + s + 1, tmo);    // kinetic term after step 1.4 (warp 1)
                         KE2 = X.ke;
-                        G = KE2 - gkT;
+                        t = fma(KE2, d4, -B0);
                     } else {
-                        G = pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
+                        t = fma(pe[j - 1] * pe[j - 1], A[j], -B);
                     }
-                    pe[j] = (pe[j] * c + d4 * G) * c;
+                    pe[j] = fma(pe[j], c, t) * c;
                     if(j == top - 1) {
                         if(lane == 0) X.pe_m2 = pe[top - 1];
                         nh_post(&X.f_pe_m2, seq + s + 1);
