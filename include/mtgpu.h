@@ -53,8 +53,11 @@ extern "C" {
 
 /* Term kinds.  Parameters follow the reference classes' parse order (see mtg_term). */
 #define MTG_KIND_NONE 0
-#define MTG_NB_LJ 1           /* p = {epsilon, sigma, alpha}         MolTwisterMDFFNonBonded_LJ.cpp:131-162 */
-#define MTG_NB_LJ1208 2       /* p = {epsilon, sigma, alpha}         MolTwisterMDFFNonBonded_LJ1208.cpp:131-170 */
+#define MTG_NB_LJ 1           /* p = {epsilon, sigma, alpha, rc}     MolTwisterMDFFNonBonded_LJ.cpp:131-162 */
+#define MTG_NB_LJ1208 2       /* p = {epsilon, sigma, alpha, rc}     MolTwisterMDFFNonBonded_LJ1208.cpp:131-170 */
+/* rc (new, production modes only): cutoff of this pair term, 0 = cutoff_radius.  The reference
+ * has one global cutoff, so per-pair cutoffs (e.g. 2.5 sigma_ab of a binary mixture) are not
+ * expressible there; reference mode ignores rc. */
 #define MTG_NB_BUCK 3         /* p = {A, rho, C}                     MolTwisterMDFFNonBonded_Buck.cpp:116-143 */
 #define MTG_NB_LJBUCK 4       /* table only                          MolTwisterMDFFNonBonded_LJBuck.cpp:181-251 */
 #define MTG_BOND_HARM 11      /* p = {k, r0}, U = k (r - r0)^2       MolTwisterMDFFBond_Harm.cpp:90-110 */
@@ -159,6 +162,8 @@ typedef struct mtg_config_desc {
     double opt_accuracy;        /* optaccuracy */
     int32_t opt_max_steps;      /* optmaxsteps */
     int32_t device;             /* CUDA device ordinal */
+    int32_t lj_shift;           /* production modes: shift LJ energies to zero at their cutoff (new) */
+    int32_t reserved;
 } mtg_config_desc;
 
 /* Thermostat/barostat state (CNHChain eta_/p_eta_, NHChain.h:55-61; CVelVerlet p_eps_, eps_,

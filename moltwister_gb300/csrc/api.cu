@@ -620,6 +620,8 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     for(int a = 0; a < 3; a++) {
         P.box[a] = sys->box[a];
         P.boxf[a] = (float)sys->box[a];
+        P.fscale[a] = (float)(sys->box[a] / 4294967296.0);
+        P.fconv[a] = 4294967296.0 / sys->box[a];
     }
     P.ensemble = cfg->ensemble;
     P.precision = cfg->precision;
@@ -708,6 +710,13 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
                 const double s2 = t.p[1] * t.p[1], s4 = s2 * s2, s6 = s4 * s2, s8 = s4 * s4, s12 = s6 * s6;
                 co[0] = 4.0 * t.p[0] * s12;
                 co[1] = 4.0 * t.p[0] * t.p[2] * (t.kind == MTG_NB_LJ ? s6 : s8);
+                // per-term cutoff^2 (0: the global cutoff applies) and energy shift U(rc)
+                const double rct = t.p[3] > 0.0 ? t.p[3] : cfg->cutoff_radius;
+                co[2] = t.p[3] > 0.0 ? t.p[3] * t.p[3] : 0.0;
+                if(cfg->lj_shift) {
+                    const double ir2 = 1.0 / (rct * rct), ir4 = ir2 * ir2, ir6 = ir4 * ir2;
+                    co[3] = co[0] * ir6 * ir6 - co[1] * (t.kind == MTG_NB_LJ ? ir6 : ir4 * ir4);
+                }
             } else if(t.kind == MTG_NB_BUCK) {
                 co[0] = t.p[0];
                 co[1] = (t.p[1] == 0.0) ? 1E-10 : 1.0 / t.p[1];
@@ -823,6 +832,23 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         rc = rc || dalloc(C, &d.rb4, (size_t)n);
         rc = rc || dalloc(C, &d.hi, (size_t)n);
         rc = rc || dalloc(C, &d.lo, (size_t)n);
+        rc = rc || dalloc(C, &d.pq, (size_t)n);
+        {
+            // per-type charge table, used when every atom of a type carries the same charge
+            std::vector<float> qt(std::max(T, 1), 0.0f);
+            std::vector<int> seen(std::max(T, 1), 0);
+            bool uniform = T <= 8;
+            for(int i = 0; i < n && uniform; i++) {
+                const float q = (float)sys->charge[i];
+                const int t = sys->type[i];
+                if(!seen[t]) { seen[t] = 1; qt[t] = q; }
+                else if(qt[t] != q) uniform = false;
+            }
+            P.qtype = uniform ? 1 : 0;
+            float* qtd = nullptr;
+            rc = rc || upload(C, &qtd, qt.data(), qt.size());
+            d.qtype = qtd;
+        }
         rc = rc || dalloc(C, &d.Fx, (size_t)n);
         rc = rc || dalloc(C, &d.Fy, (size_t)n);
         rc = rc || dalloc(C, &d.Fz, (size_t)n);
@@ -895,6 +921,7 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         if(is_mixed(C)) {
             rc = rc || add_snap(C, d.hi, sizeof(float4) * n);
             rc = rc || add_snap(C, d.lo, sizeof(float4) * n);
+            rc = rc || add_snap(C, d.pq, sizeof(uint4) * n);
             rc = rc || add_snap(C, d.Fx, sizeof(long long) * n);
             rc = rc || add_snap(C, d.Fy, sizeof(long long) * n);
             rc = rc || add_snap(C, d.Fz, sizeof(long long) * n);

@@ -33,7 +33,6 @@ int reduction_blocks(int n) {
 
 namespace {
 
-constexpr int kWarp = 32;
 
 // ---------------------------------------------------------------------------------------------
 // Prologue: sum p^2/m, then the first thermostat half-step of the coming step.
@@ -99,7 +98,15 @@ __device__ __forceinline__ void load_pos(const DevSys& d, int i, double& x, doub
     }
 }
 
-__device__ __forceinline__ void store_pos(const DevSys& d, int i, double x, double y, double z, bool mixed) {
+// 32-bit fraction of the box: round(x / L * 2^32) modulo 2^32.  The difference of two such
+// coordinates, read as a signed 32-bit integer, is the minimum-image separation in units of
+// L / 2^32, exact for any |dx| < L/2 (no cancellation at the periodic boundary).
+__device__ __forceinline__ unsigned int frac32(double x, double conv) {
+    return (unsigned int)(unsigned long long)__double2ll_rn(x * conv);
+}
+
+__device__ __forceinline__ void store_pos(const DevSys& d, const Params& P, int i, double x, double y, double z,
+                                          bool mixed) {
     if(mixed) {
         const float hx = (float)x, hy = (float)y, hz = (float)z;
         float4 h = d.hi[i], l = d.lo[i];
@@ -109,6 +116,11 @@ __device__ __forceinline__ void store_pos(const DevSys& d, int i, double x, doub
         l.z = (float)(z - double(hz));
         d.hi[i] = h;
         d.lo[i] = l;
+        uint4 q = d.pq[i];
+        q.x = frac32(x, P.fconv[0]);
+        q.y = frac32(y, P.fconv[1]);
+        q.z = frac32(z, P.fconv[2]);
+        d.pq[i] = q;
     } else {
         d.r[3 * i] = x;
         d.r[3 * i + 1] = y;
@@ -173,7 +185,7 @@ __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, int 
     x += px * dm;
     y += py * dm;
     z += pz * dm;
-    store_pos(d, k, x, y, z, MIXED);
+    store_pos(d, P, k, x, y, z, MIXED);
     // displacement since the last list build (minimum image: wrapping is not a displacement)
     const double bx = minimg_d(x - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
     const double by = minimg_d(y - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
@@ -219,7 +231,7 @@ __global__ void k_pkick2(DevSys d, Params P) {
             p2 += p * p;
             fr += f[a] * r[a];
         }
-        store_pos(d, k, r[0], r[1], r[2], MIXED);
+        store_pos(d, P, k, r[0], r[1], r[2], MIXED);
         v[0] = p2 / d.m[k];
         if(OUTPUT) {
             v[1] = fr;
@@ -441,24 +453,29 @@ __device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir
     for(int ff = 0; ff < cnt; ff++) {
         const int idx = pair * kMaxFF + ff;
         const int kind = d.nb_kind[idx];
-        R a, b, c;
+        R a, b, c, dd;
         if(sizeof(R) == 4) {
             const float4 q = reinterpret_cast<const float4*>(d.nb_parf)[idx];
-            a = (R)q.x; b = (R)q.y; c = (R)q.z;
+            a = (R)q.x; b = (R)q.y; c = (R)q.z; dd = (R)q.w;
         } else {
             a = (R)d.nb_par[4 * idx]; b = (R)d.nb_par[4 * idx + 1]; c = (R)d.nb_par[4 * idx + 2];
+            dd = (R)d.nb_par[4 * idx + 3];
         }
         if(kind == MTG_NB_LJ) {
-            // a = 4 eps sigma^12, b = 4 eps alpha sigma^6
-            const R ir6 = ir2 * ir2 * ir2;
-            const R t12 = a * ir6 * ir6, t6 = b * ir6;
-            g += (R(12) * t12 - R(6) * t6) * ir2;
-            if(energy) u += t12 - t6;
+            // a = 4 eps sigma^12, b = 4 eps alpha sigma^6, c = own cutoff^2 (0: global), d = U(rc)
+            if(c == R(0) || r2 < c) {
+                const R ir6 = ir2 * ir2 * ir2;
+                const R t12 = a * ir6 * ir6, t6 = b * ir6;
+                g += (R(12) * t12 - R(6) * t6) * ir2;
+                if(energy) u += t12 - t6 - dd;
+            }
         } else if(kind == MTG_NB_LJ1208) {
-            const R ir4 = ir2 * ir2, ir8 = ir4 * ir4;
-            const R t12 = a * ir8 * ir4, t8 = b * ir8;
-            g += (R(12) * t12 - R(8) * t8) * ir2;
-            if(energy) u += t12 - t8;
+            if(c == R(0) || r2 < c) {
+                const R ir4 = ir2 * ir2, ir8 = ir4 * ir4;
+                const R t12 = a * ir8 * ir4, t8 = b * ir8;
+                g += (R(12) * t12 - R(8) * t8) * ir2;
+                if(energy) u += t12 - t8 - dd;
+            }
         } else if(kind == MTG_NB_BUCK) {
             // a = A, b = 1/rho, c = C
             const R r = r2 * ir;
@@ -491,10 +508,10 @@ __device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir
 template<bool MIXED, class R>
 __device__ __forceinline__ void rel(const DevSys& d, const Params& P, int i, int j, R& dx, R& dy, R& dz) {
     if(MIXED) {
-        const float4 hi = d.hi[i], li = d.lo[i], hj = d.hi[j], lj = d.lo[j];
-        dx = minimg_f((hi.x - hj.x) + (li.x - lj.x), P.boxf[0], 1.0f / P.boxf[0]);
-        dy = minimg_f((hi.y - hj.y) + (li.y - lj.y), P.boxf[1], 1.0f / P.boxf[1]);
-        dz = minimg_f((hi.z - hj.z) + (li.z - lj.z), P.boxf[2], 1.0f / P.boxf[2]);
+        const uint4 qi = d.pq[i], qj = d.pq[j];
+        dx = (R)__int2float_rn((int)(qi.x - qj.x)) * (R)P.fscale[0];
+        dy = (R)__int2float_rn((int)(qi.y - qj.y)) * (R)P.fscale[1];
+        dz = (R)__int2float_rn((int)(qi.z - qj.z)) * (R)P.fscale[2];
     } else {
         dx = (R)minimg_d(d.r[3 * i] - d.r[3 * j], P.box[0], 1.0 / P.box[0]);
         dy = (R)minimg_d(d.r[3 * i + 1] - d.r[3 * j + 1], P.box[1], 1.0 / P.box[1]);
@@ -669,18 +686,28 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
 // Per type pair, staged in shared memory by the force kernel: mode 0 = no term, 1 = one 12-6 LJ
 // term with coefficients (a, b), 2 = anything else (evaluated by pair_terms from global memory).
 struct PairCoef {
-    float a, b;
-    int mode, pad;
+    float a, b;       // 4 eps sigma^12, 4 eps alpha sigma^6
+    float rc2, us;    // own cutoff^2 (0: global), energy shift
 };
 constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
 
 template<bool MIXED, bool ENERGY, class R>
 __device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, R qi,
-                                           R rc2, R rq2, R irc, R kq, const PairCoef* pc,
-                                           R& dx, R& dy, R& dz, R& g, R& u) {
+                                           R rc2, R rq2, R irc, R kq, const PairCoef* pc, const int* pmode,
+                                           const float* qt, uint4 qi4, R& dx, R& dy, R& dz, R& g, R& u) {
     const int j = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
-    rel<MIXED, R>(d, P, i, j, dx, dy, dz);
+    int tj;
+    if(MIXED) {
+        const uint4 qj4 = d.pq[j];
+        dx = (R)__int2float_rn((int)(qi4.x - qj4.x)) * (R)P.fscale[0];
+        dy = (R)__int2float_rn((int)(qi4.y - qj4.y)) * (R)P.fscale[1];
+        dz = (R)__int2float_rn((int)(qi4.z - qj4.z)) * (R)P.fscale[2];
+        tj = (int)qj4.w;
+    } else {
+        rel<MIXED, R>(d, P, i, j, dx, dy, dz);
+        tj = d.type[j];
+    }
     const R r2 = dx * dx + dy * dy + dz * dz;
     R ir;
     if(MIXED) ir = (R)rsqrtf((float)r2);
@@ -689,16 +716,18 @@ __device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int
     g = 0;
     u = 0;
     if(r2 < rc2 && r2 >= R(1e-6)) {
-        const int tj = MIXED ? __float_as_int(d.lo[j].w) : d.type[j];
         const int pr = ti * P.T + tj;
         if(MIXED && pc && pr < kSmemPairs) {
-            const PairCoef c = pc[pr];
-            if(c.mode == 1) {
-                const R ir6 = ir2 * ir2 * ir2;
-                const R t12 = (R)c.a * ir6 * ir6, t6 = (R)c.b * ir6;
-                g = (R(12) * t12 - R(6) * t6) * ir2;
-                if(ENERGY) u = t12 - t6;
-            } else if(c.mode == 2) {
+            const int mode = pmode[pr];
+            if(mode == 1) {
+                const PairCoef c = pc[pr];
+                if(c.rc2 == 0.0f || (float)r2 < c.rc2) {
+                    const R ir6 = ir2 * ir2 * ir2;
+                    const R t12 = (R)c.a * ir6 * ir6, t6 = (R)c.b * ir6;
+                    g = (R(12) * t12 - R(6) * t6) * ir2;
+                    if(ENERGY) u = t12 - t6 - (R)c.us;
+                }
+            } else if(mode == 2) {
                 pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY);
             }
         } else {
@@ -706,7 +735,7 @@ __device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int
         }
     }
     if(P.coulomb != MTG_COULOMB_ALLPAIRS && r2 < rq2) {
-        const R qj = MIXED ? (R)d.hi[j].w : (R)d.qd[j];
+        const R qj = MIXED ? (R)(qt ? qt[tj] : d.qf[j]) : (R)d.qd[j];
         const R qq = kq * qi * qj;
         if(P.coulomb == MTG_COULOMB_SHIFTED) {
             g += qq * (ir2 - irc * irc) * ir;
@@ -731,22 +760,31 @@ template<bool MIXED, bool ENERGY, int TEAM>
 __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     using R = typename std::conditional<MIXED, float, double>::type;
     __shared__ PairCoef pc_s[kSmemPairs];
+    __shared__ int pm_s[kSmemPairs];   // 0 no term, 1 one 12-6 LJ term (pc_s), 2 general (pair_terms)
+    __shared__ float qt_s[8];            // per-type charges (when charges are a function of type)
     const PairCoef* pc = nullptr;
+    const int* pmode = nullptr;
+    const float* qt = nullptr;
     if(MIXED && P.T * P.T <= kSmemPairs) {
         for(int q = threadIdx.x; q < P.T * P.T; q += blockDim.x) {
-            PairCoef c{0.0f, 0.0f, 0, 0};
+            PairCoef c{0.0f, 0.0f, 0.0f, 0.0f};
+            int mode = 0;
             const int cnt = d.nb_cnt[q];
             if(cnt == 1 && d.nb_kind[q * kMaxFF] == MTG_NB_LJ) {
-                c.mode = 1;
-                c.a = d.nb_parf[4 * (q * kMaxFF)];
-                c.b = d.nb_parf[4 * (q * kMaxFF) + 1];
+                mode = 1;
+                const float4 f = reinterpret_cast<const float4*>(d.nb_parf)[q * kMaxFF];
+                c = PairCoef{f.x, f.y, f.z, f.w};
             } else if(cnt > 0) {
-                c.mode = 2;
+                mode = 2;
             }
             pc_s[q] = c;
+            pm_s[q] = mode;
         }
+        if(P.qtype && threadIdx.x < P.T) qt_s[threadIdx.x] = d.qtype[threadIdx.x];
         __syncthreads();
         pc = pc_s;
+        pmode = pm_s;
+        if(P.qtype) qt = qt_s;
     }
     const R gmax = R(262143.0) / ((R)P.rc + (R)P.rcoul + (R)P.skin);   // keeps |g d| < 2^18
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -759,8 +797,9 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         const R rc2 = (R)P.rc * (R)P.rc;
         const R rq2 = (R)P.rcoul * (R)P.rcoul;
         const R irc = R(1) / (R)P.rcoul;
-        const int ti = MIXED ? __float_as_int(d.lo[i].w) : d.type[i];
-        const R qi = MIXED ? (R)d.hi[i].w : (R)d.qd[i];
+        const uint4 qi4 = MIXED ? d.pq[i] : make_uint4(0, 0, 0, 0);
+        const int ti = MIXED ? (int)qi4.w : d.type[i];
+        const R qi = MIXED ? (R)d.qf[i] : (R)d.qd[i];
         const R kq = MIXED ? (R)kCoulombKf : (R)1389.32;
         const int cnt = min(d.vcount[i], d.vmax);   // an overflowed build is redone; stay in the row
         const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
@@ -772,7 +811,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
 #pragma unroll
             for(int q = 0; q < 4; q++) {
                 R dx, dy, dz, g, u;
-                pair_entry<MIXED, ENERGY, R>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, kq, pc, dx, dy, dz, g, u);
+                pair_entry<MIXED, ENERGY, R>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, dx, dy, dz, g, u);
                 if(MIXED) {
                     g = fminf(fmaxf(g, -gmax), gmax);
                     fix_add(fx, (float)(g * dx));
@@ -787,7 +826,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         }
         for(; e < cnt; e += TEAM) {
             R dx, dy, dz, g, u;
-            pair_entry<MIXED, ENERGY, R>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, kq, pc, dx, dy, dz, g, u);
+            pair_entry<MIXED, ENERGY, R>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, dx, dy, dz, g, u);
             if(MIXED) {
                 g = fminf(fmaxf(g, -gmax), gmax);
                 fix_add(fx, (float)(g * dx));
@@ -852,7 +891,10 @@ __global__ void k_sync_pos(DevSys d, Params P, int to_master) {
     if(i >= P.n) return;
     if(to_master) {
         // d.r -> hi/lo (set_state)
-        store_pos(d, i, d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2], true);
+        uint4 q = d.pq[i];
+        q.w = (unsigned int)d.type[i];
+        d.pq[i] = q;
+        store_pos(d, P, i, d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2], true);
         float4 h = d.hi[i], l = d.lo[i];
         h.w = d.qf[i];
         l.w = __int_as_float(d.type[i]);
@@ -900,7 +942,7 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
             fr += f[a] * r[a];
             p2 += d.p[3 * k + a] * d.p[3 * k + a];
         }
-        store_pos(d, k, r[0], r[1], r[2], mixed);
+        store_pos(d, P, k, r[0], r[1], r[2], mixed);
         if(mode != MTG_PREC_REFERENCE) {
             const double bx = minimg_d(r[0] - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
             const double by = minimg_d(r[1] - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);

@@ -85,6 +85,9 @@ struct Params {
     int nx, ny, nz;       // reference cell counts (from the input box, MDFFMatrices.cpp:56-58)
     int pnx, pny, pnz;    // production cell counts (cell edge >= rlist), 1 = all-pairs build
     int team;             // lanes per atom in the production force gather (8, 16, 32)
+    float fscale[3];      // L / 2^32: fixed-point position unit per axis (mixed)
+    double fconv[3];      // 2^32 / L
+    int qtype;            // 1: charges are a function of the type (qtype table)
     // NPT
     int MP, nrespP;       // barostat chain length and RESPA steps
     double Pext;          // pressure / Conv_press
@@ -153,6 +156,8 @@ struct DevSys {
     // mixed
     float4* hi;           // [n] x,y,z hi, charge
     float4* lo;           // [n] x,y,z lo, type bits
+    uint4* pq;            // [n] x,y,z as 32-bit fractions of the box (wrap = minimum image), type
+    const float* qtype;   // [T] charge of each type when every atom of a type has the same charge
     long long* Fx;        // [n] fixed-point forces (SoA)
     long long* Fy;
     long long* Fz;

@@ -65,7 +65,7 @@ class ConfigDesc(C.Structure):
                 ("scale12", C.c_double), ("scale13", C.c_double), ("scale14", C.c_double), ("scale1N", C.c_double),
                 ("coulomb_cutoff", C.c_double), ("list_skin", C.c_double),
                 ("opt_learning_rate", C.c_double), ("opt_accuracy", C.c_double), ("opt_max_steps", C.c_int32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("lj_shift", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ThermoState(C.Structure):
@@ -250,6 +250,7 @@ class Engine:
         cf.list_skin = c.listskin
         cf.opt_learning_rate, cf.opt_accuracy, cf.opt_max_steps = c.optlearningrate, c.optaccuracy, c.optmaxsteps
         cf.device = device
+        cf.lj_shift = 1 if c.ljshift else 0
         self.cfgdesc = cf
         h = C.c_void_p()
         rc = self.lib.mtg_create(C.byref(d), C.byref(cf), C.byref(h))

@@ -42,12 +42,13 @@ class NonBondedTerm:
     id2: str
     kind: str
     args: Tuple[float, ...]
+    cutoff: float = 0.0   # new, production modes only: this pair's cutoff [A] (0 = cutoffradius)
 
     def params(self) -> List[float]:
         if self.kind == "LJ":
             eps, sig = self.args[0], self.args[1]
             alpha = self.args[2] if len(self.args) > 2 else 1.0
-            return [eps, sig, alpha]
+            return [eps, sig, alpha, float(self.cutoff)]
         return list(self.args)
 
     def command_args(self) -> List[str]:
@@ -123,6 +124,8 @@ class MDConfig:
       coulombcutoff : cutoff radius for "cutoff" Coulomb [A] (defaults to cutoffradius).
       listskin      : Verlet skin of the production neighbour list [A].
       clipforces    : apply the reference's per-component force clipping (NVT/NVE only).
+      ljshift       : production modes: shift LJ energies to zero at each term's cutoff (forces
+                      unchanged), for energy-conservation measurements.
     """
     timestep: float = 1.0
     timesteps: int = 50000
@@ -152,6 +155,7 @@ class MDConfig:
     coulombcutoff: Optional[float] = None
     listskin: float = 1.0
     clipforces: bool = True
+    ljshift: bool = False
 
     REFERENCE_KEYS = ("timestep", "timesteps", "outstride", "temperature", "temperaturerelax",
                       "temperaturenhlen", "temperaturerespa", "pressure", "pressurerelax",

@@ -117,6 +117,45 @@ def argon(ncell: int = 10, seed: int = 1, T: float = 120.0, rho_star: float = 0.
 
 
 # ------------------------------------------------------------------------------------------------
+# Config 3: Kob-Andersen binary LJ mixture (LJ reduced units with sigma = 1 A, eps = 1 kJ/mol,
+# m = 1 g/mol: T* = 0.75 is 90.2 K, dt* = 0.005 is 0.5 fs)
+# ------------------------------------------------------------------------------------------------
+KA_PAIRS = {("A", "A"): (1.0, 1.0), ("A", "B"): (1.5, 0.8), ("B", "B"): (0.5, 0.88)}   # (eps, sigma)
+
+
+def kob_andersen(ncell: int = 64, seed: int = 3, T_star: float = 0.75, rho_star: float = 1.2,
+                 frac_a: float = 0.8, jitter: float = 0.05, per_pair_cutoff: bool = True,
+                 dt_fs: float = 0.5) -> Tuple[MDSystem, MDConfig]:
+    """Kob-Andersen 80:20 mixture, N = 4 ncell^3 (ncell = 64: 1,048,576 atoms) at reduced
+    density rho_star: FCC sites with a seeded random A/B assignment and seeded jitter (the caller
+    relaxes it with Engine.optimize), eps/sigma AA 1/1, AB 1.5/0.8, BB 0.5/0.88, cutoff 2.5
+    sigma_ab per pair (with per_pair_cutoff; else 2.5 for every pair, the only form the reference can
+    express), energies shifted to zero at the cutoffs, Maxwell-Boltzmann momenta at T*, NVE."""
+    rng = np.random.default_rng(seed)
+    a = (4.0 / rho_star) ** (1.0 / 3.0)
+    r = fcc_positions(ncell, a)
+    N = r.shape[0]
+    if jitter > 0:
+        r = r + rng.uniform(-jitter, jitter, r.shape)
+    nb = int(round((1.0 - frac_a) * N))
+    ids = np.array(["A"] * N, dtype=object)
+    ids[rng.permutation(N)[:nb]] = "B"
+    L = ncell * a
+    m = np.ones(N)
+    T = T_star * CONV_T
+    terms = [NonBondedTerm(i, j, "LJ", (e, sg), cutoff=(2.5 * sg if per_pair_cutoff else 0.0))
+             for (i, j), (e, sg) in KA_PAIRS.items()]
+    sys_ = MDSystem(box=np.array([L, L, L]), ids=[str(x) for x in ids], r=r, q=np.zeros(N), m=m,
+                    mobile=np.ones(N, bool), nonbonded=terms)
+    sys_.mol = np.arange(N, dtype=np.int32)
+    sys_.p = maxwell_boltzmann(m, T, rng)
+    cfg = MDConfig(timestep=dt_fs, timesteps=20000, temperature=T, ensemble="NVE",
+                   cutoffradius=2.5, neighshell=0.3, listskin=0.3, coulomb="cutoff", coulombcutoff=2.5,
+                   precision="mixed", ljshift=True, clipforces=False, optlearningrate=1e-4)
+    return sys_, cfg
+
+
+# ------------------------------------------------------------------------------------------------
 # Config 2: flexible SPC/E-like water
 # ------------------------------------------------------------------------------------------------
 def random_rotation(rng: np.random.Generator) -> np.ndarray:

@@ -477,6 +477,7 @@ typedef struct orc_sys {
     int coulomb_mode;         /* 0 all pairs minimum image (reference), 1 truncated, 2 shifted force at coulomb_rc */
     double coulomb_rc;
     const double* qd;         /* n charges in FP64 (analytic mode) */
+    int lj_shift;             /* analytic mode: shift LJ energies to zero at the cutoff */
 } orc_sys;
 
 /* FunctorCalcForce::scaleForcesAndPotentials (FunctorCalcForce.cpp:95-157) as a factor */
@@ -697,15 +698,27 @@ static v3 minimg(v3 d, const double* L) {
 }
 
 /* -dU/dr for one analytic pair term and U */
-static void nb_analytic(int kind, const double* p, double R, double* mdUdr, double* u) {
-    if(kind == K_NB_LJ) {
-        double sr2 = (p[1] * p[1]) / (R * R), sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-        *u = 4.0 * p[0] * (sr12 - p[2] * sr6);
-        *mdUdr = 4.0 * p[0] * (12.0 * sr12 - 6.0 * p[2] * sr6) / R;
-    } else if(kind == K_NB_LJ1208) {
-        double sr2 = (p[1] * p[1]) / (R * R), sr4 = sr2 * sr2, sr8 = sr4 * sr4, sr12 = sr8 * sr4;
-        *u = 4.0 * p[0] * (sr12 - p[2] * sr8);
-        *mdUdr = 4.0 * p[0] * (12.0 * sr12 - 8.0 * p[2] * sr8) / R;
+/* LJ/LJ1208 p = {eps, sigma, alpha, rc}: rc > 0 is the term's own cutoff (new option of the
+ * production modes); with shift != 0 the energy is shifted to zero at the cutoff in force
+ * (rc, else rglob). */
+static void nb_analytic(int kind, const double* p, double R, double rglob, int shift, double* mdUdr, double* u) {
+    if(kind == K_NB_LJ || kind == K_NB_LJ1208) {
+        const double rct = p[3] > 0.0 ? p[3] : rglob;
+        *u = 0.0; *mdUdr = 0.0;
+        if(p[3] > 0.0 && R >= p[3]) return;
+        double srn, sr12;
+        const double n = (kind == K_NB_LJ) ? 6.0 : 8.0;
+        double sr2 = (p[1] * p[1]) / (R * R);
+        if(kind == K_NB_LJ) { srn = sr2 * sr2 * sr2; sr12 = srn * srn; }
+        else { double sr4 = sr2 * sr2; srn = sr4 * sr4; sr12 = srn * sr4; }
+        *u = 4.0 * p[0] * (sr12 - p[2] * srn);
+        *mdUdr = 4.0 * p[0] * (12.0 * sr12 - n * p[2] * srn) / R;
+        if(shift) {
+            double c2 = (p[1] * p[1]) / (rct * rct), cn, c12;
+            if(kind == K_NB_LJ) { cn = c2 * c2 * c2; c12 = cn * cn; }
+            else { double c4 = c2 * c2; cn = c4 * c4; c12 = cn * c4; }
+            *u -= 4.0 * p[0] * (c12 - p[2] * cn);
+        }
     } else if(kind == K_NB_BUCK) {
         double e = p[0] * exp(-R / p[1]), r6 = 1.0 / (R * R * R * R * R * R);
         *u = e - p[2] * r6;
@@ -807,7 +820,8 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
                 int pair = s->type[k] * T + s->type[i];
                 for(int ff = 0; ff < s->nb_cnt[pair]; ff++) {
                     double m1, u1;
-                    nb_analytic(s->nb_kind[pair * ORC_MAXFF + ff], s->nb_par + 4 * (pair * ORC_MAXFF + ff), R, &m1, &u1);
+                    nb_analytic(s->nb_kind[pair * ORC_MAXFF + ff], s->nb_par + 4 * (pair * ORC_MAXFF + ff), R, rcut,
+                                s->lj_shift, &m1, &u1);
                     md += m1; u += u1;
                 }
             }

@@ -81,7 +81,7 @@ class OrcSys(C.Structure):
                 ("bond_kind", C.c_void_p), ("bond_par", C.c_void_p),
                 ("angle_kind", C.c_void_p), ("angle_par", C.c_void_p),
                 ("dih_kind", C.c_void_p), ("dih_par", C.c_void_p),
-                ("coulomb_mode", C.c_int), ("coulomb_rc", C.c_double), ("qd", C.c_void_p)]
+                ("coulomb_mode", C.c_int), ("coulomb_rc", C.c_double), ("qd", C.c_void_p), ("lj_shift", C.c_int)]
 
 
 class OrcRun(C.Structure):
@@ -183,6 +183,7 @@ class Oracle:
         o.rc, o.shell, o.fcut = cfg.cutoffradius, cfg.neighshell, cfg.cutoffforce
         o.scale12, o.scale13, o.scale14, o.scale1N = cfg.scale12, cfg.scale13, cfg.scale14, cfg.scale1N
         o.coulomb_mode = {"allpairs": 0, "cutoff": 1, "shifted": 2}[cfg.coulomb]
+        o.lj_shift = 1 if getattr(cfg, "ljshift", False) else 0
         o.coulomb_rc = cfg.coulombcutoff if cfg.coulombcutoff is not None else cfg.cutoffradius
         return o
 
