@@ -73,6 +73,10 @@ struct mtg_ctx {
     mtg_run_stats stats{};
     // output staging
     std::vector<double> h_r, h_p;
+    // batch of replicas (P.nrep > 0)
+    std::vector<int> rep_off;          // nrep + 1 atom offsets
+    std::vector<double> h_rep_box;     // 3 per replica
+    std::vector<double> h_rrec;        // nrep * 8 records of the last output step
 
     ~mtg_ctx() {
         for(auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -460,6 +464,30 @@ void restore_snapshot(mtg_ctx* c) {
 
 // Host copies of r and p after a step; p carries the pending scale c2 of the last second
 // thermostat half-step (the kernels apply it lazily at the next kick).
+// Pending second-half scale c2 of each replica (one entry for a single system).
+int replica_c2(mtg_ctx* c, std::vector<double>& c2) {
+    if(!c->P.nrep) {
+        c2.assign(1, read_scalars(c).c2);
+        return MTG_OK;
+    }
+    std::vector<StepScalars> rs(c->P.nrep);
+    CUDA_TRY(c, cudaMemcpy(rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
+    c2.resize(rs.size());
+    for(size_t r = 0; r < rs.size(); r++) c2[r] = rs[r].c2;
+    return MTG_OK;
+}
+
+void scale_momenta(mtg_ctx* c, std::vector<double>& p, const std::vector<double>& c2) {
+    if(!c->P.nrep) {
+        if(c2[0] != 1.0)
+            for(double& v : p) v *= c2[0];
+        return;
+    }
+    for(int r = 0; r < c->P.nrep; r++)
+        if(c2[r] != 1.0)
+            for(size_t i = (size_t)3 * c->rep_off[r]; i < (size_t)3 * c->rep_off[r + 1]; i++) p[i] *= c2[r];
+}
+
 int fetch_rp(mtg_ctx* c, double c2) {
     const size_t n3 = (size_t)c->P.n * 3;
     c->h_r.resize(n3);
@@ -468,10 +496,22 @@ int fetch_rp(mtg_ctx* c, double c2) {
     CUDA_TRY(c, cudaMemcpyAsync(c->h_r.data(), c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(c->h_p.data(), c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    if(c2 != 1.0)
-        for(size_t i = 0; i < n3; i++) c->h_p[i] *= c2;
+    std::vector<double> sc(1, c2);
+    if(c->P.nrep) {
+        int rc = replica_c2(c, sc);
+        if(rc) return rc;
+    }
+    scale_momenta(c, c->h_p, sc);
     return MTG_OK;
 }
+
+// A batch of independent replicas merged into one system: atom ranges, boxes, temperatures.
+struct BatchSpec {
+    int nrep = 0;
+    std::vector<int> off, n;          // nrep + 1 offsets, nrep sizes
+    std::vector<double> box;          // 3 per replica
+    std::vector<double> temperature;  // K per replica
+};
 
 // Barostat state with momentum p_eps and strain eps: box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax
 // (VelVerlet.cpp:192-211); the saved copy equals the live one (no step pending).
@@ -490,6 +530,29 @@ BaroDev baro_at(const Params& P, double p_eps, double eps) {
     return b;
 }
 
+// Output record of the last output step: U, K, T, P, V.  For a batch the per-replica records go
+// to h_rrec and the returned record is the ensemble's: sums of U, K and V, T = 2 K / 3N over all
+// atoms, P the mean of the replicas' pressures.
+int read_records(mtg_ctx* c, double* rec) {
+    if(!c->P.nrep) {
+        CUDA_TRY(c, cudaMemcpy(rec, c->d.rec, sizeof(double) * 8, cudaMemcpyDeviceToHost));
+        return MTG_OK;
+    }
+    const int nr = c->P.nrep;
+    c->h_rrec.resize((size_t)nr * 8);
+    CUDA_TRY(c, cudaMemcpy(c->h_rrec.data(), c->d.rrec, sizeof(double) * 8 * nr, cudaMemcpyDeviceToHost));
+    for(int q = 0; q < 8; q++) rec[q] = 0.0;
+    for(int r = 0; r < nr; r++) {
+        const double* x = &c->h_rrec[(size_t)8 * r];
+        rec[0] += x[0];
+        rec[1] += x[1];
+        rec[3] += x[3] / nr;
+        rec[4] += x[4];
+    }
+    rec[2] = 2.0 * rec[1] / (3.0 * double(c->P.n));
+    return MTG_OK;
+}
+
 // Applies the pending c2 to the device momenta and rewinds the thermostat (and, under NPT, the
 // barostat) to the state after the last completed step (end of a run).
 int settle_state(mtg_ctx* c) {
@@ -504,6 +567,29 @@ int settle_state(mtg_ctx* c) {
         }
         CUDA_TRY(c, cudaMemcpy(c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
         CUDA_TRY(c, cudaMemcpy(c->d.thp, c->d.thp_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
+    }
+    if(c->P.nrep) {
+        std::vector<StepScalars> rs(c->P.nrep);
+        CUDA_TRY(c, cudaMemcpy(rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
+        std::vector<double> c2(rs.size());
+        bool any = false;
+        for(size_t r = 0; r < rs.size(); r++) {
+            c2[r] = rs[r].c2;
+            any |= (rs[r].c2 != 1.0 || rs[r].S != 1.0);
+        }
+        if(any) {
+            std::vector<double> p((size_t)c->P.n * 3);
+            CUDA_TRY(c, cudaMemcpy(p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            scale_momenta(c, p, c2);
+            CUDA_TRY(c, cudaMemcpy(c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, cudaMemcpy(c->d.ths, c->d.ths_saved, sizeof(ThermoDev) * rs.size(), cudaMemcpyDeviceToDevice));
+            for(auto& x : rs) {
+                x.c2 = 1.0;
+                x.S = 1.0;
+            }
+            CUDA_TRY(c, cudaMemcpy(c->d.rsc, rs.data(), sizeof(StepScalars) * rs.size(), cudaMemcpyHostToDevice));
+        }
+        return MTG_OK;
     }
     StepScalars s = read_scalars(c);
     if(s.c2 != 1.0 || s.S != 1.0) {
@@ -551,7 +637,7 @@ const char* mtg_last_error(const mtg_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 void mtg_destroy(mtg_ctx* ctx) { delete ctx; }
 
-int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx** out) {
+static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, const BatchSpec* bs, mtg_ctx** out) {
     g_create_error.clear();
     (void)cudaGetLastError();
     if(!sys || !cfg || !out) return fail(nullptr, MTG_E_INVALID, "null argument");
@@ -580,6 +666,8 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
                                     cfg->pressure_respa < 1 || !(cfg->pressure_relax > 0.0)))
         return fail(nullptr, MTG_E_INVALID, "NPT needs 1 <= pressure_nh_len <= MTG_MAX_NH_CHAIN, pressure_respa >= 1, pressure_relax > 0");
     if(cfg->ensemble != MTG_NVT && cfg->ensemble != MTG_NVE && cfg->ensemble != MTG_NPT) return fail(nullptr, MTG_E_INVALID, "bad ensemble");
+    if(bs && (cfg->precision == MTG_PREC_REFERENCE || cfg->ensemble == MTG_NPT))
+        return fail(nullptr, MTG_E_UNSUPPORTED, "batches run in the fp64 or mixed precision mode, NVT or NVE");
     if(cfg->temperature_nh_len < 0 || cfg->temperature_nh_len > kMaxChain) return fail(nullptr, MTG_E_INVALID, "chain length out of range");
     if(cfg->ensemble == MTG_NVT && (cfg->temperature_nh_len < 1 || cfg->temperature_respa < 1 || !(cfg->temperature > 0.0) || !(cfg->temperature_relax > 0.0)))
         return fail(nullptr, MTG_E_INVALID, "NVT needs temperature > 0, relaxation > 0, chain length >= 1, RESPA >= 1");
@@ -660,32 +748,77 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     P.ny = ref_cells(sys->box[1], cfg->cutoff_radius, cfg->neigh_shell);
     P.nz = ref_cells(sys->box[2], cfg->cutoff_radius, cfg->neigh_shell);
     if(P.nx < 1 || P.ny < 1 || P.nz < 1) return fail(nullptr, MTG_E_INVALID, "box narrower than cutoff + shell: the reference cell list is empty");
-    {
-        const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
-        int pn[3];
+    // production cell grid of one box: cell edge >= rlist, or one cell when fewer than 3 fit
+    const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
+    auto grid = [&](const double* box, int natoms, int* pn) -> int {
         for(int a = 0; a < 3; a++) {
-            pn[a] = (int)std::floor(sys->box[a] / rlist);
+            pn[a] = (int)std::floor(box[a] / rlist);
             if(pn[a] < 3) pn[a] = 1;   // small box: scan every atom once (no duplicated images)
         }
         // keep the grid modest: at most ~ n/2 cells
-        while((long long)pn[0] * pn[1] * pn[2] > std::max(27, n / 2)) {
+        while((long long)pn[0] * pn[1] * pn[2] > std::max(27, natoms / 2)) {
             for(int a = 0; a < 3; a++) pn[a] = std::max(3, pn[a] - 1);
             if(pn[0] == 3 && pn[1] == 3 && pn[2] == 3) break;
         }
-        P.pnx = pn[0];
-        P.pny = pn[1];
-        P.pnz = pn[2];
         if(P.precision != MTG_PREC_REFERENCE) {
-            const double half = 0.5 * std::min(sys->box[0], std::min(sys->box[1], sys->box[2]));
+            const double half = 0.5 * std::min(box[0], std::min(box[1], box[2]));
             if(rlist > half && (pn[0] > 1 || pn[1] > 1 || pn[2] > 1))
                 return fail(nullptr, MTG_E_INVALID, "cutoff + skin exceeds half the box");
             if(std::max((double)P.rc, (double)P.rcoul) >= half)
                 return fail(nullptr, MTG_E_INVALID, "cutoff must be below half the box (minimum image)");
         }
+        return MTG_OK;
+    };
+    std::vector<RepDev> reps;
+    {
+        int pn[3];
+        int grc = grid(sys->box, n, pn);
+        if(grc) return grc;
+        P.pnx = pn[0];
+        P.pny = pn[1];
+        P.pnz = pn[2];
     }
     c->ncell_ref = P.nx * P.ny * P.nz;
     c->ncell_prod = P.pnx * P.pny * P.pnz;
     c->nblocks_red = reduction_blocks(n);
+    if(bs) {
+        // replicas: contiguous atom ranges, whole 256-atom blocks each, own cell grid and box
+        const int nr = bs->nrep;
+        reps.resize(nr);
+        int cb = 0, bb = 0;
+        for(int r = 0; r < nr; r++) {
+            RepDev& R = reps[r];
+            R.off = bs->off[r];
+            R.n = bs->n[r];
+            R.bbase = bb;
+            R.nb = reduction_blocks(R.n);
+            bb += R.nb;
+            for(int a = 0; a < 3; a++) {
+                R.box[a] = bs->box[3 * r + a];
+                R.fconv[a] = 4294967296.0 / R.box[a];
+                R.fscale[a] = (float)(R.box[a] / 4294967296.0);
+            }
+            R.rc = P.rc;
+            R.rcoul = P.rcoul;
+            R.skin = P.skin;
+            R.kT = bs->temperature[r] / kConvT;
+            int pn[3];
+            int grc = grid(R.box, R.n, pn);
+            if(grc) return grc;
+            R.cbase = cb;
+            R.pnx = pn[0];
+            R.pny = pn[1];
+            R.pnz = pn[2];
+            cb += pn[0] * pn[1] * pn[2];
+        }
+        P.nrep = nr;
+        P.ncell_total = cb;
+        P.nblk_total = bb;
+        c->ncell_prod = cb;
+        c->nblocks_red = bb;
+        c->rep_off = bs->off;
+        c->h_rep_box = bs->box;
+    }
 
     // ---- tables ----
     const size_t TT = (size_t)T * T;
@@ -861,6 +994,37 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         rc = rc || dalloc(C, &d.baro, 1);
         rc = rc || dalloc(C, &d.thp, 1);
         rc = rc || dalloc(C, &d.thp_saved, 1);
+        if(bs) {
+            const int nr = bs->nrep;
+            std::vector<int> rep_of(n), blk_rep(P.nblk_total);
+            for(int r = 0; r < nr; r++) {
+                for(int i = reps[r].off; i < reps[r].off + reps[r].n; i++) rep_of[i] = r;
+                for(int b = reps[r].bbase; b < reps[r].bbase + reps[r].nb; b++) blk_rep[b] = r;
+            }
+            int* ip2 = nullptr;
+            rc = rc || upload(C, &ip2, rep_of.data(), rep_of.size()); d.rep_of = ip2;
+            rc = rc || upload(C, &ip2, blk_rep.data(), blk_rep.size()); d.blk_rep = ip2;
+            RepDev* rp = nullptr;
+            rc = rc || upload(C, &rp, reps.data(), reps.size()); d.reps = rp;
+            // chains: Q0 = 3 N_r kT_r tau^2, Qj = kT_r tau^2 (NHChain.cpp:115-124), per replica
+            std::vector<ThermoDev> ths(nr);
+            std::vector<StepScalars> rs(nr);
+            for(int r = 0; r < nr; r++) {
+                ThermoDev& th = ths[r];
+                for(int j = 0; j < kMaxChain; j++) th.Q[j] = 1.0;
+                if(P.M > 0) {
+                    th.Q[0] = double(3 * reps[r].n) * reps[r].kT * P.tau * P.tau;
+                    for(int j = 1; j < P.M; j++) th.Q[j] = reps[r].kT * P.tau * P.tau;
+                }
+                for(int j = 0; j < kMaxChain; j++) th.iQ[j] = 1.0 / th.Q[j];
+                rs[r].S = 1.0;
+                rs[r].c2 = 1.0;
+            }
+            rc = rc || upload(C, &d.ths, ths.data(), ths.size());
+            rc = rc || upload(C, &d.ths_saved, ths.data(), ths.size());
+            rc = rc || upload(C, &d.rsc, rs.data(), rs.size());
+            rc = rc || dalloc(C, &d.rrec, (size_t)8 * nr);
+        }
     }
     if(rc) return fail(nullptr, rc, c->err);
     // thermostat masses (NHChain.cpp:115-124): Q0 = dim N kT tau^2, Qj = kT tau^2
@@ -891,8 +1055,9 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     }
     // list capacities: start from a density estimate, grown on demand
     {
-        const double V = sys->box[0] * sys->box[1] * sys->box[2];
-        const double rho = n / V;
+        double V = sys->box[0] * sys->box[1] * sys->box[2];
+        double rho = n / V;
+        for(const RepDev& R : reps) rho = std::max(rho, R.n / (R.box[0] * R.box[1] * R.box[2]));
         const double rc3 = std::pow(cfg->cutoff_radius, 3.0);
         int est = (int)(1.3 * rho * 4.18879 * rc3) + 32;
         rc = grow_neighbors(c.get(), std::min(est, n));
@@ -913,6 +1078,11 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
         rc = rc || add_snap(C, d.th, sizeof(ThermoDev));
         rc = rc || add_snap(C, d.th_saved, sizeof(ThermoDev));
         rc = rc || add_snap(C, d.sc, sizeof(StepScalars));
+        if(bs) {
+            rc = rc || add_snap(C, d.rsc, sizeof(StepScalars) * bs->nrep);
+            rc = rc || add_snap(C, d.ths, sizeof(ThermoDev) * bs->nrep);
+            rc = rc || add_snap(C, d.ths_saved, sizeof(ThermoDev) * bs->nrep);
+        }
         if(P.ensemble == MTG_NPT) {
             rc = rc || add_snap(C, d.baro, sizeof(BaroDev));
             rc = rc || add_snap(C, d.thp, sizeof(ThermoDev));
@@ -940,6 +1110,10 @@ int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx**
     return MTG_OK;
 }
 
+int mtg_create(const mtg_system_desc* sys, const mtg_config_desc* cfg, mtg_ctx** out) {
+    return create_impl(sys, cfg, nullptr, out);
+}
+
 int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo_state* th) {
     if(!c) return MTG_E_INVALID;
     const size_t n3 = (size_t)c->P.n * 3;
@@ -955,6 +1129,7 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
         if(!finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
         CUDA_TRY(c, cudaMemcpy(c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
     }
+    if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch sets chain states per replica (mtg_batch_set_thermo)");
     if(th) {
         ThermoDev t{};
         CUDA_TRY(c, cudaMemcpy(&t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
@@ -997,6 +1172,7 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
     }
     if(p) CUDA_TRY(c, cudaMemcpyAsync(p, c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch reads chain states per replica (mtg_batch_get_thermo)");
     if(th) {
         ThermoDev t{};
         CUDA_TRY(c, cudaMemcpy(&t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
@@ -1079,7 +1255,8 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             c->stats.list_builds = s.builds - builds0;
             if(output) {
                 double rec[8];
-                CUDA_TRY(c, cudaMemcpy(rec, c->d.rec, sizeof(rec), cudaMemcpyDeviceToHost));
+                int rrc = read_records(c, rec);
+                if(rrc) return rrc;
                 if(!std::isfinite(rec[0]) || !std::isfinite(rec[1])) return fail(c, MTG_E_NONFINITE, "non-finite energy during the run");
                 if(cb) {
                     int frc = fetch_rp(c, s.c2);
@@ -1134,6 +1311,7 @@ int mtg_compute_forces(mtg_ctx* c, double* F, double* Fpi, double* U) {
 int mtg_get_cells(mtg_ctx* c, int32_t* dims, int32_t* ixyz, int32_t* cell_first, int32_t* cell_count, int32_t ncells,
                   int32_t* cell_list) {
     if(!c) return MTG_E_INVALID;
+    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "the reference cell list is not built for batches");
     CUDA_TRY(c, cudaSetDevice(c->device));
     if(dims) {
         dims[0] = c->P.nx;
@@ -1155,6 +1333,7 @@ int mtg_get_cells(mtg_ctx* c, int32_t* dims, int32_t* ixyz, int32_t* cell_first,
 
 int mtg_get_neighbors(mtg_ctx* c, int32_t max_neigh, int32_t* count, int32_t* list, int32_t* needed) {
     if(!c) return MTG_E_INVALID;
+    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "the reference neighbour list is not built for batches");
     CUDA_TRY(c, cudaSetDevice(c->device));
     if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
     for(int attempt = 0; attempt < 64; attempt++) {
@@ -1188,6 +1367,7 @@ int mtg_optimize(mtg_ctx* c, double accuracy, int max_steps, int out_stride, mtg
     // CMDLoop::runOptimization (MDLoop.cpp:143-173): F at the current positions, r += lr F,
     // U_{n+1} = U(F's positions), stop when |U_{n+1} - U_n| < accuracy after more than out_stride steps.
     if(!c || max_steps < 0) return MTG_E_INVALID;
+    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "gradient descent runs on single systems; relax replicas before batching");
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = settle_state(c);
     if(rc) return rc;
@@ -1303,6 +1483,171 @@ int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
 int mtg_get_run_stats(mtg_ctx* c, mtg_run_stats* st) {
     if(!c || !st) return MTG_E_INVALID;
     *st = c->stats;
+    return MTG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batches of replicas
+// ---------------------------------------------------------------------------------------------
+int mtg_batch_create(const mtg_system_desc* const* systems, int32_t nrep, const mtg_config_desc* cfg,
+                     const double* temperatures, mtg_ctx** out) {
+    g_create_error.clear();
+    if(!systems || nrep < 1 || !cfg || !out) return fail(nullptr, MTG_E_INVALID, "null argument or no replicas");
+    *out = nullptr;
+    const mtg_system_desc* s0 = systems[0];
+    if(!s0) return fail(nullptr, MTG_E_INVALID, "null replica");
+    const int T = s0->n_types;
+    if(T <= 0 || !s0->nb_count) return fail(nullptr, MTG_E_INVALID, "replica 0: missing types");
+    auto same_terms = [](const mtg_term* a, const mtg_term* b, int cnt) -> bool {
+        for(int q = 0; q < cnt; q++) {
+            if(a[q].kind != b[q].kind) return false;
+            for(int w = 0; w < 4; w++)
+                if(a[q].p[w] != b[q].p[w]) return false;
+        }
+        return true;
+    };
+    long long N = 0;
+    for(int r = 0; r < nrep; r++) {
+        const mtg_system_desc* s = systems[r];
+        if(!s || s->n_atoms <= 0 || !s->r || !s->mass || !s->charge || !s->type || !s->nb_count)
+            return fail(nullptr, MTG_E_INVALID, "replica " + std::to_string(r) + ": missing atom arrays");
+        if(s->n_types != T || s->n_bond_types != s0->n_bond_types || s->n_angle_types != s0->n_angle_types ||
+           s->n_dih_types != s0->n_dih_types)
+            return fail(nullptr, MTG_E_INVALID, "replica " + std::to_string(r) + ": replicas must share one force field");
+        if(s->nb_tables || s->bond_tables || s->angle_tables || s->dih_tables)
+            return fail(nullptr, MTG_E_UNSUPPORTED, "batches use the analytic terms (no tables)");
+        for(int q = 0; q < T * T; q++) {
+            if(s->nb_count[q] != s0->nb_count[q] || s->nb_count[q] < 0 || s->nb_count[q] > kMaxFF ||
+               !same_terms(s->nb_terms + q * kMaxFF, s0->nb_terms + q * kMaxFF, s->nb_count[q]))
+                return fail(nullptr, MTG_E_INVALID, "replica " + std::to_string(r) + ": replicas must share one force field");
+        }
+        if(!same_terms(s->bond_terms, s0->bond_terms, s0->n_bond_types) || !same_terms(s->angle_terms, s0->angle_terms, s0->n_angle_types) ||
+           !same_terms(s->dih_terms, s0->dih_terms, s0->n_dih_types))
+            return fail(nullptr, MTG_E_INVALID, "replica " + std::to_string(r) + ": replicas must share one force field");
+        if(temperatures && !(temperatures[r] > 0.0)) return fail(nullptr, MTG_E_INVALID, "temperatures must be positive");
+        N += s->n_atoms;
+    }
+    if(N > (long long)kIdxMask) return fail(nullptr, MTG_E_INVALID, "too many atoms in the batch");
+    // merged system: atoms concatenated, molecule indices made distinct, topology offset
+    BatchSpec bs;
+    bs.nrep = nrep;
+    std::vector<double> r3, p3, m, q;
+    std::vector<int32_t> type, mol, bonds, angles, dihs;
+    std::vector<uint8_t> mobile;
+    double big[3] = {0.0, 0.0, 0.0};
+    int off = 0, molbase = 0;
+    for(int rr = 0; rr < nrep; rr++) {
+        const mtg_system_desc* s = systems[rr];
+        const int n = s->n_atoms;
+        bs.off.push_back(off);
+        bs.n.push_back(n);
+        for(int a = 0; a < 3; a++) {
+            bs.box.push_back(s->box[a]);
+            big[a] = std::max(big[a], s->box[a]);
+        }
+        bs.temperature.push_back(temperatures ? temperatures[rr] : cfg->temperature);
+        r3.insert(r3.end(), s->r, s->r + 3 * n);
+        if(s->p) p3.insert(p3.end(), s->p, s->p + 3 * n);
+        else p3.insert(p3.end(), (size_t)3 * n, 0.0);
+        m.insert(m.end(), s->mass, s->mass + n);
+        q.insert(q.end(), s->charge, s->charge + n);
+        type.insert(type.end(), s->type, s->type + n);
+        int mmax = -1;
+        for(int i = 0; i < n; i++) {
+            const int mi = s->mol ? s->mol[i] : -1;
+            mol.push_back(mi >= 0 ? mi + molbase : -1);
+            mmax = std::max(mmax, mi);
+            mobile.push_back(s->mobile ? s->mobile[i] : 1);
+        }
+        molbase += mmax + 1;
+        auto add_topo = [&](std::vector<int32_t>& dst, int cnt, const int32_t* src, int w) {
+            for(int j = 0; j < cnt; j++)
+                for(int k = 0; k < w; k++) dst.push_back(k < w - 1 ? src[w * j + k] + off : src[w * j + k]);
+        };
+        if(s->n_bonds > 0 && s->bonds) add_topo(bonds, s->n_bonds, s->bonds, 3);
+        if(s->n_angles > 0 && s->angles) add_topo(angles, s->n_angles, s->angles, 4);
+        if(s->n_dihedrals > 0 && s->dihedrals) add_topo(dihs, s->n_dihedrals, s->dihedrals, 5);
+        off += n;
+    }
+    bs.off.push_back(off);
+    mtg_system_desc md = *s0;
+    md.n_atoms = off;
+    md.r = r3.data();
+    md.p = p3.data();
+    md.mass = m.data();
+    md.charge = q.data();
+    md.type = type.data();
+    md.mol = mol.data();
+    md.mobile = mobile.data();
+    for(int a = 0; a < 3; a++) md.box[a] = big[a];
+    md.n_bonds = (int32_t)(bonds.size() / 3);
+    md.bonds = bonds.empty() ? nullptr : bonds.data();
+    md.n_angles = (int32_t)(angles.size() / 4);
+    md.angles = angles.empty() ? nullptr : angles.data();
+    md.n_dihedrals = (int32_t)(dihs.size() / 5);
+    md.dihedrals = dihs.empty() ? nullptr : dihs.data();
+    return create_impl(&md, cfg, &bs, out);
+}
+
+int mtg_batch_info(mtg_ctx* c, int32_t* nrep, int32_t* offsets) {
+    if(!c) return MTG_E_INVALID;
+    if(nrep) *nrep = c->P.nrep;
+    if(offsets)
+        for(size_t r = 0; r < c->rep_off.size(); r++) offsets[r] = c->rep_off[r];
+    return MTG_OK;
+}
+
+int mtg_batch_get_records(mtg_ctx* c, double* rec) {
+    if(!c || !rec) return MTG_E_INVALID;
+    if(!c->P.nrep) return fail(c, MTG_E_INVALID, "not a batch");
+    if(c->h_rrec.size() != (size_t)8 * c->P.nrep) return fail(c, MTG_E_INVALID, "no output step yet");
+    for(int r = 0; r < c->P.nrep; r++) {
+        const double* x = &c->h_rrec[(size_t)8 * r];
+        double* o = rec + 6 * r;
+        o[0] = x[2];   // T
+        o[1] = x[3];   // P
+        o[2] = x[4];   // V
+        o[3] = x[0];   // U
+        o[4] = x[1];   // K
+        o[5] = x[0] + x[1];
+    }
+    return MTG_OK;
+}
+
+int mtg_batch_set_thermo(mtg_ctx* c, int32_t rep, const mtg_thermo_state* th) {
+    if(!c || !th) return MTG_E_INVALID;
+    if(rep < 0 || rep >= c->P.nrep) return fail(c, MTG_E_INVALID, "replica index out of range");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    ThermoDev t{};
+    CUDA_TRY(c, cudaMemcpy(&t, c->d.ths + rep, sizeof(t), cudaMemcpyDeviceToHost));
+    const int M = std::min<int>(th->M, kMaxChain);
+    for(int j = 0; j < M; j++) {
+        t.eta[j] = th->eta[j];
+        t.peta[j] = th->p_eta[j];
+    }
+    CUDA_TRY(c, cudaMemcpy(c->d.ths + rep, &t, sizeof(t), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d.ths_saved + rep, &t, sizeof(t), cudaMemcpyHostToDevice));
+    return MTG_OK;
+}
+
+int mtg_batch_get_thermo(mtg_ctx* c, int32_t rep, mtg_thermo_state* th) {
+    if(!c || !th) return MTG_E_INVALID;
+    if(rep < 0 || rep >= c->P.nrep) return fail(c, MTG_E_INVALID, "replica index out of range");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    ThermoDev t{};
+    CUDA_TRY(c, cudaMemcpy(&t, c->d.ths + rep, sizeof(t), cudaMemcpyDeviceToHost));
+    std::memset(th, 0, sizeof(*th));
+    th->M = c->P.M;
+    for(int j = 0; j < c->P.M; j++) {
+        th->eta[j] = t.eta[j];
+        th->p_eta[j] = t.peta[j];
+    }
+    if(c->h_rep_box.size() == (size_t)3 * c->P.nrep)
+        for(int a = 0; a < 3; a++) th->box[a] = c->h_rep_box[(size_t)3 * rep + a];
     return MTG_OK;
 }
 

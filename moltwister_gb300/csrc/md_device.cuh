@@ -386,6 +386,20 @@ __device__ inline void block_sum(double (&v)[NV], double* smem /* [32*NV] */) {
 
 // Last-block election: every block stores its partials, fences, and bumps the counter; the block
 // that observes the final count reads all partials (in block order) and resets the counter.
+// The same election among the `nblocks` blocks that share `counter` (one replica of a batch).
+__device__ inline bool last_block_of(unsigned int* counter, unsigned int nblocks) {
+    __shared__ bool is_last_of;
+    __threadfence();
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        unsigned int prev = atomicAdd(counter, 1u);
+        is_last_of = (prev == nblocks - 1);
+    }
+    __syncthreads();
+    if(is_last_of) __threadfence();
+    return is_last_of;
+}
+
 __device__ inline bool last_block(unsigned int* counter) {
     __shared__ bool is_last;
     __threadfence();

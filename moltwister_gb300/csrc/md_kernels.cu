@@ -31,7 +31,56 @@ int reduction_blocks(int n) {
     return b < 1 ? 1 : b;
 }
 
+int integration_blocks(const Params& P) { return P.nrep ? P.nblk_total : reduction_blocks(P.n); }
+
 namespace {
+
+// The system an atom or an integration block belongs to: the whole context (r < 0), or replica r
+// of a batch.  Gives the atom and block ranges, cell grid, box, cutoffs, temperature and the
+// per-system scalars, chains and output record.
+struct SysView {
+    int off, n, bbase, nb;
+    int cbase, pnx, pny, pnz;
+    double box[3];
+    double fconv[3];
+    float fscale[3];
+    float rc, rcoul, skin;
+    double kT;
+    StepScalars* sc;
+    ThermoDev* th;
+    ThermoDev* th_saved;
+    double* rec;
+};
+
+__device__ __forceinline__ SysView sys_view(const DevSys& d, const Params& P, int r) {
+    SysView v;
+    if(r < 0) {
+        v.off = 0; v.n = P.n; v.bbase = 0; v.nb = (P.n + 255) / 256;
+        v.cbase = 0; v.pnx = P.pnx; v.pny = P.pny; v.pnz = P.pnz;
+        for(int a = 0; a < 3; a++) {
+            v.box[a] = P.box[a];
+            v.fconv[a] = P.fconv[a];
+            v.fscale[a] = P.fscale[a];
+        }
+        v.rc = P.rc; v.rcoul = P.rcoul; v.skin = P.skin; v.kT = P.kT;
+        v.sc = d.sc; v.th = d.th; v.th_saved = d.th_saved; v.rec = d.rec;
+    } else {
+        const RepDev& R = d.reps[r];
+        v.off = R.off; v.n = R.n; v.bbase = R.bbase; v.nb = R.nb;
+        v.cbase = R.cbase; v.pnx = R.pnx; v.pny = R.pny; v.pnz = R.pnz;
+        for(int a = 0; a < 3; a++) {
+            v.box[a] = R.box[a];
+            v.fconv[a] = R.fconv[a];
+            v.fscale[a] = R.fscale[a];
+        }
+        v.rc = R.rc; v.rcoul = R.rcoul; v.skin = R.skin; v.kT = R.kT;
+        v.sc = d.rsc + r; v.th = d.ths + r; v.th_saved = d.ths_saved + r; v.rec = d.rrec + 8 * r;
+    }
+    return v;
+}
+
+__device__ __forceinline__ int rep_of_atom(const DevSys& d, const Params& P, int i) { return P.nrep ? d.rep_of[i] : -1; }
+__device__ __forceinline__ int rep_of_block(const DevSys& d, const Params& P) { return P.nrep ? d.blk_rep[blockIdx.x] : -1; }
 
 
 // ---------------------------------------------------------------------------------------------
@@ -39,9 +88,10 @@ namespace {
 // ---------------------------------------------------------------------------------------------
 __global__ void k_prologue(DevSys d, Params P) {
     __shared__ double smem[32 * 2];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const SysView sv = sys_view(d, P, rep_of_block(d, P));
+    const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
     double v[2] = {0.0, 0.0};   // sum p^2/m, sum F.r (NPT: G_eps of the first step, VelVerlet.cpp:60)
-    if(k < P.n) {
+    if(k < sv.off + sv.n) {
         const double px = d.p[3 * k], py = d.p[3 * k + 1], pz = d.p[3 * k + 2];
         v[0] = (px * px + py * py + pz * pz) / d.m[k];
         if(P.ensemble == MTG_NPT)
@@ -52,17 +102,17 @@ __global__ void k_prologue(DevSys d, Params P) {
         d.partial[blockIdx.x * 4] = v[0];
         d.partial[blockIdx.x * 4 + 1] = v[1];
     }
-    if(last_block(&d.sc->done_blocks)) {
+    if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
         __shared__ double tot, tot_fr;
         if(threadIdx.x == 0) {
             double KE2 = 0.0, fr = 0.0;
-            for(int b = 0; b < (int)gridDim.x; b++) {
+            for(int b = sv.bbase; b < sv.bbase + sv.nb; b++) {
                 KE2 += d.partial[b * 4];
                 fr += d.partial[b * 4 + 1];
             }
             tot = KE2;
             tot_fr = fr;
-            d.sc->done_blocks = 0;
+            sv.sc->done_blocks = 0;
         }
         __syncthreads();
         if(P.ensemble == MTG_NPT) {
@@ -73,10 +123,14 @@ __global__ void k_prologue(DevSys d, Params P) {
         if(threadIdx.x < 96) {
             double KE2 = tot;
             double c2 = 1.0, c1 = 1.0;
-            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat(P, d.sc, d.th, d.th_saved, KE2, false, &c2, &c1);
+            Params Q = P;
+            Q.n = sv.n;
+            Q.kT = sv.kT;
+            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat(Q, sv.sc, sv.th, sv.th_saved, KE2, false, &c2, &c1);
             if(threadIdx.x == 0) {
-                d.sc->S = c1;
-                d.sc->c2 = 1.0;
+                sv.sc->S = c1;
+                sv.sc->c2 = 1.0;
+                if(sv.sc->timeout) d.sc->timeout = 1;
             }
         }
     }
@@ -105,7 +159,7 @@ __device__ __forceinline__ unsigned int frac32(double x, double conv) {
     return (unsigned int)(unsigned long long)__double2ll_rn(x * conv);
 }
 
-__device__ __forceinline__ void store_pos(const DevSys& d, const Params& P, int i, double x, double y, double z,
+__device__ __forceinline__ void store_pos(const DevSys& d, const double* conv, int i, double x, double y, double z,
                                           bool mixed) {
     if(mixed) {
         const float hx = (float)x, hy = (float)y, hz = (float)z;
@@ -117,9 +171,9 @@ __device__ __forceinline__ void store_pos(const DevSys& d, const Params& P, int 
         d.hi[i] = h;
         d.lo[i] = l;
         uint4 q = d.pq[i];
-        q.x = frac32(x, P.fconv[0]);
-        q.y = frac32(y, P.fconv[1]);
-        q.z = frac32(z, P.fconv[2]);
+        q.x = frac32(x, conv[0]);
+        q.y = frac32(y, conv[1]);
+        q.z = frac32(z, conv[2]);
         d.pq[i] = q;
     } else {
         d.r[3 * i] = x;
@@ -144,18 +198,18 @@ __device__ __forceinline__ void load_force(const DevSys& d, int i, double& fx, d
 // Integration
 // ---------------------------------------------------------------------------------------------
 template<bool MIXED>
-__device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, int k, int* any);
+__device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, const SysView& v, int k);
 
+// One 256-atom block per launch block; a batch maps blocks to replicas (blk_rep).
 template<bool MIXED>
 __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const SysView v = sys_view(d, P, rep_of_block(d, P));
+    const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
+    const bool mine = k < v.off + v.n;
     if(cond) {
         // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
         // graph's IF node that wraps the list build
-        __shared__ int any;
-        if(threadIdx.x == 0) any = 0;
-        __syncthreads();
-        if(k < P.n) kick_drift_atom<MIXED>(d, P, k, &any);
+        if(mine) kick_drift_atom<MIXED>(d, P, v, k);
         if(last_block(&d.sc->done_blocks)) {
             if(threadIdx.x == 0) {
                 d.sc->done_blocks = 0;
@@ -164,13 +218,13 @@ __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
         }
         return;
     }
-    if(k >= P.n) return;
-    kick_drift_atom<MIXED>(d, P, k, nullptr);
+    if(!mine) return;
+    kick_drift_atom<MIXED>(d, P, v, k);
 }
 
 template<bool MIXED>
-__device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, int k, int* any) {
-    const double S = d.sc->S;
+__device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, const SysView& v, int k) {
+    const double S = v.sc->S;
     const double dt_2 = P.dt / 2.0;
     const double dm = P.dt / d.m[k];
     double fx, fy, fz, x, y, z;
@@ -185,14 +239,13 @@ __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, int 
     x += px * dm;
     y += py * dm;
     z += pz * dm;
-    store_pos(d, P, k, x, y, z, MIXED);
+    store_pos(d, v.fconv, k, x, y, z, MIXED);
     // displacement since the last list build (minimum image: wrapping is not a displacement)
-    const double bx = minimg_d(x - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
-    const double by = minimg_d(y - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
-    const double bz = minimg_d(z - d.r_build[3 * k + 2], P.box[2], 1.0 / P.box[2]);
-    const double h = 0.5 * double(P.skin);
+    const double bx = minimg_d(x - d.r_build[3 * k], v.box[0], 1.0 / v.box[0]);
+    const double by = minimg_d(y - d.r_build[3 * k + 1], v.box[1], 1.0 / v.box[1]);
+    const double bz = minimg_d(z - d.r_build[3 * k + 2], v.box[2], 1.0 / v.box[2]);
+    const double h = 0.5 * double(v.skin);
     if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
-    (void)any;
 }
 
 __device__ __forceinline__ double wrap_coord(double x, double Lm) {
@@ -206,9 +259,10 @@ __device__ __forceinline__ double wrap_coord(double x, double Lm) {
 template<bool MIXED, bool OUTPUT>
 __global__ void k_pkick2(DevSys d, Params P) {
     __shared__ double smem[32 * 3];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const SysView sv = sys_view(d, P, rep_of_block(d, P));
+    const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
-    if(k < P.n) {
+    if(k < sv.off + sv.n) {
         const double dt_2 = P.dt / 2.0;
         double f[3], r[3];
         load_force(d, k, f[0], f[1], f[2], MIXED);
@@ -227,11 +281,11 @@ __global__ void k_pkick2(DevSys d, Params P) {
             }
             const double p = d.p[3 * k + a] + f[a] * dt_2;
             d.p[3 * k + a] = p;
-            r[a] = wrap_coord(r[a], P.box[a]);
+            r[a] = wrap_coord(r[a], sv.box[a]);
             p2 += p * p;
             fr += f[a] * r[a];
         }
-        store_pos(d, P, k, r[0], r[1], r[2], MIXED);
+        store_pos(d, sv.fconv, k, r[0], r[1], r[2], MIXED);
         v[0] = p2 / d.m[k];
         if(OUTPUT) {
             v[1] = fr;
@@ -244,18 +298,27 @@ __global__ void k_pkick2(DevSys d, Params P) {
         d.partial[blockIdx.x * 4 + 1] = v[1];
         d.partial[blockIdx.x * 4 + 2] = v[2];
     }
-    if(last_block(&d.sc->done_blocks)) {
+    if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
         __shared__ double tot[3];
         if(threadIdx.x == 0) {
             double s[3] = {0.0, 0.0, 0.0};
-            for(int b = 0; b < (int)gridDim.x; b++)
+            for(int b = sv.bbase; b < sv.bbase + sv.nb; b++)
                 for(int q = 0; q < 3; q++) s[q] += d.partial[b * 4 + q];
             for(int q = 0; q < 3; q++) tot[q] = s[q];
-            d.sc->done_blocks = 0;
+            sv.sc->done_blocks = 0;
         }
         __syncthreads();
         if(threadIdx.x < 96) {
-            end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
+            if(P.nrep) {
+                Params Q = P;   // the replica's size, temperature and box
+                Q.n = sv.n;
+                Q.kT = sv.kT;
+                for(int a = 0; a < 3; a++) Q.box[a] = sv.box[a];
+                end_of_step(Q, sv.sc, sv.th, sv.th_saved, tot[0], tot[2], tot[1], OUTPUT, sv.rec);
+                if(threadIdx.x == 0 && sv.sc->timeout) d.sc->timeout = 1;
+            } else {
+                end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
+            }
         }
     }
 }
@@ -274,13 +337,14 @@ __global__ void k_pcell_assign(DevSys d, Params P) {
     d.r_build[3 * i + 1] = y;
     d.r_build[3 * i + 2] = z;
     d.rb4[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
-    int ix = (int)floor((x + 0.5 * P.box[0]) * P.pnx / P.box[0]);
-    int iy = (int)floor((y + 0.5 * P.box[1]) * P.pny / P.box[1]);
-    int iz = (int)floor((z + 0.5 * P.box[2]) * P.pnz / P.box[2]);
-    ix = ix < 0 ? 0 : (ix >= P.pnx ? P.pnx - 1 : ix);
-    iy = iy < 0 ? 0 : (iy >= P.pny ? P.pny - 1 : iy);
-    iz = iz < 0 ? 0 : (iz >= P.pnz ? P.pnz - 1 : iz);
-    const int c = ix + P.pnx * (iy + P.pny * iz);
+    const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
+    int ix = (int)floor((x + 0.5 * v.box[0]) * v.pnx / v.box[0]);
+    int iy = (int)floor((y + 0.5 * v.box[1]) * v.pny / v.box[1]);
+    int iz = (int)floor((z + 0.5 * v.box[2]) * v.pnz / v.box[2]);
+    ix = ix < 0 ? 0 : (ix >= v.pnx ? v.pnx - 1 : ix);
+    iy = iy < 0 ? 0 : (iy >= v.pny ? v.pny - 1 : iy);
+    iz = iz < 0 ? 0 : (iz >= v.pnz ? v.pnz - 1 : iz);
+    const int c = v.cbase + ix + v.pnx * (iy + v.pny * iz);
     d.pcell_of[i] = c;
     atomicAdd(&d.pcell_count[c], 1);
 }
@@ -355,27 +419,29 @@ __device__ __forceinline__ int excl_class(const DevSys& d, int k, int i) {
 }
 
 template<bool MIXED>
-__global__ void k_vlist(DevSys d, Params P, float rlist) {
+__global__ void k_vlist(DevSys d, Params P) {
     if(!d.sc->rebuild) return;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(i >= P.n) return;
+    const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
+    const float rlist = fmaxf(v.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? v.rcoul : 0.0f) + v.skin;
     // FP32 distances: rounding (~1e-6 A) is far inside the skin margin
     const float4 ri = d.rb4[i];
     const float rl2 = rlist * rlist;
-    const float Lx = P.boxf[0], Ly = P.boxf[1], Lz = P.boxf[2];
+    const float Lx = (float)v.box[0], Ly = (float)v.box[1], Lz = (float)v.box[2];
     const float iLx = 1.0f / Lx, iLy = 1.0f / Ly, iLz = 1.0f / Lz;
-    const int ci = d.pcell_of[i];
-    const int cx = ci % P.pnx, cy = (ci / P.pnx) % P.pny, cz = ci / (P.pnx * P.pny);
-    const int sx = P.pnx >= 3 ? 3 : 1, sy = P.pny >= 3 ? 3 : 1, sz = P.pnz >= 3 ? 3 : 1;
+    const int ci = d.pcell_of[i] - v.cbase;
+    const int cx = ci % v.pnx, cy = (ci / v.pnx) % v.pny, cz = ci / (v.pnx * v.pny);
+    const int sx = v.pnx >= 3 ? 3 : 1, sy = v.pny >= 3 ? 3 : 1, sz = v.pnz >= 3 ? 3 : 1;
     uint32_t* out = d.vlist + (size_t)i * d.vmax;
     int cnt = 0;
     for(int oz = 0; oz < sz; oz++) {
-        const int z = sz == 1 ? 0 : (cz + oz - 1 + P.pnz) % P.pnz;
+        const int z = sz == 1 ? 0 : (cz + oz - 1 + v.pnz) % v.pnz;
         for(int oy = 0; oy < sy; oy++) {
-            const int y = sy == 1 ? 0 : (cy + oy - 1 + P.pny) % P.pny;
+            const int y = sy == 1 ? 0 : (cy + oy - 1 + v.pny) % v.pny;
             for(int ox = 0; ox < sx; ox++) {
-                const int x = sx == 1 ? 0 : (cx + ox - 1 + P.pnx) % P.pnx;
-                const int c = x + P.pnx * (y + P.pny * z);
+                const int x = sx == 1 ? 0 : (cx + ox - 1 + v.pnx) % v.pnx;
+                const int c = v.cbase + x + v.pnx * (y + v.pny * z);
                 const int first = d.pcell_first[c], n = d.pcell_count[c];
                 for(int base = 0; base < n; base += 32) {
                     bool take = false;
@@ -507,15 +573,16 @@ __device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir
 // Relative vector r_i - r_j (minimum image) in the arithmetic precision R.
 template<bool MIXED, class R>
 __device__ __forceinline__ void rel(const DevSys& d, const Params& P, int i, int j, R& dx, R& dy, R& dz) {
+    const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
     if(MIXED) {
         const uint4 qi = d.pq[i], qj = d.pq[j];
-        dx = (R)__int2float_rn((int)(qi.x - qj.x)) * (R)P.fscale[0];
-        dy = (R)__int2float_rn((int)(qi.y - qj.y)) * (R)P.fscale[1];
-        dz = (R)__int2float_rn((int)(qi.z - qj.z)) * (R)P.fscale[2];
+        dx = (R)__int2float_rn((int)(qi.x - qj.x)) * (R)v.fscale[0];
+        dy = (R)__int2float_rn((int)(qi.y - qj.y)) * (R)v.fscale[1];
+        dz = (R)__int2float_rn((int)(qi.z - qj.z)) * (R)v.fscale[2];
     } else {
-        dx = (R)minimg_d(d.r[3 * i] - d.r[3 * j], P.box[0], 1.0 / P.box[0]);
-        dy = (R)minimg_d(d.r[3 * i + 1] - d.r[3 * j + 1], P.box[1], 1.0 / P.box[1]);
-        dz = (R)minimg_d(d.r[3 * i + 2] - d.r[3 * j + 2], P.box[2], 1.0 / P.box[2]);
+        dx = (R)minimg_d(d.r[3 * i] - d.r[3 * j], v.box[0], 1.0 / v.box[0]);
+        dy = (R)minimg_d(d.r[3 * i + 1] - d.r[3 * j + 1], v.box[1], 1.0 / v.box[1]);
+        dz = (R)minimg_d(d.r[3 * i + 2] - d.r[3 * j + 2], v.box[2], 1.0 / v.box[2]);
     }
 }
 
@@ -694,15 +761,16 @@ constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
 template<bool MIXED, bool ENERGY, class R>
 __device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, R qi,
                                            R rc2, R rq2, R irc, R kq, const PairCoef* pc, const int* pmode,
-                                           const float* qt, uint4 qi4, R& dx, R& dy, R& dz, R& g, R& u) {
+                                           const float* qt, uint4 qi4, const float (&fs)[3], R& dx, R& dy, R& dz,
+                                           R& g, R& u) {
     const int j = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
     int tj;
     if(MIXED) {
         const uint4 qj4 = d.pq[j];
-        dx = (R)__int2float_rn((int)(qi4.x - qj4.x)) * (R)P.fscale[0];
-        dy = (R)__int2float_rn((int)(qi4.y - qj4.y)) * (R)P.fscale[1];
-        dz = (R)__int2float_rn((int)(qi4.z - qj4.z)) * (R)P.fscale[2];
+        dx = (R)__int2float_rn((int)(qi4.x - qj4.x)) * (R)fs[0];
+        dy = (R)__int2float_rn((int)(qi4.y - qj4.y)) * (R)fs[1];
+        dz = (R)__int2float_rn((int)(qi4.z - qj4.z)) * (R)fs[2];
         tj = (int)qj4.w;
     } else {
         rel<MIXED, R>(d, P, i, j, dx, dy, dz);
@@ -739,7 +807,7 @@ __device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int
         const R qq = kq * qi * qj;
         if(P.coulomb == MTG_COULOMB_SHIFTED) {
             g += qq * (ir2 - irc * irc) * ir;
-            if(ENERGY) u += qq * (ir - irc + (r2 * ir - (R)P.rcoul) * irc * irc);
+            if(ENERGY) u += qq * (ir - irc + (r2 * ir - R(1) / irc) * irc * irc);
         } else {
             g += qq * ir2 * ir;
             if(ENERGY) u += qq * ir;
@@ -794,9 +862,11 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     Fix fx{0, 0}, fy{0, 0}, fz{0, 0}, fu{0, 0};   // mixed: exact fixed point
     double bx = 0, by = 0, bz = 0, bu = 0;        // fp64
     if(mob) {
-        const R rc2 = (R)P.rc * (R)P.rc;
-        const R rq2 = (R)P.rcoul * (R)P.rcoul;
-        const R irc = R(1) / (R)P.rcoul;
+        const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
+        const R rc2 = (R)v.rc * (R)v.rc;
+        const R rq2 = (R)v.rcoul * (R)v.rcoul;
+        const R irc = R(1) / (R)v.rcoul;
+        const float fs[3] = {v.fscale[0], v.fscale[1], v.fscale[2]};
         const uint4 qi4 = MIXED ? d.pq[i] : make_uint4(0, 0, 0, 0);
         const int ti = MIXED ? (int)qi4.w : d.type[i];
         const R qi = MIXED ? (R)d.qf[i] : (R)d.qd[i];
@@ -811,7 +881,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
 #pragma unroll
             for(int q = 0; q < 4; q++) {
                 R dx, dy, dz, g, u;
-                pair_entry<MIXED, ENERGY, R>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, dx, dy, dz, g, u);
+                pair_entry<MIXED, ENERGY, R>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, fs, dx, dy, dz, g, u);
                 if(MIXED) {
                     g = fminf(fmaxf(g, -gmax), gmax);
                     fix_add(fx, (float)(g * dx));
@@ -826,7 +896,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         }
         for(; e < cnt; e += TEAM) {
             R dx, dy, dz, g, u;
-            pair_entry<MIXED, ENERGY, R>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, dx, dy, dz, g, u);
+            pair_entry<MIXED, ENERGY, R>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, fs, dx, dy, dz, g, u);
             if(MIXED) {
                 g = fminf(fmaxf(g, -gmax), gmax);
                 fix_add(fx, (float)(g * dx));
@@ -894,7 +964,8 @@ __global__ void k_sync_pos(DevSys d, Params P, int to_master) {
         uint4 q = d.pq[i];
         q.w = (unsigned int)d.type[i];
         d.pq[i] = q;
-        store_pos(d, P, i, d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2], true);
+        const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
+        store_pos(d, v.fconv, i, d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2], true);
         float4 h = d.hi[i], l = d.lo[i];
         h.w = d.qf[i];
         l.w = __int_as_float(d.type[i]);
@@ -942,7 +1013,7 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
             fr += f[a] * r[a];
             p2 += d.p[3 * k + a] * d.p[3 * k + a];
         }
-        store_pos(d, P, k, r[0], r[1], r[2], mixed);
+        store_pos(d, P.fconv, k, r[0], r[1], r[2], mixed);
         if(mode != MTG_PREC_REFERENCE) {
             const double bx = minimg_d(r[0] - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
             const double by = minimg_d(r[1] - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
@@ -986,16 +1057,17 @@ void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s)
 }
 
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
-    k_prologue<<<reduction_blocks(P.n), 256, 0, s>>>(d, P);
+    k_prologue<<<integration_blocks(P), 256, 0, s>>>(d, P);
 }
 
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {
-    if(P.precision == MTG_PREC_MIXED) k_pkick_drift<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P, cond);
-    else k_pkick_drift<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P, cond);
+    const int nb = integration_blocks(P);
+    if(P.precision == MTG_PREC_MIXED) k_pkick_drift<true><<<nb, 256, 0, s>>>(d, P, cond);
+    else k_pkick_drift<false><<<nb, 256, 0, s>>>(d, P, cond);
 }
 
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
-    const int ncell = P.pnx * P.pny * P.pnz;
+    const int ncell = P.nrep ? P.ncell_total : P.pnx * P.pny * P.pnz;
     if(force) cudaMemsetAsync(&d.sc->rebuild, 0xff, sizeof(int32_t), s);
     // counts are cleared unconditionally; the kernels below return early when no rebuild is due
     cudaMemsetAsync(d.pcell_count, 0, sizeof(int) * ncell, s);
@@ -1004,9 +1076,8 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     k_pcell_scan<<<1, 1024, 0, s>>>(d, ncell);
     k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell);
-    const float rlist = fmaxf(P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? P.rcoul : 0.0f) + P.skin;
-    if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, rlist);
-    else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, rlist);
+    if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
+    else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     k_clear_rebuild<<<1, 32, 0, s>>>(d);
 }
 
@@ -1030,7 +1101,7 @@ void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream
 }
 
 void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
-    const int nb = reduction_blocks(P.n);
+    const int nb = integration_blocks(P);
     if(P.precision == MTG_PREC_MIXED) {
         if(output) k_pkick2<true, true><<<nb, 256, 0, s>>>(d, P);
         else k_pkick2<true, false><<<nb, 256, 0, s>>>(d, P);

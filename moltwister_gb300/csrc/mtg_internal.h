@@ -50,6 +50,20 @@ struct BaroDev {
     double L_saved[3];
 };
 
+// One replica of a batch (several independent systems advanced by the same launches): its atom
+// range, the block range of the 256-atom blocks of the integration kernels, its production cell
+// grid (global cell indices cbase ..), box and cutoffs, and its temperature.
+struct RepDev {
+    int off, n;
+    int bbase, nb;
+    int cbase, pnx, pny, pnz;
+    double box[3];
+    double fconv[3];      // 2^32 / L
+    float fscale[3];      // L / 2^32
+    float rc, rcoul, skin;
+    double kT;
+};
+
 // Scalars the step kernels exchange through device memory.
 struct StepScalars {
     double S;             // pending momentum scale: c2(previous step) * c1(this step)
@@ -88,6 +102,9 @@ struct Params {
     float fscale[3];      // L / 2^32: fixed-point position unit per axis (mixed)
     double fconv[3];      // 2^32 / L
     int qtype;            // 1: charges are a function of the type (qtype table)
+    int nrep;             // 0: one system; > 0: a batch of nrep replicas (RepDev table)
+    int ncell_total;      // batch: production cells of all replicas
+    int nblk_total;       // batch: 256-atom integration blocks of all replicas
     // NPT
     int MP, nrespP;       // barostat chain length and RESPA steps
     double Pext;          // pressure / Conv_press
@@ -168,6 +185,14 @@ struct DevSys {
     ThermoDev* th;
     ThermoDev* th_saved;
     double* rec;          // output record ring [8]
+    // batch of replicas (Params::nrep > 0)
+    const int* rep_of;    // [n] replica of each atom
+    const int* blk_rep;   // [blocks] replica of each 256-atom integration block
+    const RepDev* reps;   // [nrep]
+    StepScalars* rsc;     // [nrep] per-replica scale, energies, last-block counters
+    ThermoDev* ths;       // [nrep] per-replica chains
+    ThermoDev* ths_saved; // [nrep]
+    double* rrec;         // [nrep * 8] per-replica output records
     // NPT
     BaroDev* baro;
     ThermoDev* thp;       // barostat chain (NH_P_)
@@ -201,6 +226,7 @@ void launch_prod_sync_positions(const DevSys& d, const Params& P, bool to_master
 void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s);
 void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s);
 int reduction_blocks(int n);
+int integration_blocks(const Params& P);   // blocks of the 256-atom integration kernels
 
 // Host-side table generation (tables.cpp): out[npts*3] = (x, -dU/dx, U)
 int profile_nonbonded(int kind, const double* p, float r0, float r1, int npts, float* out);

@@ -130,6 +130,11 @@ def load_library(path: str = LIB_PATH):
         "mtg_get_run_stats": ([P, C.POINTER(RunStats)], C.c_int),
         "mtg_profile_phases": ([P, C.c_int, P], C.c_int),
         "mtg_neighbors_noalloc": ([P, C.c_int32, P, C.c_double, C.c_double, C.c_int32, P, P, P, P], C.c_int),
+        "mtg_batch_create": ([P, C.c_int32, C.POINTER(ConfigDesc), P, C.POINTER(P)], C.c_int),
+        "mtg_batch_info": ([P, P, P], C.c_int),
+        "mtg_batch_get_records": ([P, P], C.c_int),
+        "mtg_batch_set_thermo": ([P, C.c_int32, C.POINTER(ThermoState)], C.c_int),
+        "mtg_batch_get_thermo": ([P, C.c_int32, C.POINTER(ThermoState)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -178,6 +183,99 @@ def _terms_array(terms) -> C.Array:
     return arr
 
 
+def thermo_struct(thermo) -> ThermoState:
+    if not isinstance(thermo, Thermo):
+        thermo = Thermo(*thermo)
+    th = ThermoState()
+    th.M = len(thermo.eta)
+    for j in range(len(thermo.eta)):
+        th.eta[j] = float(thermo.eta[j])
+        th.p_eta[j] = float(thermo.peta[j])
+    th.p_eps, th.eps = float(thermo.p_eps), float(thermo.eps)
+    if thermo.etaP is not None:
+        th.MP = len(thermo.etaP)
+        for j in range(th.MP):
+            th.etaP[j] = float(thermo.etaP[j])
+            th.p_etaP[j] = float(thermo.petaP[j])
+    return th
+
+
+def thermo_tuple(th: ThermoState) -> Thermo:
+    return Thermo(np.array(th.eta[:th.M]), np.array(th.p_eta[:th.M]), th.p_eps, th.eps,
+                  np.array(th.etaP[:th.MP]), np.array(th.p_etaP[:th.MP]), np.array(th.box[:]))
+
+
+def system_desc(s: MDSystem, keep_list: List[object], tables: Optional[dict] = None) -> SystemDesc:
+    """mtg_system_desc of an MDSystem; the arrays it points to are appended to keep_list."""
+    n = s.n
+
+    def keep(a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep_list.append(a)
+        return a
+
+    counts, kinds, params = nonbonded_arrays(s)
+    T = counts.shape[0]
+    nb_terms = (Term * (T * T * MAXFF))()
+    _, pair_terms = s.nonbonded_pair_terms()
+    for pr in range(T * T):
+        for ff, t in enumerate(pair_terms[pr]):
+            k, p = term_params(t)
+            nb_terms[pr * MAXFF + ff].kind = k
+            for w in range(4):
+                nb_terms[pr * MAXFF + ff].p[w] = p[w]
+    keep_list.append(nb_terms)
+    bt, at, dt = _terms_array(s.bond_terms), _terms_array(s.angle_terms), _terms_array(s.dihedral_terms)
+    keep_list.extend([bt, at, dt])
+    d = SystemDesc()
+    d.n_atoms, d.n_types = n, T
+    d.r = _ptr(keep(s.r, np.float64))
+    d.p = _ptr(keep(s.p, np.float64)) if s.p is not None else None
+    d.mass = _ptr(keep(s.m, np.float64))
+    d.charge = _ptr(keep(s.q, np.float64))
+    d.type = _ptr(keep(s.type_index(), np.int32))
+    d.mol = _ptr(keep(s.mol_index(), np.int32))
+    d.mobile = _ptr(keep(s.mobile, np.uint8))
+    for a in range(3):
+        d.box[a] = float(s.box[a])
+    d.nb_count = _ptr(keep(counts.reshape(-1), np.int32))
+    d.nb_terms = C.cast(nb_terms, C.c_void_p).value
+    d.n_bond_types, d.bond_terms = len(s.bond_terms), C.cast(bt, C.c_void_p).value
+    d.n_angle_types, d.angle_terms = len(s.angle_terms), C.cast(at, C.c_void_p).value
+    d.n_dih_types, d.dih_terms = len(s.dihedral_terms), C.cast(dt, C.c_void_p).value
+    if tables is not None:
+        d.nb_tables = _ptr(keep(tables["nb"], np.float32))
+        d.bond_tables = _ptr(keep(tables["bond"], np.float32)) if len(s.bond_terms) else None
+        d.angle_tables = _ptr(keep(tables["angle"], np.float32)) if len(s.angle_terms) else None
+        d.dih_tables = _ptr(keep(tables["dih"], np.float32)) if len(s.dihedral_terms) else None
+    d.n_bonds, d.bonds = len(s.bonds), _ptr(keep(np.asarray(s.bonds).reshape(-1, 3), np.int32))
+    d.n_angles, d.angles = len(s.angles), _ptr(keep(np.asarray(s.angles).reshape(-1, 4), np.int32))
+    d.n_dihedrals, d.dihedrals = len(s.dihedrals), _ptr(keep(np.asarray(s.dihedrals).reshape(-1, 5), np.int32))
+    return d
+
+
+def config_desc(c: MDConfig, device: int = 0) -> ConfigDesc:
+    """mtg_config_desc of an MDConfig (the moldyn cfg keys plus the new ones)."""
+    cf = ConfigDesc()
+    cf.ensemble = ENSEMBLES[c.ensemble]
+    cf.temperature_nh_len, cf.temperature_respa = c.temperaturenhlen, c.temperaturerespa
+    cf.pressure_nh_len, cf.pressure_respa = c.pressurenhlen, c.pressurerespa
+    cf.precision = PREC[c.precision]
+    cf.coulomb = COULOMB[c.coulomb]
+    cf.clip_forces = 1 if c.clipforces else 0
+    cf.timestep, cf.temperature, cf.temperature_relax = c.timestep, c.temperature, c.temperaturerelax
+    cf.pressure, cf.pressure_relax = c.pressure, c.pressurerelax
+    cf.cutoff_radius, cf.neigh_shell, cf.cutoff_force = c.cutoffradius, c.neighshell, c.cutoffforce
+    cf.scale12, cf.scale13, cf.scale14, cf.scale1N = c.scale12, c.scale13, c.scale14, c.scale1N
+    cf.coulomb_cutoff = c.coulombcutoff if c.coulombcutoff is not None else c.cutoffradius
+    cf.list_skin = c.listskin
+    cf.opt_learning_rate, cf.opt_accuracy, cf.opt_max_steps = c.optlearningrate, c.optaccuracy, c.optmaxsteps
+    cf.device = device
+    cf.lj_shift = 1 if c.ljshift else 0
+    return cf
+
+
+
 class Engine:
     """One MD system on one GPU.
 
@@ -189,75 +287,17 @@ class Engine:
         self.lib = load_library()
         self.system, self.config = system, config
         s, c = system, config
-        n = s.n
         self._keep: List[object] = []
-
-        def keep(a, dtype):
-            a = np.ascontiguousarray(a, dtype=dtype)
-            self._keep.append(a)
-            return a
-
-        counts, kinds, params = nonbonded_arrays(s)
-        T = counts.shape[0]
-        nb_terms = (Term * (T * T * MAXFF))()
-        _, pair_terms = s.nonbonded_pair_terms()
-        for pr in range(T * T):
-            for ff, t in enumerate(pair_terms[pr]):
-                k, p = term_params(t)
-                nb_terms[pr * MAXFF + ff].kind = k
-                for w in range(4):
-                    nb_terms[pr * MAXFF + ff].p[w] = p[w]
-        self._keep.append(nb_terms)
-        bt, at, dt = _terms_array(s.bond_terms), _terms_array(s.angle_terms), _terms_array(s.dihedral_terms)
-        self._keep += [bt, at, dt]
-        d = SystemDesc()
-        d.n_atoms, d.n_types = n, T
-        d.r = _ptr(keep(s.r, np.float64))
-        d.p = _ptr(keep(s.p, np.float64)) if s.p is not None else None
-        d.mass = _ptr(keep(s.m, np.float64))
-        d.charge = _ptr(keep(s.q, np.float64))
-        d.type = _ptr(keep(s.type_index(), np.int32))
-        d.mol = _ptr(keep(s.mol_index(), np.int32))
-        d.mobile = _ptr(keep(s.mobile, np.uint8))
-        for a in range(3):
-            d.box[a] = float(s.box[a])
-        d.nb_count = _ptr(keep(counts.reshape(-1), np.int32))
-        d.nb_terms = C.cast(nb_terms, C.c_void_p).value
-        d.n_bond_types, d.bond_terms = len(s.bond_terms), C.cast(bt, C.c_void_p).value
-        d.n_angle_types, d.angle_terms = len(s.angle_terms), C.cast(at, C.c_void_p).value
-        d.n_dih_types, d.dih_terms = len(s.dihedral_terms), C.cast(dt, C.c_void_p).value
-        if tables is not None:
-            d.nb_tables = _ptr(keep(tables["nb"], np.float32))
-            d.bond_tables = _ptr(keep(tables["bond"], np.float32)) if len(s.bond_terms) else None
-            d.angle_tables = _ptr(keep(tables["angle"], np.float32)) if len(s.angle_terms) else None
-            d.dih_tables = _ptr(keep(tables["dih"], np.float32)) if len(s.dihedral_terms) else None
-        d.n_bonds, d.bonds = len(s.bonds), _ptr(keep(np.asarray(s.bonds).reshape(-1, 3), np.int32))
-        d.n_angles, d.angles = len(s.angles), _ptr(keep(np.asarray(s.angles).reshape(-1, 4), np.int32))
-        d.n_dihedrals, d.dihedrals = len(s.dihedrals), _ptr(keep(np.asarray(s.dihedrals).reshape(-1, 5), np.int32))
+        d = system_desc(s, self._keep, tables)
         self.desc = d
-        cf = ConfigDesc()
-        cf.ensemble = ENSEMBLES[c.ensemble]
-        cf.temperature_nh_len, cf.temperature_respa = c.temperaturenhlen, c.temperaturerespa
-        cf.pressure_nh_len, cf.pressure_respa = c.pressurenhlen, c.pressurerespa
-        cf.precision = PREC[c.precision]
-        cf.coulomb = COULOMB[c.coulomb]
-        cf.clip_forces = 1 if c.clipforces else 0
-        cf.timestep, cf.temperature, cf.temperature_relax = c.timestep, c.temperature, c.temperaturerelax
-        cf.pressure, cf.pressure_relax = c.pressure, c.pressurerelax
-        cf.cutoff_radius, cf.neigh_shell, cf.cutoff_force = c.cutoffradius, c.neighshell, c.cutoffforce
-        cf.scale12, cf.scale13, cf.scale14, cf.scale1N = c.scale12, c.scale13, c.scale14, c.scale1N
-        cf.coulomb_cutoff = c.coulombcutoff if c.coulombcutoff is not None else c.cutoffradius
-        cf.list_skin = c.listskin
-        cf.opt_learning_rate, cf.opt_accuracy, cf.opt_max_steps = c.optlearningrate, c.optaccuracy, c.optmaxsteps
-        cf.device = device
-        cf.lj_shift = 1 if c.ljshift else 0
+        cf = config_desc(c, device)
         self.cfgdesc = cf
         h = C.c_void_p()
         rc = self.lib.mtg_create(C.byref(d), C.byref(cf), C.byref(h))
         if rc != MTG_OK:
             raise MTGError(rc, self.lib.mtg_last_error(None).decode())
         self.h = h
-        self.n = n
+        self.n = s.n
         if c.ensemble == "NPT" and s.p_eps is not None:
             M = c.temperaturenhlen
             self.set_state(thermo=Thermo(s.nhT_eta if s.nhT_eta is not None else np.zeros(M),
@@ -288,19 +328,7 @@ class Engine:
         pp = None if p is None else np.ascontiguousarray(p, np.float64)
         th = None
         if thermo is not None:
-            if not isinstance(thermo, Thermo):
-                thermo = Thermo(*thermo)
-            th = ThermoState()
-            th.M = len(thermo.eta)
-            for j in range(len(thermo.eta)):
-                th.eta[j] = float(thermo.eta[j])
-                th.p_eta[j] = float(thermo.peta[j])
-            th.p_eps, th.eps = float(thermo.p_eps), float(thermo.eps)
-            if thermo.etaP is not None:
-                th.MP = len(thermo.etaP)
-                for j in range(th.MP):
-                    th.etaP[j] = float(thermo.etaP[j])
-                    th.p_etaP[j] = float(thermo.petaP[j])
+            th = thermo_struct(thermo)
         self._check(self.lib.mtg_set_state(self.h, _ptr(rr), _ptr(pp), C.byref(th) if th is not None else None))
 
     def get_state(self):
@@ -309,8 +337,8 @@ class Engine:
         p = np.zeros((self.n, 3))
         th = ThermoState()
         self._check(self.lib.mtg_get_state(self.h, _ptr(r), _ptr(p), C.byref(th)))
-        return r, p, Thermo(np.array(th.eta[:th.M]), np.array(th.p_eta[:th.M]), th.p_eps, th.eps,
-                            np.array(th.etaP[:th.MP]), np.array(th.p_etaP[:th.MP]), np.array(th.box[:]))
+        return r, p, thermo_tuple(th)
+
 
     # -- dynamics ------------------------------------------------------------------------------------
     def run(self, nsteps: int, out_stride: int = 0, callback: Optional[Callable[[OutputRecord], bool]] = None,

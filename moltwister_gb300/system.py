@@ -197,12 +197,17 @@ class MDSystem:
     p_eps: Optional[float] = None
     nhP_eta: Optional[np.ndarray] = None
     nhP_peta: Optional[np.ndarray] = None
+    # Atom-type numbering; None = first appearance of the IDs (MolTwisterState.cpp:459-487).  A batch
+    # of replicas sets one shared order so that all replicas index the same force field.
+    type_order: Optional[List[str]] = None
 
     @property
     def n(self) -> int:
         return int(self.r.shape[0])
 
     def type_names(self) -> List[str]:
+        if self.type_order is not None:
+            return list(self.type_order)
         seen: Dict[str, int] = {}
         for a in self.ids:
             if a not in seen:
