@@ -272,7 +272,9 @@ int mtg_profile_phases(mtg_ctx* ctx, int steps, double* phase_ms);
  * per type pair and bonded term types; analytic terms only) into one context whose kernels advance
  * every replica per launch: atoms are concatenated (replica r owns atoms offsets[r] ..
  * offsets[r+1]-1), each replica keeps its own box, cell grid, temperature (temperatures[r] K, or
- * cfg->temperature when NULL), Nose-Hoover chain and energies.  cfg is shared (fp64 or mixed
+ * cfg->temperature when NULL), pair cutoff (cutoffs[r] A for LJ and Coulomb, at most
+ * cfg->cutoff_radius, or the shared cutoffs when NULL: small boxes need shorter ones for the
+ * minimum image), Nose-Hoover chain and energies.  cfg is shared (fp64 or mixed
  * precision, NVT or NVE).  A replica's trajectory equals, bit for bit, the trajectory of the same
  * system run alone in mixed precision.  The returned context works with mtg_run, mtg_get_state /
  * mtg_set_state (positions and momenta of all replicas, without the chain argument),
@@ -280,7 +282,7 @@ int mtg_profile_phases(mtg_ctx* ctx, int steps, double* phase_ms);
  * totals (U, K, E and V summed, T over all atoms, P averaged) and mtg_batch_get_records gives the
  * per-replica values of the same output step. */
 int mtg_batch_create(const mtg_system_desc* const* systems, int32_t nrep, const mtg_config_desc* cfg,
-                     const double* temperatures, mtg_ctx** out);
+                     const double* temperatures, const double* cutoffs, mtg_ctx** out);
 int mtg_batch_info(mtg_ctx* ctx, int32_t* nrep, int32_t* offsets /* nrep + 1 */);
 /* rec[6 r + 0..5] = T, P, V, U, K, E of replica r at the last output step of mtg_run */
 int mtg_batch_get_records(mtg_ctx* ctx, double* rec);

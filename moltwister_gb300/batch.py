@@ -68,12 +68,13 @@ def shared_force_field(systems: Sequence[MDSystem]) -> List[MDSystem]:
 class BatchEngine(Engine):
     """nrep systems on one GPU, one launch per kernel per step for all of them.
 
-    `config` is shared (precision fp64 or mixed, NVT or NVE); `temperatures` (K) is per replica
-    (default: config.temperature).  Each replica's seeded chain state (nhT_eta / nhT_peta) is
-    injected after creation."""
+    `config` is shared (precision fp64 or mixed, NVT or NVE); `temperatures` (K) and `cutoffs` (A,
+    LJ and Coulomb, at most config.cutoffradius) are per replica (defaults: the config's).  Each
+    replica's seeded chain state (nhT_eta / nhT_peta) is injected after creation."""
 
     def __init__(self, systems: Sequence[MDSystem], config: MDConfig,
-                 temperatures: Optional[Sequence[float]] = None, device: int = 0):
+                 temperatures: Optional[Sequence[float]] = None, cutoffs: Optional[Sequence[float]] = None,
+                 device: int = 0):
         self.lib = load_library()
         self.config = config
         self._keep: List[object] = []
@@ -86,10 +87,15 @@ class BatchEngine(Engine):
         if temperatures is not None:
             temps = np.ascontiguousarray(temperatures, np.float64)
             self._keep.append(temps)
+        cuts = None
+        if cutoffs is not None:
+            cuts = np.ascontiguousarray(cutoffs, np.float64)
+            self._keep.append(cuts)
         cf = config_desc(config, device)
         self.cfgdesc = cf
         h = C.c_void_p()
-        rc = self.lib.mtg_batch_create(C.cast(arr, C.c_void_p), len(descs), C.byref(cf), _ptr(temps), C.byref(h))
+        rc = self.lib.mtg_batch_create(C.cast(arr, C.c_void_p), len(descs), C.byref(cf), _ptr(temps), _ptr(cuts),
+                                       C.byref(h))
         if rc != MTG_OK:
             raise MTGError(rc, self.lib.mtg_last_error(None).decode())
         self.h = h

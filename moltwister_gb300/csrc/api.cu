@@ -231,7 +231,11 @@ int grow_vlist(mtg_ctx* c, int needed) {
     c->vlist_buf = nullptr;
     void* p;
     cudaError_t e = cudaMalloc(&p, (size_t)c->P.n * cap * sizeof(uint32_t));
-    if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, "Verlet list allocation failed");
+    if(e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(c, MTG_E_NOMEM, "Verlet list allocation of " + std::to_string((size_t)c->P.n * cap * sizeof(uint32_t)) +
+                                        " bytes failed: " + cudaGetErrorString(e));
+    }
     c->vlist_buf = p;
     c->d.vlist = (uint32_t*)p;
     c->d.vmax = cap;
@@ -511,6 +515,7 @@ struct BatchSpec {
     std::vector<int> off, n;          // nrep + 1 offsets, nrep sizes
     std::vector<double> box;          // 3 per replica
     std::vector<double> temperature;  // K per replica
+    std::vector<double> cutoff;       // A per replica (LJ and Coulomb), empty = the shared cutoffs
 };
 
 // Barostat state with momentum p_eps and strain eps: box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax
@@ -749,8 +754,8 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     P.nz = ref_cells(sys->box[2], cfg->cutoff_radius, cfg->neigh_shell);
     if(P.nx < 1 || P.ny < 1 || P.nz < 1) return fail(nullptr, MTG_E_INVALID, "box narrower than cutoff + shell: the reference cell list is empty");
     // production cell grid of one box: cell edge >= rlist, or one cell when fewer than 3 fit
-    const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
-    auto grid = [&](const double* box, int natoms, int* pn) -> int {
+    auto grid = [&](const double* box, int natoms, int* pn, double rcv, double rqv) -> int {
+        const double rlist = std::max(rcv, P.coulomb != MTG_COULOMB_ALLPAIRS ? rqv : 0.0) + P.skin;
         for(int a = 0; a < 3; a++) {
             pn[a] = (int)std::floor(box[a] / rlist);
             if(pn[a] < 3) pn[a] = 1;   // small box: scan every atom once (no duplicated images)
@@ -764,7 +769,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             const double half = 0.5 * std::min(box[0], std::min(box[1], box[2]));
             if(rlist > half && (pn[0] > 1 || pn[1] > 1 || pn[2] > 1))
                 return fail(nullptr, MTG_E_INVALID, "cutoff + skin exceeds half the box");
-            if(std::max((double)P.rc, (double)P.rcoul) >= half)
+            if(std::max(rcv, rqv) >= half)
                 return fail(nullptr, MTG_E_INVALID, "cutoff must be below half the box (minimum image)");
         }
         return MTG_OK;
@@ -772,8 +777,9 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     std::vector<RepDev> reps;
     {
         int pn[3];
-        int grc = grid(sys->box, n, pn);
+        int grc = bs ? 0 : grid(sys->box, n, pn, P.rc, P.rcoul);
         if(grc) return grc;
+        if(bs) pn[0] = pn[1] = pn[2] = 1;   // unused: every replica has its own grid
         P.pnx = pn[0];
         P.pny = pn[1];
         P.pnz = pn[2];
@@ -798,13 +804,13 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
                 R.fconv[a] = 4294967296.0 / R.box[a];
                 R.fscale[a] = (float)(R.box[a] / 4294967296.0);
             }
-            R.rc = P.rc;
-            R.rcoul = P.rcoul;
+            R.rc = bs->cutoff.empty() ? P.rc : (float)bs->cutoff[r];
+            R.rcoul = bs->cutoff.empty() ? P.rcoul : (float)bs->cutoff[r];
             R.skin = P.skin;
             R.kT = bs->temperature[r] / kConvT;
             int pn[3];
-            int grc = grid(R.box, R.n, pn);
-            if(grc) return grc;
+            int grc = grid(R.box, R.n, pn, R.rc, R.rcoul);
+            if(grc) return fail(nullptr, grc, "replica " + std::to_string(r) + ": " + g_create_error);
             R.cbase = cb;
             R.pnx = pn[0];
             R.pny = pn[1];
@@ -1055,11 +1061,14 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     }
     // list capacities: start from a density estimate, grown on demand
     {
-        double V = sys->box[0] * sys->box[1] * sys->box[2];
-        double rho = n / V;
+        // density of the system, or of the densest replica of a batch (the merged box is not one)
+        const double V = sys->box[0] * sys->box[1] * sys->box[2];
+        double rho = bs ? 0.0 : n / V;
         for(const RepDev& R : reps) rho = std::max(rho, R.n / (R.box[0] * R.box[1] * R.box[2]));
         const double rc3 = std::pow(cfg->cutoff_radius, 3.0);
-        int est = (int)(1.3 * rho * 4.18879 * rc3) + 32;
+        // the reference list is used every step only in reference mode; elsewhere (parity hooks)
+        // it starts small and grows on demand
+        int est = P.precision == MTG_PREC_REFERENCE ? (int)(1.3 * rho * 4.18879 * rc3) + 32 : 16;
         rc = grow_neighbors(c.get(), std::min(est, n));
         if(rc) return fail(nullptr, rc, c->err);
         double rl = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
@@ -1490,7 +1499,7 @@ int mtg_get_run_stats(mtg_ctx* c, mtg_run_stats* st) {
 // Batches of replicas
 // ---------------------------------------------------------------------------------------------
 int mtg_batch_create(const mtg_system_desc* const* systems, int32_t nrep, const mtg_config_desc* cfg,
-                     const double* temperatures, mtg_ctx** out) {
+                     const double* temperatures, const double* cutoffs, mtg_ctx** out) {
     g_create_error.clear();
     if(!systems || nrep < 1 || !cfg || !out) return fail(nullptr, MTG_E_INVALID, "null argument or no replicas");
     *out = nullptr;
@@ -1525,6 +1534,8 @@ int mtg_batch_create(const mtg_system_desc* const* systems, int32_t nrep, const 
            !same_terms(s->dih_terms, s0->dih_terms, s0->n_dih_types))
             return fail(nullptr, MTG_E_INVALID, "replica " + std::to_string(r) + ": replicas must share one force field");
         if(temperatures && !(temperatures[r] > 0.0)) return fail(nullptr, MTG_E_INVALID, "temperatures must be positive");
+        if(cutoffs && !(cutoffs[r] > 0.0 && cutoffs[r] <= cfg->cutoff_radius))
+            return fail(nullptr, MTG_E_INVALID, "replica cutoffs must be positive and at most cutoff_radius");
         N += s->n_atoms;
     }
     if(N > (long long)kIdxMask) return fail(nullptr, MTG_E_INVALID, "too many atoms in the batch");
@@ -1546,6 +1557,7 @@ int mtg_batch_create(const mtg_system_desc* const* systems, int32_t nrep, const 
             big[a] = std::max(big[a], s->box[a]);
         }
         bs.temperature.push_back(temperatures ? temperatures[rr] : cfg->temperature);
+        if(cutoffs) bs.cutoff.push_back(cutoffs[rr]);
         r3.insert(r3.end(), s->r, s->r + 3 * n);
         if(s->p) p3.insert(p3.end(), s->p, s->p + 3 * n);
         else p3.insert(p3.end(), (size_t)3 * n, 0.0);

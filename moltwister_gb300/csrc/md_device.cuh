@@ -45,6 +45,16 @@ __device__ __forceinline__ double nh_exp(double x) {
 // CMt::exp (Integrators/Math.cpp:29-38): linear above x = 1.
 __device__ __forceinline__ double cmt_exp(double x) { return (x > 1.0) ? 2.71828 * x : nh_exp(x); }
 
+// The chain integrator's constants.  The reference (fixed = false) uses w0 = 1/(1 - 2^(1/3)) for
+// its order-3 Suzuki-Yoshida weights (NHChain.cpp:45-52), CMt::exp and the clamp p_eta[0] > 15 ->
+// 10 (NHChain.cpp:61-65).  With those, chains of large systems diverge: Q_0 grows with N while
+// Q_j (j > 0) does not, so the upper chain velocities grow, the linear branch of CMt::exp breaks
+// the cancellation between the negative and positive Suzuki-Yoshida stages, and p_eta[0] > 15 is
+// the normal state of a large system.  The production modes (fixed = true) use the published
+// weight w0 = 1/(2 - 2^(1/3)), the exponential itself and no clamp.
+__device__ __forceinline__ double sy_w0(bool fixed) { return fixed ? 1.0 / (2.0 - cbrt(2.0)) : 1.0 / (1.0 - cbrt(2.0)); }
+__device__ __forceinline__ double chain_exp(double x, bool fixed) { return fixed ? nh_exp(x) : cmt_exp(x); }
+
 // One call of CNHChain::propagator with the thermostat functor CFctT (NHChain.cpp:54-113,
 // MDLoop.cpp:29-60), executed by all 32 lanes of one warp.  The particles enter only through
 // G(0) = sum p^2/m - g kT and through the momentum scalings; since a scaling by c multiplies
@@ -53,12 +63,14 @@ __device__ __forceinline__ double cmt_exp(double x) { return (x > 1.0) ? 2.71828
 // work that is independent across chain elements -- the exponentials of step 1.2 and the eta
 // updates of step 1.3 -- is spread over lanes, so it costs one instruction stream, not M.
 // The two identical exponentials of each update (NHChain.cpp:72-78, 92-98) are evaluated once, and
-// 1/Q_j comes precomputed in th.iQ.  Suzuki-Yoshida weights as the reference sets them:
-// w0 = 1/(1 - 2^(1/3)) (NHChain.cpp:45-52).  Lane j writes eta[j] and peta[j] back.
-__device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, double kT, double dt, int M, int nresp) {
+// 1/Q_j comes precomputed in th.iQ.  Suzuki-Yoshida weights, exponential and p_eta[0] clamp as
+// sy_w0 / chain_exp describe (the reference's, or the published ones with `fixed`).  Lane j
+// writes eta[j] and peta[j] back.
+__device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, double kT, double dt, int M, int nresp,
+                                       bool fixed) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const double w0 = 1.0 / (1.0 - cbrt(2.0));
+    const double w0 = sy_w0(fixed);
     const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
     double scale = 1.0;
     if(M <= 0) return scale;
@@ -69,7 +81,7 @@ __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, dou
     }
     double eta_mine = (lane < M) ? th.eta[lane] : 0.0;
     const double gkT = g * kT;
-    if(pe[0] > 15.0) pe[0] = 10.0;
+    if(!fixed && pe[0] > 15.0) pe[0] = 10.0;
     for(int mu = 0; mu < 3; mu++) {
         const double Dt = w[mu] * dt / double(nresp);
         const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
@@ -82,7 +94,7 @@ __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, dou
                 double v = 0.0, q = 0.0;
                 for(int j = 0; j < M - 1; j++)
                     if(j == lane) { v = pe[j + 1]; q = iQ[j + 1]; }
-                cl = cmt_exp(d8 * (v * q));
+                cl = chain_exp(d8 * (v * q), fixed);
             }
             double c_last = 1.0;
             for(int j = 0; j < M - 1; j++) {
@@ -100,13 +112,13 @@ __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, dou
             }
             // 1.4
             {
-                const double c = cmt_exp(-(d2 * (pe[0] * iQ[0])));
+                const double c = chain_exp(-(d2 * (pe[0] * iQ[0])), fixed);
                 scale *= c;
                 KE2 *= c * c;
             }
             // 1.5 (the first update reuses the exponential of pe[M-1], unchanged since 1.2)
             for(int j = M - 2; j >= 0; j--) {
-                const double c = (j == M - 2) ? c_last : cmt_exp(d8 * (pe[j + 1] * iQ[j + 1]));
+                const double c = (j == M - 2) ? c_last : chain_exp(d8 * (pe[j + 1] * iQ[j + 1]), fixed);
                 const double G = (j == 0) ? KE2 - gkT : pe[j - 1] * pe[j - 1] * iQ[j - 1] - kT;
                 pe[j] = (pe[j] * c + d4 * G) * c;
             }
@@ -178,8 +190,8 @@ __device__ __forceinline__ double exp_tiny(double x) {
 }
 
 // CMt::exp with branch tests on the bit pattern (x > 1) instead of FP64 comparisons
-__device__ __forceinline__ double cmt_exp_bits(double x) {
-    if(__double_as_longlong(x) > 0x3ff0000000000000LL) return 2.71828 * x;
+__device__ __forceinline__ double cmt_exp_bits(double x, bool fixed) {
+    if(!fixed && __double_as_longlong(x) > 0x3ff0000000000000LL) return 2.71828 * x;
     return nh_exp(x);
 }
 
@@ -187,11 +199,12 @@ __device__ __forceinline__ double cmt_exp_bits(double x) {
 // continue from `seq` (a counter shared by successive calls so flags only grow).  Returns the new
 // counter value.
 template<int MM>
-__device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, double dt, int M_rt, int nresp, int seq) {
+__device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, double dt, int M_rt, int nresp, int seq,
+                                         bool fixed) {
     constexpr int CAP = MM > 0 ? MM : kMaxChain;   // register arrays when the length is known
     const int M = MM > 0 ? MM : M_rt;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const double w0 = 1.0 / (1.0 - cbrt(2.0));
+    const double w0 = sy_w0(fixed);
     const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
     const double gkT = g * kT;
     const int top = M - 1;
@@ -209,7 +222,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         }
         double KE2 = X.KE2;
         double eta_mine = (lane < top) ? X.eta[lane] : 0.0;
-        if(pe[0] > 15.0) pe[0] = 10.0;
+        if(!fixed && pe[0] > 15.0) pe[0] = 10.0;
         int s = 0;
         for(int mu = 0; mu < 3; mu++) {
             const double Dt = w[mu] * dt / double(nresp);
@@ -244,7 +257,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                         x = xprev[j];
                     } else {
                         x = pe[j + 1] * D[j];
-                        c = cmt_exp_bits(x);
+                        c = cmt_exp_bits(x, fixed);
                     }
                     c12[j] = c;
                     x12[j] = x;
@@ -276,7 +289,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                            __double_as_longlong(xn) <= half_bits && __double_as_longlong(x12[j]) <= half_bits)
                             c = c12[j] * exp_tiny(dx);
                         else
-                            c = cmt_exp_bits(xn);
+                            c = cmt_exp_bits(xn, fixed);
                         cprev[j] = c;
                         xprev[j] = xn;
                     }
@@ -314,7 +327,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
             const double d2 = (w[mu] * dt / double(nresp)) / 2.0;
             for(int it = 0; it < nresp; it++, s++) {
                 nh_wait(&X.f_pe0, seq + s + 1, tmo);
-                const double c = cmt_exp_bits(-(d2 * (X.pe0 * iQ0)));
+                const double c = cmt_exp_bits(-(d2 * (X.pe0 * iQ0)), fixed);
                 scale *= c;
                 KE2 *= c * c;
                 if(lane == 0) X.ke = KE2;
@@ -331,7 +344,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         double pt = X.pe[top];
         double eta_t = X.eta[top];
         double pm = X.pe[top - 1];
-        if(top - 1 == 0 && pm > 15.0) pm = 10.0;    // the guard on p_eta[0] (NHChain.cpp:61-65)
+        if(!fixed && top - 1 == 0 && pm > 15.0) pm = 10.0;    // the guard on p_eta[0] (NHChain.cpp:61-65)
         int s = 0;
         for(int mu = 0; mu < 3; mu++) {
             const double Dt = w[mu] * dt / double(nresp);
@@ -345,7 +358,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                     pt += d4p * (pm * pm * iQm - kT);
                 }
                 pt += d4 * (pm * pm * iQm - kT);          // 1.1
-                const double c = cmt_exp_bits(d8 * (pt * iQt));
+                const double c = cmt_exp_bits(d8 * (pt * iQt), fixed);
                 if(lane == 0) X.etop = c;
                 nh_post(&X.f_etop, seq + s + 1);
                 eta_t += d2 * (pt * iQt);                   // 1.3 for the top element
@@ -413,15 +426,16 @@ __device__ inline bool last_block(unsigned int* counter) {
     return is_last;
 }
 
-__device__ inline int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq) {
+__device__ inline int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
+                                       bool fixed) {
     switch(M) {
-    case 2: return nh_chain_half_3w_t<2>(X, g, kT, dt, M, nresp, seq);
-    case 3: return nh_chain_half_3w_t<3>(X, g, kT, dt, M, nresp, seq);
-    case 4: return nh_chain_half_3w_t<4>(X, g, kT, dt, M, nresp, seq);
-    case 5: return nh_chain_half_3w_t<5>(X, g, kT, dt, M, nresp, seq);
-    case 6: return nh_chain_half_3w_t<6>(X, g, kT, dt, M, nresp, seq);
-    case 8: return nh_chain_half_3w_t<8>(X, g, kT, dt, M, nresp, seq);
-    default: return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq);
+    case 2: return nh_chain_half_3w_t<2>(X, g, kT, dt, M, nresp, seq, fixed);
+    case 3: return nh_chain_half_3w_t<3>(X, g, kT, dt, M, nresp, seq, fixed);
+    case 4: return nh_chain_half_3w_t<4>(X, g, kT, dt, M, nresp, seq, fixed);
+    case 5: return nh_chain_half_3w_t<5>(X, g, kT, dt, M, nresp, seq, fixed);
+    case 6: return nh_chain_half_3w_t<6>(X, g, kT, dt, M, nresp, seq, fixed);
+    case 8: return nh_chain_half_3w_t<8>(X, g, kT, dt, M, nresp, seq, fixed);
+    default: return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq, fixed);
     }
 }
 
@@ -439,6 +453,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
                                         double g, int M, int nresp, double* KE_full) {
     __shared__ NhExchange X;
     const int tid = threadIdx.x;
+    const bool fixed = P.precision != MTG_PREC_REFERENCE;
     double c2 = 1.0, c1 = 1.0;
     double KEf = KE2;
     if(M >= 2) {
@@ -456,7 +471,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         bar96();
         int seq = 0;
         if(second_half) {
-            seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq);
+            seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed);
             bar96();
             c2 = X.scale;
             if(tid < M) {
@@ -474,7 +489,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         }
         const double KE_after2 = X.KE2;
         bar96();
-        seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq);
+        seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed);
         bar96();
         c1 = X.scale;
         KEf = X.KE2;
@@ -487,7 +502,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         bar96();   // X is reused by the next chain of this block
     } else if(M == 1 && tid < 32) {
         if(second_half) {
-            c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, M, nresp);
+            c2 = nh_chain_half(*th, KE2, g, P.kT, P.dt, M, nresp, fixed);
             __threadfence_block();
             if(tid == 0) {
                 th_saved->eta[0] = th->eta[0];
@@ -499,7 +514,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         }
         __syncwarp();
         double KEn = KE2;
-        c1 = nh_chain_half(*th, KEn, g, P.kT, P.dt, M, nresp);
+        c1 = nh_chain_half(*th, KEn, g, P.kT, P.dt, M, nresp, fixed);
         KEf = KEn;
     }
     *c2_out = c2;

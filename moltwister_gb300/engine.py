@@ -130,7 +130,7 @@ def load_library(path: str = LIB_PATH):
         "mtg_get_run_stats": ([P, C.POINTER(RunStats)], C.c_int),
         "mtg_profile_phases": ([P, C.c_int, P], C.c_int),
         "mtg_neighbors_noalloc": ([P, C.c_int32, P, C.c_double, C.c_double, C.c_int32, P, P, P, P], C.c_int),
-        "mtg_batch_create": ([P, C.c_int32, C.POINTER(ConfigDesc), P, C.POINTER(P)], C.c_int),
+        "mtg_batch_create": ([P, C.c_int32, C.POINTER(ConfigDesc), P, P, C.POINTER(P)], C.c_int),
         "mtg_batch_info": ([P, P, P], C.c_int),
         "mtg_batch_get_records": ([P, P], C.c_int),
         "mtg_batch_set_thermo": ([P, C.c_int32, C.POINTER(ThermoState)], C.c_int),

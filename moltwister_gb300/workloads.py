@@ -156,6 +156,63 @@ def kob_andersen(ncell: int = 64, seed: int = 3, T_star: float = 0.75, rho_star:
 
 
 # ------------------------------------------------------------------------------------------------
+# Config 5: ensembles of argon and water replicas of uneven size
+# ------------------------------------------------------------------------------------------------
+ARGON_RC = 2.5 * 3.405
+
+
+def argon_n(n: int, seed: int, T: float, rho_star: float = 0.8, sigma: float = 3.405, eps: float = 0.996,
+            jitter: float = 0.05) -> Tuple[MDSystem, MDConfig]:
+    """LJ argon with exactly n atoms at reduced density rho_star: n sites drawn (seeded) from the
+    smallest simple cubic lattice with at least n sites in the box, jittered; the LJ term carries
+    its own cutoff 2.5 sigma."""
+    rng = np.random.default_rng(seed)
+    L = (n / rho_star) ** (1.0 / 3.0) * sigma
+    m = int(math.ceil(n ** (1.0 / 3.0) - 1e-9))
+    a = L / m
+    g = np.arange(m)
+    sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) * a - L / 2.0 + a / 2.0
+    r = sites[rng.permutation(sites.shape[0])[:n]] + rng.uniform(-jitter, jitter, (n, 3))
+    mass = np.full(n, M_AR)
+    sys_ = MDSystem(box=np.array([L, L, L]), ids=["Ar"] * n, r=r, q=np.zeros(n), m=mass, mobile=np.ones(n, bool),
+                    nonbonded=[NonBondedTerm("Ar", "Ar", "LJ", (eps, sigma), cutoff=ARGON_RC)])
+    sys_.mol = np.arange(n, dtype=np.int32)
+    sys_.p = maxwell_boltzmann(mass, T, rng)
+    cfg = MDConfig(timestep=0.5, temperature=T, temperaturerelax=20.0, cutoffradius=ARGON_RC, ensemble="NVT")
+    sys_.nhT_eta, sys_.nhT_peta = nh_initial(cfg.temperaturenhlen, n, T, cfg.temperaturerelax, rng)
+    return sys_, cfg
+
+
+def replica_spec(nrep: int = 512, seed: int = 5, nmin: int = 200, nmax: int = 20000,
+                 tmin: float = 80.0, tmax: float = 400.0):
+    """[(kind, n_atoms, T, seed)] of a seeded replica ensemble: kind 'argon' or 'water' by seed,
+    sizes uniform in [nmin, nmax] (water rounded down to whole molecules), temperatures uniform in
+    [tmin, tmax] K."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(nrep):
+        kind = "argon" if rng.random() < 0.5 else "water"
+        n = int(rng.integers(nmin, nmax + 1))
+        if kind == "water":
+            n = max(3 * (n // 3), 3 * ((nmin + 2) // 3))
+        out.append((kind, n, float(rng.uniform(tmin, tmax)), int(rng.integers(1 << 30))))
+    return out
+
+
+def make_replica(kind: str, n: int, T: float, seed: int, rc_max: float = 10.0):
+    """(system, pair cutoff) of one replica: argon (LJ cutoff 2.5 sigma) or water (cutoff rc_max),
+    the cutoff shortened to below half the box when the box is small."""
+    if kind == "argon":
+        s, _ = argon_n(n, seed, T)
+        rc = ARGON_RC
+    else:
+        nm = n // 3
+        s, _ = water(n_mol=nm, L=water_box_length(nm), seed=seed, T=T, rc=rc_max)
+        rc = rc_max
+    return s, min(rc, 0.5 * float(s.box.min()) - 0.05)
+
+
+# ------------------------------------------------------------------------------------------------
 # Config 2: flexible SPC/E-like water
 # ------------------------------------------------------------------------------------------------
 def random_rotation(rng: np.random.Generator) -> np.ndarray:

@@ -229,3 +229,21 @@ def test_mixed_nve_conserves_energy():
     slope = np.polyfit(t_ns, E, 1)[0]
     drift = abs(slope) / (s.n * kT)
     assert drift < 1e-2, drift
+
+
+def test_production_chain_stays_finite_on_large_systems():
+    """An 11,681-atom argon replica at 96 K whose chain diverges (NaN after ~350 steps) with the
+    reference's Suzuki-Yoshida weights, CMt::exp and p_eta[0] clamp stays finite and near its
+    temperature with the production modes' chain integrator."""
+    from moltwister_gb300 import workloads as W
+    from moltwister_gb300.system import MDConfig
+    spec = W.replica_spec(64, seed=5)
+    kind, n, T, seed = spec[51]
+    s, rc = W.make_replica(kind, n, T, seed)
+    cfg = MDConfig(timestep=0.5, ensemble="NVT", temperature=T, temperaturerelax=20.0, cutoffradius=rc,
+                   neighshell=1.0, coulomb="shifted", coulombcutoff=rc, listskin=1.0, precision="mixed")
+    e = engine(s, cfg)
+    recs = e.run(3000, out_stride=100)
+    T_K = np.array([r.T for r in recs]) * 120.272
+    assert np.all(np.isfinite(T_K))
+    assert abs(T_K[-10:].mean() - T) < 0.15 * T, (T_K[-10:], T)
