@@ -162,7 +162,8 @@ typedef struct mtg_config_desc {
     double opt_accuracy;        /* optaccuracy */
     int32_t opt_max_steps;      /* optmaxsteps */
     int32_t device;             /* CUDA device ordinal */
-    int32_t lj_shift;           /* production modes: shift LJ energies to zero at their cutoff (new) */
+    int32_t lj_shift;           /* production modes, LJ at its cutoff (new): 0 truncated, 1 energy
+                                   shifted to zero, 2 force shifted: F - F(rc), U - U(rc) + (r - rc) F(rc) */
     int32_t reserved;
 } mtg_config_desc;
 
@@ -264,6 +265,57 @@ int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
  * rebuild is due), [2] force gather, [3] kick + wrap + reductions + thermostat.
  * The state advances by `steps` steps exactly as mtg_run would advance it. */
 int mtg_profile_phases(mtg_ctx* ctx, int steps, double* phase_ms);
+
+/* ---- Force-field parameters and gradients (no counterpart in the reference, which has no
+ * derivatives) ----
+ *
+ * A parameter is one scalar of the MDFF terms: the epsilon or sigma of the LJ term of a type pair
+ * (index = row * n_types + col; both orders of the pair follow), a direction in charge space
+ * (q_i = theta * dq[i] for every atom with dq[i] != 0, e.g. dq = 1 on O and -1/2 on H makes theta
+ * the oxygen charge of a neutral water), or k / r0 of a harmonic bond type, or k / theta0 [deg] of a
+ * harmonic angle type (index = term type).  Gradients use the analytic terms of the fp64 / mixed
+ * modes, in FP64 arithmetic (forward-mode dual numbers for the force tangents). */
+#define MTG_P_LJ_EPS 1
+#define MTG_P_LJ_SIGMA 2
+#define MTG_P_CHARGE 3
+#define MTG_P_BOND_K 4
+#define MTG_P_BOND_R0 5
+#define MTG_P_ANGLE_K 6
+#define MTG_P_ANGLE_THETA0 7
+typedef struct mtg_param {
+    int32_t kind;
+    int32_t index;
+    const double* dq;          /* MTG_P_CHARGE: [n_atoms] direction */
+} mtg_param;
+
+int mtg_get_params(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, double* values);
+/* Changes the parameters and recomputes the forces (fp64 / mixed modes). */
+int mtg_set_params(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, const double* values);
+/* Total potential energy at the current positions and its derivatives d U / d theta_k. */
+int mtg_energy_grad(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, double* U, double* grad);
+
+/* Short-trajectory loss: from the current state, `nsteps` plain velocity-Verlet steps (NVE, no
+ * force clipping, whatever the context's ensemble), and the squared deviation
+ *     L = sum_b (gbar_b - target_b)^2
+ * of the Gaussian-smeared pair correlation of types type_a and type_b averaged over the positions
+ * after each step: g_b = V / (N_pairs 4 pi x_b^2) sum_pairs K(r_ij - x_b), x_b = (b + 1/2) rmax /
+ * nbins, K the unit-area Gaussian of standard deviation `width` taken where |r_ij - x_b| <= 8 width
+ * (pairs of the Verlet list, which must reach rmax + 8 width; bonded exclusions are not counted).  The gradient dL/dtheta comes from the discrete adjoint of the
+ * velocity-Verlet recursion, run backwards with states stored every checkpoint_every steps and the
+ * positions in between recomputed (memory: (nsteps / checkpoint_every + checkpoint_every) position
+ * sets).  With grad == NULL (or nparams == 0) only the loss is evaluated.  The context's state is
+ * unchanged on return. */
+typedef struct mtg_loss_desc {
+    int32_t nsteps;
+    int32_t checkpoint_every;
+    int32_t type_a, type_b;
+    int32_t nbins;
+    int32_t reserved;
+    double rmax, width;
+    const double* target;      /* [nbins] */
+} mtg_loss_desc;
+int mtg_loss_grad(mtg_ctx* ctx, const mtg_loss_desc* loss_desc, int32_t nparams, const mtg_param* params,
+                  double* loss, double* grad, double* rdf /* [nbins] or NULL: gbar */);
 
 /* ---- Batches of independent replicas (no counterpart in the reference, which runs one system
  * per `moldyn run`) ----

@@ -28,6 +28,7 @@ UNITS = [
     ("ref_kernels.cu", ["-fmad=false"]),
     ("md_kernels.cu", ["-Xptxas", "-v"] if os.environ.get("MTG_PTXAS_VERBOSE") else []),
     ("api.cu", []),
+    ("adjoint.cu", []),
     ("tables.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 

@@ -53,6 +53,15 @@ struct mtg_ctx {
     // host mirrors
     std::vector<double> h_mass;
     std::vector<int> h_type;
+    // force-field parameters as given (for mtg_set_params / gradients)
+    std::vector<mtg_term> h_nb_terms;          // [T*T*5]
+    std::vector<int> h_nb_count;               // [T*T]
+    std::vector<double> h_nb_coef;             // [T*T*5*4] device coefficients
+    std::vector<double> h_nb_fs;               // [T*T*5] LJ force at the cutoff (force-shifted LJ)
+    std::vector<double> h_bond_par, h_angle_par, h_dih_par;   // device layouts
+    std::vector<int> h_bond_kind, h_angle_kind, h_dih_kind;
+    std::vector<double> h_charge;
+    bool has_tables = false;
     // buffers
     std::vector<void*> bufs;         // owned device allocations
     void* nbr_buf = nullptr;         // reference neighbour list (growable)
@@ -509,6 +518,26 @@ int fetch_rp(mtg_ctx* c, double c2) {
     return MTG_OK;
 }
 
+// Cutoff terms of a 12-6 / 12-8 LJ term with device coefficients co (a, b): the energy constant
+// (mode 1: U(rc); mode 2: U(rc) + rc F(rc)) and the force at the cutoff F(rc) (mode 2), for the
+// term's own cutoff or the global one.
+void lj_shift_terms(const mtg_term& t, const double* co, double rc_global, int mode, double* ushift, double* fcut) {
+    *ushift = 0.0;
+    *fcut = 0.0;
+    if(mode == 0) return;
+    const double rct = t.p[3] > 0.0 ? t.p[3] : rc_global;
+    const bool six = t.kind == MTG_NB_LJ;
+    const double ir = 1.0 / rct, ir2 = ir * ir, ir4 = ir2 * ir2, ir6 = ir4 * ir2, irn = six ? ir6 : ir4 * ir4;
+    const double Uc = co[0] * ir6 * ir6 - co[1] * irn;
+    const double Fc = (12.0 * co[0] * ir6 * ir6 - (six ? 6.0 : 8.0) * co[1] * irn) * ir;
+    if(mode == 1) {
+        *ushift = Uc;
+    } else {
+        *ushift = Uc + rct * Fc;
+        *fcut = Fc;
+    }
+}
+
 // A batch of independent replicas merged into one system: atom ranges, boxes, temperatures.
 struct BatchSpec {
     int nrep = 0;
@@ -663,6 +692,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     }
     if(cfg->precision < MTG_PREC_REFERENCE || cfg->precision > MTG_PREC_MIXED) return fail(nullptr, MTG_E_INVALID, "bad precision");
     if(cfg->coulomb < MTG_COULOMB_ALLPAIRS || cfg->coulomb > MTG_COULOMB_SHIFTED) return fail(nullptr, MTG_E_INVALID, "bad coulomb mode");
+    if(cfg->lj_shift < 0 || cfg->lj_shift > 2) return fail(nullptr, MTG_E_INVALID, "lj_shift must be 0, 1 or 2");
     if(cfg->precision == MTG_PREC_REFERENCE && cfg->coulomb != MTG_COULOMB_ALLPAIRS)
         return fail(nullptr, MTG_E_INVALID, "the reference precision mode has all-pairs Coulomb only");
     if(cfg->ensemble == MTG_NPT && cfg->precision != MTG_PREC_REFERENCE)
@@ -726,6 +756,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     P.M = cfg->ensemble == MTG_NVE ? 0 : cfg->temperature_nh_len;
     P.nresp = cfg->temperature_respa;
     P.fcut = cfg->cutoff_force;
+    P.lj_shift = cfg->lj_shift;
     if(P.ensemble == MTG_NPT) {
         // SimulationBox.cpp:58-76: NH_P_ shares T; W = kT tauP^2, P_ = pressure / Conv_press, V0 = Lx Ly Lz
         const double tauP = cfg->pressure_relax / kConvt;
@@ -831,6 +862,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     std::vector<float> nb_tab(TT * kMaxFF * kNpts * 3, 0.0f);
     std::vector<int> nb_kind(TT * kMaxFF, 0);
     std::vector<double> nb_coef(TT * kMaxFF * 4, 0.0);
+    std::vector<double> nb_fs(TT * kMaxFF, 0.0);
     std::vector<float> nb_coeff(TT * kMaxFF * 4, 0.0f);
     const float rcf = (float)cfg->cutoff_radius;
     for(size_t q = 0; q < TT; q++) {
@@ -849,13 +881,9 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
                 const double s2 = t.p[1] * t.p[1], s4 = s2 * s2, s6 = s4 * s2, s8 = s4 * s4, s12 = s6 * s6;
                 co[0] = 4.0 * t.p[0] * s12;
                 co[1] = 4.0 * t.p[0] * t.p[2] * (t.kind == MTG_NB_LJ ? s6 : s8);
-                // per-term cutoff^2 (0: the global cutoff applies) and energy shift U(rc)
-                const double rct = t.p[3] > 0.0 ? t.p[3] : cfg->cutoff_radius;
+                // per-term cutoff^2 (0: the global cutoff applies), energy shift and cutoff force
                 co[2] = t.p[3] > 0.0 ? t.p[3] * t.p[3] : 0.0;
-                if(cfg->lj_shift) {
-                    const double ir2 = 1.0 / (rct * rct), ir4 = ir2 * ir2, ir6 = ir4 * ir2;
-                    co[3] = co[0] * ir6 * ir6 - co[1] * (t.kind == MTG_NB_LJ ? ir6 : ir4 * ir4);
-                }
+                lj_shift_terms(t, co, cfg->cutoff_radius, cfg->lj_shift, &co[3], &nb_fs[idx]);
             } else if(t.kind == MTG_NB_BUCK) {
                 co[0] = t.p[0];
                 co[1] = (t.p[1] == 0.0) ? 1E-10 : 1.0 / t.p[1];
@@ -902,6 +930,15 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     }
     c->h_mass.assign(sys->mass, sys->mass + n);
     c->h_type = type;
+    c->h_nb_terms.assign(sys->nb_terms, sys->nb_terms + TT * kMaxFF);
+    c->h_nb_count.assign(sys->nb_count, sys->nb_count + TT);
+    c->h_nb_coef = nb_coef;
+    c->h_nb_fs = nb_fs;
+    c->h_charge.assign(sys->charge, sys->charge + n);
+    c->has_tables = sys->nb_tables || sys->bond_tables || sys->angle_tables || sys->dih_tables;
+    for(int k : nb_kind) c->has_tables |= (k == 99);
+    for(int k : bkind) c->has_tables |= (k == 99 || k == MTG_BOND_LJC);
+    for(int k : akind) c->has_tables |= (k == 99 || k == MTG_ANGLE_CLASS2);
     AtomLists L = build_atom_lists(n, sys->n_bonds, sys->bonds, sys->n_angles, sys->angles, sys->n_dihedrals, sys->dihedrals);
 
     DevSys& d = c->d;
@@ -935,8 +972,19 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         rc = rc || upload(C, &ip, nb_kind.data(), nb_kind.size()); d.nb_kind = ip;
         rc = rc || upload(C, &dp, nb_coef.data(), nb_coef.size()); d.nb_par = dp;
         rc = rc || upload(C, &f, nb_coeff.data(), nb_coeff.size()); d.nb_parf = f;
+        {
+            std::vector<float> fsf(nb_fs.begin(), nb_fs.end());
+            rc = rc || upload(C, &dp, nb_fs.data(), nb_fs.size()); d.nb_fs = dp;
+            rc = rc || upload(C, &f, fsf.data(), fsf.size()); d.nb_fsf = f;
+        }
         // angle parameters on the device: (k, theta0 in radians, toRad, 0)
         for(size_t t = 0; t < akind.size(); t++) apar[4 * t + 1] = apar[4 * t + 1] * apar[4 * t + 2];
+        c->h_bond_par = bpar;
+        c->h_angle_par = apar;
+        c->h_dih_par = dpar;
+        c->h_bond_kind = bkind;
+        c->h_angle_kind = akind;
+        c->h_dih_kind = dkind;
         std::vector<float> bparf(bpar.begin(), bpar.end()), aparf(apar.begin(), apar.end()), dparf(dpar.begin(), dpar.end());
         rc = rc || upload(C, &ip, bkind.data(), bkind.size()); d.bond_kind = ip;
         rc = rc || upload(C, &dp, bpar.data(), bpar.size()); d.bond_par = dp;
@@ -1660,6 +1708,509 @@ int mtg_batch_get_thermo(mtg_ctx* c, int32_t rep, mtg_thermo_state* th) {
     }
     if(c->h_rep_box.size() == (size_t)3 * c->P.nrep)
         for(int a = 0; a < 3; a++) th->box[a] = c->h_rep_box[(size_t)3 * rep + a];
+    return MTG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Force-field parameters and gradients
+// ---------------------------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// Device buffer freed with the scope.
+struct DBuf {
+    void* p = nullptr;
+    ~DBuf() { if(p) cudaFree(p); }
+    template<class T> T* as() { return static_cast<T*>(p); }
+};
+int dbuf(mtg_ctx* c, DBuf& b, size_t bytes) {
+    if(cudaMalloc(&b.p, std::max<size_t>(bytes, 8)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(c, MTG_E_NOMEM, "gradient work buffer allocation failed");
+    }
+    cudaMemsetAsync(b.p, 0, std::max<size_t>(bytes, 8), c->stream);
+    return MTG_OK;
+}
+
+// LJ term (first 12-6 / 12-8 entry) of type pair q, or -1.
+int lj_slot(const mtg_ctx* c, int q) {
+    for(int ff = 0; ff < c->h_nb_count[q]; ff++) {
+        const int k = c->h_nb_terms[q * kMaxFF + ff].kind;
+        if(k == MTG_NB_LJ || k == MTG_NB_LJ1208) return q * kMaxFF + ff;
+    }
+    return -1;
+}
+
+int check_param(mtg_ctx* c, const mtg_param& p) {
+    const int T = c->P.T;
+    switch(p.kind) {
+    case MTG_P_LJ_EPS:
+    case MTG_P_LJ_SIGMA:
+        if(p.index < 0 || p.index >= T * T || lj_slot(c, p.index) < 0) return fail(c, MTG_E_INVALID, "no LJ term on that type pair");
+        return MTG_OK;
+    case MTG_P_CHARGE:
+        if(!p.dq) return fail(c, MTG_E_INVALID, "charge parameter needs its dq direction");
+        for(int i = 0; i < c->P.n; i++)
+            if(p.dq[i] != 0.0) return MTG_OK;
+        return fail(c, MTG_E_INVALID, "charge direction dq is zero");
+    case MTG_P_BOND_K:
+    case MTG_P_BOND_R0:
+        if(p.index < 0 || p.index >= (int)c->h_bond_kind.size() || c->h_bond_kind[p.index] != MTG_BOND_HARM)
+            return fail(c, MTG_E_INVALID, "bond parameters need a harmonic bond type");
+        return MTG_OK;
+    case MTG_P_ANGLE_K:
+    case MTG_P_ANGLE_THETA0:
+        if(p.index < 0 || p.index >= (int)c->h_angle_kind.size() || c->h_angle_kind[p.index] != MTG_ANGLE_HARM)
+            return fail(c, MTG_E_INVALID, "angle parameters need a harmonic angle type");
+        return MTG_OK;
+    default:
+        return fail(c, MTG_E_INVALID, "unknown parameter kind");
+    }
+}
+
+// Device coefficients of an LJ term from (eps, sigma, alpha, rc) (as mtg_create packs them).
+void lj_coef(const mtg_ctx* c, const mtg_term& t, double* co, double* fs) {
+    const double s2 = t.p[1] * t.p[1], s4 = s2 * s2, s6 = s4 * s2, s8 = s4 * s4, s12 = s6 * s6;
+    co[0] = 4.0 * t.p[0] * s12;
+    co[1] = 4.0 * t.p[0] * t.p[2] * (t.kind == MTG_NB_LJ ? s6 : s8);
+    lj_shift_terms(t, co, c->cfg.cutoff_radius, c->cfg.lj_shift, &co[3], fs);
+}
+
+double get_param(const mtg_ctx* c, const mtg_param& p) {
+    switch(p.kind) {
+    case MTG_P_LJ_EPS: return c->h_nb_terms[lj_slot(c, p.index)].p[0];
+    case MTG_P_LJ_SIGMA: return c->h_nb_terms[lj_slot(c, p.index)].p[1];
+    case MTG_P_CHARGE:
+        for(int i = 0; i < c->P.n; i++)
+            if(p.dq[i] != 0.0) return c->h_charge[i] / p.dq[i];
+        return 0.0;
+    case MTG_P_BOND_K: return c->h_bond_par[4 * p.index];
+    case MTG_P_BOND_R0: return c->h_bond_par[4 * p.index + 1];
+    case MTG_P_ANGLE_K: return c->h_angle_par[4 * p.index];
+    case MTG_P_ANGLE_THETA0: return c->h_angle_par[4 * p.index + 1] / c->h_angle_par[4 * p.index + 2];
+    }
+    return 0.0;
+}
+
+// Host-side parameter change; device arrays are refreshed by push_params.
+void put_param(mtg_ctx* c, const mtg_param& p, double v) {
+    const int T = c->P.T;
+    switch(p.kind) {
+    case MTG_P_LJ_EPS:
+    case MTG_P_LJ_SIGMA: {
+        const int r = p.index / T, col = p.index % T;
+        for(int q : {r * T + col, col * T + r}) {
+            const int slot = lj_slot(c, q);
+            if(slot < 0) continue;
+            c->h_nb_terms[slot].p[p.kind == MTG_P_LJ_EPS ? 0 : 1] = v;
+            lj_coef(c, c->h_nb_terms[slot], &c->h_nb_coef[4 * slot], &c->h_nb_fs[slot]);
+        }
+        break;
+    }
+    case MTG_P_CHARGE:
+        for(int i = 0; i < c->P.n; i++)
+            if(p.dq[i] != 0.0) c->h_charge[i] = v * p.dq[i];
+        break;
+    case MTG_P_BOND_K: c->h_bond_par[4 * p.index] = v; break;
+    case MTG_P_BOND_R0: c->h_bond_par[4 * p.index + 1] = v; break;
+    case MTG_P_ANGLE_K: c->h_angle_par[4 * p.index] = v; break;
+    case MTG_P_ANGLE_THETA0: c->h_angle_par[4 * p.index + 1] = v * c->h_angle_par[4 * p.index + 2]; break;
+    }
+}
+
+int push_params(mtg_ctx* c) {
+    DevSys& d = c->d;
+    const int n = c->P.n;
+    std::vector<float> f(c->h_nb_coef.begin(), c->h_nb_coef.end());
+    CUDA_TRY(c, cudaMemcpy((void*)d.nb_par, c->h_nb_coef.data(), c->h_nb_coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy((void*)d.nb_parf, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    std::vector<float> fsf(c->h_nb_fs.begin(), c->h_nb_fs.end());
+    CUDA_TRY(c, cudaMemcpy((void*)d.nb_fs, c->h_nb_fs.data(), c->h_nb_fs.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy((void*)d.nb_fsf, fsf.data(), fsf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    auto push = [&](const std::vector<double>& h, const double* dd, const float* df) -> int {
+        std::vector<float> hf(h.begin(), h.end());
+        CUDA_TRY(c, cudaMemcpy((void*)dd, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy((void*)df, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        return MTG_OK;
+    };
+    int rc = push(c->h_bond_par, d.bond_par, d.bond_parf);
+    rc = rc ? rc : push(c->h_angle_par, d.angle_par, d.angle_parf);
+    if(rc) return rc;
+    std::vector<float> qf(n);
+    for(int i = 0; i < n; i++) qf[i] = (float)c->h_charge[i];
+    CUDA_TRY(c, cudaMemcpy(d.qd, c->h_charge.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(d.qf, qf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    // per-type charge table (and whether it describes every atom)
+    const int T = c->P.T;
+    std::vector<float> qt(std::max(T, 1), 0.0f);
+    std::vector<int> seen(std::max(T, 1), 0);
+    bool uniform = T <= 8;
+    for(int i = 0; i < n && uniform; i++) {
+        const int t = c->h_type[i];
+        if(!seen[t]) { seen[t] = 1; qt[t] = qf[i]; }
+        else if(qt[t] != qf[i]) uniform = false;
+    }
+    CUDA_TRY(c, cudaMemcpy((void*)d.qtype, qt.data(), sizeof(float) * qt.size(), cudaMemcpyHostToDevice));
+    if((uniform ? 1 : 0) != c->P.qtype) {
+        c->P.qtype = uniform ? 1 : 0;
+        c->generation++;   // captured graphs hold the old flag
+    }
+    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, true, c->stream);   // charges also live in hi.w
+    return MTG_OK;
+}
+
+// Tangent tables of parameter p (host vectors sized like the device ones), uploaded to buf.
+struct TangentSet {
+    DBuf nb, fs, q, bond, angle;
+    AdjTangents t{};
+};
+int make_tangents(mtg_ctx* c, const mtg_param& p, TangentSet& ts) {
+    const int T = c->P.T, n = c->P.n;
+    ts.t = AdjTangents{};
+    switch(p.kind) {
+    case MTG_P_LJ_EPS:
+    case MTG_P_LJ_SIGMA: {
+        // a = 4 eps sigma^12, b = 4 eps alpha sigma^n are linear in eps and powers of sigma; the
+        // cutoff constants (energy shift, force at the cutoff) are linear in (a, b)
+        std::vector<double> nt(c->h_nb_coef.size(), 0.0), ft(c->h_nb_fs.size(), 0.0);
+        const int r = p.index / T, col = p.index % T;
+        for(int q : {r * T + col, col * T + r}) {
+            const int slot = lj_slot(c, q);
+            if(slot < 0) continue;
+            const mtg_term& tm = c->h_nb_terms[slot];
+            const double e = tm.p[0], sg = tm.p[1], al = tm.p[2];
+            const double nn = tm.kind == MTG_NB_LJ ? 6.0 : 8.0;
+            double co_t[4] = {0.0, 0.0, 0.0, 0.0};
+            if(p.kind == MTG_P_LJ_EPS) {
+                co_t[0] = 4.0 * std::pow(sg, 12.0);
+                co_t[1] = 4.0 * al * std::pow(sg, nn);
+            } else {
+                co_t[0] = 48.0 * e * std::pow(sg, 11.0);
+                co_t[1] = 4.0 * e * al * nn * std::pow(sg, nn - 1.0);
+            }
+            double us_t, fs_t;
+            lj_shift_terms(tm, co_t, c->cfg.cutoff_radius, c->cfg.lj_shift, &us_t, &fs_t);
+            nt[4 * slot] = co_t[0];
+            nt[4 * slot + 1] = co_t[1];
+            nt[4 * slot + 3] = us_t;
+            ft[slot] = fs_t;
+        }
+        int rc = dbuf(c, ts.nb, nt.size() * sizeof(double));
+        if(!rc) rc = dbuf(c, ts.fs, ft.size() * sizeof(double));
+        if(rc) return rc;
+        CUDA_TRY(c, cudaMemcpy(ts.nb.p, nt.data(), nt.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(ts.fs.p, ft.data(), ft.size() * sizeof(double), cudaMemcpyHostToDevice));
+        ts.t.nb_par_t = ts.nb.as<double>();
+        ts.t.nb_fs_t = ts.fs.as<double>();
+        return MTG_OK;
+    }
+    case MTG_P_CHARGE: {
+        int rc = dbuf(c, ts.q, sizeof(double) * n);
+        if(rc) return rc;
+        CUDA_TRY(c, cudaMemcpy(ts.q.p, p.dq, sizeof(double) * n, cudaMemcpyHostToDevice));
+        ts.t.q_t = ts.q.as<double>();
+        return MTG_OK;
+    }
+    case MTG_P_BOND_K:
+    case MTG_P_BOND_R0: {
+        std::vector<double> bt(c->h_bond_par.size(), 0.0);
+        bt[4 * p.index + (p.kind == MTG_P_BOND_K ? 0 : 1)] = 1.0;
+        int rc = dbuf(c, ts.bond, bt.size() * sizeof(double));
+        if(rc) return rc;
+        CUDA_TRY(c, cudaMemcpy(ts.bond.p, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice));
+        ts.t.bond_par_t = ts.bond.as<double>();
+        return MTG_OK;
+    }
+    case MTG_P_ANGLE_K:
+    case MTG_P_ANGLE_THETA0: {
+        std::vector<double> at(c->h_angle_par.size(), 0.0);
+        if(p.kind == MTG_P_ANGLE_K) at[4 * p.index] = 1.0;
+        else at[4 * p.index + 1] = c->h_angle_par[4 * p.index + 2];   // d(theta0 rad)/d(theta0 deg)
+        int rc = dbuf(c, ts.angle, at.size() * sizeof(double));
+        if(rc) return rc;
+        CUDA_TRY(c, cudaMemcpy(ts.angle.p, at.data(), at.size() * sizeof(double), cudaMemcpyHostToDevice));
+        ts.t.angle_par_t = ts.angle.as<double>();
+        return MTG_OK;
+    }
+    }
+    return MTG_E_INVALID;
+}
+
+// FP64 positions of the current state in d.r (mixed: assembled from hi + lo).
+void positions_to_r(mtg_ctx* c) {
+    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+}
+
+// Places FP64 positions `pos` as the current positions and rebuilds the Verlet list there.
+void place_positions(mtg_ctx* c, const double* pos) {
+    if(pos != c->d.r)
+        cudaMemcpyAsync(c->d.r, pos, sizeof(double) * 3 * c->P.n, cudaMemcpyDeviceToDevice, c->stream);
+    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, true, c->stream);
+    launch_prod_build(c->d, c->P, true, c->stream);
+}
+
+// Ordered sum of x.y over n entries (device partials, host total).
+int dot(mtg_ctx* c, int n, const double* x, const double* y, DBuf& part, double* out) {
+    const int nb = dot_blocks(n);
+    launch_dot_blocks(n, x, y, part.as<double>(), c->stream);
+    std::vector<double> h(nb);
+    CUDA_TRY(c, cudaMemcpyAsync(h.data(), part.p, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    double s = 0.0;
+    for(double v : h) s += v;
+    *out = s;
+    return MTG_OK;
+}
+
+int grad_preflight(mtg_ctx* c, int32_t np, const mtg_param* params) {
+    if(is_reference(c)) return fail(c, MTG_E_UNSUPPORTED, "gradients use the analytic terms of the fp64 / mixed modes");
+    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "gradients are taken per system, not for batches");
+    if(c->has_tables) return fail(c, MTG_E_UNSUPPORTED, "tabulated terms have no derivative");
+    if(np < 0 || (np > 0 && !params)) return MTG_E_INVALID;
+    for(int k = 0; k < np; k++) {
+        int rc = check_param(c, params[k]);
+        if(rc) return rc;
+    }
+    return MTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mtg_get_params(mtg_ctx* c, int32_t np, const mtg_param* params, double* values) {
+    if(!c || !values) return MTG_E_INVALID;
+    for(int k = 0; k < np; k++) {
+        int rc = check_param(c, params[k]);
+        if(rc) return rc;
+        values[k] = get_param(c, params[k]);
+    }
+    return MTG_OK;
+}
+
+int mtg_set_params(mtg_ctx* c, int32_t np, const mtg_param* params, const double* values) {
+    if(!c || !values) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if(is_reference(c)) return fail(c, MTG_E_UNSUPPORTED, "the reference mode keeps its tables; set parameters in fp64 / mixed");
+    int rc = settle_state(c);
+    if(rc) return rc;
+    for(int k = 0; k < np; k++) {
+        rc = check_param(c, params[k]);
+        if(rc) return rc;
+        if(!std::isfinite(values[k])) return fail(c, MTG_E_NONFINITE, "non-finite parameter value");
+    }
+    for(int k = 0; k < np; k++) put_param(c, params[k], values[k]);
+    rc = push_params(c);
+    if(rc) return rc;
+    return compute_forces_now(c, true);
+}
+
+int mtg_energy_grad(mtg_ctx* c, int32_t np, const mtg_param* params, double* U, double* grad) {
+    if(!c) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = grad_preflight(c, np, params);
+    if(rc) return rc;
+    rc = settle_state(c);
+    if(rc) return rc;
+    const int n = c->P.n;
+    positions_to_r(c);
+    place_positions(c, c->d.r);
+    launch_prod_force(c->d, c->P, true, c->stream);
+    if(is_mixed(c)) launch_prod_forces_to_double(c->d, c->P, c->stream);
+    DBuf Ft, Ut, part;
+    if((rc = dbuf(c, Ft, sizeof(double) * 3 * n)) || (rc = dbuf(c, Ut, sizeof(double) * n)) ||
+       (rc = dbuf(c, part, sizeof(double) * dot_blocks(3 * n))))
+        return rc;
+    if(U) {
+        rc = dot(c, n, c->d.U, nullptr, part, U);
+        if(rc) return rc;
+    }
+    for(int k = 0; k < np; k++) {
+        TangentSet ts;
+        rc = make_tangents(c, params[k], ts);
+        if(rc) return rc;
+        launch_force_tangent(c->d, c->P, c->d.r, ts.t, Ft.as<double>(), Ut.as<double>(), c->stream);
+        CUDA_TRY(c, cudaGetLastError());
+        rc = dot(c, n, Ut.as<double>(), nullptr, part, &grad[k]);
+        if(rc) return rc;
+    }
+    return MTG_OK;
+}
+
+int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_param* params, double* loss, double* grad,
+                  double* rdf) {
+    if(!c || !L || !L->target) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = grad_preflight(c, np, params);
+    if(rc) return rc;
+    const int T = c->P.T, n = c->P.n, n3 = 3 * n;
+    const int S = L->nsteps, K = L->checkpoint_every > 0 ? L->checkpoint_every : L->nsteps;
+    if(S < 1 || L->nbins < 1 || !(L->rmax > 0.0) || !(L->width > 0.0) || L->type_a < 0 || L->type_a >= T ||
+       L->type_b < 0 || L->type_b >= T)
+        return fail(c, MTG_E_INVALID, "bad loss description");
+    const double rlist = std::max((double)c->P.rc, (double)c->P.rcoul) + c->P.skin;
+    if(L->rmax + 8.0 * L->width > rlist) return fail(c, MTG_E_INVALID, "rmax + 8 width must lie inside the Verlet-list radius");
+    rc = settle_state(c);
+    if(rc) return rc;
+    // the differentiated trajectory is plain velocity Verlet (NVE, no force clipping)
+    const Params saved = c->P;
+    struct Restore {
+        mtg_ctx* c;
+        Params P;
+        ~Restore() {
+            if(c->P.ensemble != P.ensemble || c->P.M != P.M || c->P.clip != P.clip) c->generation++;
+            c->P = P;
+        }
+    } restore{c, saved};
+    c->P.ensemble = MTG_NVE;
+    c->P.M = 0;
+    c->P.clip = 0;
+    const int nck = (S + K - 1) / K + 1;
+    DBuf ck_r, ck_p, seg, rows, hist, lam_r, lam_v, Ft, part, invm, cb, r0, p0;
+    if((rc = dbuf(c, ck_r, sizeof(double) * n3 * nck)) || (rc = dbuf(c, ck_p, sizeof(double) * n3 * nck)) ||
+       (rc = dbuf(c, seg, sizeof(double) * n3 * (K + 1))) || (rc = dbuf(c, rows, sizeof(double) * n * L->nbins)) ||
+       (rc = dbuf(c, hist, sizeof(double) * L->nbins)) || (rc = dbuf(c, lam_r, sizeof(double) * n3)) ||
+       (rc = dbuf(c, lam_v, sizeof(double) * n3)) || (rc = dbuf(c, Ft, sizeof(double) * n3)) ||
+       (rc = dbuf(c, part, sizeof(double) * dot_blocks(n3))) || (rc = dbuf(c, invm, sizeof(double) * n)) ||
+       (rc = dbuf(c, cb, sizeof(double) * L->nbins)) || (rc = dbuf(c, r0, sizeof(double) * n3)) ||
+       (rc = dbuf(c, p0, sizeof(double) * n3)))
+        return rc;
+    {
+        // 1/m for mobile atoms, 0 for immobile ones (their positions never change)
+        std::vector<double> im(n);
+        std::vector<int> mob(n);
+        CUDA_TRY(c, cudaMemcpy(mob.data(), c->d.mobile, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        for(int i = 0; i < n; i++) im[i] = mob[i] ? 1.0 / c->h_mass[i] : 0.0;
+        CUDA_TRY(c, cudaMemcpy(invm.p, im.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    }
+    AdjRdf rs{L->type_a, L->type_b, L->nbins, L->rmax, L->width};
+    const double dt = c->P.dt;
+    double* R = c->d.r;
+    // initial state
+    positions_to_r(c);
+    CUDA_TRY(c, cudaMemcpyAsync(r0.p, R, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(p0.p, c->d.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+    auto restore_state = [&](const double* r, const double* p) -> int {
+        CUDA_TRY(c, cudaMemcpyAsync(c->d.p, p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+        place_positions(c, r);
+        int rc2 = compute_forces_now(c, false);
+        if(rc2) return rc2;
+        launch_prologue(c->d, c->P, c->stream);   // pending scale S = 1 (NVE)
+        return MTG_OK;
+    };
+    auto step = [&]() -> int {
+        launch_prod_kick_drift(c->d, c->P, c->stream);
+        launch_prod_build(c->d, c->P, false, c->stream);
+        launch_prod_force(c->d, c->P, false, c->stream);
+        launch_prod_kick2(c->d, c->P, false, c->stream);
+        positions_to_r(c);
+        CUDA_TRY(c, cudaGetLastError());
+        return MTG_OK;
+    };
+    // ---- forward: checkpoints every K steps, pair correlation after every step ----
+    for(int attempt = 0;; attempt++) {
+        clear_overflow(c);
+        rc = restore_state(r0.as<double>(), p0.as<double>());
+        if(rc) return rc;
+        CUDA_TRY(c, cudaMemsetAsync(hist.p, 0, sizeof(double) * L->nbins, c->stream));
+        for(int t = 0; t < S; t++) {
+            if(t % K == 0) {
+                CUDA_TRY(c, cudaMemcpyAsync(ck_r.as<double>() + (size_t)(t / K) * n3, R, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+                CUDA_TRY(c, cudaMemcpyAsync(ck_p.as<double>() + (size_t)(t / K) * n3, c->d.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+            }
+            rc = step();
+            if(rc) return rc;
+            launch_rdf_rows(c->d, c->P, R, rs, rows.as<double>(), c->stream);
+            launch_rdf_reduce(rows.as<double>(), n, L->nbins, hist.as<double>(), c->stream);
+        }
+        StepScalars sc = read_scalars(c);
+        if(!sc.overflow) break;
+        if(attempt > 8) return fail(c, MTG_E_OVERFLOW, "neighbour list did not converge");
+        rc = grow_vlist(c, sc.needed);
+        if(rc) return rc;
+    }
+    // ---- loss ----
+    std::vector<double> h(L->nbins), norm(L->nbins), gbar(L->nbins), w(L->nbins);
+    CUDA_TRY(c, cudaMemcpy(h.data(), hist.p, sizeof(double) * L->nbins, cudaMemcpyDeviceToHost));
+    long long na = 0, nb = 0;
+    for(int i = 0; i < n; i++) {
+        na += (c->h_type[i] == L->type_a);
+        nb += (c->h_type[i] == L->type_b);
+    }
+    const double npairs = (L->type_a == L->type_b) ? 0.5 * double(na) * double(na - 1) : double(na) * double(nb);
+    const double V = c->P.box[0] * c->P.box[1] * c->P.box[2];
+    const double dr = L->rmax / L->nbins;
+    double Lval = 0.0;
+    for(int b = 0; b < L->nbins; b++) {
+        const double x = (b + 0.5) * dr;
+        norm[b] = (npairs > 0.0) ? V / (npairs * 4.0 * M_PI * x * x) : 0.0;
+        gbar[b] = norm[b] * h[b] / S;
+        const double dev = gbar[b] - L->target[b];
+        Lval += dev * dev;
+        w[b] = 2.0 * dev / S * norm[b];   // dL/d(sum_pairs K(r - x_b)) at each frame
+    }
+    if(loss) *loss = Lval;
+    if(rdf) std::memcpy(rdf, gbar.data(), sizeof(double) * L->nbins);
+    CUDA_TRY(c, cudaMemcpy(cb.p, w.data(), sizeof(double) * L->nbins, cudaMemcpyHostToDevice));
+    if(np == 0 || !grad) {
+        rc = restore_state(r0.as<double>(), p0.as<double>());
+        if(rc) return rc;
+        return compute_forces_now(c, true);
+    }
+    // ---- backward: leapfrog adjoint, segment by segment from the last checkpoint ----
+    std::vector<TangentSet> ts(np);
+    for(int k = 0; k < np; k++) {
+        rc = make_tangents(c, params[k], ts[k]);
+        if(rc) return rc;
+    }
+    DBuf gdev;   // gradient accumulated on the device, read once at the end
+    if((rc = dbuf(c, gdev, sizeof(double) * np))) return rc;
+    double* lr = lam_r.as<double>();
+    double* lv = lam_v.as<double>();
+    AdjTangents hv{};
+    hv.vpos = lv;
+    bool first = true;
+    for(int s0 = ((S - 1) / K) * K; s0 >= 0; s0 -= K) {
+        const int s1 = std::min(s0 + K, S);
+        rc = restore_state(ck_r.as<double>() + (size_t)(s0 / K) * n3, ck_p.as<double>() + (size_t)(s0 / K) * n3);
+        if(rc) return rc;
+        double* sg = seg.as<double>();
+        CUDA_TRY(c, cudaMemcpyAsync(sg, R, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+        for(int t = s0 + 1; t <= s1; t++) {
+            rc = step();
+            if(rc) return rc;
+            CUDA_TRY(c, cudaMemcpyAsync(sg + (size_t)(t - s0) * n3, R, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
+        }
+        for(int t = s1; t > s0; t--) {
+            const double* pt = sg + (size_t)(t - s0) * n3;
+            const double* pm = sg + (size_t)(t - 1 - s0) * n3;
+            if(first) {
+                // lambda_r = dL/dr_S
+                place_positions(c, pt);
+                launch_rdf_adjoint(c->d, c->P, R, rs, cb.as<double>(), lr, c->stream);
+                first = false;
+            }
+            launch_axpy(n3, dt, lr, invm.as<double>(), lv, c->stream);          // lambda_v += dt lambda_r / m
+            place_positions(c, pm);
+            const double wk = (t - 1 >= 1) ? dt : 0.5 * dt;
+            launch_force_tangent(c->d, c->P, R, hv, Ft.as<double>(), nullptr, c->stream);
+            launch_axpy(n3, wk, Ft.as<double>(), nullptr, lr, c->stream);       // lambda_r += w J lambda_v
+            for(int k = 0; k < np; k++) {
+                launch_force_tangent(c->d, c->P, R, ts[k].t, Ft.as<double>(), nullptr, c->stream);
+                launch_dot_accum(n3, lv, Ft.as<double>(), wk, part.as<double>(), gdev.as<double>() + k, c->stream);
+            }
+            if(t - 1 >= 1) launch_rdf_adjoint(c->d, c->P, R, rs, cb.as<double>(), lr, c->stream);
+            CUDA_TRY(c, cudaGetLastError());
+        }
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(grad, gdev.p, sizeof(double) * np, cudaMemcpyDeviceToHost, c->stream));
+    // back to the initial state
+    rc = restore_state(r0.as<double>(), p0.as<double>());
+    if(rc) return rc;
+    rc = compute_forces_now(c, true);
+    if(rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return MTG_OK;
 }
 

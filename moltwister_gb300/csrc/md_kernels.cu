@@ -514,7 +514,8 @@ __device__ __forceinline__ long long fix_total(const Fix& a) { return ((long lon
 // -dU/dr / r (= g) and U of the analytic pair terms for type pair `pair`; table kinds interpolate.
 // ir2 = 1/r^2 and ir = 1/r are passed in (rsqrt in FP32).
 template<class R>
-__device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir, R ir2, R& g, R& u, bool energy) {
+__device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir, R ir2, R& g, R& u, bool energy,
+                                           int P_lj_shift) {
     const int cnt = d.nb_cnt[pair];
     for(int ff = 0; ff < cnt; ff++) {
         const int idx = pair * kMaxFF + ff;
@@ -528,12 +529,18 @@ __device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir
             dd = (R)d.nb_par[4 * idx + 3];
         }
         if(kind == MTG_NB_LJ) {
-            // a = 4 eps sigma^12, b = 4 eps alpha sigma^6, c = own cutoff^2 (0: global), d = U(rc)
+            // a = 4 eps sigma^12, b = 4 eps alpha sigma^6, c = own cutoff^2 (0: global), d = energy
+            // shift; force-shifted LJ also subtracts F(rc) (fs) and adds r F(rc) to the energy
             if(c == R(0) || r2 < c) {
                 const R ir6 = ir2 * ir2 * ir2;
                 const R t12 = a * ir6 * ir6, t6 = b * ir6;
                 g += (R(12) * t12 - R(6) * t6) * ir2;
                 if(energy) u += t12 - t6 - dd;
+                if(P_lj_shift == 2) {
+                    const R fs = sizeof(R) == 4 ? (R)d.nb_fsf[idx] : (R)d.nb_fs[idx];
+                    g -= fs * ir;
+                    if(energy) u += r2 * ir * fs;
+                }
             }
         } else if(kind == MTG_NB_LJ1208) {
             if(c == R(0) || r2 < c) {
@@ -541,6 +548,11 @@ __device__ __forceinline__ void pair_terms(const DevSys& d, int pair, R r2, R ir
                 const R t12 = a * ir8 * ir4, t8 = b * ir8;
                 g += (R(12) * t12 - R(8) * t8) * ir2;
                 if(energy) u += t12 - t8 - dd;
+                if(P_lj_shift == 2) {
+                    const R fs = sizeof(R) == 4 ? (R)d.nb_fsf[idx] : (R)d.nb_fs[idx];
+                    g -= fs * ir;
+                    if(energy) u += r2 * ir * fs;
+                }
             }
         } else if(kind == MTG_NB_BUCK) {
             // a = A, b = 1/rho, c = C
@@ -755,6 +767,7 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
 struct PairCoef {
     float a, b;       // 4 eps sigma^12, 4 eps alpha sigma^6
     float rc2, us;    // own cutoff^2 (0: global), energy shift
+    float fs, pad0, pad1, pad2;   // force at the cutoff (force-shifted LJ)
 };
 constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
 
@@ -792,14 +805,14 @@ __device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int
                 if(c.rc2 == 0.0f || (float)r2 < c.rc2) {
                     const R ir6 = ir2 * ir2 * ir2;
                     const R t12 = (R)c.a * ir6 * ir6, t6 = (R)c.b * ir6;
-                    g = (R(12) * t12 - R(6) * t6) * ir2;
-                    if(ENERGY) u = t12 - t6 - (R)c.us;
+                    g = (R(12) * t12 - R(6) * t6) * ir2 - (R)c.fs * ir;
+                    if(ENERGY) u = t12 - t6 - (R)c.us + r2 * ir * (R)c.fs;
                 }
             } else if(mode == 2) {
-                pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY);
+                pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
             }
         } else {
-            pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY);
+            pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
         }
     }
     if(P.coulomb != MTG_COULOMB_ALLPAIRS && r2 < rq2) {
@@ -835,13 +848,13 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     const float* qt = nullptr;
     if(MIXED && P.T * P.T <= kSmemPairs) {
         for(int q = threadIdx.x; q < P.T * P.T; q += blockDim.x) {
-            PairCoef c{0.0f, 0.0f, 0.0f, 0.0f};
+            PairCoef c{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             int mode = 0;
             const int cnt = d.nb_cnt[q];
             if(cnt == 1 && d.nb_kind[q * kMaxFF] == MTG_NB_LJ) {
                 mode = 1;
                 const float4 f = reinterpret_cast<const float4*>(d.nb_parf)[q * kMaxFF];
-                c = PairCoef{f.x, f.y, f.z, f.w};
+                c = PairCoef{f.x, f.y, f.z, f.w, P.lj_shift == 2 ? d.nb_fsf[q * kMaxFF] : 0.0f, 0.0f, 0.0f, 0.0f};
             } else if(cnt > 0) {
                 mode = 2;
             }

@@ -102,6 +102,7 @@ struct Params {
     float fscale[3];      // L / 2^32: fixed-point position unit per axis (mixed)
     double fconv[3];      // 2^32 / L
     int qtype;            // 1: charges are a function of the type (qtype table)
+    int lj_shift;         // 0 truncated LJ, 1 energy shifted at the cutoff, 2 force shifted
     int nrep;             // 0: one system; > 0: a batch of nrep replicas (RepDev table)
     int ncell_total;      // batch: production cells of all replicas
     int nblk_total;       // batch: 256-atom integration blocks of all replicas
@@ -137,6 +138,8 @@ struct DevSys {
     const int* nb_kind;
     const double* nb_par;     // [pair*5+ff][4]
     const float* nb_parf;     // [pair*5+ff][4] (FP32 copy)
+    const double* nb_fs;      // [pair*5+ff] force at the LJ cutoff (force-shifted LJ), else 0
+    const float* nb_fsf;
     const int* bond_kind;
     const double* bond_par;   // [type][4]; angles hold (k, theta0 [rad], toRad, 0)
     const float* bond_parf;   // FP32 copies for the mixed kernels
@@ -227,6 +230,34 @@ void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t
 void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s);
 int reduction_blocks(int n);
 int integration_blocks(const Params& P);   // blocks of the 256-atom integration kernels
+
+// Adjoint kernels (adjoint.cu): tangents of the analytic forces and energies in FP64 dual numbers,
+// the smeared pair correlation of two types and its position gradient, vector kernels.
+struct AdjTangents {
+    const double* vpos;       // [3n] position tangents, or null
+    const double* nb_par_t;   // [T*T*5*4], or null
+    const double* nb_fs_t;    // [T*T*5], or null
+    const double* q_t;        // [n], or null
+    const double* bond_par_t; // [ntypes*4], or null
+    const double* angle_par_t;
+    const double* dih_par_t;
+};
+struct AdjRdf {
+    int ta, tb, nbins;
+    double rmax, width;
+};
+void launch_force_tangent(const DevSys& d, const Params& P, const double* pos, const AdjTangents& t, double* Ft, double* Ut,
+                          cudaStream_t s);
+void launch_rdf_rows(const DevSys& d, const Params& P, const double* pos, const AdjRdf& r, double* rows, cudaStream_t s);
+void launch_rdf_reduce(const double* rows, int n, int nbins, double* hist, cudaStream_t s);
+void launch_rdf_adjoint(const DevSys& d, const Params& P, const double* pos, const AdjRdf& r, const double* cb, double* grad,
+                        cudaStream_t s);
+void launch_axpy(int n3, double a, const double* x, const double* scale, double* y, cudaStream_t s);
+int dot_blocks(int n);
+void launch_dot_blocks(int n, const double* x, const double* y, double* out, cudaStream_t s);
+void launch_inv_mass(int n, const double* m, double* im, cudaStream_t s);
+// out[0] += w * sum_k x[k] y[k] (deterministic; part holds dot_blocks(n) partials)
+void launch_dot_accum(int n, const double* x, const double* y, double w, double* part, double* out, cudaStream_t s);
 
 // Host-side table generation (tables.cpp): out[npts*3] = (x, -dU/dx, U)
 int profile_nonbonded(int kind, const double* p, float r0, float r1, int npts, float* out);

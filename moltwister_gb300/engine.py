@@ -10,7 +10,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 from dataclasses import dataclass
-from typing import NamedTuple, Callable, List, Optional
+from typing import Callable, List, NamedTuple, Optional, Tuple
 
 import numpy as np
 
@@ -87,6 +87,16 @@ class Thermo(NamedTuple):
     box: Optional[np.ndarray] = None
 
 
+class Param(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int32), ("dq", C.c_void_p)]
+
+
+class LossDesc(C.Structure):
+    _fields_ = [("nsteps", C.c_int32), ("checkpoint_every", C.c_int32), ("type_a", C.c_int32),
+                ("type_b", C.c_int32), ("nbins", C.c_int32), ("reserved", C.c_int32),
+                ("rmax", C.c_double), ("width", C.c_double), ("target", C.c_void_p)]
+
+
 class Output(C.Structure):
     _fields_ = [("step", C.c_int64), ("T", C.c_double), ("P", C.c_double), ("V", C.c_double),
                 ("U", C.c_double), ("K", C.c_double), ("E", C.c_double),
@@ -135,6 +145,10 @@ def load_library(path: str = LIB_PATH):
         "mtg_batch_get_records": ([P, P], C.c_int),
         "mtg_batch_set_thermo": ([P, C.c_int32, C.POINTER(ThermoState)], C.c_int),
         "mtg_batch_get_thermo": ([P, C.c_int32, C.POINTER(ThermoState)], C.c_int),
+        "mtg_get_params": ([P, C.c_int32, P, P], C.c_int),
+        "mtg_set_params": ([P, C.c_int32, P, P], C.c_int),
+        "mtg_energy_grad": ([P, C.c_int32, P, P, P], C.c_int),
+        "mtg_loss_grad": ([P, C.POINTER(LossDesc), C.c_int32, P, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -271,7 +285,7 @@ def config_desc(c: MDConfig, device: int = 0) -> ConfigDesc:
     cf.list_skin = c.listskin
     cf.opt_learning_rate, cf.opt_accuracy, cf.opt_max_steps = c.optlearningrate, c.optaccuracy, c.optmaxsteps
     cf.device = device
-    cf.lj_shift = 1 if c.ljshift else 0
+    cf.lj_shift = int(c.ljshift)
     return cf
 
 
@@ -377,6 +391,41 @@ class Engine:
         self._check(self.lib.mtg_optimize(self.h, float(accuracy), int(max_steps), int(out_stride), cb, None))
         return records
 
+    # -- parameters and gradients ---------------------------------------------------------------
+    def get_params(self, params) -> np.ndarray:
+        arr, keep = _param_array(params)
+        out = np.zeros(len(params))
+        self._check(self.lib.mtg_get_params(self.h, len(params), C.cast(arr, C.c_void_p), _ptr(out)))
+        return out
+
+    def set_params(self, params, values) -> None:
+        arr, keep = _param_array(params)
+        v = np.ascontiguousarray(values, np.float64)
+        self._check(self.lib.mtg_set_params(self.h, len(params), C.cast(arr, C.c_void_p), _ptr(v)))
+
+    def energy_grad(self, params) -> Tuple[float, np.ndarray]:
+        """(U, dU/dtheta) at the current positions."""
+        arr, keep = _param_array(params)
+        U = np.zeros(1)
+        g = np.zeros(len(params))
+        self._check(self.lib.mtg_energy_grad(self.h, len(params), C.cast(arr, C.c_void_p), _ptr(U), _ptr(g)))
+        return float(U[0]), g
+
+    def loss_grad(self, loss, params, with_grad: bool = True) -> Tuple[float, np.ndarray, np.ndarray]:
+        """(L, dL/dtheta, gbar) of a pair-correlation trajectory loss (mtg_loss_grad); `loss` has
+        the fields of mtg_loss_desc (see moltwister_gb300.grad.RDFLoss).  with_grad=False evaluates
+        the loss only."""
+        arr, keep = _param_array(params)
+        tgt = np.ascontiguousarray(loss.target, np.float64)
+        d = LossDesc(int(loss.nsteps), int(loss.checkpoint_every), int(loss.type_a), int(loss.type_b),
+                     int(loss.nbins), 0, float(loss.rmax), float(loss.width), tgt.ctypes.data)
+        L = np.zeros(1)
+        g = np.zeros(len(params))
+        gbar = np.zeros(int(loss.nbins))
+        self._check(self.lib.mtg_loss_grad(self.h, C.byref(d), len(params), C.cast(arr, C.c_void_p), _ptr(L),
+                                           _ptr(g) if with_grad else None, _ptr(gbar)))
+        return float(L[0]), g, gbar
+
     def stats(self) -> dict:
         st = RunStats()
         self._check(self.lib.mtg_get_run_stats(self.h, C.byref(st)))
@@ -416,6 +465,20 @@ class Engine:
         lst = np.zeros((self.n, m), np.int32)
         self._check(self.lib.mtg_get_neighbors(self.h, m, _ptr(count), _ptr(lst), _ptr(need)))
         return count, lst
+
+
+def _param_array(params):
+    """ctypes mtg_param array of (kind, index, dq) tuples; returns (array, arrays kept alive)."""
+    arr = (Param * max(len(params), 1))()
+    keep = []
+    for k, (kind, index, dq) in enumerate(params):
+        arr[k].kind, arr[k].index = int(kind), int(index)
+        if dq is not None:
+            a = np.ascontiguousarray(dq, np.float64)
+            keep.append(a)
+            arr[k].dq = a.ctypes.data
+    keep.append(arr)
+    return arr, keep
 
 
 def neighbors_noalloc(r_ptr: int, n: int, box, cutoff: float, shell: float, max_neigh: int,

@@ -124,8 +124,9 @@ class MDConfig:
       coulombcutoff : cutoff radius for "cutoff" Coulomb [A] (defaults to cutoffradius).
       listskin      : Verlet skin of the production neighbour list [A].
       clipforces    : apply the reference's per-component force clipping (NVT/NVE only).
-      ljshift       : production modes: shift LJ energies to zero at each term's cutoff (forces
-                      unchanged), for energy-conservation measurements.
+      ljshift       : production modes, LJ at each term's cutoff: 0 truncated (the reference),
+                      1 energy shifted to zero (forces unchanged), 2 force shifted (force and
+                      energy continuous: smooth trajectories for gradients).
     """
     timestep: float = 1.0
     timesteps: int = 50000
@@ -155,7 +156,7 @@ class MDConfig:
     coulombcutoff: Optional[float] = None
     listskin: float = 1.0
     clipforces: bool = True
-    ljshift: bool = False
+    ljshift: int = 0
 
     REFERENCE_KEYS = ("timestep", "timesteps", "outstride", "temperature", "temperaturerelax",
                       "temperaturenhlen", "temperaturerespa", "pressure", "pressurerelax",

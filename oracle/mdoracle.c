@@ -477,7 +477,7 @@ typedef struct orc_sys {
     int coulomb_mode;         /* 0 all pairs minimum image (reference), 1 truncated, 2 shifted force at coulomb_rc */
     double coulomb_rc;
     const double* qd;         /* n charges in FP64 (analytic mode) */
-    int lj_shift;             /* analytic mode: shift LJ energies to zero at the cutoff */
+    int lj_shift;             /* analytic mode: 1 shift LJ energies to zero at the cutoff, 2 shift forces too */
 } orc_sys;
 
 /* FunctorCalcForce::scaleForcesAndPotentials (FunctorCalcForce.cpp:95-157) as a factor */
@@ -699,8 +699,8 @@ static v3 minimg(v3 d, const double* L) {
 
 /* -dU/dr for one analytic pair term and U */
 /* LJ/LJ1208 p = {eps, sigma, alpha, rc}: rc > 0 is the term's own cutoff (new option of the
- * production modes); with shift != 0 the energy is shifted to zero at the cutoff in force
- * (rc, else rglob). */
+ * production modes); shift 1 shifts the energy to zero at the cutoff in force (rc, else rglob),
+ * shift 2 shifts the force as well. */
 static void nb_analytic(int kind, const double* p, double R, double rglob, int shift, double* mdUdr, double* u) {
     if(kind == K_NB_LJ || kind == K_NB_LJ1208) {
         const double rct = p[3] > 0.0 ? p[3] : rglob;
@@ -718,6 +718,11 @@ static void nb_analytic(int kind, const double* p, double R, double rglob, int s
             if(kind == K_NB_LJ) { cn = c2 * c2 * c2; c12 = cn * cn; }
             else { double c4 = c2 * c2; cn = c4 * c4; c12 = cn * c4; }
             *u -= 4.0 * p[0] * (c12 - p[2] * cn);
+            if(shift == 2) {   /* force shifted: F - F(rc), U - U(rc) + (r - rc) F(rc) */
+                const double Fc = 4.0 * p[0] * (12.0 * c12 - n * p[2] * cn) / rct;
+                *mdUdr -= Fc;
+                *u += (R - rct) * Fc;
+            }
         }
     } else if(kind == K_NB_BUCK) {
         double e = p[0] * exp(-R / p[1]), r6 = 1.0 / (R * R * R * R * R * R);

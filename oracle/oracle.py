@@ -183,7 +183,7 @@ class Oracle:
         o.rc, o.shell, o.fcut = cfg.cutoffradius, cfg.neighshell, cfg.cutoffforce
         o.scale12, o.scale13, o.scale14, o.scale1N = cfg.scale12, cfg.scale13, cfg.scale14, cfg.scale1N
         o.coulomb_mode = {"allpairs": 0, "cutoff": 1, "shifted": 2}[cfg.coulomb]
-        o.lj_shift = 1 if getattr(cfg, "ljshift", False) else 0
+        o.lj_shift = int(getattr(cfg, "ljshift", 0))
         o.coulomb_rc = cfg.coulombcutoff if cfg.coulombcutoff is not None else cfg.cutoffradius
         return o
 

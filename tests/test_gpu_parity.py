@@ -247,3 +247,17 @@ def test_production_chain_stays_finite_on_large_systems():
     T_K = np.array([r.T for r in recs]) * 120.272
     assert np.all(np.isfinite(T_K))
     assert abs(T_K[-10:].mean() - T) < 0.15 * T, (T_K[-10:], T)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_force_shifted_lj(prec):
+    """Force-shifted LJ (ljshift = 2, a new option) against the FP64 oracle."""
+    from oracle import oracle as O
+    s, cfg = analytic_case("shifted")
+    cfg.precision = prec
+    cfg.ljshift = 2
+    F, U = engine(s, cfg).forces()
+    Fo, Uo = O.Oracle(s, cfg).forces_fp64()
+    rel = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
+    assert rel < (1e-10 if prec == "fp64" else 1e-5), rel
+    assert abs(U.sum() - Uo.sum()) < (1e-9 if prec == "fp64" else 1e-5) * abs(Uo.sum())

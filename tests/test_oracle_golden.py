@@ -111,3 +111,18 @@ def test_analytic_close_to_tables_where_reference_is_valid():
     F, _ = O.Oracle(s, cfg).forces_fp64()
     rel = np.sqrt(((F - d["F"]) ** 2).sum() / (d["F"] ** 2).sum())
     assert rel < 1e-4
+
+
+def test_force_shifted_lj_forces_are_energy_gradient():
+    """Oracle, ljshift = 2: the LJ force and energy are continuous at the cutoff and F = -grad U."""
+    from moltwister_gb300 import workloads as W
+    s, cfg = W.kob_andersen(ncell=3, seed=5, jitter=0.1)
+    cfg.precision = "fp64"
+    cfg.ljshift = 2
+    orc = O.Oracle(s, cfg)
+    F, U = orc.forces_fp64()
+    h = 1e-6
+    for k, a in [(0, 0), (5, 1), (17, 2)]:
+        r = s.r.copy(); r[k, a] += h; orc.set_positions(r); Up = orc.forces_fp64()[1].sum()
+        r = s.r.copy(); r[k, a] -= h; orc.set_positions(r); Um = orc.forces_fp64()[1].sum()
+        assert abs(F[k, a] + (Up - Um) / (2 * h)) < 1e-6 * max(1.0, abs(F[k, a]))
