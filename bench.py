@@ -124,6 +124,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def reduce_over_ranks(ms: float, atom_steps: float, device=None):
+    """(largest timed-region ms over ranks, atom-steps of all ranks); the local values when no
+    process group is initialised.  Replicas only: no data crosses ranks but these two scalars."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return ms, atom_steps
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    a = torch.tensor([atom_steps], dtype=torch.float64, device=device)
+    dist.all_reduce(a, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(a.item())
+
+
 def flush_l2():
     import torch
     buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -228,13 +242,11 @@ def our_arm(args):
     with ClockSampler(local) as clk:
         ms, builds, launches = timed_device(e, args.steps)
     torch.cuda.synchronize()
+    ms, atom_steps = reduce_over_ranks(ms, float(n * args.steps), device="cuda")
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = world * n * args.steps / (ms / 1e3)
+    value = atom_steps / (ms / 1e3)
 
     # per-phase timing (same stream, CUDA events) for the roofline
     phases = e.profile_phases(200)

@@ -317,6 +317,26 @@ typedef struct mtg_loss_desc {
 int mtg_loss_grad(mtg_ctx* ctx, const mtg_loss_desc* loss_desc, int32_t nparams, const mtg_param* params,
                   double* loss, double* grad, double* rdf /* [nbins] or NULL: gbar */);
 
+/* Pair-distance histogram of `moldyn`'s sibling analysis command `calculate paircorrelation`
+ * (Cmd/MolTwisterCmdCalculate/CmdPairCorrelation.cpp:182-215) for the current positions: every
+ * ordered pair (i of type_a, j of type_b, including i == j when the types are equal), distance
+ * across the periodic box, pairs closer than ignore_below skipped (the command's `ignoredistbelow`,
+ * -1 for none), bin int((R - rmin) / (rmax - rmin) * nbins).  The counts are added to profile[nbins]
+ * so that successive calls accumulate frames; the command's normalisation to g(r) is a host step
+ * (moltwister_gb300.analysis.pair_correlation).  nbins <= 8192. */
+int mtg_pair_histogram(mtg_ctx* ctx, int32_t type_a, int32_t type_b, int32_t nbins, double rmin, double rmax,
+                       double ignore_below, int64_t* profile);
+
+/* Trajectory files of the output step, byte for byte as the reference writes them.
+ * mtg_dcd_append creates the file with its header (num_steps / out_stride sets, time step in fs)
+ * if it does not exist, then appends one record: the box truncated to integers as
+ * CMDLoop::appendToDCDFile passes it (MDLoop.cpp:248-258, Utilities/DCDFile.cpp:670-729), FP32
+ * coordinates.  mtg_xyz_append appends one frame as CMDLoop::appendToXYZFile (MDLoop.cpp:229-246).
+ * Host-only; r is the host copy an mtg_run callback receives. */
+int mtg_dcd_append(const char* path, int32_t n_atoms, const double* r, const double box[3], int32_t num_steps,
+                   int32_t out_stride, double timestep_fs);
+int mtg_xyz_append(const char* path, int32_t n_atoms, const double* r, const char* const* ids, int32_t step);
+
 /* ---- Batches of independent replicas (no counterpart in the reference, which runs one system
  * per `moldyn run`) ----
  *

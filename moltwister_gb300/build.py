@@ -30,6 +30,7 @@ UNITS = [
     ("api.cu", []),
     ("adjoint.cu", []),
     ("tables.cpp", ["-Xcompiler", "-ffp-contract=off"]),
+    ("writers.cpp", []),
 ]
 
 

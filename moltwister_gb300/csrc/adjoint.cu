@@ -433,9 +433,50 @@ __global__ void k_inv_mass(int n, const double* m, double* im) {
     if(k < n) im[k] = 1.0 / m[k];
 }
 
+// Pair-distance histogram of CCmdPairCorrelation::execute for one frame
+// (Cmd/MolTwisterCmdCalculate/CmdPairCorrelation.cpp:182-215): every ordered pair (i in A, j in B),
+// distance across the periodic box as C3DVector::distToAcrossPBC (Utilities/3DVector.cpp:44-66),
+// pairs closer than ignore_below skipped, bin int((R - rmin) / (rmax - rmin) * nbins).  The
+// arithmetic is spelled out with round-to-nearest intrinsics so no contraction changes a bin.
+__global__ void k_pair_hist(const double* pos, const int* ia, int na, const int* ib, int nb, double wx, double wy, double wz,
+                            double rmin, double rmax, int nbins, double ignore_below, unsigned long long* prof) {
+    extern __shared__ unsigned int hist_s[];
+    for(int b = threadIdx.x; b < nbins; b += blockDim.x) hist_s[b] = 0u;
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if(t < na) {
+        const int i = ia[t];
+        const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+        const double span = __dsub_rn(rmax, rmin);
+        for(int q = 0; q < nb; q++) {
+            const int j = ib[q];
+            double dX = __dsub_rn(xi, pos[3 * j]), dY = __dsub_rn(yi, pos[3 * j + 1]), dZ = __dsub_rn(zi, pos[3 * j + 2]);
+            dX = (dX < 0.0) ? -dX : dX;
+            dY = (dY < 0.0) ? -dY : dY;
+            dZ = (dZ < 0.0) ? -dZ : dZ;
+            if(dX > wx / 2.0) dX = __dsub_rn(wx, dX);
+            if(dY > wy / 2.0) dY = __dsub_rn(wy, dY);
+            if(dZ > wz / 2.0) dZ = __dsub_rn(wz, dZ);
+            const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dX, dX), __dmul_rn(dY, dY)), __dmul_rn(dZ, dZ)));
+            if(R < ignore_below) continue;
+            const int n = (int)__dmul_rn(__ddiv_rn(__dsub_rn(R, rmin), span), double(nbins));
+            if(n >= 0 && n < nbins) atomicAdd(&hist_s[n], 1u);
+        }
+    }
+    __syncthreads();
+    for(int b = threadIdx.x; b < nbins; b += blockDim.x)
+        if(hist_s[b]) atomicAdd(&prof[b], (unsigned long long)hist_s[b]);
+}
+
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
+
+void launch_pair_hist(const double* pos, const int* ia, int na, const int* ib, int nb, const double* box, double rmin,
+                      double rmax, int nbins, double ignore_below, unsigned long long* prof, cudaStream_t s) {
+    k_pair_hist<<<nblk(na, 128), 128, sizeof(unsigned int) * nbins, s>>>(pos, ia, na, ib, nb, box[0], box[1], box[2], rmin,
+                                                                        rmax, nbins, ignore_below, prof);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Launchers (declared in mtg_internal.h)

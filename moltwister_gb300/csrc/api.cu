@@ -2214,6 +2214,43 @@ int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_para
     return MTG_OK;
 }
 
+int mtg_pair_histogram(mtg_ctx* c, int32_t type_a, int32_t type_b, int32_t nbins, double rmin, double rmax,
+                       double ignore_below, int64_t* profile) {
+    if(!c || !profile || nbins < 1 || nbins > 8192 || !(rmax != rmin)) return MTG_E_INVALID;
+    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "pair histograms are taken per system");
+    if(type_a < 0 || type_a >= c->P.T || type_b < 0 || type_b >= c->P.T) return fail(c, MTG_E_INVALID, "type out of range");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = settle_state(c);
+    if(rc) return rc;
+    std::vector<int> ia, ib;
+    for(int i = 0; i < c->P.n; i++) {
+        if(c->h_type[i] == type_a) ia.push_back(i);
+        if(c->h_type[i] == type_b) ib.push_back(i);
+    }
+    if(ia.empty() || ib.empty()) return MTG_OK;
+    DBuf dia, dib, prof;
+    if((rc = dbuf(c, dia, sizeof(int) * ia.size())) || (rc = dbuf(c, dib, sizeof(int) * ib.size())) ||
+       (rc = dbuf(c, prof, sizeof(unsigned long long) * nbins)))
+        return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(dia.p, ia.data(), sizeof(int) * ia.size(), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(dib.p, ib.data(), sizeof(int) * ib.size(), cudaMemcpyHostToDevice, c->stream));
+    positions_to_r(c);
+    double box[3] = {c->P.box[0], c->P.box[1], c->P.box[2]};
+    if(c->P.ensemble == MTG_NPT) {
+        BaroDev b{};
+        CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+        for(int a = 0; a < 3; a++) box[a] = b.L[a];
+    }
+    launch_pair_hist(c->d.r, dia.as<int>(), (int)ia.size(), dib.as<int>(), (int)ib.size(), box, rmin, rmax, nbins, ignore_below,
+                     prof.as<unsigned long long>(), c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    std::vector<unsigned long long> h(nbins);
+    CUDA_TRY(c, cudaMemcpyAsync(h.data(), prof.p, sizeof(unsigned long long) * nbins, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    for(int b = 0; b < nbins; b++) profile[b] += (int64_t)h[b];
+    return MTG_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------------------------

@@ -149,6 +149,9 @@ def load_library(path: str = LIB_PATH):
         "mtg_set_params": ([P, C.c_int32, P, P], C.c_int),
         "mtg_energy_grad": ([P, C.c_int32, P, P, P], C.c_int),
         "mtg_loss_grad": ([P, C.POINTER(LossDesc), C.c_int32, P, P, P, P], C.c_int),
+        "mtg_pair_histogram": ([P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, P], C.c_int),
+        "mtg_dcd_append": ([C.c_char_p, C.c_int32, P, P, C.c_int32, C.c_int32, C.c_double], C.c_int),
+        "mtg_xyz_append": ([C.c_char_p, C.c_int32, P, P, C.c_int32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -425,6 +428,14 @@ class Engine:
         self._check(self.lib.mtg_loss_grad(self.h, C.byref(d), len(params), C.cast(arr, C.c_void_p), _ptr(L),
                                            _ptr(g) if with_grad else None, _ptr(gbar)))
         return float(L[0]), g, gbar
+
+    def pair_histogram(self, type_a: int, type_b: int, nbins: int, rmin: float, rmax: float,
+                       ignore_below: float = -1.0, profile: Optional[np.ndarray] = None) -> np.ndarray:
+        """Adds the current frame's ordered-pair distance counts to profile (int64[nbins])."""
+        prof = np.zeros(nbins, np.int64) if profile is None else profile
+        self._check(self.lib.mtg_pair_histogram(self.h, int(type_a), int(type_b), int(nbins), float(rmin), float(rmax),
+                                                float(ignore_below), _ptr(prof)))
+        return prof
 
     def stats(self) -> dict:
         st = RunStats()

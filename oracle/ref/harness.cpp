@@ -38,6 +38,9 @@
 #include "Cmd/MolTwisterCmdMolDyn/MDLoop/Printf.h"
 #include "Cmd/MolTwisterCmdMolDyn/Config/MolDynConfig.h"
 #include "Cmd/Tools/MolTwisterStateTools.h"
+#include "Utilities/DCDFile.h"
+#include <functional>
+#include <tuple>
 
 namespace {
 
@@ -366,6 +369,24 @@ int cmdRun(const SysIn& s, const std::string& out, int nsteps, int stride) {
     return 0;
 }
 
+// dcd: two DCD records (the input positions and the positions shifted by +0.125 A) written
+// through the reference's CDCDFile::createDCDFileIfNotExists / appendToDCDFile
+// (Utilities/DCDFile.cpp:670-729), as CMDLoop::appendToDCDFile calls them (MDLoop.cpp:248-258).
+int cmdDcd(const SysIn& s, const std::string& out, int nsteps, int stride, double dt) {
+    const int N = (int)s.atoms.size();
+    remove(out.c_str());
+    for(int rec = 0; rec < 2; rec++) {
+        const double sh = 0.125 * rec;
+        std::function<std::tuple<double, double, double>(const int&)> pos = [&s, sh](const int& i) -> std::tuple<double, double, double> {
+            const AtomIn& a = s.atoms[i];
+            return std::tuple<double, double, double>(a.x + sh, a.y + sh, a.z + sh);
+        };
+        CDCDFile::createDCDFileIfNotExists(out, nsteps, stride, dt, N);
+        CDCDFile::appendToDCDFile(out, N, {s.L[0], s.L[1], s.L[2]}, pos);
+    }
+    return 0;
+}
+
 int cmdTime(const SysIn& s, int nsteps) {
     CMolTwisterState st; buildState(s, st);
     SMolDynConfigStruct cfg = makeCfg(s);
@@ -396,7 +417,7 @@ int cmdTime(const SysIn& s, int nsteps) {
 
 int main(int argc, char** argv) {
     if(argc < 3) {
-        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS\n");
+        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT\n");
         return 1;
     }
     std::string cmd = argv[1];
@@ -404,6 +425,7 @@ int main(int argc, char** argv) {
     if(cmd == "static" && argc >= 4) return cmdStatic(s, argv[3]);
     if(cmd == "run" && argc >= 6) return cmdRun(s, argv[3], atoi(argv[4]), atoi(argv[5]));
     if(cmd == "time" && argc >= 4) return cmdTime(s, atoi(argv[3]));
+    if(cmd == "dcd" && argc >= 7) return cmdDcd(s, argv[3], atoi(argv[4]), atoi(argv[5]), atof(argv[6]));
     fprintf(stderr, "bad arguments\n");
     return 1;
 }

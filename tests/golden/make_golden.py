@@ -101,6 +101,22 @@ def pack(name, s, c, steps, stride):
     return path
 
 
+def make_dcd(name="water648_nvt"):
+    """dcd_<name>.bin: two records written by the reference's CDCDFile (the system's positions and
+    the same shifted by +0.125 A), header for 100 steps every 25 at dt 0.5 fs."""
+    import tempfile
+    from oracle.sysfile import run_harness
+    s, c, _, _ = cases()[name]
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.dcd")
+        run_harness(["dcd", out, 100, 25, 0.5], s, c)
+        data = open(out, "rb").read()
+    path = os.path.join(OUT, f"dcd_{name}.bin")
+    with open(path, "wb") as fh:
+        fh.write(data)
+    return path
+
+
 def main(only=()):
     for name, (s, c, steps, stride) in cases().items():
         if only and name not in only:
@@ -110,4 +126,7 @@ def main(only=()):
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]))
+    if sys.argv[1:] == ["dcd"]:
+        print(make_dcd())
+    else:
+        main(tuple(sys.argv[1:]))
