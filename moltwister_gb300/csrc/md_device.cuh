@@ -164,21 +164,33 @@ struct NhExchange {
 // Bounded wait for a flag of another warp of the block: spins on shared memory for the first
 // 4096 polls (the partner is normally a few hundred cycles away), then backs off; gives up after
 // 2^22 polls and records a timeout.
+// Flag hand-over between warps of a block with release / acquire ordering at CTA scope: the
+// posting lane's earlier shared-memory stores (the value) are visible to a waiter once it observes
+// the flag, without a full block fence on either side.
+__device__ __forceinline__ int ld_acquire_cta(volatile int* p) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];"
+                 : "=r"(v)
+                 : "r"((unsigned)__cvta_generic_to_shared((void*)p))
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_cta(volatile int* p, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared((void*)p)), "r"(v)
+                 : "memory");
+}
+
 __device__ __forceinline__ void nh_wait(volatile int* flag, int seq, int* timeout) {
     for(int it = 0; it < (1 << 22); it++) {
-        if(*flag >= seq) {
-            __threadfence_block();
-            return;
-        }
+        if(ld_acquire_cta(flag) >= seq) return;
         if(it >= 4096) __nanosleep(32);
     }
     *timeout = 1;
 }
 
+// Lane 0 posts; it is also the lane that stored the value being handed over.
 __device__ __forceinline__ void nh_post(volatile int* flag, int seq) {
-    __threadfence_block();
-    __syncwarp();
-    if((threadIdx.x & 31) == 0) *flag = seq;
+    if((threadIdx.x & 31) == 0) st_release_cta(flag, seq);
 }
 
 // e^x for |x| <= 2^-10 by its Taylor series to order 4 (remainder below 1e-17)
