@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -232,6 +233,44 @@ int grow_neighbors(mtg_ctx* c, int needed) {
     c->d.nbr_max = cap;
     c->generation++;
     return MTG_OK;
+}
+
+// Production list radius per type pair before the skin (DevSys::pair_cut): 0 when the pair has no
+// short-range term, its own LJ cutoff when every term of the pair has one, FLT_MAX (the global
+// cutoff) otherwise.  Coulomb widens every pair to rcoul on the device when charges are on.  The
+// pair (full_a, full_b) keeps the full list radius (a pair-correlation loss reads its pairs from
+// the list).
+std::vector<float> pair_cuts(const mtg_ctx* c, int full_a, int full_b) {
+    const int T = c->P.T;
+    std::vector<float> pc((size_t)T * T, 0.0f);
+    for(int a = 0; a < T; a++)
+        for(int b = 0; b < T; b++) {
+            const int q = a * T + b;
+            float v = 0.0f;
+            for(int ff = 0; ff < c->h_nb_count[q]; ff++) {
+                const mtg_term& t = c->h_nb_terms[(size_t)q * kMaxFF + ff];
+                const bool own = (t.kind == MTG_NB_LJ || t.kind == MTG_NB_LJ1208) && t.p[3] > 0.0;
+                v = own ? std::max(v, (float)t.p[3]) : FLT_MAX;
+            }
+            if((a == full_a && b == full_b) || (a == full_b && b == full_a)) v = -1.0f;
+            pc[q] = v;
+        }
+    return pc;
+}
+
+int upload_pair_cuts(mtg_ctx* c, int full_a, int full_b) {
+    const std::vector<float> pc = pair_cuts(c, full_a, full_b);
+    CUDA_TRY(c, cudaMemcpyAsync((void*)c->d.pair_cut, pc.data(), sizeof(float) * pc.size(), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MTG_OK;
+}
+
+// 1 when the production kernels have Coulomb work: a cutoff mode and some nonzero charge.
+int charges_on(const mtg_ctx* c) {
+    if(c->P.coulomb == MTG_COULOMB_ALLPAIRS) return 0;
+    for(double q : c->h_charge)
+        if(q != 0.0) return 1;
+    return 0;
 }
 
 int grow_vlist(mtg_ctx* c, int needed) {
@@ -505,7 +544,7 @@ int fetch_rp(mtg_ctx* c, double c2) {
     const size_t n3 = (size_t)c->P.n * 3;
     c->h_r.resize(n3);
     c->h_p.resize(n3);
-    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
     CUDA_TRY(c, cudaMemcpyAsync(c->h_r.data(), c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(c->h_p.data(), c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -590,6 +629,8 @@ int read_records(mtg_ctx* c, double* rec) {
 // Applies the pending c2 to the device momenta and rewinds the thermostat (and, under NPT, the
 // barostat) to the state after the last completed step (end of a run).
 int settle_state(mtg_ctx* c) {
+    // mixed: the kernels advance the double-float mirrors; bring the FP64 masters up to date
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
     if(c->P.ensemble == MTG_NPT) {
         BaroDev b{};
         CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
@@ -616,6 +657,7 @@ int settle_state(mtg_ctx* c) {
             CUDA_TRY(c, cudaMemcpy(p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
             scale_momenta(c, p, c2);
             CUDA_TRY(c, cudaMemcpy(c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
+            if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
             CUDA_TRY(c, cudaMemcpy(c->d.ths, c->d.ths_saved, sizeof(ThermoDev) * rs.size(), cudaMemcpyDeviceToDevice));
             for(auto& x : rs) {
                 x.c2 = 1.0;
@@ -631,6 +673,7 @@ int settle_state(mtg_ctx* c) {
         CUDA_TRY(c, cudaMemcpy(p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
         for(double& v : p) v *= s.c2;
         CUDA_TRY(c, cudaMemcpy(c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
+        if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
         CUDA_TRY(c, cudaMemcpy(c->d.th, c->d.th_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
         s.c2 = 1.0;
         s.S = 1.0;
@@ -976,6 +1019,9 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             std::vector<float> fsf(nb_fs.begin(), nb_fs.end());
             rc = rc || upload(C, &dp, nb_fs.data(), nb_fs.size()); d.nb_fs = dp;
             rc = rc || upload(C, &f, fsf.data(), fsf.size()); d.nb_fsf = f;
+            const std::vector<float> pcut = pair_cuts(c.get(), -1, -1);
+            rc = rc || upload(C, &f, pcut.data(), pcut.size()); d.pair_cut = f;
+            P.qon = charges_on(c.get());
         }
         // angle parameters on the device: (k, theta0 in radians, toRad, 0)
         for(size_t t = 0; t < akind.size(); t++) apar[4 * t + 1] = apar[4 * t + 1] * apar[4 * t + 2];
@@ -1020,6 +1066,8 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         rc = rc || dalloc(C, &d.hi, (size_t)n);
         rc = rc || dalloc(C, &d.lo, (size_t)n);
         rc = rc || dalloc(C, &d.pq, (size_t)n);
+        rc = rc || dalloc(C, &d.ph, (size_t)n);
+        rc = rc || dalloc(C, &d.pl, (size_t)n);
         {
             // per-type charge table, used when every atom of a type carries the same charge
             std::vector<float> qt(std::max(T, 1), 0.0f);
@@ -1124,7 +1172,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         rc = grow_vlist(c.get(), std::min(vest, n));
         if(rc) return fail(nullptr, rc, c->err);
     }
-    if(is_mixed(c.get())) launch_prod_sync_positions(d, P, true, c->stream);
+    if(is_mixed(c.get())) launch_prod_sync(d, P, kSyncFromMaster, c->stream);
     // snapshot set for chunk rollback
     {
         mtg_ctx* C = c.get();
@@ -1149,6 +1197,8 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             rc = rc || add_snap(C, d.hi, sizeof(float4) * n);
             rc = rc || add_snap(C, d.lo, sizeof(float4) * n);
             rc = rc || add_snap(C, d.pq, sizeof(uint4) * n);
+            rc = rc || add_snap(C, d.ph, sizeof(float4) * n);
+            rc = rc || add_snap(C, d.pl, sizeof(float4) * n);
             rc = rc || add_snap(C, d.Fx, sizeof(long long) * n);
             rc = rc || add_snap(C, d.Fy, sizeof(long long) * n);
             rc = rc || add_snap(C, d.Fz, sizeof(long long) * n);
@@ -1180,12 +1230,12 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
     if(r) {
         if(!finite_all(r, n3)) return fail(c, MTG_E_NONFINITE, "non-finite positions");
         CUDA_TRY(c, cudaMemcpy(c->d.r, r, n3 * sizeof(double), cudaMemcpyHostToDevice));
-        if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, true, c->stream);
     }
     if(p) {
         if(!finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
         CUDA_TRY(c, cudaMemcpy(c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
     }
+    if((r || p) && is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
     if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch sets chain states per replica (mtg_batch_set_thermo)");
     if(th) {
         ThermoDev t{};
@@ -1224,7 +1274,7 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
     if(rc) return rc;
     const size_t n3 = (size_t)c->P.n * 3;
     if(r) {
-        if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+        if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
         CUDA_TRY(c, cudaMemcpyAsync(r, c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
     if(p) CUDA_TRY(c, cudaMemcpyAsync(p, c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -1376,7 +1426,7 @@ int mtg_get_cells(mtg_ctx* c, int32_t* dims, int32_t* ixyz, int32_t* cell_first,
         dims[2] = c->P.nz;
     }
     if((cell_first || cell_count) && ncells < c->ncell_ref) return fail(c, MTG_E_INVALID, "cell arrays too small");
-    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
     launch_ref_cells(c->d, c->P, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     const int n = c->P.n;
@@ -1392,7 +1442,7 @@ int mtg_get_neighbors(mtg_ctx* c, int32_t max_neigh, int32_t* count, int32_t* li
     if(!c) return MTG_E_INVALID;
     if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "the reference neighbour list is not built for batches");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
     for(int attempt = 0; attempt < 64; attempt++) {
         clear_overflow(c);
         launch_ref_cells(c->d, c->P, c->stream);
@@ -1856,7 +1906,14 @@ int push_params(mtg_ctx* c) {
         c->P.qtype = uniform ? 1 : 0;
         c->generation++;   // captured graphs hold the old flag
     }
-    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, true, c->stream);   // charges also live in hi.w
+    const int qon = charges_on(c);
+    if(qon != c->P.qon) {
+        c->P.qon = qon;
+        c->generation++;
+        // charges switched on: the list must reach rcoul for every pair
+        if(!is_reference(c)) cudaMemsetAsync(&c->d.sc->rebuild, 0xff, sizeof(int32_t), c->stream);
+    }
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);   // charges also live in hi.w
     return MTG_OK;
 }
 
@@ -1939,14 +1996,14 @@ int make_tangents(mtg_ctx* c, const mtg_param& p, TangentSet& ts) {
 
 // FP64 positions of the current state in d.r (mixed: assembled from hi + lo).
 void positions_to_r(mtg_ctx* c) {
-    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, false, c->stream);
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
 }
 
 // Places FP64 positions `pos` as the current positions and rebuilds the Verlet list there.
 void place_positions(mtg_ctx* c, const double* pos) {
     if(pos != c->d.r)
         cudaMemcpyAsync(c->d.r, pos, sizeof(double) * 3 * c->P.n, cudaMemcpyDeviceToDevice, c->stream);
-    if(is_mixed(c)) launch_prod_sync_positions(c->d, c->P, true, c->stream);
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncPositionsFromMaster, c->stream);
     launch_prod_build(c->d, c->P, true, c->stream);
 }
 
@@ -2061,8 +2118,14 @@ int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_para
         ~Restore() {
             if(c->P.ensemble != P.ensemble || c->P.M != P.M || c->P.clip != P.clip) c->generation++;
             c->P = P;
+            // per-pair list radii again (the current list keeps the loss pair's extra partners,
+            // which the force kernels skip by their cutoffs, until the next rebuild)
+            (void)upload_pair_cuts(c, -1, -1);
         }
     } restore{c, saved};
+    // the loss pair's partners out to the full list radius (the rebuild below places them)
+    rc = upload_pair_cuts(c, L->type_a, L->type_b);
+    if(rc) return rc;
     c->P.ensemble = MTG_NVE;
     c->P.M = 0;
     c->P.clip = 0;
@@ -2094,6 +2157,7 @@ int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_para
     auto restore_state = [&](const double* r, const double* p) -> int {
         CUDA_TRY(c, cudaMemcpyAsync(c->d.p, p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
         place_positions(c, r);
+        if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
         int rc2 = compute_forces_now(c, false);
         if(rc2) return rc2;
         launch_prologue(c->d, c->P, c->stream);   // pending scale S = 1 (NVE)

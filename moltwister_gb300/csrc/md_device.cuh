@@ -646,6 +646,68 @@ __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2,
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Double-float arithmetic for the mixed-mode integrator.  The FP64 unit of this GPU runs at a
+// small fraction of the FP32 rate (64-bit conversions included), so per-atom FP64 work made the
+// kick and drift kernels slower than the force gather at 10^6 atoms.  A value is the unevaluated
+// sum h + l of two floats with |l| <= ulp(h)/2 (about 48 significant bits); the error-free
+// transformations below are Knuth's two-sum, Dekker's fast two-sum and the FMA-based exact
+// product.  The _rn intrinsics keep the compiler from contracting or reordering them.
+// ---------------------------------------------------------------------------------------------
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {   // |a| >= |b| (or a = 0)
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const DF s = two_sum(a.h, b.h);
+    const DF t = two_sum(a.l, b.l);
+    const DF u = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return fast_two_sum(u.h, __fadd_rn(u.l, t.l));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_mul_f(DF a, float b) {
+    const float p = __fmul_rn(a.h, b);
+    return fast_two_sum(p, __fmaf_rn(a.l, b, __fmaf_rn(a.h, b, -p)));
+}
+// FP64 <-> double-float (FP64 instructions: used once per block or outside the step loop)
+__device__ __forceinline__ DF df_of(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_val(DF a) { return (double)a.h + (double)a.l; }
+// Fixed-point force q (units 2^-26) as a double-float: q = a 2^22 + b with 0 <= b < 2^22, both
+// parts converted by 32-bit conversions (exact for |q| < 2^46, i.e. |F| < 2^20 kJ/(mol A)).
+__device__ __forceinline__ DF df_fix(long long q) {
+    const int a = (int)(q >> 22);
+    const int b = (int)(q & 0x3FFFFFLL);
+    return two_sum(__fmul_rn(__int2float_rn(a), 0.0625f), __fmul_rn(__int2float_rn(b), 1.4901161193847656e-08f));
+}
+// Box fraction round(x * conv) modulo 2^32 (conv = 2^32 / L) from double-float operands, to
+// within one unit (L / 2^32): the product's high part is reduced modulo 2^32 exactly, then the
+// integer parts of both halves are added.
+__device__ __forceinline__ unsigned int frac32_df(DF x, DF conv) {
+    const DF y = df_mul(x, conv);
+    const float k = rintf(__fmul_rn(y.h, 2.3283064365386963e-10f));
+    const float t = __fsub_rn(y.h, __fmul_rn(k, 4294967296.0f));
+    const float ti = rintf(t);
+    const float r = __fadd_rn(__fsub_rn(t, ti), y.l);
+    return (unsigned int)__float2int_rn(ti) + (unsigned int)__float2int_rn(r);
+}
+
 // Minimum image by rounding (production kernels).
 __device__ __forceinline__ float minimg_f(float d, float L, float invL) { return d - L * rintf(d * invL); }
 __device__ __forceinline__ double minimg_d(double d, double L, double invL) { return d - L * rint(d * invL); }

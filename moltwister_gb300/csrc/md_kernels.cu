@@ -83,6 +83,37 @@ __device__ __forceinline__ int rep_of_atom(const DevSys& d, const Params& P, int
 __device__ __forceinline__ int rep_of_block(const DevSys& d, const Params& P) { return P.nrep ? d.blk_rep[blockIdx.x] : -1; }
 
 
+// Totals of one system's block partials (blocks b0 .. b0+nb-1, four doubles each), summed by the
+// whole last block: thread t adds blocks t, t + blockDim, ... in order, then the fixed shuffle
+// tree of block_sum.  Deterministic; thread 0 receives the totals.  (The reference-precision
+// kernels keep a single-thread sum in block order.)
+template<int NV>
+__device__ __forceinline__ void system_totals(const double* partial, int b0, int nb, double (&s)[NV], double* smem) {
+#pragma unroll
+    for(int q = 0; q < NV; q++) s[q] = 0.0;
+    for(int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+        for(int q = 0; q < NV; q++) s[q] += partial[(size_t)(b0 + b) * 4 + q];
+    block_sum<NV>(s, smem);
+}
+
+// Block sum of a double-float per thread: shuffle tree in double-float, then FP64 over the
+// warps by thread 0 (the only thread that receives the result).
+__device__ __forceinline__ double block_sum_df(DF v, double* smem) {
+    for(int o = 16; o > 0; o >>= 1) {
+        const DF w{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)};
+        v = df_add(v, w);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if(lane == 0) smem[warp] = df_val(v);
+    __syncthreads();
+    double t = 0.0;
+    if(threadIdx.x == 0)
+        for(int w = 0; w < nw; w++) t += smem[w];
+    __syncthreads();
+    return t;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Prologue: sum p^2/m, then the first thermostat half-step of the coming step.
 // ---------------------------------------------------------------------------------------------
@@ -92,7 +123,13 @@ __global__ void k_prologue(DevSys d, Params P) {
     const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
     double v[2] = {0.0, 0.0};   // sum p^2/m, sum F.r (NPT: G_eps of the first step, VelVerlet.cpp:60)
     if(k < sv.off + sv.n) {
-        const double px = d.p[3 * k], py = d.p[3 * k + 1], pz = d.p[3 * k + 2];
+        double px = d.p[3 * k], py = d.p[3 * k + 1], pz = d.p[3 * k + 2];
+        if(P.precision == MTG_PREC_MIXED) {   // mixed: the double-float mirrors are current
+            const float4 h = d.ph[k], l = d.pl[k];
+            px = (double)h.x + (double)l.x;
+            py = (double)h.y + (double)l.y;
+            pz = (double)h.z + (double)l.z;
+        }
         v[0] = (px * px + py * py + pz * pz) / d.m[k];
         if(P.ensemble == MTG_NPT)
             v[1] = d.F[3 * k] * d.r[3 * k] + d.F[3 * k + 1] * d.r[3 * k + 1] + d.F[3 * k + 2] * d.r[3 * k + 2];
@@ -104,14 +141,17 @@ __global__ void k_prologue(DevSys d, Params P) {
     }
     if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
         __shared__ double tot, tot_fr;
+        double s2[2] = {0.0, 0.0};
+        if(P.precision != MTG_PREC_REFERENCE) system_totals<2>(d.partial, sv.bbase, sv.nb, s2, smem);
         if(threadIdx.x == 0) {
-            double KE2 = 0.0, fr = 0.0;
-            for(int b = sv.bbase; b < sv.bbase + sv.nb; b++) {
-                KE2 += d.partial[b * 4];
-                fr += d.partial[b * 4 + 1];
+            if(P.precision == MTG_PREC_REFERENCE) {
+                for(int b = sv.bbase; b < sv.bbase + sv.nb; b++) {
+                    s2[0] += d.partial[b * 4];
+                    s2[1] += d.partial[b * 4 + 1];
+                }
             }
-            tot = KE2;
-            tot_fr = fr;
+            tot = s2[0];
+            tot_fr = s2[1];
             sv.sc->done_blocks = 0;
         }
         __syncthreads();
@@ -152,28 +192,24 @@ __device__ __forceinline__ void load_pos(const DevSys& d, int i, double& x, doub
     }
 }
 
-// 32-bit fraction of the box: round(x / L * 2^32) modulo 2^32.  The difference of two such
-// coordinates, read as a signed 32-bit integer, is the minimum-image separation in units of
-// L / 2^32, exact for any |dx| < L/2 (no cancellation at the periodic boundary).
-__device__ __forceinline__ unsigned int frac32(double x, double conv) {
-    return (unsigned int)(unsigned long long)__double2ll_rn(x * conv);
-}
+// Mixed mode also keeps each coordinate as a 32-bit fraction of the box, round(x / L * 2^32)
+// modulo 2^32 (frac32_df).  The difference of two such coordinates, read as a signed 32-bit
+// integer, is the minimum-image separation in units of L / 2^32, exact for any |dx| < L/2 (no
+// cancellation at the periodic boundary).
 
 __device__ __forceinline__ void store_pos(const DevSys& d, const double* conv, int i, double x, double y, double z,
                                           bool mixed) {
     if(mixed) {
-        const float hx = (float)x, hy = (float)y, hz = (float)z;
+        const DF X = df_of(x), Y = df_of(y), Z = df_of(z);
         float4 h = d.hi[i], l = d.lo[i];
-        h.x = hx; h.y = hy; h.z = hz;
-        l.x = (float)(x - double(hx));
-        l.y = (float)(y - double(hy));
-        l.z = (float)(z - double(hz));
+        h.x = X.h; h.y = Y.h; h.z = Z.h;
+        l.x = X.l; l.y = Y.l; l.z = Z.l;
         d.hi[i] = h;
         d.lo[i] = l;
         uint4 q = d.pq[i];
-        q.x = frac32(x, conv[0]);
-        q.y = frac32(y, conv[1]);
-        q.z = frac32(z, conv[2]);
+        q.x = frac32_df(X, df_of(conv[0]));
+        q.y = frac32_df(Y, df_of(conv[1]));
+        q.z = frac32_df(Z, df_of(conv[2]));
         d.pq[i] = q;
     } else {
         d.r[3 * i] = x;
@@ -256,6 +292,21 @@ __device__ __forceinline__ double wrap_coord(double x, double Lm) {
     return x;
 }
 
+// End-of-step scalar work of a system's last block (warps 0..2): thermostat and output record,
+// with the replica's size, temperature and box for a batch.
+__device__ __forceinline__ void step_end(const DevSys& d, const Params& P, const SysView& sv, const double* tot, bool output) {
+    if(P.nrep) {
+        Params Q = P;
+        Q.n = sv.n;
+        Q.kT = sv.kT;
+        for(int a = 0; a < 3; a++) Q.box[a] = sv.box[a];
+        end_of_step(Q, sv.sc, sv.th, sv.th_saved, tot[0], tot[2], tot[1], output, sv.rec);
+        if(threadIdx.x == 0 && sv.sc->timeout) d.sc->timeout = 1;
+    } else {
+        end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], output, d.rec);
+    }
+}
+
 template<bool MIXED, bool OUTPUT>
 __global__ void k_pkick2(DevSys d, Params P) {
     __shared__ double smem[32 * 3];
@@ -300,26 +351,160 @@ __global__ void k_pkick2(DevSys d, Params P) {
     }
     if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
         __shared__ double tot[3];
+        double s3[3];
+        system_totals<3>(d.partial, sv.bbase, sv.nb, s3, smem);
         if(threadIdx.x == 0) {
-            double s[3] = {0.0, 0.0, 0.0};
-            for(int b = sv.bbase; b < sv.bbase + sv.nb; b++)
-                for(int q = 0; q < 3; q++) s[q] += d.partial[b * 4 + q];
-            for(int q = 0; q < 3; q++) tot[q] = s[q];
+            for(int q = 0; q < 3; q++) tot[q] = s3[q];
             sv.sc->done_blocks = 0;
         }
         __syncthreads();
-        if(threadIdx.x < 96) {
-            if(P.nrep) {
-                Params Q = P;   // the replica's size, temperature and box
-                Q.n = sv.n;
-                Q.kT = sv.kT;
-                for(int a = 0; a < 3; a++) Q.box[a] = sv.box[a];
-                end_of_step(Q, sv.sc, sv.th, sv.th_saved, tot[0], tot[2], tot[1], OUTPUT, sv.rec);
-                if(threadIdx.x == 0 && sv.sc->timeout) d.sc->timeout = 1;
-            } else {
-                end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
+        if(threadIdx.x < 96) step_end(d, P, sv, tot, OUTPUT);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Mixed-precision integration in double-float arithmetic (no FP64 instruction per atom).
+// Per block, thread 0 turns the FP64 scalars into double-float constants.
+// ---------------------------------------------------------------------------------------------
+struct MixK {
+    DF S, dt, dt2, fcut;
+    DF conv[3], L[3];
+    float Lf[3], iLf[3], L2f[3];
+    float h2, fcutf;
+    long long fcut_q;
+};
+
+__device__ __forceinline__ void mix_consts(const SysView& v, const Params& P, MixK& K) {
+    K.S = df_of(v.sc->S);
+    K.dt = df_of(P.dt);
+    K.dt2 = df_of(P.dt / 2.0);
+    for(int a = 0; a < 3; a++) {
+        K.conv[a] = df_of(v.fconv[a]);
+        K.L[a] = df_of(v.box[a]);
+        K.Lf[a] = (float)v.box[a];
+        K.iLf[a] = (float)(1.0 / v.box[a]);
+        K.L2f[a] = (float)(0.5 * v.box[a]);
+    }
+    const float hs = 0.5f * v.skin;
+    K.h2 = hs * hs;
+    K.fcut = df_of(P.fcut);
+    K.fcutf = (float)P.fcut;
+    K.fcut_q = (long long)(P.fcut * kFixScale);
+}
+
+// p <- S p + dt/2 F, r <- r + dt p / m (VelVerlet.cpp:74-93 with the pending thermostat scale),
+// box fractions, and the half-skin displacement test against the positions of the last list build.
+__global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond) {
+    __shared__ MixK K;
+    const SysView v = sys_view(d, P, rep_of_block(d, P));
+    if(threadIdx.x == 0) mix_consts(v, P, K);
+    __syncthreads();
+    const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
+    if(k < v.off + v.n) {
+        const float4 h = d.hi[k], l = d.lo[k], ph = d.ph[k], pl = d.pl[k], rb = d.rb4[k];
+        const DF dtm = df_mul(K.dt, DF{ph.w, pl.w});
+        const long long fq[3] = {d.Fx[k], d.Fy[k], d.Fz[k]};
+        DF p[3] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}};
+        DF x[3] = {{h.x, l.x}, {h.y, l.y}, {h.z, l.z}};
+        const float rbv[3] = {rb.x, rb.y, rb.z};
+        unsigned int q[3];
+        float d2 = 0.0f;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            p[a] = df_add(df_mul(p[a], K.S), df_mul(df_fix(fq[a]), K.dt2));
+            x[a] = df_add(x[a], df_mul(p[a], dtm));
+            q[a] = frac32_df(x[a], K.conv[a]);
+            const float dd = minimg_f(__fsub_rn(x[a].h, rbv[a]) + x[a].l, K.Lf[a], K.iLf[a]);
+            d2 += dd * dd;
+        }
+        d.ph[k] = make_float4(p[0].h, p[1].h, p[2].h, ph.w);
+        d.pl[k] = make_float4(p[0].l, p[1].l, p[2].l, pl.w);
+        d.hi[k] = make_float4(x[0].h, x[1].h, x[2].h, h.w);
+        d.lo[k] = make_float4(x[0].l, x[1].l, x[2].l, l.w);
+        d.pq[k] = make_uint4(q[0], q[1], q[2], (unsigned int)__float_as_int(l.w));
+        if(d2 > K.h2) d.sc->rebuild = 1;
+    }
+    if(cond) {
+        // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
+        // graph's IF node that wraps the list build
+        if(last_block(&d.sc->done_blocks)) {
+            if(threadIdx.x == 0) {
+                d.sc->done_blocks = 0;
+                cudaGraphSetConditional(cond, d.sc->rebuild ? 1u : 0u);
             }
         }
+    }
+}
+
+// Second kick with force clipping (VelVerlet.cpp:87,96-122), wrap into [-L/2, L/2) (the box
+// fractions are periodic and stay as they are), sum p^2/m (and on output steps F.r and U), then
+// the end-of-step scalar work of the last block.
+template<bool OUTPUT>
+__global__ void k_mkick2(DevSys d, Params P) {
+    __shared__ MixK K;
+    __shared__ double smem[32 * 3];
+    const SysView sv = sys_view(d, P, rep_of_block(d, P));
+    if(threadIdx.x == 0) mix_consts(sv, P, K);
+    __syncthreads();
+    const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
+    DF ke{0.0f, 0.0f};
+    double v[3] = {0.0, 0.0, 0.0};
+    if(k < sv.off + sv.n) {
+        float4 h = d.hi[k], l = d.lo[k];
+        const float4 ph = d.ph[k], pl = d.pl[k];
+        long long fq[3] = {d.Fx[k], d.Fy[k], d.Fz[k]};
+        DF p[3] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}};
+        DF x[3] = {{h.x, l.x}, {h.y, l.y}, {h.z, l.z}};
+        DF p2{0.0f, 0.0f};
+        bool wrapped = false;
+        double fr = 0.0;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            DF f = df_fix(fq[a]);
+            if(P.clip && P.fcut > 0.0 && fabsf(f.h) > K.fcutf) {
+                const bool pos = f.h >= 0.0f;
+                f = pos ? K.fcut : df_neg(K.fcut);
+                const long long c = pos ? K.fcut_q : -K.fcut_q;
+                if(a == 0) d.Fx[k] = c; else if(a == 1) d.Fy[k] = c; else d.Fz[k] = c;
+            }
+            p[a] = df_add(p[a], df_mul(f, K.dt2));
+            if(x[a].h >= K.L2f[a] || x[a].h < -K.L2f[a]) {
+                const float m = floorf(__fmul_rn(__fadd_rn(x[a].h, K.L2f[a]), K.iLf[a]));
+                x[a] = df_add(x[a], df_mul_f(K.L[a], -m));
+                wrapped = true;
+            }
+            p2 = df_add(p2, df_mul(p[a], p[a]));
+            if(OUTPUT) fr += df_val(f) * df_val(x[a]);
+        }
+        d.ph[k] = make_float4(p[0].h, p[1].h, p[2].h, ph.w);
+        d.pl[k] = make_float4(p[0].l, p[1].l, p[2].l, pl.w);
+        if(wrapped) {
+            d.hi[k] = make_float4(x[0].h, x[1].h, x[2].h, h.w);
+            d.lo[k] = make_float4(x[0].l, x[1].l, x[2].l, l.w);
+        }
+        ke = df_mul(p2, DF{ph.w, pl.w});
+        if(OUTPUT) {
+            v[1] = fr;
+            v[2] = d.U[k];
+        }
+    }
+    const double ke_blk = block_sum_df(ke, smem);
+    if(OUTPUT) block_sum<3>(v, smem);
+    if(threadIdx.x == 0) {
+        d.partial[blockIdx.x * 4 + 0] = ke_blk;
+        d.partial[blockIdx.x * 4 + 1] = v[1];
+        d.partial[blockIdx.x * 4 + 2] = v[2];
+    }
+    if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
+        __shared__ double tot[3];
+        double s3[3];
+        system_totals<3>(d.partial, sv.bbase, sv.nb, s3, smem);
+        if(threadIdx.x == 0) {
+            for(int q = 0; q < 3; q++) tot[q] = s3[q];
+            sv.sc->done_blocks = 0;
+        }
+        __syncthreads();
+        if(threadIdx.x < 96) step_end(d, P, sv, tot, OUTPUT);
     }
 }
 
@@ -336,7 +521,7 @@ __global__ void k_pcell_assign(DevSys d, Params P) {
     d.r_build[3 * i] = x;
     d.r_build[3 * i + 1] = y;
     d.r_build[3 * i + 2] = z;
-    d.rb4[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    d.rb4[i] = make_float4((float)x, (float)y, (float)z, __int_as_float(d.type[i]));
     const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
     int ix = (int)floor((x + 0.5 * v.box[0]) * v.pnx / v.box[0]);
     int iy = (int)floor((y + 0.5 * v.box[1]) * v.pny / v.box[1]);
@@ -424,10 +609,19 @@ __global__ void k_vlist(DevSys d, Params P) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(i >= P.n) return;
     const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
-    const float rlist = fmaxf(v.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? v.rcoul : 0.0f) + v.skin;
+    const float rfull = fmaxf(v.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? v.rcoul : 0.0f);
     // FP32 distances: rounding (~1e-6 A) is far inside the skin margin
     const float4 ri = d.rb4[i];
-    const float rl2 = rlist * rlist;
+    const int ti = __float_as_int(ri.w);
+    // list radius of pair (ti, tj): its own short-range cutoff (at most rc), widened to rcoul when
+    // charges are on, plus the skin; a pair outside that radius cannot interact before the next
+    // rebuild, which comes once any atom has moved half the skin
+    const float rq = P.qon ? v.rcoul : 0.0f;
+    auto list_r2 = [&](int tj) -> float {
+        const float c = d.pair_cut[ti * P.T + tj];
+        const float r = (c < 0.0f) ? rfull : fmaxf(fminf(c, v.rc), rq);
+        return r > 0.0f ? (r + v.skin) * (r + v.skin) : -1.0f;
+    };
     const float Lx = (float)v.box[0], Ly = (float)v.box[1], Lz = (float)v.box[2];
     const float iLx = 1.0f / Lx, iLy = 1.0f / Ly, iLz = 1.0f / Lz;
     const int ci = d.pcell_of[i] - v.cbase;
@@ -453,7 +647,7 @@ __global__ void k_vlist(DevSys d, Params P) {
                             const float dx = minimg_f(ri.x - rj.x, Lx, iLx);
                             const float dy = minimg_f(ri.y - rj.y, Ly, iLy);
                             const float dz = minimg_f(ri.z - rj.z, Lz, iLz);
-                            if(dx * dx + dy * dy + dz * dz < rl2) {
+                            if(dx * dx + dy * dy + dz * dz < list_r2(__float_as_int(rj.w))) {
                                 const int cls = excl_class(d, i, j);
                                 if(P.scale[cls] != 0.0f) {
                                     take = true;
@@ -489,26 +683,32 @@ struct Acc {
     R x, y, z;
 };
 
-// Fixed-point accumulation of FP32 contributions (mixed mode) without the FP64 unit.
-// A contribution f becomes round(f * 2^26) exactly, split over two int32 accumulators:
-//   h += round(f * 2^4)                  (adding 1.5 * 2^23 rounds a float of magnitude < 2^22 to an
-//   l += round((f * 2^4 - h_i) * 2^22)    integer held in the low mantissa bits)
+// Fixed-point accumulation of FP32 contributions (mixed mode) without the FP64 unit (which also
+// executes 64-bit conversions, at a small fraction of the FP32 rate on this GPU).
+// A contribution f becomes round(f * 2^26) exactly, split over two int32 accumulators.  With
+// x = 16 f (|x| < 2^22) and M = 1.5 * 2^23:
+//   tx = x + M          rounds x to the integer grid (the sum lies in [2^23, 2^24), ulp 1)
+//   rx = x + (M - tx)   the remainder x - round(x), exact (|rx| <= 1/2)
+//   ty = rx * 2^22 + M  (one fused operation; the product is exact) rounds it to the 2^-22 grid
+//   h += bits(tx) - bits(M) = round(x),   l += bits(ty) - bits(M)
 // and the lane's total is h * 2^22 + l in units of 2^-26 kJ/(mol A).  Every step is exact in FP32,
 // so the fixed-point value of each contribution, and hence every sum of them, is independent of
-// the order of summation.  |f| is clamped to 2^18 (no physical pair force comes near it).
+// the order of summation and of zero contributions.  Callers pass x = 16 f with |f| clamped to
+// 2^18 (no physical pair force comes near it); the scale 16 folds into the force factor.
 struct Fix {
     int h, l;
 };
-__device__ __forceinline__ void fix_add(Fix& a, float f) {
-    const float M = 12582912.0f;                 // 1.5 * 2^23
-    const float x = __fmul_rn(f, 16.0f);
+__device__ __forceinline__ void fix_add16(Fix& a, float x) {
+    const float M = 12582912.0f;
     const float tx = __fadd_rn(x, M);
-    const float rx = __fsub_rn(x, __fsub_rn(tx, M));
+    const float rx = __fadd_rn(x, __fsub_rn(M, tx));
     a.h += __float_as_int(tx) - __float_as_int(M);
-    const float ty = __fadd_rn(__fmul_rn(rx, 4194304.0f), M);
+    const float ty = __fmaf_rn(rx, 4194304.0f, M);
     a.l += __float_as_int(ty) - __float_as_int(M);
 }
-__device__ __forceinline__ void fix_add_clamped(Fix& a, float f) { fix_add(a, fminf(fmaxf(f, -262143.0f), 262143.0f)); }
+__device__ __forceinline__ void fix_add_clamped(Fix& a, float f) {
+    fix_add16(a, __fmul_rn(fminf(fmaxf(f, -262143.0f), 262143.0f), 16.0f));
+}
 __device__ __forceinline__ long long fix_total(const Fix& a) { return ((long long)a.h << 22) + (long long)a.l; }
 
 // -dU/dr / r (= g) and U of the analytic pair terms for type pair `pair`; table kinds interpolate.
@@ -761,113 +961,146 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
     }
 }
 
-// One neighbour-list entry of atom i: force factor g (F_i += g * d) and pair energy u.
-// Per type pair, staged in shared memory by the force kernel: mode 0 = no term, 1 = one 12-6 LJ
-// term with coefficients (a, b), 2 = anything else (evaluated by pair_terms from global memory).
-struct PairCoef {
-    float a, b;       // 4 eps sigma^12, 4 eps alpha sigma^6
-    float rc2, us;    // own cutoff^2 (0: global), energy shift
-    float fs, pad0, pad1, pad2;   // force at the cutoff (force-shifted LJ)
-};
-constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
-
-template<bool MIXED, bool ENERGY, class R>
-__device__ __forceinline__ void pair_entry(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, R qi,
-                                           R rc2, R rq2, R irc, R kq, const PairCoef* pc, const int* pmode,
-                                           const float* qt, uint4 qi4, const float (&fs)[3], R& dx, R& dy, R& dz,
-                                           R& g, R& u) {
+// One neighbour-list entry of atom i (FP64 path): force factor g (F_i += g * d) and pair energy u.
+template<bool ENERGY>
+__device__ __forceinline__ void pair_entry_d(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, double qi,
+                                             double rc2, double rq2, double irc, double& dx, double& dy, double& dz,
+                                             double& g, double& u) {
     const int j = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
-    int tj;
-    if(MIXED) {
-        const uint4 qj4 = d.pq[j];
-        dx = (R)__int2float_rn((int)(qi4.x - qj4.x)) * (R)fs[0];
-        dy = (R)__int2float_rn((int)(qi4.y - qj4.y)) * (R)fs[1];
-        dz = (R)__int2float_rn((int)(qi4.z - qj4.z)) * (R)fs[2];
-        tj = (int)qj4.w;
-    } else {
-        rel<MIXED, R>(d, P, i, j, dx, dy, dz);
-        tj = d.type[j];
-    }
-    const R r2 = dx * dx + dy * dy + dz * dz;
-    R ir;
-    if(MIXED) ir = (R)rsqrtf((float)r2);
-    else ir = R(1) / sqrt(r2);
-    const R ir2 = ir * ir;
+    rel<false, double>(d, P, i, j, dx, dy, dz);
+    const int tj = d.type[j];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double ir = 1.0 / sqrt(r2);
+    const double ir2 = ir * ir;
     g = 0;
     u = 0;
-    if(r2 < rc2 && r2 >= R(1e-6)) {
-        const int pr = ti * P.T + tj;
-        if(MIXED && pc && pr < kSmemPairs) {
-            const int mode = pmode[pr];
-            if(mode == 1) {
-                const PairCoef c = pc[pr];
-                if(c.rc2 == 0.0f || (float)r2 < c.rc2) {
-                    const R ir6 = ir2 * ir2 * ir2;
-                    const R t12 = (R)c.a * ir6 * ir6, t6 = (R)c.b * ir6;
-                    g = (R(12) * t12 - R(6) * t6) * ir2 - (R)c.fs * ir;
-                    if(ENERGY) u = t12 - t6 - (R)c.us + r2 * ir * (R)c.fs;
-                }
-            } else if(mode == 2) {
-                pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
-            }
-        } else {
-            pair_terms<R>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
-        }
-    }
-    if(P.coulomb != MTG_COULOMB_ALLPAIRS && r2 < rq2) {
-        const R qj = MIXED ? (R)(qt ? qt[tj] : d.qf[j]) : (R)d.qd[j];
-        const R qq = kq * qi * qj;
+    if(r2 < rc2 && r2 >= 1e-6) pair_terms<double>(d, ti * P.T + tj, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
+    if(P.qon && r2 < rq2) {
+        const double qq = 1389.32 * qi * d.qd[j];
         if(P.coulomb == MTG_COULOMB_SHIFTED) {
             g += qq * (ir2 - irc * irc) * ir;
-            if(ENERGY) u += qq * (ir - irc + (r2 * ir - R(1) / irc) * irc * irc);
+            if(ENERGY) u += qq * (ir - irc + (r2 * ir - 1.0 / irc) * irc * irc);
         } else {
             g += qq * ir2 * ir;
             if(ENERGY) u += qq * ir;
         }
     }
     if(cls) {
-        const R sc = (R)P.scale[cls];
+        const double sc = (double)P.scale[cls];
         g *= sc;
         u *= sc;
     }
     if(!(ENERGY && j > i)) u = 0;
 }
 
+// Per type pair, staged in shared memory by the mixed force kernel: a single 12-6 LJ term
+// (a, b, fs) with own2 = its squared own cutoff (FLT_MAX: the global cutoff only); own2 = 0 for a
+// pair without short-range terms (the LJ arithmetic then runs on zero coefficients and is
+// discarded, which costs less than a divergent branch); own2 < 0 for anything else (evaluated by
+// pair_terms from global memory).
+struct PairCoef {
+    float a, b;       // 4 eps sigma^12, 4 eps alpha sigma^6
+    float own2;       // see above
+    float fs;         // force at the cutoff (force-shifted LJ), else 0
+};
+constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
+
+// One list entry of atom i in FP32 (mixed path), added to the fixed-point sums (fx, fy, fz, fu).
+// The cutoff tests select instead of branching: out-of-range entries, about a quarter of a list
+// with a skin, would otherwise split the warp.  g is clamped to gmax so that |g d| < 2^18.
+template<bool ENERGY>
+__device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, float qi,
+                                           float rc2, float rq2, float irc, float gmax, const PairCoef* pc,
+                                           const float* us, const float* qt, uint4 qi4, const float (&fs)[3],
+                                           Fix& fx, Fix& fy, Fix& fz, Fix& fu) {
+    const int j = (int)(ent & kIdxMask);
+    const int cls = (int)(ent >> kClassShift);
+    const uint4 qj4 = d.pq[j];
+    const float dx = __int2float_rn((int)(qi4.x - qj4.x)) * fs[0];
+    const float dy = __int2float_rn((int)(qi4.y - qj4.y)) * fs[1];
+    const float dz = __int2float_rn((int)(qi4.z - qj4.z)) * fs[2];
+    const int tj = (int)qj4.w;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float ir = rsqrtf(r2);
+    const float ir2 = ir * ir;
+    const bool live = r2 >= 1e-6f;
+    float g = 0.0f, u = 0.0f;
+    const int pr = ti * P.T + tj;
+    if(pc) {
+        const PairCoef c = pc[pr];
+        if(c.own2 < 0.0f) {
+            if(live && r2 < rc2) pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
+        } else {
+            const bool in = live && r2 < fminf(rc2, c.own2);
+            const float ir6 = ir2 * ir2 * ir2;
+            const float t12 = c.a * ir6 * ir6, t6 = c.b * ir6;
+            const float gl = (12.0f * t12 - 6.0f * t6) * ir2 - c.fs * ir;
+            g = in ? gl : 0.0f;
+            if(ENERGY) u = in ? t12 - t6 - us[pr] + r2 * ir * c.fs : 0.0f;
+        }
+    } else if(live && r2 < rc2) {
+        pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
+    }
+    if(P.qon) {
+        const float qq = kCoulombKf * qi * (qt ? qt[tj] : d.qf[j]);
+        const bool inq = live && r2 < rq2;
+        float gq, uq = 0.0f;
+        if(P.coulomb == MTG_COULOMB_SHIFTED) {
+            gq = qq * (ir2 - irc * irc) * ir;
+            if(ENERGY) uq = qq * (ir - irc + (r2 * ir - 1.0f / irc) * irc * irc);
+        } else {
+            gq = qq * ir2 * ir;
+            if(ENERGY) uq = qq * ir;
+        }
+        g += inq ? gq : 0.0f;
+        if(ENERGY) u += inq ? uq : 0.0f;
+    }
+    if(cls) {
+        const float sc = P.scale[cls];
+        g *= sc;
+        u *= sc;
+    }
+    const float g16 = __fmul_rn(fminf(fmaxf(g, -gmax), gmax), 16.0f);
+    fix_add16(fx, __fmul_rn(g16, dx));
+    fix_add16(fy, __fmul_rn(g16, dy));
+    fix_add16(fz, __fmul_rn(g16, dz));
+    if(ENERGY && j > i) fix_add_clamped(fu, u);
+}
+
 // Force gather: TEAM lanes per atom (8, 16 or 32; chosen per system by the autotuner), each lane
 // walking its share of the atom's neighbour-list row four entries at a time so that four gathers
-// are in flight per lane.  Bonded terms of the atom are spread over the team's lanes.
+// are in flight per lane.  Bonded terms of the atom are spread over the team's lanes.  Mixed:
+// every contribution is rounded to the 2^-26 fixed-point grid and summed as an integer, so
+// forces do not depend on the team size, on the list order or on out-of-range list entries.
 template<bool MIXED, bool ENERGY, int TEAM>
 __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     using R = typename std::conditional<MIXED, float, double>::type;
     __shared__ PairCoef pc_s[kSmemPairs];
-    __shared__ int pm_s[kSmemPairs];   // 0 no term, 1 one 12-6 LJ term (pc_s), 2 general (pair_terms)
+    __shared__ float us_s[kSmemPairs];   // energy shift of the staged LJ term
     __shared__ float qt_s[8];            // per-type charges (when charges are a function of type)
     const PairCoef* pc = nullptr;
-    const int* pmode = nullptr;
     const float* qt = nullptr;
     if(MIXED && P.T * P.T <= kSmemPairs) {
         for(int q = threadIdx.x; q < P.T * P.T; q += blockDim.x) {
-            PairCoef c{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-            int mode = 0;
+            PairCoef c{0.0f, 0.0f, 0.0f, 0.0f};
+            float us = 0.0f;
             const int cnt = d.nb_cnt[q];
             if(cnt == 1 && d.nb_kind[q * kMaxFF] == MTG_NB_LJ) {
-                mode = 1;
                 const float4 f = reinterpret_cast<const float4*>(d.nb_parf)[q * kMaxFF];
-                c = PairCoef{f.x, f.y, f.z, f.w, P.lj_shift == 2 ? d.nb_fsf[q * kMaxFF] : 0.0f, 0.0f, 0.0f, 0.0f};
+                c = PairCoef{f.x, f.y, f.z > 0.0f ? f.z : FLT_MAX, P.lj_shift == 2 ? d.nb_fsf[q * kMaxFF] : 0.0f};
+                us = f.w;
             } else if(cnt > 0) {
-                mode = 2;
+                c.own2 = -1.0f;
             }
             pc_s[q] = c;
-            pm_s[q] = mode;
+            us_s[q] = us;
         }
         if(P.qtype && threadIdx.x < P.T) qt_s[threadIdx.x] = d.qtype[threadIdx.x];
         __syncthreads();
         pc = pc_s;
-        pmode = pm_s;
         if(P.qtype) qt = qt_s;
     }
-    const R gmax = R(262143.0) / ((R)P.rc + (R)P.rcoul + (R)P.skin);   // keeps |g d| < 2^18
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = gt / TEAM, lane = gt % TEAM;
     const bool active = i < P.n;
@@ -879,46 +1112,46 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         const R rc2 = (R)v.rc * (R)v.rc;
         const R rq2 = (R)v.rcoul * (R)v.rcoul;
         const R irc = R(1) / (R)v.rcoul;
-        const float fs[3] = {v.fscale[0], v.fscale[1], v.fscale[2]};
-        const uint4 qi4 = MIXED ? d.pq[i] : make_uint4(0, 0, 0, 0);
-        const int ti = MIXED ? (int)qi4.w : d.type[i];
-        const R qi = MIXED ? (R)d.qf[i] : (R)d.qd[i];
-        const R kq = MIXED ? (R)kCoulombKf : (R)1389.32;
         const int cnt = min(d.vcount[i], d.vmax);   // an overflowed build is redone; stay in the row
         const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
-        int e = lane;
-        for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
-            uint32_t ent[4];
+        if constexpr(MIXED) {
+            const float fs[3] = {v.fscale[0], v.fscale[1], v.fscale[2]};
+            const float gmax = 262143.0f / (v.rc + v.rcoul + v.skin);   // |d| < rc + rcoul + skin
+            const uint4 qi4 = d.pq[i];
+            const int ti = (int)qi4.w;
+            const float qi = d.qf[i];
+            int e = lane;
+            for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
+                uint32_t ent[4];
 #pragma unroll
-            for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
+                for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
 #pragma unroll
-            for(int q = 0; q < 4; q++) {
-                R dx, dy, dz, g, u;
-                pair_entry<MIXED, ENERGY, R>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, fs, dx, dy, dz, g, u);
-                if(MIXED) {
-                    g = fminf(fmaxf(g, -gmax), gmax);
-                    fix_add(fx, (float)(g * dx));
-                    fix_add(fy, (float)(g * dy));
-                    fix_add(fz, (float)(g * dz));
-                    if(ENERGY) fix_add_clamped(fu, (float)u);
-                } else {
-                    bx += (double)(g * dx); by += (double)(g * dy); bz += (double)(g * dz);
-                    if(ENERGY) bu += (double)u;
+                for(int q = 0; q < 4; q++)
+                    pair_mixed<ENERGY>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
+            }
+            for(; e < cnt; e += TEAM)
+                pair_mixed<ENERGY>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
+        } else {
+            const int ti = d.type[i];
+            const double qi = d.qd[i];
+            int e = lane;
+            for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
+                uint32_t ent[4];
+#pragma unroll
+                for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
+#pragma unroll
+                for(int q = 0; q < 4; q++) {
+                    double dx, dy, dz, g, u;
+                    pair_entry_d<ENERGY>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
+                    bx += g * dx; by += g * dy; bz += g * dz;
+                    if(ENERGY) bu += u;
                 }
             }
-        }
-        for(; e < cnt; e += TEAM) {
-            R dx, dy, dz, g, u;
-            pair_entry<MIXED, ENERGY, R>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, kq, pc, pmode, qt, qi4, fs, dx, dy, dz, g, u);
-            if(MIXED) {
-                g = fminf(fmaxf(g, -gmax), gmax);
-                fix_add(fx, (float)(g * dx));
-                fix_add(fy, (float)(g * dy));
-                fix_add(fz, (float)(g * dz));
-                if(ENERGY) fix_add_clamped(fu, (float)u);
-            } else {
-                bx += (double)(g * dx); by += (double)(g * dy); bz += (double)(g * dz);
-                if(ENERGY) bu += (double)u;
+            for(; e < cnt; e += TEAM) {
+                double dx, dy, dz, g, u;
+                pair_entry_d<ENERGY>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
+                bx += g * dx; by += g * dy; bz += g * dz;
+                if(ENERGY) bu += u;
             }
         }
         // bonded terms of atom i, one entry per lane
@@ -969,27 +1202,32 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
 }
 
 // Conversions between the mixed-mode position/force formats and the FP64 host-facing arrays.
-__global__ void k_sync_pos(DevSys d, Params P, int to_master) {
+// Master FP64 arrays <-> mixed-mode mirrors (SyncMode).  From the masters the box fractions are
+// computed by frac32_df, the same function the drift uses, so a round trip leaves them unchanged.
+__global__ void k_sync(DevSys d, Params P, int mode) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= P.n) return;
-    if(to_master) {
-        // d.r -> hi/lo (set_state)
-        uint4 q = d.pq[i];
-        q.w = (unsigned int)d.type[i];
-        d.pq[i] = q;
-        const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
-        store_pos(d, v.fconv, i, d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2], true);
-        float4 h = d.hi[i], l = d.lo[i];
-        h.w = d.qf[i];
-        l.w = __int_as_float(d.type[i]);
-        d.hi[i] = h;
-        d.lo[i] = l;
-    } else {
-        double x, y, z;
-        load_pos(d, i, x, y, z, true);
-        d.r[3 * i] = x;
-        d.r[3 * i + 1] = y;
-        d.r[3 * i + 2] = z;
+    if(mode == kSyncToMaster) {
+        const float4 h = d.hi[i], l = d.lo[i], ph = d.ph[i], pl = d.pl[i];
+        d.r[3 * i] = (double)h.x + (double)l.x;
+        d.r[3 * i + 1] = (double)h.y + (double)l.y;
+        d.r[3 * i + 2] = (double)h.z + (double)l.z;
+        d.p[3 * i] = (double)ph.x + (double)pl.x;
+        d.p[3 * i + 1] = (double)ph.y + (double)pl.y;
+        d.p[3 * i + 2] = (double)ph.z + (double)pl.z;
+        return;
+    }
+    const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
+    const DF x = df_of(d.r[3 * i]), y = df_of(d.r[3 * i + 1]), z = df_of(d.r[3 * i + 2]);
+    d.hi[i] = make_float4(x.h, y.h, z.h, d.qf[i]);
+    d.lo[i] = make_float4(x.l, y.l, z.l, __int_as_float(d.type[i]));
+    d.pq[i] = make_uint4(frac32_df(x, df_of(v.fconv[0])), frac32_df(y, df_of(v.fconv[1])), frac32_df(z, df_of(v.fconv[2])),
+                         (unsigned int)d.type[i]);
+    if(mode == kSyncFromMaster) {
+        const DF px = df_of(d.p[3 * i]), py = df_of(d.p[3 * i + 1]), pz = df_of(d.p[3 * i + 2]);
+        const DF im = df_of(1.0 / d.m[i]);
+        d.ph[i] = make_float4(px.h, py.h, pz.h, im.h);
+        d.pl[i] = make_float4(px.l, py.l, pz.l, im.l);
     }
 }
 
@@ -1020,11 +1258,18 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
         double f[3], r[3];
         load_force(d, k, f[0], f[1], f[2], mixed);
         load_pos(d, k, r[0], r[1], r[2], mixed);
+        double pk[3] = {d.p[3 * k], d.p[3 * k + 1], d.p[3 * k + 2]};
+        if(mixed) {   // the double-float mirrors are current
+            const float4 h = d.ph[k], l = d.pl[k];
+            pk[0] = (double)h.x + (double)l.x;
+            pk[1] = (double)h.y + (double)l.y;
+            pk[2] = (double)h.z + (double)l.z;
+        }
         double fr = 0.0, p2 = 0.0;
         for(int a = 0; a < 3; a++) {
             r[a] = r[a] + f[a] * lr;
             fr += f[a] * r[a];
-            p2 += d.p[3 * k + a] * d.p[3 * k + a];
+            p2 += pk[a] * pk[a];
         }
         store_pos(d, P.fconv, k, r[0], r[1], r[2], mixed);
         if(mode != MTG_PREC_REFERENCE) {
@@ -1075,7 +1320,7 @@ void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
 
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {
     const int nb = integration_blocks(P);
-    if(P.precision == MTG_PREC_MIXED) k_pkick_drift<true><<<nb, 256, 0, s>>>(d, P, cond);
+    if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
     else k_pkick_drift<false><<<nb, 256, 0, s>>>(d, P, cond);
 }
 
@@ -1116,16 +1361,16 @@ void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream
 void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
     const int nb = integration_blocks(P);
     if(P.precision == MTG_PREC_MIXED) {
-        if(output) k_pkick2<true, true><<<nb, 256, 0, s>>>(d, P);
-        else k_pkick2<true, false><<<nb, 256, 0, s>>>(d, P);
+        if(output) k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
+        else k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
     } else {
         if(output) k_pkick2<false, true><<<nb, 256, 0, s>>>(d, P);
         else k_pkick2<false, false><<<nb, 256, 0, s>>>(d, P);
     }
 }
 
-void launch_prod_sync_positions(const DevSys& d, const Params& P, bool to_master, cudaStream_t s) {
-    k_sync_pos<<<nblk(P.n, 256), 256, 0, s>>>(d, P, to_master ? 1 : 0);
+void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s) {
+    k_sync<<<nblk(P.n, 256), 256, 0, s>>>(d, P, (int)mode);
 }
 
 void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s) {

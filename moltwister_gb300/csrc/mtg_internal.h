@@ -102,6 +102,7 @@ struct Params {
     float fscale[3];      // L / 2^32: fixed-point position unit per axis (mixed)
     double fconv[3];      // 2^32 / L
     int qtype;            // 1: charges are a function of the type (qtype table)
+    int qon;              // 1: cutoff Coulomb with some charge nonzero (production); 0: no Coulomb work
     int lj_shift;         // 0 truncated LJ, 1 energy shifted at the cutoff, 2 force shifted
     int nrep;             // 0: one system; > 0: a batch of nrep replicas (RepDev table)
     int ncell_total;      // batch: production cells of all replicas
@@ -140,6 +141,9 @@ struct DevSys {
     const float* nb_parf;     // [pair*5+ff][4] (FP32 copy)
     const double* nb_fs;      // [pair*5+ff] force at the LJ cutoff (force-shifted LJ), else 0
     const float* nb_fsf;
+    // production list radius per type pair, before the skin: 0 no short-range term, FLT_MAX the
+    // global cutoff, > 0 the pair's own LJ cutoff, < 0 the full list radius max(rc, rcoul)
+    const float* pair_cut;
     const int* bond_kind;
     const double* bond_par;   // [type][4]; angles hold (k, theta0 [rad], toRad, 0)
     const float* bond_parf;   // FP32 copies for the mixed kernels
@@ -177,6 +181,8 @@ struct DevSys {
     float4* hi;           // [n] x,y,z hi, charge
     float4* lo;           // [n] x,y,z lo, type bits
     uint4* pq;            // [n] x,y,z as 32-bit fractions of the box (wrap = minimum image), type
+    float4* ph;           // [n] mixed: momenta x,y,z hi, 1/m hi (double-float pairs with pl)
+    float4* pl;           // [n] mixed: momenta x,y,z lo, 1/m lo
     const float* qtype;   // [T] charge of each type when every atom of a type has the same charge
     long long* Fx;        // [n] fixed-point forces (SoA)
     long long* Fy;
@@ -225,7 +231,10 @@ void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cu
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s);
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s);
 void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s);
-void launch_prod_sync_positions(const DevSys& d, const Params& P, bool to_master, cudaStream_t s);
+// Mixed mode keeps positions and momenta as double-float pairs (hi/lo, ph/pl) plus the box
+// fractions pq; the FP64 arrays r and p are the masters the host reads and writes.
+enum SyncMode { kSyncToMaster = 0, kSyncFromMaster = 1, kSyncPositionsFromMaster = 2 };
+void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s);
 void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s);
 void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s);
 int reduction_blocks(int n);

@@ -213,22 +213,28 @@ def test_kob_andersen_per_pair_cutoffs(prec):
     assert abs(U.sum() - Uo.sum()) < (1e-9 if prec == "fp64" else 1e-5) * abs(Uo.sum())
 
 
-def test_mixed_nve_conserves_energy():
-    """NVE in mixed precision on a 2,048-atom Kob-Andersen mixture: the total energy's linear
-    drift over 4,000 steps (2 ps) stays below 1e-2 kT per atom per ns (the benchmark measures the
-    1e-4 target on 10^6 atoms over 20,000 steps)."""
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_nve_conserves_energy(prec):
+    """NVE on a 16,384-atom Kob-Andersen mixture (energies shifted at the cutoffs, as in the
+    benchmark): the linear drift of the total energy over 8,000 steps (4 ps) stays below 2e-2 kT
+    per atom per ns in FP64 and in mixed precision (double-float integration, FP32 pair forces).
+    The fitted slope of so short a window carries the velocity-Verlet energy fluctuation as noise,
+    about 2.5e-3 kT per atom per ns here (it scales as N^-1/2 and window^-3/2), so the bound
+    catches a broken integrator, not the 1e-4 target, which the Kob-Andersen benchmark measures
+    on 10^6 atoms over a long window with its standard error."""
     from moltwister_gb300 import workloads as W
-    s, cfg = W.kob_andersen(ncell=8, seed=6)
+    s, cfg = W.kob_andersen(ncell=16, seed=6)
+    cfg.precision = prec
     e = engine(s, cfg)
     e.optimize(200)
-    e.run(2000)                                        # equilibrate the relaxed lattice start
-    recs = e.run(4000, out_stride=100)
+    e.run(1000)                                        # equilibrate the relaxed lattice start
+    recs = e.run(8000, out_stride=100)
     t_ns = np.array([r.step for r in recs], float) * cfg.timestep * 1e-6
     E = np.array([r.U + r.K for r in recs])
     kT = cfg.temperature / 120.272
     slope = np.polyfit(t_ns, E, 1)[0]
     drift = abs(slope) / (s.n * kT)
-    assert drift < 1e-2, drift
+    assert drift < 2e-2, drift
 
 
 def test_production_chain_stays_finite_on_large_systems():
