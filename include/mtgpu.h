@@ -323,7 +323,7 @@ int mtg_loss_grad(mtg_ctx* ctx, const mtg_loss_desc* loss_desc, int32_t nparams,
  * across the periodic box, pairs closer than ignore_below skipped (the command's `ignoredistbelow`,
  * -1 for none), bin int((R - rmin) / (rmax - rmin) * nbins).  The counts are added to profile[nbins]
  * so that successive calls accumulate frames; the command's normalisation to g(r) is a host step
- * (moltwister_gb300.analysis.pair_correlation).  nbins <= 8192. */
+ * (moltwister_gb300.analysis.PairCorrelation).  nbins <= 8192. */
 int mtg_pair_histogram(mtg_ctx* ctx, int32_t type_a, int32_t type_b, int32_t nbins, double rmin, double rmax,
                        double ignore_below, int64_t* profile);
 
