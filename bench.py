@@ -37,7 +37,7 @@ CHUNK = 100
 SIGMA_O, EPS_O = 3.166, 0.650
 # DRAM bytes (read + write) of one k_pforce launch on this workload, from the ncu capture
 # summarised in profiles/k_pforce_water9000_mixed.md (cold L2: ncu flushes caches per pass)
-FORCE_DRAM_BYTES_PER_LAUNCH = 21.36e6
+FORCE_DRAM_BYTES_PER_LAUNCH = 21.25e6
 
 
 def make_system(precision: str = "mixed"):
@@ -265,8 +265,8 @@ def our_arm(args):
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "fp32+int64", "data": "synthetic",
            "config": {"workload": WORKLOAD, "atoms": n, "molecules": n // 3, "box_A": 44.8, "dt_fs": 0.5,
-                      "precision": "mixed (FP32 pair/bonded arithmetic, int64 fixed-point forces, FP64 positions/"
-                                   "thermostat/reductions)",
+                      "precision": "mixed (FP32 pair/bonded arithmetic, int64 fixed-point forces, double-float "
+                                   "positions and momenta, FP64 thermostat and block sums)",
                       "coulomb": "shifted-force cutoff 10 A (new option; the reference is all-pairs)",
                       "lj_cutoff_A": 10.0, "prep": "400 gradient-descent steps (lr 2e-5), untimed",
                       "list_skin_A": cfg.listskin, "ensemble": "NVT Nose-Hoover M=4 RESPA 4",

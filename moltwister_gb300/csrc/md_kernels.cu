@@ -233,11 +233,9 @@ __device__ __forceinline__ void load_force(const DevSys& d, int i, double& fx, d
 // ---------------------------------------------------------------------------------------------
 // Integration
 // ---------------------------------------------------------------------------------------------
-template<bool MIXED>
 __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, const SysView& v, int k);
 
-// One 256-atom block per launch block; a batch maps blocks to replicas (blk_rep).
-template<bool MIXED>
+// FP64 mode.  One 256-atom block per launch block; a batch maps blocks to replicas (blk_rep).
 __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond) {
     const SysView v = sys_view(d, P, rep_of_block(d, P));
     const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
@@ -245,7 +243,7 @@ __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
     if(cond) {
         // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
         // graph's IF node that wraps the list build
-        if(mine) kick_drift_atom<MIXED>(d, P, v, k);
+        if(mine) kick_drift_atom(d, P, v, k);
         if(last_block(&d.sc->done_blocks)) {
             if(threadIdx.x == 0) {
                 d.sc->done_blocks = 0;
@@ -255,17 +253,16 @@ __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
         return;
     }
     if(!mine) return;
-    kick_drift_atom<MIXED>(d, P, v, k);
+    kick_drift_atom(d, P, v, k);
 }
 
-template<bool MIXED>
 __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, const SysView& v, int k) {
     const double S = v.sc->S;
     const double dt_2 = P.dt / 2.0;
     const double dm = P.dt / d.m[k];
     double fx, fy, fz, x, y, z;
-    load_force(d, k, fx, fy, fz, MIXED);
-    load_pos(d, k, x, y, z, MIXED);
+    load_force(d, k, fx, fy, fz, false);
+    load_pos(d, k, x, y, z, false);
     double px = d.p[3 * k] * S + fx * dt_2;
     double py = d.p[3 * k + 1] * S + fy * dt_2;
     double pz = d.p[3 * k + 2] * S + fz * dt_2;
@@ -275,11 +272,12 @@ __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, cons
     x += px * dm;
     y += py * dm;
     z += pz * dm;
-    store_pos(d, v.fconv, k, x, y, z, MIXED);
-    // displacement since the last list build (minimum image: wrapping is not a displacement)
-    const double bx = minimg_d(x - d.r_build[3 * k], v.box[0], 1.0 / v.box[0]);
-    const double by = minimg_d(y - d.r_build[3 * k + 1], v.box[1], 1.0 / v.box[1]);
-    const double bz = minimg_d(z - d.r_build[3 * k + 2], v.box[2], 1.0 / v.box[2]);
+    store_pos(d, v.fconv, k, x, y, z, false);
+    // displacement since the last list build (minimum image: wrapping is not a displacement);
+    // fconv 2^-32 = 1/L rounded, without a division
+    const double bx = minimg_d(x - d.r_build[3 * k], v.box[0], v.fconv[0] * 0x1p-32);
+    const double by = minimg_d(y - d.r_build[3 * k + 1], v.box[1], v.fconv[1] * 0x1p-32);
+    const double bz = minimg_d(z - d.r_build[3 * k + 2], v.box[2], v.fconv[2] * 0x1p-32);
     const double h = 0.5 * double(v.skin);
     if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
 }
@@ -307,7 +305,8 @@ __device__ __forceinline__ void step_end(const DevSys& d, const Params& P, const
     }
 }
 
-template<bool MIXED, bool OUTPUT>
+// FP64 mode: second kick, clipping, pbcWrap, sums, end-of-step work.
+template<bool OUTPUT>
 __global__ void k_pkick2(DevSys d, Params P) {
     __shared__ double smem[32 * 3];
     const SysView sv = sys_view(d, P, rep_of_block(d, P));
@@ -316,19 +315,14 @@ __global__ void k_pkick2(DevSys d, Params P) {
     if(k < sv.off + sv.n) {
         const double dt_2 = P.dt / 2.0;
         double f[3], r[3];
-        load_force(d, k, f[0], f[1], f[2], MIXED);
-        load_pos(d, k, r[0], r[1], r[2], MIXED);
+        load_force(d, k, f[0], f[1], f[2], false);
+        load_pos(d, k, r[0], r[1], r[2], false);
         double p2 = 0.0, fr = 0.0;
 #pragma unroll
         for(int a = 0; a < 3; a++) {
             if(P.clip && P.fcut > 0.0 && fabs(f[a]) > P.fcut) {
                 f[a] = ((f[a] >= 0.0) ? 1.0 : -1.0) * P.fcut;
-                if(MIXED) {
-                    long long q = (long long)(f[a] * kFixScale);
-                    if(a == 0) d.Fx[k] = q; else if(a == 1) d.Fy[k] = q; else d.Fz[k] = q;
-                } else {
-                    d.F[3 * k + a] = f[a];
-                }
+                d.F[3 * k + a] = f[a];
             }
             const double p = d.p[3 * k + a] + f[a] * dt_2;
             d.p[3 * k + a] = p;
@@ -336,7 +330,7 @@ __global__ void k_pkick2(DevSys d, Params P) {
             p2 += p * p;
             fr += f[a] * r[a];
         }
-        store_pos(d, sv.fconv, k, r[0], r[1], r[2], MIXED);
+        store_pos(d, sv.fconv, k, r[0], r[1], r[2], false);
         v[0] = p2 / d.m[k];
         if(OUTPUT) {
             v[1] = fr;
@@ -1321,7 +1315,7 @@ void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {
     const int nb = integration_blocks(P);
     if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
-    else k_pkick_drift<false><<<nb, 256, 0, s>>>(d, P, cond);
+    else k_pkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
 }
 
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
@@ -1364,8 +1358,8 @@ void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream
         if(output) k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
         else k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
     } else {
-        if(output) k_pkick2<false, true><<<nb, 256, 0, s>>>(d, P);
-        else k_pkick2<false, false><<<nb, 256, 0, s>>>(d, P);
+        if(output) k_pkick2<true><<<nb, 256, 0, s>>>(d, P);
+        else k_pkick2<false><<<nb, 256, 0, s>>>(d, P);
     }
 }
 
