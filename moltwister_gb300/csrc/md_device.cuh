@@ -11,10 +11,13 @@ namespace mtg {
 // exp(x) for the thermostat.  Small arguments, which are the normal case (|x| = Dt/8 p_eta/Q is of
 // order 1e-2), use the Taylor series of e^x with the remainder below 1e-17 relative (degree 8 for
 // |x| <= 2^-5, degree 11 for |x| <= 2^-3); larger ones call exp().  On this GPU every FP64
-// instruction costs about as much as thirty FP32 ones, so the instruction count is what matters.
+// instruction costs about as much as thirty FP32 ones and the SM's FP64 unit is shared by the
+// chain's warps, so the instruction count is what matters: Horner's scheme (one FMA per degree;
+// Estrin's shorter dependency chain needs more instructions and measured slower), and the range
+// tests compare bit patterns on the integer units.
 __device__ __forceinline__ double nh_exp(double x) {
-    const double ax = fabs(x);
-    if(ax <= 0.03125) {
+    const long long ax = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+    if(ax <= 0x3fa0000000000000LL) {            // |x| <= 2^-5
         double p = 1.0 / 40320.0;
         p = fma(p, x, 1.0 / 5040.0);
         p = fma(p, x, 1.0 / 720.0);
@@ -25,7 +28,7 @@ __device__ __forceinline__ double nh_exp(double x) {
         p = fma(p, x, 1.0);
         return fma(p, x, 1.0);
     }
-    if(ax <= 0.125) {
+    if(ax <= 0x3fc0000000000000LL) {            // |x| <= 2^-3
         double p = 1.0 / 39916800.0;
         p = fma(p, x, 1.0 / 3628800.0);
         p = fma(p, x, 1.0 / 362880.0);
@@ -254,7 +257,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                 if(j == lane) E = d2 * iQ[j];
             for(int it = 0; it < nresp; it++, s++) {
                 double etop = 0.0;
-                double c12[CAP], x12[CAP];
+                double c12[CAP], x12[CAP], t12[CAP];
                 // 1.2
 #pragma unroll
                 for(int j = 0; j < top; j++) {
@@ -274,6 +277,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                     c12[j] = c;
                     x12[j] = x;
                     const double t = (j == 0) ? fma(KE2, d4, -B0) : fma(pe[j - 1] * pe[j - 1], A[j], -B);
+                    t12[j] = t;
                     pe[j] = fma(pe[j], c, t) * c;
                     if(j == 0) {
                         if(lane == 0) X.pe0 = pe[0];
@@ -311,7 +315,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                         KE2 = X.ke;
                         t = fma(KE2, d4, -B0);
                     } else {
-                        t = fma(pe[j - 1] * pe[j - 1], A[j], -B);
+                        t = t12[j];   // p_eta[j-1] is as step 1.2 left it: the same driving term
                     }
                     pe[j] = fma(pe[j], c, t) * c;
                     if(j == top - 1) {

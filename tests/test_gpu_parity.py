@@ -151,6 +151,61 @@ def test_mixed_mode_bit_reproducible():
     assert np.array_equal(r1, r2) and np.array_equal(p1, p2)
 
 
+def test_mixed_state_round_trip():
+    """Mixed mode keeps positions and momenta as double-float pairs and box fractions on the
+    device; the host reads and writes FP64.  Reading the state changes nothing (50 + read + 50
+    steps is bit-identical to 100 steps), and writing it back changes it by at most the FP64
+    rounding of a double-float whose low part lies more than 53 bits below its high part: NVE,
+    the state read and written back after 50 steps, then 50 more steps within 1e-10 of the
+    straight run (the difference of ~1e-16 grows with the dynamics' divergence)."""
+    from moltwister_gb300 import workloads as W
+    s, cfg = W.kob_andersen(ncell=6, seed=9)
+    e1 = engine(s, cfg)
+    e1.run(100)
+    r1, p1, _ = e1.get_state()
+    e3 = engine(s, cfg)
+    e3.run(50)
+    e3.get_state()
+    e3.run(50)
+    r3, p3, _ = e3.get_state()
+    assert np.array_equal(r1, r3) and np.array_equal(p1, p3)
+    e2 = engine(s, cfg)
+    e2.run(50)
+    r, p, _ = e2.get_state()
+    e2.set_state(r=r, p=p)
+    r0, p0, _ = e2.get_state()
+    assert np.array_equal(r, r0) and np.array_equal(p, p0)
+    e2.run(50)
+    r2, p2, _ = e2.get_state()
+    assert np.abs(r1 - r2).max() < 1e-10 * np.abs(r1).max()
+    assert np.abs(p1 - p2).max() < 1e-10 * np.abs(p1).max()
+
+
+def test_mixed_integrator_tracks_fp64_on_a_regular_orbit():
+    """Two bonded atoms (harmonic bond, no other interaction) oscillate on a regular orbit, so
+    trajectories do not diverge: after 4,000 NVE steps (77 periods) the double-float integrator
+    with FP32 forces agrees with the FP64 path to 2e-5 in positions (A) and momenta (relative to
+    their amplitude).  The FP32 force's relative error of ~1e-7 shifts the frequency by as much,
+    a phase error of ~5e-5 rad after 77 periods on a 0.15 A amplitude; an integrator error
+    (a wrong factor in a kick or the drift) would show at the 1e-2 level."""
+    from moltwister_gb300.system import BondTerm, MDConfig, MDSystem
+    r = np.array([[0.0, 0.0, 0.0], [1.15, 0.1, -0.05]])
+    s = MDSystem(box=np.array([20.0, 20.0, 20.0]), ids=["A", "B"], r=r, q=np.zeros(2), m=np.array([12.0, 16.0]),
+                 mobile=np.ones(2, bool), bond_terms=[BondTerm("A", "B", "Harm", (2000.0, 1.0))],
+                 bonds=np.array([[0, 1, 0]], np.int32))
+    s.p = np.array([[0.5, -0.2, 0.1], [-0.5, 0.2, -0.1]])
+    out = {}
+    for prec in ("fp64", "mixed"):
+        cfg = MDConfig(timestep=0.5, ensemble="NVE", cutoffradius=5.0, neighshell=0.5, listskin=0.5,
+                       precision=prec, coulomb="cutoff", coulombcutoff=5.0, clipforces=False)
+        e = engine(s, cfg)
+        e.run(4000)
+        out[prec] = e.get_state()[:2]
+    (r64, p64), (rm, pm) = out["fp64"], out["mixed"]
+    assert np.abs(rm - r64).max() < 2e-5, np.abs(rm - r64).max()
+    assert np.abs(pm - p64).max() < 2e-5 * np.abs(p64).max(), np.abs(pm - p64).max()
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_production_chain_terms(prec):
     """Bonds (Harm, Morse), angles, dihedrals (Harm), Buckingham + LJ, immobile atoms."""
