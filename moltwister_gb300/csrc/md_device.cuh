@@ -142,6 +142,68 @@ __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, dou
 }
 
 // ---------------------------------------------------------------------------------------------
+// Double-float arithmetic for the mixed-mode integrator.  The FP64 unit of this GPU runs at a
+// small fraction of the FP32 rate (64-bit conversions included), so per-atom FP64 work made the
+// kick and drift kernels slower than the force gather at 10^6 atoms.  A value is the unevaluated
+// sum h + l of two floats with |l| <= ulp(h)/2 (about 48 significant bits); the error-free
+// transformations below are Knuth's two-sum, Dekker's fast two-sum and the FMA-based exact
+// product.  The _rn intrinsics keep the compiler from contracting or reordering them.
+// ---------------------------------------------------------------------------------------------
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {   // |a| >= |b| (or a = 0)
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const DF s = two_sum(a.h, b.h);
+    const DF t = two_sum(a.l, b.l);
+    const DF u = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return fast_two_sum(u.h, __fadd_rn(u.l, t.l));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_mul_f(DF a, float b) {
+    const float p = __fmul_rn(a.h, b);
+    return fast_two_sum(p, __fmaf_rn(a.l, b, __fmaf_rn(a.h, b, -p)));
+}
+// FP64 <-> double-float (FP64 instructions: used once per block or outside the step loop)
+__device__ __forceinline__ DF df_of(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_val(DF a) { return (double)a.h + (double)a.l; }
+// Fixed-point force q (units 2^-26) as a double-float: q = a 2^22 + b with 0 <= b < 2^22, both
+// parts converted by 32-bit conversions (exact for |q| < 2^46, i.e. |F| < 2^20 kJ/(mol A)).
+__device__ __forceinline__ DF df_fix(long long q) {
+    const int a = (int)(q >> 22);
+    const int b = (int)(q & 0x3FFFFFLL);
+    return two_sum(__fmul_rn(__int2float_rn(a), 0.0625f), __fmul_rn(__int2float_rn(b), 1.4901161193847656e-08f));
+}
+// Box fraction round(x * conv) modulo 2^32 (conv = 2^32 / L) from double-float operands, to
+// within one unit (L / 2^32): the product's high part is reduced modulo 2^32 exactly, then the
+// integer parts of both halves are added.
+__device__ __forceinline__ unsigned int frac32_df(DF x, DF conv) {
+    const DF y = df_mul(x, conv);
+    const float k = rintf(__fmul_rn(y.h, 2.3283064365386963e-10f));
+    const float t = __fsub_rn(y.h, __fmul_rn(k, 4294967296.0f));
+    const float ti = rintf(t);
+    const float r = __fadd_rn(__fsub_rn(t, ti), y.l);
+    return (unsigned int)__float2int_rn(ti) + (unsigned int)__float2int_rn(r);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Thermostat chain on three warps.  The FP64 units of this GPU serve one sub-partition each at
 // about 30 ns per dependent instruction, so the chain's time is its critical path.  The critical
 // recurrence (steps 1.2 and 1.5 for p_eta[0..M-2]) runs on warp 0; warp 1 computes the step-1.4
@@ -160,6 +222,7 @@ struct NhExchange {
     double iQ[kMaxChain];
     double KE2, scale;
     double pe0, ke, pe_m2, etop;            // slots
+    DF dpe0, dke, dpe_m2, detop;            // the same slots of the double-float chain
     volatile int f_pe0, f_ke, f_pe_m2, f_etop;
     int timeout;
 };
@@ -391,6 +454,226 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
     return seq + nsub;
 }
 
+// ---------------------------------------------------------------------------------------------
+// The same three-warp chain in double-float arithmetic, for the mixed precision mode (published
+// Suzuki-Yoshida weight, exponential, no clamp).  Each FP64 instruction of the chain's critical
+// warp costs about 100 cycles on this GPU (measured with clock64: 3,340 cycles of arithmetic per
+// substep for 33 FP64 instructions); a double-float multiply or add is a handful of dependent FP32
+// operations of 4 cycles each.  Exponentials of small arguments take the x^4 tail of the Taylor
+// series in FP32 (it is below 2e-8, so FP32's relative error leaves 3e-15 absolute) and the low
+// orders in double-float.  State enters and leaves as FP64 in X; values between warps move as
+// double-float pairs through the d* slots.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
+__device__ __forceinline__ DF df_scale(DF a, float pow2) { return {a.h * pow2, a.l * pow2}; }   // exact
+
+// e^x, |x| <= 2^-5 in double-float; larger arguments through FP64
+__device__ __forceinline__ DF df_exp_chain(DF x) {
+    if(fabsf(x.h) <= 0.03125f) {
+        const float xf = x.h;
+        float t = fmaf(xf, 1.0f / 40320.0f, 1.0f / 5040.0f);
+        t = fmaf(t, xf, 1.0f / 720.0f);
+        t = fmaf(t, xf, 1.0f / 120.0f);
+        t = fmaf(t, xf, 1.0f / 24.0f);
+        const float x2f = xf * xf;
+        const float tail = t * (x2f * x2f);                                  // x^4/24 + ... + x^8/8!
+        const DF sixth{0x1.555556p-3f, -0x1.555556p-28f};                     // 1/6
+        const DF a = df_add(df_mul(x, sixth), DF{0.5f, 0.0f});               // 1/2 + x/6
+        const DF b = df_add(df_mul(df_mul(x, x), a), DF{tail, 0.0f});         // x^2/2 + x^3/6 + tail
+        return df_add(df_add(DF{1.0f, 0.0f}, x), b);
+    }
+    return df_of(nh_exp(df_val(x)));
+}
+
+// e^x, |x| <= 2^-10: 1 + x + x^2/2 in double-float, x^3/6 + x^4/24 (below 2e-10) in FP32
+__device__ __forceinline__ DF df_exp_tiny(DF x) {
+    const float xf = x.h;
+    const float tail = (xf * xf) * (xf * fmaf(xf, 1.0f / 24.0f, 1.0f / 6.0f));
+    const DF x2h = df_mul(x, DF{0.5f * x.h, 0.5f * x.l});
+    return df_add(df_add(DF{1.0f, 0.0f}, x), df_add(x2h, DF{tail, 0.0f}));
+}
+
+template<int MM>
+__device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, double dt, int M_rt, int nresp, int seq) {
+    constexpr int CAP = MM > 0 ? MM : kMaxChain;
+    const int M = MM > 0 ? MM : M_rt;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double w0 = sy_w0(true);
+    const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
+    const double gkT = g * kT;
+    const int top = M - 1;
+    const int nsub = 3 * nresp;
+    int* tmo = &X.timeout;
+    const float tiny = 0.0009765625f;   // 2^-10
+    if(warp == 0) {
+        // ---------------- main: p_eta[0..M-2], steps 1.2 and 1.5 ----------------
+        // FP64 -> double-float once per call; every per-stage constant is then a double-float
+        // product (the Suzuki-Yoshida stages have two distinct weights)
+        DF pe[CAP], iQ[CAP], cprev[CAP], xprev[CAP];
+#pragma unroll
+        for(int j = 0; j < M; j++) {
+            pe[j] = df_of(X.pe[j]);
+            iQ[j] = df_of(X.iQ[j]);
+        }
+        DF KE2 = df_of(X.KE2);
+        DF eta_mine = df_of((lane < top) ? X.eta[lane] : 0.0);
+        const DF kTD = df_of(kT), gkTD = df_of(gkT);
+        const DF DtW[2] = {df_of(w[0] * dt / double(nresp)), df_of(w[1] * dt / double(nresp))};
+        DF iQl{0.0f, 0.0f};
+#pragma unroll
+        for(int j = 0; j < top; j++)
+            if(j == lane) iQl = iQ[j];
+        int s = 0;
+        for(int mu = 0; mu < 3; mu++) {
+            const DF Dt = DtW[mu == 1 ? 1 : 0];
+            const DF d8 = df_scale(Dt, -0.125f), d4D = df_scale(Dt, 0.25f), d2 = df_scale(Dt, 0.5f);
+            DF A[CAP], D[CAP];
+#pragma unroll
+            for(int j = 0; j < top; j++) {
+                A[j] = (j > 0) ? df_mul(d4D, iQ[j - 1]) : DF{0.0f, 0.0f};
+                D[j] = df_mul(d8, iQ[j + 1]);
+            }
+            const DF nB = df_neg(df_mul(d4D, kTD)), nB0 = df_neg(df_mul(d4D, gkTD));
+            const DF E = df_mul(d2, iQl);
+            for(int it = 0; it < nresp; it++, s++) {
+                DF etop{1.0f, 0.0f};
+                DF c12[CAP], x12[CAP], t12[CAP];
+                // 1.2
+#pragma unroll
+                for(int j = 0; j < top; j++) {
+                    DF c, x;
+                    if(j == top - 1) {
+                        nh_wait(&X.f_etop, seq + s + 1, tmo);      // exponential of p_eta[M-1] (warp 2)
+                        etop = X.detop;
+                        c = etop;
+                        x = DF{0.0f, 0.0f};
+                    } else if(it > 0) {
+                        c = cprev[j];
+                        x = xprev[j];
+                    } else {
+                        x = df_mul(pe[j + 1], D[j]);
+                        c = df_exp_chain(x);
+                    }
+                    c12[j] = c;
+                    x12[j] = x;
+                    const DF t = (j == 0) ? df_fma(KE2, d4D, nB0) : df_fma(df_mul(pe[j - 1], pe[j - 1]), A[j], nB);
+                    t12[j] = t;
+                    pe[j] = df_mul(df_fma(pe[j], c, t), c);
+                    if(j == 0) {
+                        if(lane == 0) X.dpe0 = pe[0];
+                        nh_post(&X.f_pe0, seq + s + 1);
+                    }
+                }
+                // 1.3 (this warp's elements)
+                {
+                    DF v{0.0f, 0.0f};
+#pragma unroll
+                    for(int j = 0; j < top; j++)
+                        if(j == lane) v = pe[j];
+                    if(lane < top) eta_mine = df_fma(v, E, eta_mine);
+                }
+                // 1.5
+#pragma unroll
+                for(int j = top - 1; j >= 0; j--) {
+                    DF c;
+                    if(j == top - 1) {
+                        c = etop;
+                    } else {
+                        const DF xn = df_mul(pe[j + 1], D[j]);
+                        const DF dx = df_add(xn, df_neg(x12[j]));
+                        if(fabsf(dx.h) <= tiny && xn.h <= 0.5f && x12[j].h <= 0.5f)
+                            c = df_mul(c12[j], df_exp_tiny(dx));
+                        else
+                            c = df_exp_chain(xn);
+                        cprev[j] = c;
+                        xprev[j] = xn;
+                    }
+                    DF t;
+                    if(j == 0) {
+                        nh_wait(&X.f_ke, seq + s + 1, tmo);    // kinetic term after step 1.4 (warp 1)
+                        KE2 = X.dke;
+                        t = df_fma(KE2, d4D, nB0);
+                    } else {
+                        t = t12[j];
+                    }
+                    pe[j] = df_mul(df_fma(pe[j], c, t), c);
+                    if(j == top - 1) {
+                        if(lane == 0) X.dpe_m2 = pe[top - 1];
+                        nh_post(&X.f_pe_m2, seq + s + 1);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if(lane < top) {
+            DF v{0.0f, 0.0f};
+#pragma unroll
+            for(int j = 0; j < top; j++)
+                if(j == lane) v = pe[j];
+            X.pe[lane] = df_val(v);
+            X.eta[lane] = df_val(eta_mine);
+        }
+    } else if(warp == 1) {
+        // ---------------- warp 1: step 1.4, kinetic term, momentum scale ----------------
+        const DF iQ0 = df_of(X.iQ[0]);
+        DF KE2 = df_of(X.KE2), scale{1.0f, 0.0f};
+        const DF D1W[2] = {df_neg(df_mul(df_of(w[0] * dt / double(nresp)), df_scale(iQ0, 0.5f))),
+                           df_neg(df_mul(df_of(w[1] * dt / double(nresp)), df_scale(iQ0, 0.5f)))};
+        int s = 0;
+        for(int mu = 0; mu < 3; mu++) {
+            const DF D1 = D1W[mu == 1 ? 1 : 0];
+            for(int it = 0; it < nresp; it++, s++) {
+                nh_wait(&X.f_pe0, seq + s + 1, tmo);
+                const DF c = df_exp_chain(df_mul(X.dpe0, D1));
+                scale = df_mul(scale, c);
+                KE2 = df_mul(KE2, df_mul(c, c));
+                if(lane == 0) X.dke = KE2;
+                nh_post(&X.f_ke, seq + s + 1);
+            }
+        }
+        if(lane == 0) {
+            X.KE2 = df_val(KE2);
+            X.scale = df_val(scale);
+        }
+    } else if(warp == 2) {
+        // ---------------- warp 2: p_eta[M-1] (steps 1.1, 1.6), its exponential, eta[M-1] ----------------
+        const DF iQt = df_of(X.iQ[top]);
+        const DF iQm = df_of(X.iQ[top - 1]), nkT = df_of(-kT);
+        const DF DtW[2] = {df_of(w[0] * dt / double(nresp)), df_of(w[1] * dt / double(nresp))};
+        DF pt = df_of(X.pe[top]);
+        DF eta_t = df_of(X.eta[top]);
+        DF pm = df_of(X.pe[top - 1]);
+        DF d4prev{0.0f, 0.0f};
+        int s = 0;
+        for(int mu = 0; mu < 3; mu++) {
+            const DF Dt = DtW[mu == 1 ? 1 : 0];
+            const DF d4 = df_scale(Dt, 0.25f), Dtop = df_mul(df_scale(Dt, -0.125f), iQt), Etop = df_mul(df_scale(Dt, 0.5f), iQt);
+            for(int it = 0; it < nresp; it++, s++) {
+                if(s > 0) {
+                    // 1.6 of the previous substep, with that substep's Dt
+                    nh_wait(&X.f_pe_m2, seq + s, tmo);
+                    pm = X.dpe_m2;
+                    pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
+                }
+                pt = df_fma(d4, df_fma(df_mul(pm, pm), iQm, nkT), pt);         // 1.1
+                const DF c = df_exp_chain(df_mul(pt, Dtop));
+                if(lane == 0) X.detop = c;
+                nh_post(&X.f_etop, seq + s + 1);
+                eta_t = df_fma(pt, Etop, eta_t);                               // 1.3 for the top element
+                d4prev = d4;
+            }
+        }
+        nh_wait(&X.f_pe_m2, seq + nsub, tmo);             // 1.6 of the last substep
+        pm = X.dpe_m2;
+        pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
+        if(lane == 0) {
+            X.pe[top] = df_val(pt);
+            X.eta[top] = df_val(eta_t);
+        }
+    }
+    return seq + nsub;
+}
+
 // Deterministic block sum of NV doubles (fixed shuffle tree, then fixed order over warps).
 template<int NV>
 __device__ inline void block_sum(double (&v)[NV], double* smem /* [32*NV] */) {
@@ -443,7 +726,18 @@ __device__ inline bool last_block(unsigned int* counter) {
 }
 
 __device__ inline int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
-                                       bool fixed) {
+                                       bool fixed, bool dfloat = false) {
+    if(dfloat) {
+        switch(M) {
+        case 2: return nh_chain_half_3w_df<2>(X, g, kT, dt, M, nresp, seq);
+        case 3: return nh_chain_half_3w_df<3>(X, g, kT, dt, M, nresp, seq);
+        case 4: return nh_chain_half_3w_df<4>(X, g, kT, dt, M, nresp, seq);
+        case 5: return nh_chain_half_3w_df<5>(X, g, kT, dt, M, nresp, seq);
+        case 6: return nh_chain_half_3w_df<6>(X, g, kT, dt, M, nresp, seq);
+        case 8: return nh_chain_half_3w_df<8>(X, g, kT, dt, M, nresp, seq);
+        default: return nh_chain_half_3w_df<0>(X, g, kT, dt, M, nresp, seq);
+        }
+    }
     switch(M) {
     case 2: return nh_chain_half_3w_t<2>(X, g, kT, dt, M, nresp, seq, fixed);
     case 3: return nh_chain_half_3w_t<3>(X, g, kT, dt, M, nresp, seq, fixed);
@@ -470,6 +764,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
     __shared__ NhExchange X;
     const int tid = threadIdx.x;
     const bool fixed = P.precision != MTG_PREC_REFERENCE;
+    const bool dfloat = P.precision == MTG_PREC_MIXED;   // double-float chain in the mixed mode
     double c2 = 1.0, c1 = 1.0;
     double KEf = KE2;
     if(M >= 2) {
@@ -487,7 +782,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         bar96();
         int seq = 0;
         if(second_half) {
-            seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed);
+            seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed, dfloat);
             bar96();
             c2 = X.scale;
             if(tid < M) {
@@ -505,7 +800,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         }
         const double KE_after2 = X.KE2;
         bar96();
-        seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed);
+        seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed, dfloat);
         bar96();
         c1 = X.scale;
         KEf = X.KE2;
@@ -648,68 +943,6 @@ __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2,
             b->Lf[a] = (float)b->L[a];
         }
     }
-}
-
-// ---------------------------------------------------------------------------------------------
-// Double-float arithmetic for the mixed-mode integrator.  The FP64 unit of this GPU runs at a
-// small fraction of the FP32 rate (64-bit conversions included), so per-atom FP64 work made the
-// kick and drift kernels slower than the force gather at 10^6 atoms.  A value is the unevaluated
-// sum h + l of two floats with |l| <= ulp(h)/2 (about 48 significant bits); the error-free
-// transformations below are Knuth's two-sum, Dekker's fast two-sum and the FMA-based exact
-// product.  The _rn intrinsics keep the compiler from contracting or reordering them.
-// ---------------------------------------------------------------------------------------------
-struct DF {
-    float h, l;
-};
-__device__ __forceinline__ DF two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-__device__ __forceinline__ DF fast_two_sum(float a, float b) {   // |a| >= |b| (or a = 0)
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ DF df_add(DF a, DF b) {
-    const DF s = two_sum(a.h, b.h);
-    const DF t = two_sum(a.l, b.l);
-    const DF u = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
-    return fast_two_sum(u.h, __fadd_rn(u.l, t.l));
-}
-__device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
-__device__ __forceinline__ DF df_mul(DF a, DF b) {
-    const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
-    return fast_two_sum(p, e);
-}
-__device__ __forceinline__ DF df_mul_f(DF a, float b) {
-    const float p = __fmul_rn(a.h, b);
-    return fast_two_sum(p, __fmaf_rn(a.l, b, __fmaf_rn(a.h, b, -p)));
-}
-// FP64 <-> double-float (FP64 instructions: used once per block or outside the step loop)
-__device__ __forceinline__ DF df_of(double x) {
-    const float h = __double2float_rn(x);
-    return {h, __double2float_rn(x - (double)h)};
-}
-__device__ __forceinline__ double df_val(DF a) { return (double)a.h + (double)a.l; }
-// Fixed-point force q (units 2^-26) as a double-float: q = a 2^22 + b with 0 <= b < 2^22, both
-// parts converted by 32-bit conversions (exact for |q| < 2^46, i.e. |F| < 2^20 kJ/(mol A)).
-__device__ __forceinline__ DF df_fix(long long q) {
-    const int a = (int)(q >> 22);
-    const int b = (int)(q & 0x3FFFFFLL);
-    return two_sum(__fmul_rn(__int2float_rn(a), 0.0625f), __fmul_rn(__int2float_rn(b), 1.4901161193847656e-08f));
-}
-// Box fraction round(x * conv) modulo 2^32 (conv = 2^32 / L) from double-float operands, to
-// within one unit (L / 2^32): the product's high part is reduced modulo 2^32 exactly, then the
-// integer parts of both halves are added.
-__device__ __forceinline__ unsigned int frac32_df(DF x, DF conv) {
-    const DF y = df_mul(x, conv);
-    const float k = rintf(__fmul_rn(y.h, 2.3283064365386963e-10f));
-    const float t = __fsub_rn(y.h, __fmul_rn(k, 4294967296.0f));
-    const float ti = rintf(t);
-    const float r = __fadd_rn(__fsub_rn(t, ti), y.l);
-    return (unsigned int)__float2int_rn(ti) + (unsigned int)__float2int_rn(r);
 }
 
 // Minimum image by rounding (production kernels).
