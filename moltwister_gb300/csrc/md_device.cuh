@@ -464,7 +464,14 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
 // orders in double-float.  State enters and leaves as FP64 in X; values between warps move as
 // double-float pairs through the d* slots.
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
+// The chain uses the shorter double-float sum (one two-sum of the high parts, the low parts added
+// in FP32): its error is 2^-47 of |a| + |b| rather than of |a + b|, which for the chain's momenta,
+// whose scale is set by their largest terms, is as good and 4 dependent operations shorter.
+__device__ __forceinline__ DF df_addq(DF a, DF b) {
+    const DF s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_addq(df_mul(a, b), c); }
 __device__ __forceinline__ DF df_scale(DF a, float pow2) { return {a.h * pow2, a.l * pow2}; }   // exact
 
 // e^x, |x| <= 2^-5 in double-float; larger arguments through FP64
@@ -478,9 +485,9 @@ __device__ __forceinline__ DF df_exp_chain(DF x) {
         const float x2f = xf * xf;
         const float tail = t * (x2f * x2f);                                  // x^4/24 + ... + x^8/8!
         const DF sixth{0x1.555556p-3f, -0x1.555556p-28f};                     // 1/6
-        const DF a = df_add(df_mul(x, sixth), DF{0.5f, 0.0f});               // 1/2 + x/6
-        const DF b = df_add(df_mul(df_mul(x, x), a), DF{tail, 0.0f});         // x^2/2 + x^3/6 + tail
-        return df_add(df_add(DF{1.0f, 0.0f}, x), b);
+        const DF a = df_addq(df_mul(x, sixth), DF{0.5f, 0.0f});               // 1/2 + x/6
+        const DF b = df_addq(df_mul(df_mul(x, x), a), DF{tail, 0.0f});         // x^2/2 + x^3/6 + tail
+        return df_addq(df_addq(DF{1.0f, 0.0f}, x), b);
     }
     return df_of(nh_exp(df_val(x)));
 }
@@ -490,7 +497,7 @@ __device__ __forceinline__ DF df_exp_tiny(DF x) {
     const float xf = x.h;
     const float tail = (xf * xf) * (xf * fmaf(xf, 1.0f / 24.0f, 1.0f / 6.0f));
     const DF x2h = df_mul(x, DF{0.5f * x.h, 0.5f * x.l});
-    return df_add(df_add(DF{1.0f, 0.0f}, x), df_add(x2h, DF{tail, 0.0f}));
+    return df_addq(df_addq(DF{1.0f, 0.0f}, x), df_addq(x2h, DF{tail, 0.0f}));
 }
 
 template<int MM>
@@ -580,7 +587,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
                         c = etop;
                     } else {
                         const DF xn = df_mul(pe[j + 1], D[j]);
-                        const DF dx = df_add(xn, df_neg(x12[j]));
+                        const DF dx = df_addq(xn, df_neg(x12[j]));
                         if(fabsf(dx.h) <= tiny && xn.h <= 0.5f && x12[j].h <= 0.5f)
                             c = df_mul(c12[j], df_exp_tiny(dx));
                         else

@@ -491,10 +491,13 @@ __global__ void k_mkick2(DevSys d, Params P) {
     }
     if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
         __shared__ double tot[3];
-        double s3[3];
-        system_totals<3>(d.partial, sv.bbase, sv.nb, s3, smem);
+        constexpr int NV = OUTPUT ? 3 : 1;   // F.r and U only on output steps
+        double sv3[NV];
+        system_totals<NV>(d.partial, sv.bbase, sv.nb, sv3, smem);
         if(threadIdx.x == 0) {
-            for(int q = 0; q < 3; q++) tot[q] = s3[q];
+            tot[0] = sv3[0];
+            tot[1] = OUTPUT ? sv3[NV > 1 ? 1 : 0] : 0.0;
+            tot[2] = OUTPUT ? sv3[NV > 2 ? 2 : 0] : 0.0;
             sv.sc->done_blocks = 0;
         }
         __syncthreads();
