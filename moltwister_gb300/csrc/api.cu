@@ -394,7 +394,10 @@ int enqueue_step(mtg_ctx* c, bool output) {
 }
 
 // Kernels per step when no list rebuild is due (reference mode rebuilds every step).
-int kernels_per_step(const mtg_ctx* c) { return (is_reference(c) || !c->conditional) ? 9 : 3; }
+int kernels_per_step(const mtg_ctx* c) {
+    // mixed mode ends a step with a second kernel (k_mstep_end)
+    return ((is_reference(c) || !c->conditional) ? 9 : 3) + (is_mixed(c) ? 1 : 0);
+}
 
 template<class F>
 int capture_segment(mtg_ctx* c, cudaGraph_t* out, F&& body) {

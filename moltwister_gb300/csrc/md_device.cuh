@@ -170,9 +170,9 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
 __device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
 __device__ __forceinline__ DF df_mul(DF a, DF b) {
     const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
-    return fast_two_sum(p, e);
+    const float c = __fmaf_rn(a.l, b.h, __fmul_rn(a.h, b.l));   // cross terms, beside p
+    const float e = __fmaf_rn(a.h, b.h, -p);                    // exact error of p
+    return fast_two_sum(p, __fadd_rn(e, c));
 }
 __device__ __forceinline__ DF df_mul_f(DF a, float b) {
     const float p = __fmul_rn(a.h, b);

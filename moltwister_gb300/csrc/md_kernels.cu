@@ -431,8 +431,9 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
 }
 
 // Second kick with force clipping (VelVerlet.cpp:87,96-122), wrap into [-L/2, L/2) (the box
-// fractions are periodic and stay as they are), sum p^2/m (and on output steps F.r and U), then
-// the end-of-step scalar work of the last block.
+// fractions are periodic and stay as they are), block sums of p^2/m (and on output steps F.r and
+// U).  The end-of-step scalar work runs in k_mstep_end: kept out of this kernel, the double-float
+// chain's registers do not limit the occupancy of the per-atom pass.
 template<bool OUTPUT>
 __global__ void k_mkick2(DevSys d, Params P) {
     __shared__ MixK K;
@@ -489,20 +490,25 @@ __global__ void k_mkick2(DevSys d, Params P) {
         d.partial[blockIdx.x * 4 + 1] = v[1];
         d.partial[blockIdx.x * 4 + 2] = v[2];
     }
-    if(last_block_of(&sv.sc->done_blocks, (unsigned)sv.nb)) {
-        __shared__ double tot[3];
-        constexpr int NV = OUTPUT ? 3 : 1;   // F.r and U only on output steps
-        double sv3[NV];
-        system_totals<NV>(d.partial, sv.bbase, sv.nb, sv3, smem);
-        if(threadIdx.x == 0) {
-            tot[0] = sv3[0];
-            tot[1] = OUTPUT ? sv3[NV > 1 ? 1 : 0] : 0.0;
-            tot[2] = OUTPUT ? sv3[NV > 2 ? 2 : 0] : 0.0;
-            sv.sc->done_blocks = 0;
-        }
-        __syncthreads();
-        if(threadIdx.x < 96) step_end(d, P, sv, tot, OUTPUT);
+}
+
+// End of a mixed-precision step, one 96-thread block per system (per replica of a batch): the
+// system's totals from its block partials, then the thermostat half-steps and the output record.
+template<bool OUTPUT>
+__global__ void __launch_bounds__(96, 1) k_mstep_end(DevSys d, Params P) {
+    __shared__ double smem[32 * 3];
+    __shared__ double tot[3];
+    const SysView sv = sys_view(d, P, P.nrep ? (int)blockIdx.x : -1);
+    constexpr int NV = OUTPUT ? 3 : 1;   // F.r and U only on output steps
+    double sv3[NV];
+    system_totals<NV>(d.partial, sv.bbase, sv.nb, sv3, smem);
+    if(threadIdx.x == 0) {
+        tot[0] = sv3[0];
+        tot[1] = OUTPUT ? sv3[NV > 1 ? 1 : 0] : 0.0;
+        tot[2] = OUTPUT ? sv3[NV > 2 ? 2 : 0] : 0.0;
     }
+    __syncthreads();
+    step_end(d, P, sv, tot, OUTPUT);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1358,8 +1364,14 @@ void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream
 void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
     const int nb = integration_blocks(P);
     if(P.precision == MTG_PREC_MIXED) {
-        if(output) k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
-        else k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
+        const int nsys = P.nrep ? P.nrep : 1;
+        if(output) {
+            k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
+            k_mstep_end<true><<<nsys, 96, 0, s>>>(d, P);
+        } else {
+            k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
+            k_mstep_end<false><<<nsys, 96, 0, s>>>(d, P);
+        }
     } else {
         if(output) k_pkick2<true><<<nb, 256, 0, s>>>(d, P);
         else k_pkick2<false><<<nb, 256, 0, s>>>(d, P);

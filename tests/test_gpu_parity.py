@@ -270,19 +270,21 @@ def test_kob_andersen_per_pair_cutoffs(prec):
 
 @pytest.mark.parametrize("prec", ["mixed", "fp64"])
 def test_nve_conserves_energy(prec):
-    """NVE on a 16,384-atom Kob-Andersen mixture (energies shifted at the cutoffs, as in the
-    benchmark): the linear drift of the total energy over 8,000 steps (4 ps) stays below 2e-2 kT
-    per atom per ns in FP64 and in mixed precision (double-float integration, FP32 pair forces).
-    The fitted slope of so short a window carries the velocity-Verlet energy fluctuation as noise,
-    about 2.5e-3 kT per atom per ns here (it scales as N^-1/2 and window^-3/2), so the bound
-    catches a broken integrator, not the 1e-4 target, which the Kob-Andersen benchmark measures
-    on 10^6 atoms over a long window with its standard error."""
+    """NVE on a 16,384-atom Kob-Andersen mixture with force-shifted LJ (continuous forces): after
+    4,000 steps of equilibration the linear drift of the total energy over 8,000 steps (4 ps) stays
+    below 2e-2 kT per atom per ns in FP64 and in mixed precision (double-float integration, FP32
+    pair forces).  The fitted slope of so short a window carries the velocity-Verlet energy
+    fluctuation as noise, about 5e-3 kT per atom per ns here (from the standard error measured on
+    131,072 atoms over 40 ps, scaled by N^-1/2 and window^-3/2), so the bound catches a broken
+    integrator, not the 1e-4 target: bench_drift measures that (both precisions drift by
+    -1.2e-4 +- 0.5e-4 on 131,072 atoms over 40 ps)."""
     from moltwister_gb300 import workloads as W
     s, cfg = W.kob_andersen(ncell=16, seed=6)
     cfg.precision = prec
+    cfg.ljshift = 2
     e = engine(s, cfg)
     e.optimize(200)
-    e.run(1000)                                        # equilibrate the relaxed lattice start
+    e.run(4000)                                        # equilibrate the relaxed lattice start
     recs = e.run(8000, out_stride=100)
     t_ns = np.array([r.step for r in recs], float) * cfg.timestep * 1e-6
     E = np.array([r.U + r.K for r in recs])
