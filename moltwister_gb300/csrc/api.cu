@@ -4,8 +4,9 @@
 // Step loop.  One MD step is the reference sequence (MDLoop.cpp:128-133) mapped to kernels:
 //   kick+drift (first thermostat half-step folded in as a pending momentum scale)
 //   -> [reference: cell list + neighbour list every step | production: Verlet list if due]
-//   -> force gather -> clip + kick + pbc wrap + KE reduction, whose last block runs the
-//   thermostat's second half-step and the next step's first half-step.
+//   -> force gather -> clip + kick + pbc wrap + KE block sums -> the system's totals and the
+//   thermostat's second half-step and the next step's first half-step (the last block of the kick
+//   in the reference and fp64 modes, a one-block-per-system kernel in the mixed mode).
 // Steps are captured into CUDA graphs, one chunk per output interval; the state at the start of
 // a chunk is kept so that a chunk whose neighbour list overflowed is redone after growing it.
 #include <cuda_runtime.h>

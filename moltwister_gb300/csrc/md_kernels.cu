@@ -3,10 +3,12 @@
 //
 // Layout in HBM (per atom):
 //   FP64 mode : r double[3] (master), p double[3], F double[3]
-//   mixed     : hi float4 (x,y,z hi, charge), lo float4 (x,y,z lo, type bits) -- the positions,
-//               held as FP32 hi+lo pairs and updated in FP64 -- p double[3], F int64 x3 (SoA,
-//               2^32 units per kJ/mol/A: per-pair contributions are rounded to fixed point and
-//               summed exactly, so the result does not depend on summation order), inv_m float.
+//   mixed     : hi float4 (x,y,z hi, charge), lo float4 (x,y,z lo, type bits) -- the positions
+//               as double-float pairs -- pq uint4 (x,y,z as 32-bit box fractions, type), ph / pl
+//               float4 (momenta as double-float pairs, 1/m in .w), F int64 x3 (SoA, 2^26 units
+//               per kJ/mol/A: per-pair contributions are rounded to fixed point and summed
+//               exactly, so the result does not depend on summation order); r and p double[3]
+//               are the masters the host reads and writes (k_sync).
 // Neighbour list: [atom][slot] uint32, atom index in the low 29 bits and the exclusion class of
 // the pair (none, 1-2, 1-3, 1-4, same molecule; FunctorCalcForce.cpp:95-157) in the top 3 bits.
 // Pairs whose class scale is exactly 0 are left out of the list.  Rebuilt when an atom has moved
@@ -681,11 +683,6 @@ __global__ void k_vlist(DevSys d, Params P) {
 // ---------------------------------------------------------------------------------------------
 // Force gather
 // ---------------------------------------------------------------------------------------------
-template<class R>
-struct Acc {
-    R x, y, z;
-};
-
 // Fixed-point accumulation of FP32 contributions (mixed mode) without the FP64 unit (which also
 // executes 64-bit conversions, at a small fraction of the FP32 rate on this GPU).
 // A contribution f becomes round(f * 2^26) exactly, split over two int32 accumulators.  With
