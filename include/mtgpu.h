@@ -74,8 +74,8 @@ extern "C" {
                                  order, all-pairs minimum-image Coulomb.  The parity mode. */
 #define MTG_PREC_FP64 1       /* analytic terms in FP64, Verlet list with skin */
 #define MTG_PREC_MIXED 2      /* analytic terms in FP32, forces summed as int64 fixed point
-                                 (deterministic), positions as FP32 hi+lo pairs updated in FP64,
-                                 FP64 reductions and thermostat */
+                                 (deterministic), positions, momenta and the thermostat chain as
+                                 double-float (FP32 hi+lo) pairs, FP64 system sums */
 
 /* Coulomb treatment (new key `coulomb`). */
 #define MTG_COULOMB_ALLPAIRS 0 /* the reference: minimum image over all pairs, no cutoff
