@@ -1,0 +1,75 @@
+"""Input validation of mtg_create (no GPU needed: every check runs before any device work).  The
+reference prints and carries on; the C ABI returns a negative MTG_E_* code with a message, and the
+binding raises MTGError with that code."""
+import numpy as np
+import pytest
+
+from moltwister_gb300 import engine as E
+from moltwister_gb300 import workloads as W
+
+INVALID, UNSUPPORTED, NONFINITE = -1, -6, -7
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from moltwister_gb300.build import build
+    build()
+
+
+def create_code(s, c):
+    with pytest.raises(E.MTGError) as ei:
+        E.Engine(s, c)
+    return ei.value.code, str(ei.value)
+
+
+def test_bad_lj_shift():
+    s, c = W.argon(ncell=2)
+    c.precision = "mixed"
+    c.ljshift = 3
+    code, msg = create_code(s, c)
+    assert code == INVALID and "lj_shift" in msg
+
+
+def test_npt_outside_reference_mode():
+    s, c = W.argon(ncell=2)
+    c.precision, c.ensemble = "fp64", "NPT"
+    c.coulomb = "cutoff"
+    code, msg = create_code(s, c)
+    assert code == UNSUPPORTED and "NPT" in msg
+
+
+def test_reference_mode_has_all_pairs_coulomb_only():
+    s, c = W.argon(ncell=2)
+    c.coulomb = "cutoff"
+    code, msg = create_code(s, c)
+    assert code == INVALID and "all-pairs" in msg
+
+
+def test_all_pairs_coulomb_with_charges_in_production_modes():
+    s, c = W.water(n_mol=8, L=12.0, seed=2)
+    c.precision, c.coulomb = "mixed", "allpairs"
+    code, msg = create_code(s, c)
+    assert code == UNSUPPORTED and "all-pairs" in msg
+
+
+def test_non_finite_positions():
+    s, c = W.argon(ncell=2)
+    s.r = s.r.copy()
+    s.r[3, 1] = np.nan
+    code, _ = create_code(s, c)
+    assert code == NONFINITE
+
+
+def test_non_positive_mass():
+    s, c = W.argon(ncell=2)
+    s.m = s.m.copy()
+    s.m[0] = 0.0
+    code, msg = create_code(s, c)
+    assert code == INVALID and "mass" in msg
+
+
+def test_non_positive_box():
+    s, c = W.argon(ncell=2)
+    s.box = np.array([s.box[0], 0.0, s.box[2]])
+    code, msg = create_code(s, c)
+    assert code == INVALID and "box" in msg
