@@ -73,3 +73,27 @@ def test_non_positive_box():
     s.box = np.array([s.box[0], 0.0, s.box[2]])
     code, msg = create_code(s, c)
     assert code == INVALID and "box" in msg
+
+
+def batch_code(systems, c, **kw):
+    from moltwister_gb300.batch import BatchEngine
+    with pytest.raises(E.MTGError) as ei:
+        BatchEngine(systems, c, **kw)
+    return ei.value.code, str(ei.value)
+
+
+def test_batch_needs_a_production_mode():
+    a, c = W.argon(ncell=2, seed=1)
+    b, _ = W.argon(ncell=3, seed=2)
+    code, msg = batch_code([a, b], c)                     # the argon config is reference precision
+    assert code == UNSUPPORTED and "batches" in msg
+
+
+def test_batch_temperatures_and_cutoffs_are_checked():
+    a, c = W.argon(ncell=2, seed=1)
+    b, _ = W.argon(ncell=3, seed=2)
+    c.precision = "mixed"
+    code, msg = batch_code([a, b], c, temperatures=[120.0, -5.0])
+    assert code == INVALID and "temperatures" in msg
+    code, msg = batch_code([a, b], c, cutoffs=[c.cutoffradius, 2.0 * c.cutoffradius])
+    assert code == INVALID and "cutoffs" in msg
