@@ -10,9 +10,9 @@ namespace mtg {
 
 // exp(x) for the thermostat.  Small arguments, which are the normal case (|x| = Dt/8 p_eta/Q is of
 // order 1e-2), use the Taylor series of e^x with the remainder below 1e-17 relative (degree 8 for
-// |x| <= 2^-5, degree 11 for |x| <= 2^-3); larger ones call exp().  On this GPU every FP64
-// instruction costs about as much as thirty FP32 ones and the SM's FP64 unit is shared by the
-// chain's warps, so the instruction count is what matters: Horner's scheme (one FMA per degree;
+// |x| <= 2^-5, degree 11 for |x| <= 2^-3); larger ones call exp().  On this GPU an FP64
+// instruction costs about 100 cycles in the chain's warps whether or not it depends on the one
+// before, so the instruction count is what matters: Horner's scheme (one FMA per degree;
 // Estrin's shorter dependency chain needs more instructions and measured slower), and the range
 // tests compare bit patterns on the integer units.
 __device__ __forceinline__ double nh_exp(double x) {
