@@ -262,8 +262,11 @@ int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
  * MDLoop.cpp:434-456): runs `steps` un-captured steps with CUDA events around each phase on the
  * context's stream and returns the mean device milliseconds per step of
  * phase_ms[0] kick+drift, [1] list build (cell list / Verlet list; the early-exit kernels when no
- * rebuild is due), [2] force gather, [3] kick + wrap + reductions + thermostat.
- * The state advances by `steps` steps exactly as mtg_run would advance it. */
+ * rebuild is due), [2] force gather, [3] second kick + wrap + block sums (in the reference and FP64
+ * modes also the system totals and the thermostat chain, which run in that kernel's last block),
+ * [4] mixed mode's step-end kernel (system totals, thermostat chain, output record; 0 otherwise).
+ * phase_ms holds 5 values.  The state advances by `steps` steps exactly as mtg_run would advance
+ * it. */
 int mtg_profile_phases(mtg_ctx* ctx, int steps, double* phase_ms);
 
 /* ---- Force-field parameters and gradients (no counterpart in the reference, which has no
@@ -393,10 +396,11 @@ int mtg_batch_get_thermo(mtg_ctx* ctx, int32_t rep, mtg_thermo_state* th);
  * Limits the caller must respect: the scratch array is shared by every call on a device, so calls
  * whose work overlaps in time (other streams, other host threads, or a second call enqueued on
  * another stream before the first finished) race on it and must be serialised by the caller;
- * calls enqueued one after another on the same stream are safe.  The first call on each device
- * looks up the array's address (cudaGetSymbolAddress, which may load the module), so make that
- * first call before any stream capture begins on that device.  Errors are reported through
- * mtg_last_error(NULL) of the calling thread. */
+ * calls enqueued one after another on the same stream are safe.  Every call looks up the array's
+ * address in the current context (cudaGetSymbolAddress), so a device reset or a caller-made
+ * context between calls is followed; the first call on each device also loads the module there,
+ * so make that first call before any stream capture begins on that device.  Errors are reported
+ * through mtg_last_error(NULL) of the calling thread. */
 #define MTG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int mtg_neighbors_noalloc(const double* d_r, int32_t n, const double box[3], double cutoff, double shell,
                           int32_t max_neigh, int32_t* d_count, int32_t* d_list, int32_t* needed, void* stream);

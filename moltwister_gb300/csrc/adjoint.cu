@@ -275,11 +275,12 @@ __global__ void k_force_tangent(DevSys d, Params P, const double* pos, Tangents 
             rc = R.rc;
             rq = R.rcoul;
         }
-        const int cnt = min(d.vcount[i], d.vmax);
-        const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
+        const int si = d.slot_of[i];   // list rows and entries are slots (cell order)
+        const int cnt = min(d.vcount[si], d.vmax);
+        const uint32_t* lst = d.vlist + (size_t)si * d.vmax;
         for(int e = lane; e < cnt; e += 32) {
             const uint32_t ent = lst[e];
-            const int j = (int)(ent & kIdxMask), cls = (int)(ent >> kClassShift);
+            const int j = d.pcell_list[ent & kIdxMask], cls = (int)(ent >> kClassShift);
             const D3 dv = rel_d(d, P, pos, i, j, tg.vpos);
             D3 f;
             Dual u;
@@ -333,10 +334,11 @@ __global__ void k_rdf_rows(DevSys d, Params P, const double* pos, RdfSpec s, dou
     const int ti = d.type[i];
     if(ti != s.ta && ti != s.tb) return;
     const double iw2 = 1.0 / (s.width * s.width), norm = 1.0 / (s.width * 2.5066282746310002);
-    const int cnt = min(d.vcount[i], d.vmax);
-    const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
+    const int si = d.slot_of[i];
+    const int cnt = min(d.vcount[si], d.vmax);
+    const uint32_t* lst = d.vlist + (size_t)si * d.vmax;
     for(int e = 0; e < cnt; e++) {
-        const int j = (int)(lst[e] & kIdxMask);
+        const int j = d.pcell_list[lst[e] & kIdxMask];
         const int tj = d.type[j];
         const bool pair = (s.ta == s.tb) ? (ti == s.ta && tj == s.tb && j > i) : (ti == s.ta && tj == s.tb);
         if(!pair) continue;
@@ -368,10 +370,11 @@ __global__ void k_rdf_adjoint(DevSys d, Params P, const double* pos, RdfSpec s, 
     if(ti != s.ta && ti != s.tb) return;
     const double iw2 = 1.0 / (s.width * s.width), norm = 1.0 / (s.width * 2.5066282746310002);
     double gx = 0.0, gy = 0.0, gz = 0.0;
-    const int cnt = min(d.vcount[i], d.vmax);
-    const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
+    const int si = d.slot_of[i];
+    const int cnt = min(d.vcount[si], d.vmax);
+    const uint32_t* lst = d.vlist + (size_t)si * d.vmax;
     for(int e = 0; e < cnt; e++) {
-        const int j = (int)(lst[e] & kIdxMask);
+        const int j = d.pcell_list[lst[e] & kIdxMask];
         const int tj = d.type[j];
         const bool pair = (ti == s.ta && tj == s.tb) || (ti == s.tb && tj == s.ta);
         if(!pair) continue;

@@ -342,16 +342,20 @@ struct TuneKey {
     }
 };
 std::map<TuneKey, int> g_tuned;
+std::mutex g_tuned_mutex;   // contexts may be created on several host threads at once
 
 int autotune_force(mtg_ctx* c) {
     const Params& P = c->P;
     const double V = P.box[0] * P.box[1] * P.box[2];
     const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
     TuneKey key{P.precision, (int)std::floor(std::log2((double)P.n)), (int)std::lround(rlist * 10.0), (int)std::lround(100.0 * P.n / V)};
-    auto it = g_tuned.find(key);
-    if(it != g_tuned.end()) {
-        c->P.team = it->second;
-        return MTG_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mutex);
+        auto it = g_tuned.find(key);
+        if(it != g_tuned.end()) {
+            c->P.team = it->second;
+            return MTG_OK;
+        }
     }
     const int teams[3] = {8, 16, 32};
     float best = 1e30f;
@@ -371,7 +375,10 @@ int autotune_force(mtg_ctx* c) {
         }
     }
     c->P.team = best_team;
-    g_tuned[key] = best_team;
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mutex);
+        g_tuned[key] = best_team;
+    }
     // leave the forces of the chosen variant in place
     launch_prod_force(c->d, c->P, true, c->stream);
     CUDA_TRY(c, cudaGetLastError());
@@ -1063,13 +1070,25 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         rc = rc || dalloc(C, &d.pcell_first, (size_t)c->ncell_prod);
         rc = rc || dalloc(C, &d.pcell_count, (size_t)c->ncell_prod);
         rc = rc || dalloc(C, &d.pcell_cursor, (size_t)c->ncell_prod);
-        rc = rc || dalloc(C, &d.pcell_list, (size_t)n);
+        {
+            // slot order starts as the identity; every list build replaces it with cell order
+            std::vector<int> ident(n);
+            for(int i = 0; i < n; i++) ident[i] = i;
+            int* q = nullptr;
+            rc = rc || upload(C, &q, ident.data(), ident.size());
+            d.pcell_list = q;
+            q = nullptr;
+            rc = rc || upload(C, &q, ident.data(), ident.size());
+            d.slot_of = q;
+        }
         rc = rc || dalloc(C, &d.vcount, (size_t)n);
         rc = rc || dalloc(C, &d.r_build, (size_t)3 * n);
         rc = rc || dalloc(C, &d.rb4, (size_t)n);
+        rc = rc || dalloc(C, &d.rb4s, (size_t)n);
         rc = rc || dalloc(C, &d.hi, (size_t)n);
         rc = rc || dalloc(C, &d.lo, (size_t)n);
         rc = rc || dalloc(C, &d.pq, (size_t)n);
+        rc = rc || dalloc(C, &d.pqs, (size_t)n);
         rc = rc || dalloc(C, &d.ph, (size_t)n);
         rc = rc || dalloc(C, &d.pl, (size_t)n);
         {
@@ -1547,9 +1566,9 @@ int mtg_optimize(mtg_ctx* c, double accuracy, int max_steps, int out_stride, mtg
 int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
     if(!c || steps <= 0 || !phase_ms) return MTG_E_INVALID;
     CUDA_TRY(c, cudaSetDevice(c->device));
-    cudaEvent_t ev[5];
+    cudaEvent_t ev[6];
     for(auto& e : ev) CUDA_TRY(c, cudaEventCreate(&e));
-    double acc[4] = {0, 0, 0, 0};
+    double acc[5] = {0, 0, 0, 0, 0};
     launch_prologue(c->d, c->P, c->stream);
     take_snapshot(c);
     clear_overflow(c);
@@ -1569,10 +1588,12 @@ int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
         else launch_prod_force(c->d, c->P, false, c->stream);
         cudaEventRecord(ev[3], c->stream);
         if(is_reference(c)) launch_ref_kick2(c->d, c->P, false, c->stream);
-        else launch_prod_kick2(c->d, c->P, false, c->stream);
+        else launch_prod_kick2(c->d, c->P, false, c->stream, kKick2Atoms);
         cudaEventRecord(ev[4], c->stream);
-        CUDA_TRY(c, cudaEventSynchronize(ev[4]));
-        for(int q = 0; q < 4; q++) {
+        if(!is_reference(c)) launch_prod_kick2(c->d, c->P, false, c->stream, kKick2StepEnd);
+        cudaEventRecord(ev[5], c->stream);
+        CUDA_TRY(c, cudaEventSynchronize(ev[5]));
+        for(int q = 0; q < 5; q++) {
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
             acc[q] += ms;
@@ -1587,7 +1608,7 @@ int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
         if(rc) return rc;
         return fail(c, MTG_E_OVERFLOW, "list grew during profiling; state restored, call again");
     }
-    for(int q = 0; q < 4; q++) phase_ms[q] = acc[q] / steps;
+    for(int q = 0; q < 5; q++) phase_ms[q] = acc[q] / steps;
     return settle_state(c);
 }
 
@@ -1674,13 +1695,24 @@ int mtg_batch_create(const mtg_system_desc* const* systems, int32_t nrep, const 
             mobile.push_back(s->mobile ? s->mobile[i] : 1);
         }
         molbase += mmax + 1;
-        auto add_topo = [&](std::vector<int32_t>& dst, int cnt, const int32_t* src, int w) {
+        // a topology index must name an atom of its own replica: offset into the merged system,
+        // an index in [n, N) would silently join atoms of different replicas
+        auto add_topo = [&](std::vector<int32_t>& dst, int cnt, const int32_t* src, int w) -> bool {
             for(int j = 0; j < cnt; j++)
-                for(int k = 0; k < w; k++) dst.push_back(k < w - 1 ? src[w * j + k] + off : src[w * j + k]);
+                for(int k = 0; k < w; k++) {
+                    const int32_t v = src[w * j + k];
+                    if(k < w - 1 && (v < 0 || v >= n)) return false;
+                    dst.push_back(k < w - 1 ? v + off : v);
+                }
+            return true;
         };
-        if(s->n_bonds > 0 && s->bonds) add_topo(bonds, s->n_bonds, s->bonds, 3);
-        if(s->n_angles > 0 && s->angles) add_topo(angles, s->n_angles, s->angles, 4);
-        if(s->n_dihedrals > 0 && s->dihedrals) add_topo(dihs, s->n_dihedrals, s->dihedrals, 5);
+        if((s->n_bonds > 0 && s->bonds && !add_topo(bonds, s->n_bonds, s->bonds, 3)) ||
+           (s->n_angles > 0 && s->angles && !add_topo(angles, s->n_angles, s->angles, 4)) ||
+           (s->n_dihedrals > 0 && s->dihedrals && !add_topo(dihs, s->n_dihedrals, s->dihedrals, 5))) {
+            char msg[160];
+            std::snprintf(msg, sizeof msg, "replica %d: a bond, angle or dihedral index lies outside its %d atoms", rr, n);
+            return fail(nullptr, MTG_E_INVALID, msg);
+        }
         off += n;
     }
     bs.off.push_back(off);
@@ -2330,23 +2362,17 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[MTG_NOALLOC_SCR
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_addr[kMaxDevices] = {};
-
 size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Address of g_noalloc_scratch on `dev` (the current device), looked up once per device.
-cudaError_t noalloc_scratch(int dev, void** out) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if(!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if(e != cudaSuccess) return e;
-        g_noalloc_addr[dev] = p;
-    }
-    *out = g_noalloc_addr[dev];
-    return cudaSuccess;
+// Address of g_noalloc_scratch in the current device's context, looked up on every call.  The
+// lookup is a host-side table read once the module is loaded; caching it per device number would
+// go stale when the caller resets the device or makes another context current.  The first call on
+// a device also loads this library's module there.
+cudaError_t noalloc_scratch(void** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if(e == cudaSuccess) *out = p;
+    return e;
 }
 
 // True when p is device (or managed) memory usable by device `dev`.
@@ -2396,14 +2422,14 @@ extern "C" int mtg_neighbors_noalloc(const double* d_r, int32_t n, const double 
     }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if(e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if(e != cudaSuccess || dev < 0) {
         (void)cudaGetLastError();
         return fail(nullptr, MTG_E_CUDA, "mtg_neighbors_noalloc: no current CUDA device");
     }
     if(!on_device(d_r, dev) || !on_device(d_count, dev) || (d_list && !on_device(d_list, dev)))
         return fail(nullptr, MTG_E_INVALID, "mtg_neighbors_noalloc: d_r, d_count and d_list must be device memory of the current device");
     void* base = nullptr;
-    e = noalloc_scratch(dev, &base);
+    e = noalloc_scratch(&base);
     if(e != cudaSuccess) {
         (void)cudaGetLastError();
         return fail(nullptr, MTG_E_CUDA, std::string("mtg_neighbors_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));

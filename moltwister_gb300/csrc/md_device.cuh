@@ -732,28 +732,24 @@ __device__ inline bool last_block(unsigned int* counter) {
     return is_last;
 }
 
-__device__ inline int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
-                                       bool fixed, bool dfloat = false) {
-    if(dfloat) {
-        switch(M) {
-        case 2: return nh_chain_half_3w_df<2>(X, g, kT, dt, M, nresp, seq);
-        case 3: return nh_chain_half_3w_df<3>(X, g, kT, dt, M, nresp, seq);
-        case 4: return nh_chain_half_3w_df<4>(X, g, kT, dt, M, nresp, seq);
-        case 5: return nh_chain_half_3w_df<5>(X, g, kT, dt, M, nresp, seq);
-        case 6: return nh_chain_half_3w_df<6>(X, g, kT, dt, M, nresp, seq);
-        case 8: return nh_chain_half_3w_df<8>(X, g, kT, dt, M, nresp, seq);
-        default: return nh_chain_half_3w_df<0>(X, g, kT, dt, M, nresp, seq);
-        }
-    }
-    switch(M) {
-    case 2: return nh_chain_half_3w_t<2>(X, g, kT, dt, M, nresp, seq, fixed);
-    case 3: return nh_chain_half_3w_t<3>(X, g, kT, dt, M, nresp, seq, fixed);
-    case 4: return nh_chain_half_3w_t<4>(X, g, kT, dt, M, nresp, seq, fixed);
-    case 5: return nh_chain_half_3w_t<5>(X, g, kT, dt, M, nresp, seq, fixed);
-    case 6: return nh_chain_half_3w_t<6>(X, g, kT, dt, M, nresp, seq, fixed);
-    case 8: return nh_chain_half_3w_t<8>(X, g, kT, dt, M, nresp, seq, fixed);
-    default: return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq, fixed);
-    }
+// One chain half-step on warps 0..2.  Kept out of line: a kernel calls it for both half-steps,
+// and one body per kernel keeps the code (and its compile time) small.  Chains of the default
+// length 4 use register arrays; other lengths run the runtime-length form in its own function, so
+// that its local arrays do not reach the default path.
+static __device__ __noinline__ int nh_chain_half_3w_m4(NhExchange& X, double g, double kT, double dt, int nresp, int seq,
+                                                bool fixed, bool dfloat) {
+    if(dfloat) return nh_chain_half_3w_df<4>(X, g, kT, dt, 4, nresp, seq);
+    return nh_chain_half_3w_t<4>(X, g, kT, dt, 4, nresp, seq, fixed);
+}
+static __device__ __noinline__ int nh_chain_half_3w_any(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
+                                                 bool fixed, bool dfloat) {
+    if(dfloat) return nh_chain_half_3w_df<0>(X, g, kT, dt, M, nresp, seq);
+    return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq, fixed);
+}
+__device__ __forceinline__ int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
+                                                bool fixed, bool dfloat) {
+    return M == 4 ? nh_chain_half_3w_m4(X, g, kT, dt, nresp, seq, fixed, dfloat)
+                  : nh_chain_half_3w_any(X, g, kT, dt, M, nresp, seq, fixed, dfloat);
 }
 
 __device__ __forceinline__ void bar96() { asm volatile("bar.sync 1, 96;" ::: "memory"); }

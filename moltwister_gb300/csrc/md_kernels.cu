@@ -4,20 +4,22 @@
 // Layout in HBM (per atom):
 //   FP64 mode : r double[3] (master), p double[3], F double[3]
 //   mixed     : hi float4 (x,y,z hi, charge), lo float4 (x,y,z lo, type bits) -- the positions
-//               as double-float pairs -- pq uint4 (x,y,z as 32-bit box fractions, type), ph / pl
-//               float4 (momenta as double-float pairs, 1/m in .w), F int64 x3 (SoA, 2^26 units
-//               per kJ/mol/A: per-pair contributions are rounded to fixed point and summed
-//               exactly, so the result does not depend on summation order); r and p double[3]
-//               are the masters the host reads and writes (k_sync).
-// Neighbour list: [atom][slot] uint32, atom index in the low 29 bits and the exclusion class of
-// the pair (none, 1-2, 1-3, 1-4, same molecule; FunctorCalcForce.cpp:95-157) in the top 3 bits.
-// Pairs whose class scale is exactly 0 are left out of the list.  Rebuilt when an atom has moved
-// more than skin/2 since the last build.
+//               as double-float pairs -- pq uint4 (x,y,z as 32-bit box fractions, type) with a
+//               copy pqs in cell order, ph / pl float4 (momenta as double-float pairs, 1/m in .w),
+//               F int64 x3 (SoA, 2^26 units per kJ/mol/A); r and p double[3] are the masters the
+//               host reads and writes (k_sync).
+// Neighbour list: one row per slot (the atom's position in cell order at the last build) of
+// uint32 entries, the partner's slot in the low 29 bits and the exclusion class of the pair (none,
+// 1-2, 1-3, 1-4, same molecule; FunctorCalcForce.cpp:95-157) in the top 3 bits.  Pairs whose class
+// scale is exactly 0 are left out of the list.  Rebuilt when an atom has moved more than skin/2
+// since the last build.
 //
 // The force gather keeps the reference's structure (FunctorCalcForce.cpp:159-281): each atom sums
 // its own bonded terms, its neighbours and (cutoff) Coulomb, using the full list, so no atomics are
-// needed and the energy bookkeeping (pair energy on the lower index, angle energy on the centre,
-// half the dihedral energy on each centre atom) is the reference's.
+// needed and the energy bookkeeping (pair energy once per pair, angle energy on the centre, half
+// the dihedral energy on each centre atom) follows the reference.  Mixed mode sums each group of
+// 16 consecutive row entries in FP32 and adds the group exactly to an int64 fixed-point total, so
+// a force depends only on the list, not on the lane count or scheduling.
 #include <float.h>
 #include <stdint.h>
 
@@ -213,6 +215,7 @@ __device__ __forceinline__ void store_pos(const DevSys& d, const double* conv, i
         q.y = frac32_df(Y, df_of(conv[1]));
         q.z = frac32_df(Z, df_of(conv[2]));
         d.pq[i] = q;
+        d.pqs[d.slot_of[i]] = q;
     } else {
         d.r[3 * i] = x;
         d.r[3 * i + 1] = y;
@@ -417,7 +420,9 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
         d.pl[k] = make_float4(p[0].l, p[1].l, p[2].l, pl.w);
         d.hi[k] = make_float4(x[0].h, x[1].h, x[2].h, h.w);
         d.lo[k] = make_float4(x[0].l, x[1].l, x[2].l, l.w);
-        d.pq[k] = make_uint4(q[0], q[1], q[2], (unsigned int)__float_as_int(l.w));
+        const uint4 qk = make_uint4(q[0], q[1], q[2], (unsigned int)__float_as_int(l.w));
+        d.pq[k] = qk;
+        d.pqs[d.slot_of[k]] = qk;   // the force gather reads positions in cell (slot) order
         if(d2 > K.h2) d.sc->rebuild = 1;
     }
     if(cond) {
@@ -584,7 +589,11 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
     d.vcount[d.pcell_first[c] + slot] = i;   // vcount doubles as scratch until the list kernel
 }
 
-__global__ void k_pcell_rank(DevSys d, int ncell) {
+// Atoms of a cell ordered by index (a rank pass, deterministic).  The position in the resulting
+// cell order is the atom's slot: the Verlet list is kept per slot with partners named by slot,
+// and the positions the force gather reads are copied into slot order, so the partners of the
+// atoms a block works on lie in a compact, cache-resident range.
+__global__ void k_pcell_rank(DevSys d, int ncell, bool mixed) {
     if(!d.sc->rebuild) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(warp >= ncell) return;
@@ -594,7 +603,11 @@ __global__ void k_pcell_rank(DevSys d, int ncell) {
         const int v = tmp[first + a];
         int rank = 0;
         for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < v);
-        d.pcell_list[first + rank] = v;
+        const int slot = first + rank;
+        d.pcell_list[slot] = v;
+        d.slot_of[v] = slot;
+        d.rb4s[slot] = d.rb4[v];
+        if(mixed) d.pqs[slot] = d.pq[v];
     }
 }
 
@@ -611,12 +624,13 @@ __device__ __forceinline__ int excl_class(const DevSys& d, int k, int i) {
 template<bool MIXED>
 __global__ void k_vlist(DevSys d, Params P) {
     if(!d.sc->rebuild) return;
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if(i >= P.n) return;
+    const int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if(si >= P.n) return;
+    const int i = d.pcell_list[si];
     const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
     const float rfull = fmaxf(v.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? v.rcoul : 0.0f);
     // FP32 distances: rounding (~1e-6 A) is far inside the skin margin
-    const float4 ri = d.rb4[i];
+    const float4 ri = d.rb4s[si];
     const int ti = __float_as_int(ri.w);
     // list radius of pair (ti, tj): its own short-range cutoff (at most rc), widened to rcoul when
     // charges are on, plus the skin; a pair outside that radius cannot interact before the next
@@ -632,7 +646,7 @@ __global__ void k_vlist(DevSys d, Params P) {
     const int ci = d.pcell_of[i] - v.cbase;
     const int cx = ci % v.pnx, cy = (ci / v.pnx) % v.pny, cz = ci / (v.pnx * v.pny);
     const int sx = v.pnx >= 3 ? 3 : 1, sy = v.pny >= 3 ? 3 : 1, sz = v.pnz >= 3 ? 3 : 1;
-    uint32_t* out = d.vlist + (size_t)i * d.vmax;
+    uint32_t* out = d.vlist + (size_t)si * d.vmax;
     int cnt = 0;
     for(int oz = 0; oz < sz; oz++) {
         const int z = sz == 1 ? 0 : (cz + oz - 1 + v.pnz) % v.pnz;
@@ -646,17 +660,17 @@ __global__ void k_vlist(DevSys d, Params P) {
                     bool take = false;
                     uint32_t entry = 0;
                     if(base + lane < n) {
-                        const int j = d.pcell_list[first + base + lane];
-                        if(j != i) {
-                            const float4 rj = d.rb4[j];
+                        const int sj = first + base + lane;
+                        if(sj != si) {
+                            const float4 rj = d.rb4s[sj];
                             const float dx = minimg_f(ri.x - rj.x, Lx, iLx);
                             const float dy = minimg_f(ri.y - rj.y, Ly, iLy);
                             const float dz = minimg_f(ri.z - rj.z, Lz, iLz);
                             if(dx * dx + dy * dy + dz * dz < list_r2(__float_as_int(rj.w))) {
-                                const int cls = excl_class(d, i, j);
+                                const int cls = excl_class(d, i, d.pcell_list[sj]);
                                 if(P.scale[cls] != 0.0f) {
                                     take = true;
-                                    entry = (uint32_t)j | ((uint32_t)cls << kClassShift);
+                                    entry = (uint32_t)sj | ((uint32_t)cls << kClassShift);
                                 }
                             }
                         }
@@ -672,7 +686,7 @@ __global__ void k_vlist(DevSys d, Params P) {
         }
     }
     if(lane == 0) {
-        d.vcount[i] = cnt;
+        d.vcount[si] = cnt;
         if(cnt > d.vmax) {
             d.sc->overflow = 1;
             atomicMax(&d.sc->needed, cnt);
@@ -1006,17 +1020,18 @@ struct PairCoef {
 };
 constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
 
-// One list entry of atom i in FP32 (mixed path), added to the fixed-point sums (fx, fy, fz, fu).
-// The cutoff tests select instead of branching: out-of-range entries, about a quarter of a list
-// with a skin, would otherwise split the warp.  g is clamped to gmax so that |g d| < 2^18.
+// One list entry of the atom in slot si in FP32 (mixed path): adds g d to (ax, ay, az) and, for
+// the pair's lower slot, its energy to au.  The cutoff tests select instead of branching:
+// out-of-range entries, about a quarter of a list with a skin, would otherwise split the warp.
+// An entry naming the atom itself (the padding of a row's last group) contributes exact zeros.
 template<bool ENERGY>
-__device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, float qi,
-                                           float rc2, float rq2, float irc, float gmax, const PairCoef* pc,
-                                           const float* us, const float* qt, uint4 qi4, const float (&fs)[3],
-                                           Fix& fx, Fix& fy, Fix& fz, Fix& fu) {
-    const int j = (int)(ent & kIdxMask);
+__device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int si, uint32_t ent, int ti, float qi,
+                                           float rc2, float rq2, float irc, const PairCoef* pc, const float* us,
+                                           const float* qt, uint4 qi4, const float (&fs)[3], float& ax, float& ay,
+                                           float& az, float& au) {
+    const int sj = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
-    const uint4 qj4 = d.pq[j];
+    const uint4 qj4 = d.pqs[sj];
     const float dx = __int2float_rn((int)(qi4.x - qj4.x)) * fs[0];
     const float dy = __int2float_rn((int)(qi4.y - qj4.y)) * fs[1];
     const float dz = __int2float_rn((int)(qi4.z - qj4.z)) * fs[2];
@@ -1043,7 +1058,7 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
         pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
     }
     if(P.qon) {
-        const float qq = kCoulombKf * qi * (qt ? qt[tj] : d.qf[j]);
+        const float qq = kCoulombKf * qi * (qt ? qt[tj] : d.qf[d.pcell_list[sj]]);
         const bool inq = live && r2 < rq2;
         float gq, uq = 0.0f;
         if(P.coulomb == MTG_COULOMB_SHIFTED) {
@@ -1061,18 +1076,24 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
         g *= sc;
         u *= sc;
     }
-    const float g16 = __fmul_rn(fminf(fmaxf(g, -gmax), gmax), 16.0f);
-    fix_add16(fx, __fmul_rn(g16, dx));
-    fix_add16(fy, __fmul_rn(g16, dy));
-    fix_add16(fz, __fmul_rn(g16, dz));
-    if(ENERGY && j > i) fix_add_clamped(fu, u);
+    ax = __fmaf_rn(g, dx, ax);
+    ay = __fmaf_rn(g, dy, ay);
+    az = __fmaf_rn(g, dz, az);
+    if(ENERGY && sj > si) au += u;
 }
 
-// Force gather: TEAM lanes per atom (8, 16 or 32; chosen per system by the autotuner), each lane
-// walking its share of the atom's neighbour-list row four entries at a time so that four gathers
-// are in flight per lane.  Bonded terms of the atom are spread over the team's lanes.  Mixed:
-// every contribution is rounded to the 2^-26 fixed-point grid and summed as an integer, so
-// forces do not depend on the team size, on the list order or on out-of-range list entries.
+// Entries of a Verlet-list row are taken in groups of kGroup consecutive entries.  A group is
+// summed in FP32 in list order, then added to the atom's int64 fixed-point total exactly, so the
+// force depends only on the row (its content and order, both fixed by the list build), not on
+// how many lanes share the row or which lane takes which group.
+constexpr int kGroup = 16;
+
+// Force gather: TEAM lanes per atom (8, 16 or 32; chosen per system by the autotuner), atoms taken
+// in cell (slot) order so that a block's neighbour gathers stay within a compact, cache-resident
+// range of the slot-ordered positions.  Mixed: lane l takes groups l, l + TEAM, ... of the row,
+// loading each group's 16 entries as four 16-byte vectors so that all its position gathers are in
+// flight together.  FP64: four entries per lane in flight, summed in FP64.  Bonded terms of the
+// atom are spread over the team's lanes.
 template<bool MIXED, bool ENERGY, int TEAM>
 __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     using R = typename std::conditional<MIXED, float, double>::type;
@@ -1102,8 +1123,9 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         if(P.qtype) qt = qt_s;
     }
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = gt / TEAM, lane = gt % TEAM;
-    const bool active = i < P.n;
+    const int si = gt / TEAM, lane = gt % TEAM;
+    const bool active = si < P.n;
+    const int i = active ? d.pcell_list[si] : 0;
     const bool mob = active && d.mobile[i] != 0;
     Fix fx{0, 0}, fy{0, 0}, fz{0, 0}, fu{0, 0};   // mixed: exact fixed point
     double bx = 0, by = 0, bz = 0, bu = 0;        // fp64
@@ -1112,33 +1134,44 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         const R rc2 = (R)v.rc * (R)v.rc;
         const R rq2 = (R)v.rcoul * (R)v.rcoul;
         const R irc = R(1) / (R)v.rcoul;
-        const int cnt = min(d.vcount[i], d.vmax);   // an overflowed build is redone; stay in the row
-        const uint32_t* lst = d.vlist + (size_t)i * d.vmax;
+        const int cnt = min(d.vcount[si], d.vmax);   // an overflowed build is redone; stay in the row
+        const uint32_t* lst = d.vlist + (size_t)si * d.vmax;
         if constexpr(MIXED) {
             const float fs[3] = {v.fscale[0], v.fscale[1], v.fscale[2]};
-            const float gmax = 262143.0f / (v.rc + v.rcoul + v.skin);   // |d| < rc + rcoul + skin
-            const uint4 qi4 = d.pq[i];
+            const uint4 qi4 = d.pqs[si];
             const int ti = (int)qi4.w;
             const float qi = d.qf[i];
-            int e = lane;
-            for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
-                uint32_t ent[4];
+            // rows start on 128-byte boundaries (vmax is a multiple of 32) and a group never
+            // crosses the row's end, so the vector loads stay inside the row
+            for(int e0 = lane * kGroup; e0 < cnt; e0 += TEAM * kGroup) {
+                float ax = 0.0f, ay = 0.0f, az = 0.0f, au = 0.0f;
 #pragma unroll
-                for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
+                for(int c = 0; c < kGroup / 4; c++) {
+                    const uint4 E = __ldg(reinterpret_cast<const uint4*>(lst + e0) + c);
+                    const uint32_t ent[4] = {E.x, E.y, E.z, E.w};
 #pragma unroll
-                for(int q = 0; q < 4; q++)
-                    pair_mixed<ENERGY>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
+                    for(int q = 0; q < 4; q++) {
+                        const uint32_t use = (e0 + 4 * c + q < cnt) ? ent[q] : (uint32_t)si;
+                        pair_mixed<ENERGY>(d, P, si, use, ti, qi, rc2, rq2, irc, pc, us_s, qt, qi4, fs, ax, ay, az, au);
+                    }
+                }
+                fix_add_clamped(fx, ax);
+                fix_add_clamped(fy, ay);
+                fix_add_clamped(fz, az);
+                if(ENERGY) fix_add_clamped(fu, au);
             }
-            for(; e < cnt; e += TEAM)
-                pair_mixed<ENERGY>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
         } else {
             const int ti = d.type[i];
             const double qi = d.qd[i];
+            // list entries name slots; the FP64 path works on atom indices
+            auto atom_entry = [&](uint32_t ent) -> uint32_t {
+                return (uint32_t)d.pcell_list[ent & kIdxMask] | (ent & ~kIdxMask);
+            };
             int e = lane;
             for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
                 uint32_t ent[4];
 #pragma unroll
-                for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
+                for(int q = 0; q < 4; q++) ent[q] = atom_entry(__ldg(lst + e + q * TEAM));
 #pragma unroll
                 for(int q = 0; q < 4; q++) {
                     double dx, dy, dz, g, u;
@@ -1149,7 +1182,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
             }
             for(; e < cnt; e += TEAM) {
                 double dx, dy, dz, g, u;
-                pair_entry_d<ENERGY>(d, P, i, __ldg(lst + e), ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
+                pair_entry_d<ENERGY>(d, P, i, atom_entry(__ldg(lst + e)), ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
                 bx += g * dx; by += g * dy; bz += g * dz;
                 if(ENERGY) bu += u;
             }
@@ -1221,8 +1254,10 @@ __global__ void k_sync(DevSys d, Params P, int mode) {
     const DF x = df_of(d.r[3 * i]), y = df_of(d.r[3 * i + 1]), z = df_of(d.r[3 * i + 2]);
     d.hi[i] = make_float4(x.h, y.h, z.h, d.qf[i]);
     d.lo[i] = make_float4(x.l, y.l, z.l, __int_as_float(d.type[i]));
-    d.pq[i] = make_uint4(frac32_df(x, df_of(v.fconv[0])), frac32_df(y, df_of(v.fconv[1])), frac32_df(z, df_of(v.fconv[2])),
-                         (unsigned int)d.type[i]);
+    const uint4 qi = make_uint4(frac32_df(x, df_of(v.fconv[0])), frac32_df(y, df_of(v.fconv[1])),
+                                frac32_df(z, df_of(v.fconv[2])), (unsigned int)d.type[i]);
+    d.pq[i] = qi;
+    d.pqs[d.slot_of[i]] = qi;
     if(mode == kSyncFromMaster) {
         const DF px = df_of(d.p[3 * i]), py = df_of(d.p[3 * i + 1]), pz = df_of(d.p[3 * i + 2]);
         const DF im = df_of(1.0 / d.m[i]);
@@ -1333,7 +1368,7 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     k_pcell_scan<<<1, 1024, 0, s>>>(d, ncell);
     k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell);
+    k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell, P.precision == MTG_PREC_MIXED);
     if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     k_clear_rebuild<<<1, 32, 0, s>>>(d);
@@ -1358,18 +1393,19 @@ void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream
     }
 }
 
-void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s) {
+void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s, int parts) {
     const int nb = integration_blocks(P);
     if(P.precision == MTG_PREC_MIXED) {
         const int nsys = P.nrep ? P.nrep : 1;
-        if(output) {
-            k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
-            k_mstep_end<true><<<nsys, 96, 0, s>>>(d, P);
-        } else {
-            k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
-            k_mstep_end<false><<<nsys, 96, 0, s>>>(d, P);
+        if(parts & kKick2Atoms) {
+            if(output) k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
+            else k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
         }
-    } else {
+        if(parts & kKick2StepEnd) {
+            if(output) k_mstep_end<true><<<nsys, 96, 0, s>>>(d, P);
+            else k_mstep_end<false><<<nsys, 96, 0, s>>>(d, P);
+        }
+    } else if(parts & kKick2Atoms) {
         if(output) k_pkick2<true><<<nb, 256, 0, s>>>(d, P);
         else k_pkick2<false><<<nb, 256, 0, s>>>(d, P);
     }

@@ -171,16 +171,19 @@ struct DevSys {
     int* pcell_first;     // [pncell]
     int* pcell_count;     // [pncell]
     int* pcell_cursor;    // [pncell]
-    int* pcell_list;      // [n]
-    uint32_t* vlist;      // [n * vmax]
-    int* vcount;          // [n]
+    int* pcell_list;      // [n] atoms in cell order: slot -> atom (identity before the first build)
+    int* slot_of;         // [n] atom -> slot (inverse of pcell_list)
+    uint32_t* vlist;      // [n * vmax] one row per slot; entries are slots of the partners
+    int* vcount;          // [n] per slot
     int vmax;
     double* r_build;      // [3n] positions at the last build (displacement check)
-    float4* rb4;          // [n]  the same in FP32 (list distances)
+    float4* rb4;          // [n]  the same in FP32 (displacement test), per atom
+    float4* rb4s;         // [n]  the same per slot (list distances)
     // mixed
     float4* hi;           // [n] x,y,z hi, charge
     float4* lo;           // [n] x,y,z lo, type bits
     uint4* pq;            // [n] x,y,z as 32-bit fractions of the box (wrap = minimum image), type
+    uint4* pqs;           // [n] the same per slot (cell order), refreshed wherever pq is written
     float4* ph;           // [n] mixed: momenta x,y,z hi, 1/m hi (double-float pairs with pl)
     float4* pl;           // [n] mixed: momenta x,y,z lo, 1/m lo
     const float* qtype;   // [T] charge of each type when every atom of a type has the same charge
@@ -230,7 +233,11 @@ void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s);
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond = 0);
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s);
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s);
-void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s);
+// Second half of the step: the per-atom kick and block sums (kKick2Atoms) and, in mixed mode, the
+// one-block-per-system step end with the thermostat chain (kKick2StepEnd; FP64 mode runs its chain
+// in the last block of the per-atom kernel).
+enum Kick2Parts { kKick2Atoms = 1, kKick2StepEnd = 2, kKick2All = 3 };
+void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s, int parts = kKick2All);
 // Mixed mode keeps positions and momenta as double-float pairs (hi/lo, ph/pl) plus the box
 // fractions pq; the FP64 arrays r and p are the masters the host reads and writes.
 enum SyncMode { kSyncToMaster = 0, kSyncFromMaster = 1, kSyncPositionsFromMaster = 2 };

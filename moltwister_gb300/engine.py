@@ -446,9 +446,9 @@ class Engine:
 
     def profile_phases(self, steps: int) -> dict:
         """Mean device ms per step of each phase (C ABI mtg_profile_phases)."""
-        out = np.zeros(4)
+        out = np.zeros(5)
         self._check(self.lib.mtg_profile_phases(self.h, int(steps), _ptr(out)))
-        return {"kick_drift": out[0], "list": out[1], "force": out[2], "kick_reduce": out[3]}
+        return {"kick_drift": out[0], "list": out[1], "force": out[2], "kick_reduce": out[3], "step_end": out[4]}
 
     # -- parity hooks ----------------------------------------------------------------------------------
     def forces(self):

@@ -2,7 +2,7 @@
 
 Run from the repository root after building the oracle harness (needs the reference sources):
 
-    make -C oracle/ref REF=/root/reference && python tests/golden/make_golden.py [case ...]
+    make -C oracle/ref REF=<MolTwister source tree> && python tests/golden/make_golden.py [case ...]
 
 Each case is a seeded synthetic system (moltwister_gb300/workloads.py).  The harness
 (oracle/ref/harness.cpp, linked from the unmodified reference sources) builds the
@@ -65,11 +65,39 @@ def cases():
     return out
 
 
-def pack(name, s, c, steps, stride):
+def big_cases():
+    """The two BASELINE-sized parity cases.  Their neighbour lists are stored as one 64-bit hash
+    per atom (golden_cases.neighbour_hash) and their trajectories without forces, which keeps the
+    fixtures near a megabyte each."""
+    out = {}
+    # argon, 4,000 atoms: FCC 10^3 cells, cutoff 2.5 sigma, shell 2 A -> 5^3 cells, NVT, dt 2 fs
+    s, c = W.argon(ncell=10, seed=1)
+    out["argon4000_nvt"] = (s, c, 100, 50)
+    # flexible water, 9,000 atoms in a 44.8 A box, reference all-pairs Coulomb, 10 A cutoff and
+    # shell 2 A -> 3^3 cells, NVT 300 K, dt 0.5 fs
+    s, c = W.water(n_mol=3000, L=44.8, seed=2, rc=10.0, dt=0.5)
+    out["water9000_ref"] = (s, c, 100, 50)
+    return out
+
+
+def pack(name, s, c, steps, stride, big=False):
     st = harness_static(s, c)
     tr = harness_run(s, c, steps, stride)
     cnt = st["neigh_count"]
     maxc = int(cnt.max()) if cnt.size else 0
+    if big:
+        from tests.golden_cases import neighbour_hash
+        nb = dict(neigh_count=cnt, neigh_hash=neighbour_hash(cnt, st["neigh_list"][:, :maxc]),
+                  neigh_max=np.array(maxc))
+        traj = dict(traj_r=tr["traj_r"], traj_p=tr["traj_p"])
+        # a short prefix (one record) that the CPU oracle can replay within seconds
+        k = 10 if s.n <= 4000 else 4
+        pre = harness_run(s, c, k, k)
+        traj.update(prefix_steps=np.array(k), prefix_r=pre["traj_r"][-1], prefix_p=pre["traj_p"][-1],
+                    prefix_scalars=pre["traj_scalars"][-1])
+    else:
+        nb = dict(neigh_count=cnt, neigh_list=st["neigh_list"][:, :maxc])
+        traj = dict(traj_r=tr["traj_r"], traj_p=tr["traj_p"], traj_F=tr["traj_F"], traj_U=tr["traj_U"])
     terms = {
         "nonbonded": [dataclasses.asdict(t) for t in s.nonbonded],
         "bond_terms": [dataclasses.asdict(t) for t in s.bond_terms],
@@ -90,9 +118,7 @@ def pack(name, s, c, steps, stride):
         atom_type=st["atom_type"], atom_mol=st["atom_mol"],
         bonds=st["bonds"], angles=st["angles"], dihedrals=st["dihedrals"],
         cell_dims=st["cell_dims"], atom_cell=st["atom_cell"], cell_ptr=st["cell_ptr"], cell_list=st["cell_list"],
-        neigh_count=cnt, neigh_list=st["neigh_list"][:, :maxc],
-        F=st["F"], U=st["U"],
-        traj_r=tr["traj_r"], traj_p=tr["traj_p"], traj_F=tr["traj_F"], traj_U=tr["traj_U"],
+        F=st["F"], U=st["U"], **nb, **traj,
         traj_scalars=tr["traj_scalars"], traj_nhT=tr["traj_nhT"],
         traj_nhP=tr["traj_nhP"], traj_peps=tr["traj_peps"],
     )
@@ -118,10 +144,11 @@ def make_dcd(name="water648_nvt"):
 
 
 def main(only=()):
-    for name, (s, c, steps, stride) in cases().items():
+    todo = [(k, v, False) for k, v in cases().items()] + [(k, v, True) for k, v in big_cases().items()]
+    for name, (s, c, steps, stride), big in todo:
         if only and name not in only:
             continue
-        p = pack(name, s, c, steps, stride)
+        p = pack(name, s, c, steps, stride, big=big)
         print(f"{name}: {os.path.getsize(p) / 1024:.0f} KiB")
 
 

@@ -15,6 +15,38 @@ from moltwister_gb300.system import (AngleTerm, BondTerm, DihedralTerm, MDConfig
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+def neighbour_hash(count: np.ndarray, lists: np.ndarray) -> np.ndarray:
+    """One 64-bit FNV-1a hash per atom over its ordered neighbour indices (int32, little endian
+    bytes), for fixtures too large to store whole lists: equal hashes and counts stand for equal
+    ordered lists.  `lists` is [n, >= max(count)]; entries past an atom's count are ignored."""
+    count = np.asarray(count, np.int64)
+    lists = np.asarray(lists)
+    h = np.full(count.shape[0], 0xCBF29CE484222325, np.uint64)
+    prime = np.uint64(0x100000001B3)
+    width = int(count.max()) if count.size else 0
+    with np.errstate(over="ignore"):
+        for col in range(width):
+            live = col < count
+            v = lists[:, col].astype(np.int64).astype(np.uint32)
+            g = h.copy()
+            for b in range(4):
+                g = (g ^ ((v >> np.uint32(8 * b)) & np.uint32(0xFF)).astype(np.uint64)) * prime
+            h = np.where(live, g, h)
+    return h
+
+
+def neighbours_match(d, cnt: np.ndarray, lst: np.ndarray) -> bool:
+    """Ordered neighbour lists equal to a fixture's (whole lists, or hashes for the large cases)."""
+    if not np.array_equal(cnt, d["neigh_count"]):
+        return False
+    if "neigh_hash" in d:
+        return bool(np.array_equal(neighbour_hash(cnt, lst), d["neigh_hash"]))
+    for k in range(cnt.shape[0]):
+        if not np.array_equal(lst[k, :cnt[k]], d["neigh_list"][k, :cnt[k]]):
+            return False
+    return True
+
+
 def names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
 

@@ -97,3 +97,14 @@ def test_batch_temperatures_and_cutoffs_are_checked():
     assert code == INVALID and "temperatures" in msg
     code, msg = batch_code([a, b], c, cutoffs=[c.cutoffradius, 2.0 * c.cutoffradius])
     assert code == INVALID and "cutoffs" in msg
+
+
+def test_batch_topology_index_outside_its_replica():
+    # a bond index in [n_r, N) exists in the merged system but would join atoms of two replicas
+    w, c = W.water(n_mol=8, L=12.0, seed=2)
+    a, _ = W.argon(ncell=2, seed=1)
+    c.precision, c.coulomb, c.coulombcutoff = "mixed", "shifted", 5.0
+    w.bonds = np.asarray(w.bonds).copy()
+    w.bonds[0, 1] = w.n + 1
+    code, msg = batch_code([w, a], c)
+    assert code == INVALID and "replica 0" in msg and "outside" in msg

@@ -32,10 +32,8 @@ def test_cells_and_neighbours_bit_exact(name):
     assert np.array_equal(cp, d["cell_ptr"])
     assert np.array_equal(cl, d["cell_list"])
     cnt, lst = orc.neigh_list()
-    assert np.array_equal(cnt, d["neigh_count"])
-    m = d["neigh_list"].shape[1]
-    for k in range(s.n):
-        assert np.array_equal(lst[k, :cnt[k]], d["neigh_list"][k, :cnt[k]])
+    assert G.neighbours_match(d, cnt, lst)
+    m = d["neigh_list"].shape[1] if "neigh_list" in d else int(d["neigh_max"])
     assert m == cnt.max()
 
 
@@ -50,6 +48,15 @@ def test_forces_bit_exact(name):
 @pytest.mark.parametrize("name", CASES)
 def test_trajectory_bit_exact(name):
     s, cfg, d = G.load(name)
+    if "prefix_steps" in d:
+        # the BASELINE-sized cases: the oracle replays the reference's short prefix run (the
+        # 100-step trajectory is checked against the GPU, which the oracle is pinned to here)
+        k = int(d["prefix_steps"])
+        o = O.Oracle(s, cfg).run_ref(k, k)
+        assert np.array_equal(o["r"][-1], d["prefix_r"])
+        assert np.array_equal(o["p"][-1], d["prefix_p"])
+        assert np.array_equal(o["scal"][-1], d["prefix_scalars"][1:6])
+        return
     o = O.Oracle(s, cfg).run_ref(int(d["steps"]), int(d["stride"]))
     assert np.array_equal(o["r"], d["traj_r"])
     assert np.array_equal(o["p"], d["traj_p"])
