@@ -348,10 +348,17 @@ class Engine:
             th = thermo_struct(thermo)
         self._check(self.lib.mtg_set_state(self.h, _ptr(rr), _ptr(pp), C.byref(th) if th is not None else None))
 
-    def get_state(self):
-        """(r, p, Thermo) after the last completed step."""
-        r = np.zeros((self.n, 3))
-        p = np.zeros((self.n, 3))
+    def get_state(self, out=None):
+        """(r, p, Thermo) after the last completed step.  `out` = (r, p): C-contiguous float64
+        [n, 3] arrays to fill (for instance views of pinned host memory) instead of new ones."""
+        if out is not None:
+            r, p = out
+            for a in (r, p):
+                if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError("get_state(out=...) needs C-contiguous float64 arrays of shape (n, 3)")
+        else:
+            r = np.zeros((self.n, 3))
+            p = np.zeros((self.n, 3))
         th = ThermoState()
         self._check(self.lib.mtg_get_state(self.h, _ptr(r), _ptr(p), C.byref(th)))
         return r, p, thermo_tuple(th)

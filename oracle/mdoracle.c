@@ -412,6 +412,8 @@ int orc_neigh_list(int n, const double* r, const float* L, float rc, int nx, int
     /* pbc_ of the functor: rLow = double(low), rHigh = double(low + width) computed in float */
     const double w[3] = {(double)(lx + L[0]) - (double)lx, (double)(ly + L[1]) - (double)ly, (double)(lz + L[2]) - (double)lz};
     int maxc = 0;
+    /* atoms are independent: each writes only its own count and row */
+#pragma omp parallel for schedule(static, 64) reduction(max : maxc)
     for(int k = 0; k < n; k++) {
         int c = 0;
         double x0 = r[3 * k], y0 = r[3 * k + 1], z0 = r[3 * k + 2];
@@ -539,6 +541,8 @@ int orc_forces_ref(const orc_sys* s, const int* ncount, const int* nlist, int ma
     const double w[3] = {(double)Lf[0] / 2.0 - (-(double)Lf[0] / 2.0), (double)Lf[1] / 2.0 - (-(double)Lf[1] / 2.0),
                          (double)Lf[2] / 2.0 - (-(double)Lf[2] / 2.0)};
     const int T = s->ntypes;
+    /* each atom sums its own terms in the reference's order, so the threads change no result */
+#pragma omp parallel for schedule(dynamic, 16)
     for(int k = 0; k < s->n; k++) {
         v3 Fk = mk(0, 0, 0);
         float Uk = 0.0f;
@@ -656,8 +660,42 @@ int orc_forces_ref(const orc_sys* s, const int* ncount, const int* nlist, int ma
             Fk.x += f.x; Fk.y += f.y; Fk.z += f.z;
             Uk += u;
         }
-        /* Coulomb, all atoms (FunctorCalcForce.cpp:258-278, 514-535) */
         const float qk = s->q[k];
+        if(s->coulomb_mode != 0) {
+            /* Not in the reference: Coulomb cut off at coulomb_rc (<= the list cutoff), taken over
+             * the same neighbour list with the reference's pair arithmetic (float R, double K),
+             * plain (mode 1) or shifted-force (mode 2).  It lets the CPU baseline run the same
+             * physics as the production GPU modes. */
+            const double rq = s->coulomb_rc;
+            for(int e = 0; e < ncount[k]; e++) {
+                int i = nlist[(size_t)k * maxn + e];
+                float u = 0.0f;
+                v3 ri = mk(s->r[3 * i], s->r[3 * i + 1], s->r[3 * i + 2]);
+                same_side(rk, &ri, w);
+                v3 rv = sub(rk, ri);
+                float R = (float)nrm(rv);
+                if(!((double)R < rq) || R == 0.0f) continue;
+                double K = (double)(COULOMB_KF * qk * s->q[i]);
+                double Rd = (double)R, g;
+                if(s->coulomb_mode == 2) {
+                    g = K * (1.0 / (Rd * Rd) - 1.0 / (rq * rq)) / Rd;
+                    if(i > k) u += (float)(K * (1.0 / Rd - 1.0 / rq + (Rd - rq) / (rq * rq)));
+                } else {
+                    g = K / (Rd * Rd * Rd);
+                    if(i > k) u += (float)K / R;
+                }
+                v3 f = scl(rv, g);
+                int ap;
+                float sc = exclusion_scale(s, k, i, &ap);
+                if(ap) { f = scl(f, (double)sc); u *= sc; }
+                Fk.x += f.x; Fk.y += f.y; Fk.z += f.z;
+                Uk += u;
+            }
+            F[3 * k] = Fk.x; F[3 * k + 1] = Fk.y; F[3 * k + 2] = Fk.z;
+            U[k] = Uk;
+            continue;
+        }
+        /* Coulomb, all atoms (FunctorCalcForce.cpp:258-278, 514-535) */
         for(int i = 0; i < s->n; i++) {
             float u = 0.0f;
             v3 ri = mk(s->r[3 * i], s->r[3 * i + 1], s->r[3 * i + 2]);
@@ -736,6 +774,7 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
     const int T = s->ntypes;
     const double rc2 = rcut * rcut;
     const double crc2 = s->coulomb_rc * s->coulomb_rc;
+#pragma omp parallel for schedule(dynamic, 16)
     for(int k = 0; k < s->n; k++) {
         double fx = 0, fy = 0, fz = 0, uk = 0;
         F[3 * k] = F[3 * k + 1] = F[3 * k + 2] = 0.0;
