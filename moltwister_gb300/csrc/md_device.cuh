@@ -681,152 +681,6 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
     return seq + nsub;
 }
 
-// The same half-step on one warp, as one instruction stream: the three warps' work above in
-// dependency order, with the same double-float operations on the same operands, so the result is
-// bit for bit that of the three-warp form.  Without hand-overs between warps the critical path is
-// the arithmetic alone, and the compiler overlaps the independent parts (the momentum scale of
-// step 1.4 and the top element's steps 1.6 / 1.1 with the main recurrence).  Lane l keeps eta[l]
-// for l < M-1; all lanes compute the same chain.
-template<int MM>
-__device__ inline void nh_chain_half_1w_df(NhExchange& X, double g, double kT, double dt, int M_rt, int nresp) {
-    constexpr int CAP = MM > 0 ? MM : kMaxChain;
-    const int M = MM > 0 ? MM : M_rt;
-    const int lane = threadIdx.x & 31;
-    const double w0 = sy_w0(true);
-    const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
-    const double gkT = g * kT;
-    const int top = M - 1;
-    const float tiny = 0.0009765625f;   // 2^-10
-    DF pe[CAP], iQ[CAP], cprev[CAP], xprev[CAP];
-#pragma unroll
-    for(int j = 0; j < CAP; j++) {
-        if(j < M) {
-            pe[j] = df_of(X.pe[j]);
-            iQ[j] = df_of(X.iQ[j]);
-        }
-    }
-    DF KE2 = df_of(X.KE2);
-    DF eta_mine = df_of((lane < top) ? X.eta[lane] : 0.0);
-    const DF kTD = df_of(kT), gkTD = df_of(gkT);
-    const DF DtW[2] = {df_of(w[0] * dt / double(nresp)), df_of(w[1] * dt / double(nresp))};
-    DF iQl{0.0f, 0.0f};
-#pragma unroll
-    for(int j = 0; j < CAP; j++)
-        if(j < top && j == lane) iQl = iQ[j];
-    // momentum scale (step 1.4)
-    const DF iQ0 = iQ[0];
-    DF scale{1.0f, 0.0f};
-    const DF D1W[2] = {df_neg(df_mul(DtW[0], df_scale(iQ0, 0.5f))), df_neg(df_mul(DtW[1], df_scale(iQ0, 0.5f)))};
-    // top element p_eta[M-1] (steps 1.1, 1.6)
-    const DF iQt = df_of(X.iQ[top]);
-    const DF iQm = df_of(X.iQ[top - 1]), nkT = df_of(-kT);
-    DF pt = df_of(X.pe[top]);
-    DF eta_t = df_of(X.eta[top]);
-    DF d4prev{0.0f, 0.0f};
-    int s = 0;
-    for(int mu = 0; mu < 3; mu++) {
-        const DF Dt = DtW[mu == 1 ? 1 : 0];
-        const DF d8 = df_scale(Dt, -0.125f), d4D = df_scale(Dt, 0.25f), d2 = df_scale(Dt, 0.5f);
-        DF A[CAP], D[CAP];
-#pragma unroll
-        for(int j = 0; j < CAP; j++) {
-            if(j < top) {
-                A[j] = (j > 0) ? df_mul(d4D, iQ[j - 1]) : DF{0.0f, 0.0f};
-                D[j] = df_mul(d8, iQ[j + 1]);
-            }
-        }
-        const DF nB = df_neg(df_mul(d4D, kTD)), nB0 = df_neg(df_mul(d4D, gkTD));
-        const DF E = df_mul(d2, iQl);
-        const DF D1 = D1W[mu == 1 ? 1 : 0];
-        const DF d4t = df_scale(Dt, 0.25f), Dtop = df_mul(df_scale(Dt, -0.125f), iQt), Etop = df_mul(df_scale(Dt, 0.5f), iQt);
-        for(int it = 0; it < nresp; it++, s++) {
-            // 1.6 of the previous substep, then 1.1 (the element below the top is unchanged between)
-            const DF pm = pe[top - 1];
-            if(s > 0) pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
-            pt = df_fma(d4t, df_fma(df_mul(pm, pm), iQm, nkT), pt);
-            const DF etop = df_exp_chain(df_mul(pt, Dtop));
-            eta_t = df_fma(pt, Etop, eta_t);
-            d4prev = d4t;
-            DF c12[CAP], x12[CAP], t12[CAP];
-            // 1.2
-#pragma unroll
-            for(int j = 0; j < CAP; j++) {
-                if(j >= top) continue;
-                DF c, x;
-                if(j == top - 1) {
-                    c = etop;
-                    x = DF{0.0f, 0.0f};
-                } else if(it > 0) {
-                    c = cprev[j];
-                    x = xprev[j];
-                } else {
-                    x = df_mul(pe[j + 1], D[j]);
-                    c = df_exp_chain(x);
-                }
-                c12[j] = c;
-                x12[j] = x;
-                const DF t = (j == 0) ? df_fma(KE2, d4D, nB0) : df_fma(df_mul(pe[j - 1], pe[j - 1]), A[j], nB);
-                t12[j] = t;
-                pe[j] = df_mul(df_fma(pe[j], c, t), c);
-            }
-            // 1.3
-            {
-                DF v{0.0f, 0.0f};
-#pragma unroll
-                for(int j = 0; j < CAP; j++)
-                    if(j < top && j == lane) v = pe[j];
-                if(lane < top) eta_mine = df_fma(v, E, eta_mine);
-            }
-            // 1.4
-            {
-                const DF c = df_exp_chain(df_mul(pe[0], D1));
-                scale = df_mul(scale, c);
-                KE2 = df_mul(KE2, df_mul(c, c));
-            }
-            // 1.5
-#pragma unroll
-            for(int j = CAP - 1; j >= 0; j--) {
-                if(j > top - 1) continue;
-                DF c;
-                if(j == top - 1) {
-                    c = etop;
-                } else {
-                    const DF xn = df_mul(pe[j + 1], D[j]);
-                    const DF dx = df_addq(xn, df_neg(x12[j]));
-                    if(fabsf(dx.h) <= tiny && xn.h <= 0.5f && x12[j].h <= 0.5f)
-                        c = df_mul(c12[j], df_exp_tiny(dx));
-                    else
-                        c = df_exp_chain(xn);
-                    cprev[j] = c;
-                    xprev[j] = xn;
-                }
-                const DF t = (j == 0) ? df_fma(KE2, d4D, nB0) : t12[j];
-                pe[j] = df_mul(df_fma(pe[j], c, t), c);
-            }
-        }
-    }
-    {
-        const DF pm = pe[top - 1];
-        pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);   // 1.6 of the last substep
-    }
-    __syncwarp();
-    if(lane < top) {
-        DF v{0.0f, 0.0f};
-#pragma unroll
-        for(int j = 0; j < CAP; j++)
-            if(j < top && j == lane) v = pe[j];
-        X.pe[lane] = df_val(v);
-        X.eta[lane] = df_val(eta_mine);
-    }
-    if(lane == 0) {
-        X.pe[top] = df_val(pt);
-        X.eta[top] = df_val(eta_t);
-        X.KE2 = df_val(KE2);
-        X.scale = df_val(scale);
-    }
-    __syncwarp();
-}
-
 // Deterministic block sum of NV doubles (fixed shuffle tree, then fixed order over warps).
 template<int NV>
 __device__ inline void block_sum(double (&v)[NV], double* smem /* [32*NV] */) {
@@ -878,30 +732,20 @@ __device__ inline bool last_block(unsigned int* counter) {
     return is_last;
 }
 
-// One chain half-step on warps 0..2.  Kept out of line: a kernel calls it for both half-steps,
-// and one body per kernel keeps the code (and its compile time) small.  Chains of the default
-// length 4 use register arrays; other lengths run the runtime-length form in its own function, so
-// that its local arrays do not reach the default path.
-static __device__ __noinline__ int nh_chain_half_3w_m4(NhExchange& X, double g, double kT, double dt, int nresp, int seq,
-                                                bool fixed, bool dfloat) {
-    if(dfloat) {
-        if(threadIdx.x < 32) nh_chain_half_1w_df<4>(X, g, kT, dt, 4, nresp);
-        return seq + 3 * nresp;
-    }
-    return nh_chain_half_3w_t<4>(X, g, kT, dt, 4, nresp, seq, fixed);
-}
-static __device__ __noinline__ int nh_chain_half_3w_any(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
-                                                 bool fixed, bool dfloat) {
-    if(dfloat) {
-        if(threadIdx.x < 32) nh_chain_half_1w_df<0>(X, g, kT, dt, M, nresp);
-        return seq + 3 * nresp;
-    }
-    return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq, fixed);
-}
+// One chain half-step on warps 0..2, inlined into each kernel that runs one.  DFLOAT selects the
+// double-float family (mixed mode) or the FP64 family at compile time, so a kernel carries only
+// the family it uses: register arrays for the default chain length 4, the runtime-length form
+// for any other.
+template<bool DFLOAT>
 __device__ __forceinline__ int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
-                                                bool fixed, bool dfloat) {
-    return M == 4 ? nh_chain_half_3w_m4(X, g, kT, dt, nresp, seq, fixed, dfloat)
-                  : nh_chain_half_3w_any(X, g, kT, dt, M, nresp, seq, fixed, dfloat);
+                                                bool fixed) {
+    if constexpr(DFLOAT) {
+        if(M == 4) return nh_chain_half_3w_df<4>(X, g, kT, dt, M, nresp, seq);
+        return nh_chain_half_3w_df<0>(X, g, kT, dt, M, nresp, seq);
+    } else {
+        if(M == 4) return nh_chain_half_3w_t<4>(X, g, kT, dt, M, nresp, seq, fixed);
+        return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq, fixed);
+    }
 }
 
 __device__ __forceinline__ void bar96() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
@@ -913,13 +757,13 @@ __device__ __forceinline__ void bar96() { asm volatile("bar.sync 1, 96;" ::: "me
 // momentum, KE2 after the second half-step and, in *KE_full, after both.  The particle chain has
 // g = 3N (CFctT, MDLoop.cpp:29-60); the barostat's chain g = 1 with KE2 = p_eps^2/W (CFctP,
 // MDLoop.cpp:62-83).
+template<bool DFLOAT>
 __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
                                         double& KE2, bool second_half, double* c2_out, double* c1_out,
                                         double g, int M, int nresp, double* KE_full) {
     __shared__ NhExchange X;
     const int tid = threadIdx.x;
     const bool fixed = P.precision != MTG_PREC_REFERENCE;
-    const bool dfloat = P.precision == MTG_PREC_MIXED;   // double-float chain in the mixed mode
     double c2 = 1.0, c1 = 1.0;
     double KEf = KE2;
     if(M >= 2) {
@@ -937,7 +781,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         bar96();
         int seq = 0;
         if(second_half) {
-            seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed, dfloat);
+            seq = nh_chain_half_3w<DFLOAT>(X, g, P.kT, P.dt, M, nresp, seq, fixed);
             bar96();
             c2 = X.scale;
             if(tid < M) {
@@ -955,7 +799,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         }
         const double KE_after2 = X.KE2;
         bar96();
-        seq = nh_chain_half_3w(X, g, P.kT, P.dt, M, nresp, seq, fixed, dfloat);
+        seq = nh_chain_half_3w<DFLOAT>(X, g, P.kT, P.dt, M, nresp, seq, fixed);
         bar96();
         c1 = X.scale;
         KEf = X.KE2;
@@ -988,17 +832,19 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
     if(KE_full) *KE_full = KEf;
 }
 
+template<bool DFLOAT>
 __device__ inline void thermostat(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
                                   double& KE2, bool second_half, double* c2_out, double* c1_out) {
-    thermostat_chain(P, sc, th, th_saved, KE2, second_half, c2_out, c1_out, double(3 * P.n), P.M, P.nresp, nullptr);
+    thermostat_chain<DFLOAT>(P, sc, th, th_saved, KE2, second_half, c2_out, c1_out, double(3 * P.n), P.M, P.nresp, nullptr);
 }
 
 // End-of-step scalar work of the last block, run by its warps 0..2 (threadIdx.x < 96): the
 // thermostat half-steps and the output scalars.
+template<bool DFLOAT>
 __device__ inline void end_of_step(const Params& P, StepScalars* sc, ThermoDev* th, ThermoDev* th_saved,
                                    double KE2, double U, double vir, bool output, double* rec) {
     double c2 = 1.0, c1 = 1.0;
-    if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat(P, sc, th, th_saved, KE2, true, &c2, &c1);
+    if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat<DFLOAT>(P, sc, th, th_saved, KE2, true, &c2, &c1);
     if(threadIdx.x == 0) {
         sc->c2 = c2;
         sc->S = c2 * c1;
@@ -1051,12 +897,12 @@ __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2,
     }
     bar96();
     double c2 = 1.0, c1 = 1.0, KEf = KE2;
-    thermostat_chain(P, d.sc, d.th, d.th_saved, KE2, second_half, &c2, &c1, double(3 * P.n), P.M, P.nresp, &KEf);
+    thermostat_chain<false>(P, d.sc, d.th, d.th_saved, KE2, second_half, &c2, &c1, double(3 * P.n), P.M, P.nresp, &KEf);
     bar96();
     if(tid == 0) sh_kep = b->p_eps * b->p_eps / P.W;
     bar96();
     double KEp = sh_kep, c2p = 1.0, c1p = 1.0;
-    thermostat_chain(P, d.sc, d.thp, d.thp_saved, KEp, second_half, &c2p, &c1p, 1.0, P.MP, P.nrespP, nullptr);
+    thermostat_chain<false>(P, d.sc, d.thp, d.thp_saved, KEp, second_half, &c2p, &c1p, 1.0, P.MP, P.nrespP, nullptr);
     bar96();
     if(tid == 0) {
         StepScalars* sc = d.sc;

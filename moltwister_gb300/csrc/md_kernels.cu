@@ -121,6 +121,7 @@ __device__ __forceinline__ double block_sum_df(DF v, double* smem) {
 // ---------------------------------------------------------------------------------------------
 // Prologue: sum p^2/m, then the first thermostat half-step of the coming step.
 // ---------------------------------------------------------------------------------------------
+template<bool DFLOAT>
 __global__ void k_prologue(DevSys d, Params P) {
     __shared__ double smem[32 * 2];
     const SysView sv = sys_view(d, P, rep_of_block(d, P));
@@ -170,7 +171,8 @@ __global__ void k_prologue(DevSys d, Params P) {
             Params Q = P;
             Q.n = sv.n;
             Q.kT = sv.kT;
-            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat(Q, sv.sc, sv.th, sv.th_saved, KE2, false, &c2, &c1);
+            if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT)
+                thermostat<DFLOAT>(Q, sv.sc, sv.th, sv.th_saved, KE2, false, &c2, &c1);
             if(threadIdx.x == 0) {
                 sv.sc->S = c1;
                 sv.sc->c2 = 1.0;
@@ -297,16 +299,17 @@ __device__ __forceinline__ double wrap_coord(double x, double Lm) {
 
 // End-of-step scalar work of a system's last block (warps 0..2): thermostat and output record,
 // with the replica's size, temperature and box for a batch.
+template<bool DFLOAT>
 __device__ __forceinline__ void step_end(const DevSys& d, const Params& P, const SysView& sv, const double* tot, bool output) {
     if(P.nrep) {
         Params Q = P;
         Q.n = sv.n;
         Q.kT = sv.kT;
         for(int a = 0; a < 3; a++) Q.box[a] = sv.box[a];
-        end_of_step(Q, sv.sc, sv.th, sv.th_saved, tot[0], tot[2], tot[1], output, sv.rec);
+        end_of_step<DFLOAT>(Q, sv.sc, sv.th, sv.th_saved, tot[0], tot[2], tot[1], output, sv.rec);
         if(threadIdx.x == 0 && sv.sc->timeout) d.sc->timeout = 1;
     } else {
-        end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], output, d.rec);
+        end_of_step<DFLOAT>(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], output, d.rec);
     }
 }
 
@@ -357,7 +360,7 @@ __global__ void k_pkick2(DevSys d, Params P) {
             sv.sc->done_blocks = 0;
         }
         __syncthreads();
-        if(threadIdx.x < 96) step_end(d, P, sv, tot, OUTPUT);
+        if(threadIdx.x < 96) step_end<false>(d, P, sv, tot, OUTPUT);
     }
 }
 
@@ -515,7 +518,7 @@ __global__ void __launch_bounds__(96, 1) k_mstep_end(DevSys d, Params P) {
         tot[2] = OUTPUT ? sv3[NV > 2 ? 2 : 0] : 0.0;
     }
     __syncthreads();
-    step_end(d, P, sv, tot, OUTPUT);
+    step_end<true>(d, P, sv, tot, OUTPUT);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1350,7 +1353,8 @@ void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s)
 }
 
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
-    k_prologue<<<integration_blocks(P), 256, 0, s>>>(d, P);
+    if(P.precision == MTG_PREC_MIXED) k_prologue<true><<<integration_blocks(P), 256, 0, s>>>(d, P);
+    else k_prologue<false><<<integration_blocks(P), 256, 0, s>>>(d, P);
 }
 
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {

@@ -540,7 +540,7 @@ __global__ void k_kick2(DevSys d, Params P) {
         if(threadIdx.x < 96) {
             // the virial uses momenta after the thermostat: sum (c2 p)^2/m = c2^2 sum p^2/m,
             // folded in by end_of_step through KE2
-            end_of_step(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
+            end_of_step<false>(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], OUTPUT, d.rec);
         }
     }
 }
