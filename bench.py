@@ -40,7 +40,7 @@ CHUNK = 100
 SIGMA_O, EPS_O = 3.166, 0.650
 
 
-def make_system(precision: str = "mixed", coulomb: str = "shifted"):
+def make_system(precision: str = "mixed", coulomb: str = "cutoff"):
     from moltwister_gb300 import workloads as W
     s, cfg = W.water(n_mol=3000, L=44.8, seed=2, rc=10.0, dt=0.5)
     cfg.precision = precision
@@ -392,7 +392,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--coulomb", default="shifted", choices=["shifted", "cutoff"])
+    ap.add_argument("--coulomb", default="cutoff", choices=["cutoff", "shifted"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

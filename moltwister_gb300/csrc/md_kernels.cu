@@ -17,9 +17,8 @@
 // The force gather keeps the reference's structure (FunctorCalcForce.cpp:159-281): each atom sums
 // its own bonded terms, its neighbours and (cutoff) Coulomb, using the full list, so no atomics are
 // needed and the energy bookkeeping (pair energy once per pair, angle energy on the centre, half
-// the dihedral energy on each centre atom) follows the reference.  Mixed mode sums each group of
-// 16 consecutive row entries in FP32 and adds the group exactly to an int64 fixed-point total, so
-// a force depends only on the list, not on the lane count or scheduling.
+// the dihedral energy on each centre atom) follows the reference.  Mixed mode rounds every pair
+// contribution to int64 fixed point exactly, so a force does not depend on the summation order.
 #include <float.h>
 #include <stdint.h>
 
@@ -1023,15 +1022,17 @@ struct PairCoef {
 };
 constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
 
-// One list entry of the atom in slot si in FP32 (mixed path): adds g d to (ax, ay, az) and, for
-// the pair's lower slot, its energy to au.  The cutoff tests select instead of branching:
-// out-of-range entries, about a quarter of a list with a skin, would otherwise split the warp.
-// An entry naming the atom itself (the padding of a row's last group) contributes exact zeros.
+// One list entry of the atom in slot si in FP32 (mixed path), added to the fixed-point sums
+// (fx, fy, fz, fu): every contribution is rounded to the 2^-26 grid exactly and summed as an
+// integer, so a force depends neither on the order of the list nor on out-of-range entries nor on
+// how its row is split over lanes.  The cutoff tests select instead of branching: out-of-range
+// entries, about a quarter of a list with a skin, would otherwise split the warp.  g is clamped
+// to gmax so that |g d| < 2^18.
 template<bool ENERGY>
 __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int si, uint32_t ent, int ti, float qi,
-                                           float rc2, float rq2, float irc, const PairCoef* pc, const float* us,
-                                           const float* qt, uint4 qi4, const float (&fs)[3], float& ax, float& ay,
-                                           float& az, float& au) {
+                                           float rc2, float rq2, float irc, float gmax, const PairCoef* pc,
+                                           const float* us, const float* qt, uint4 qi4, const float (&fs)[3], Fix& fx,
+                                           Fix& fy, Fix& fz, Fix& fu) {
     const int sj = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
     const uint4 qj4 = d.pqs[sj];
@@ -1079,24 +1080,20 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
         g *= sc;
         u *= sc;
     }
-    ax = __fmaf_rn(g, dx, ax);
-    ay = __fmaf_rn(g, dy, ay);
-    az = __fmaf_rn(g, dz, az);
-    if(ENERGY && sj > si) au += u;
+    const float g16 = __fmul_rn(fminf(fmaxf(g, -gmax), gmax), 16.0f);
+    fix_add16(fx, __fmul_rn(g16, dx));
+    fix_add16(fy, __fmul_rn(g16, dy));
+    fix_add16(fz, __fmul_rn(g16, dz));
+    if(ENERGY && sj > si) fix_add_clamped(fu, u);
 }
-
-// Entries of a Verlet-list row are taken in groups of kGroup consecutive entries.  A group is
-// summed in FP32 in list order, then added to the atom's int64 fixed-point total exactly, so the
-// force depends only on the row (its content and order, both fixed by the list build), not on
-// how many lanes share the row or which lane takes which group.
-constexpr int kGroup = 16;
 
 // Force gather: TEAM lanes per atom (8, 16 or 32; chosen per system by the autotuner), atoms taken
 // in cell (slot) order so that a block's neighbour gathers stay within a compact, cache-resident
-// range of the slot-ordered positions.  Mixed: lane l takes groups l, l + TEAM, ... of the row,
-// loading each group's 16 entries as four 16-byte vectors so that all its position gathers are in
-// flight together.  FP64: four entries per lane in flight, summed in FP64.  Bonded terms of the
-// atom are spread over the team's lanes.
+// range of the slot-ordered positions; each lane walks its share of the row four entries at a time
+// so that four gathers are in flight per lane.  Bonded terms of the atom are spread over the
+// team's lanes.  Mixed: every contribution is rounded to the 2^-26 fixed-point grid and summed as
+// an integer, so forces do not depend on the team size, on the list order or on out-of-range
+// list entries.
 template<bool MIXED, bool ENERGY, int TEAM>
 __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     using R = typename std::conditional<MIXED, float, double>::type;
@@ -1141,28 +1138,21 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         const uint32_t* lst = d.vlist + (size_t)si * d.vmax;
         if constexpr(MIXED) {
             const float fs[3] = {v.fscale[0], v.fscale[1], v.fscale[2]};
+            const float gmax = 262143.0f / (v.rc + v.rcoul + v.skin);   // |d| < rc + rcoul + skin
             const uint4 qi4 = d.pqs[si];
             const int ti = (int)qi4.w;
             const float qi = d.qf[i];
-            // rows start on 128-byte boundaries (vmax is a multiple of 32) and a group never
-            // crosses the row's end, so the vector loads stay inside the row
-            for(int e0 = lane * kGroup; e0 < cnt; e0 += TEAM * kGroup) {
-                float ax = 0.0f, ay = 0.0f, az = 0.0f, au = 0.0f;
+            int e = lane;
+            for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
+                uint32_t ent[4];
 #pragma unroll
-                for(int c = 0; c < kGroup / 4; c++) {
-                    const uint4 E = __ldg(reinterpret_cast<const uint4*>(lst + e0) + c);
-                    const uint32_t ent[4] = {E.x, E.y, E.z, E.w};
+                for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
 #pragma unroll
-                    for(int q = 0; q < 4; q++) {
-                        const uint32_t use = (e0 + 4 * c + q < cnt) ? ent[q] : (uint32_t)si;
-                        pair_mixed<ENERGY>(d, P, si, use, ti, qi, rc2, rq2, irc, pc, us_s, qt, qi4, fs, ax, ay, az, au);
-                    }
-                }
-                fix_add_clamped(fx, ax);
-                fix_add_clamped(fy, ay);
-                fix_add_clamped(fz, az);
-                if(ENERGY) fix_add_clamped(fu, au);
+                for(int q = 0; q < 4; q++)
+                    pair_mixed<ENERGY>(d, P, si, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
             }
+            for(; e < cnt; e += TEAM)
+                pair_mixed<ENERGY>(d, P, si, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
         } else {
             const int ti = d.type[i];
             const double qi = d.qd[i];
