@@ -164,7 +164,10 @@ typedef struct mtg_config_desc {
     int32_t device;             /* CUDA device ordinal */
     int32_t lj_shift;           /* production modes, LJ at its cutoff (new): 0 truncated, 1 energy
                                    shifted to zero, 2 force shifted: F - F(rc), U - U(rc) + (r - rc) F(rc) */
-    int32_t reserved;
+    int32_t initial_max_neighbours; /* first capacity of the neighbour lists per atom (CNeighList::init,
+                                   MDFFMatrices.cpp:93-99, which starts at 10); 0 = sized from the
+                                   density.  Lists that overflow grow to need + 10 (reference) or need
+                                   + 25 % (production) and the step or chunk is redone. */
 } mtg_config_desc;
 
 /* Thermostat/barostat state (CNHChain eta_/p_eta_, NHChain.h:55-61; CVelVerlet p_eps_, eps_,
@@ -257,6 +260,13 @@ typedef struct mtg_run_stats {
     int32_t force_team;         /* lanes per atom chosen by the force-kernel autotuner */
 } mtg_run_stats;
 int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
+
+/* Limit of every bounded device wait of this context (the thermostat chain's hand-overs between
+ * warps), in polls of the flag; the default is 2^22.  A wait that runs out ends its kernel with
+ * the values it has and the run returns MTG_E_TIMEOUT; the context stays usable after
+ * mtg_set_state.  0 makes every wait give up at once (for testing the error path).  No counterpart
+ * in the reference, which has no device waits. */
+int mtg_set_wait_limit(mtg_ctx* ctx, int32_t polls);
 
 /* Profiling hook (no counterpart in the reference, which only prints a per-step wall time,
  * MDLoop.cpp:434-456): runs `steps` un-captured steps with CUDA events around each phase on the

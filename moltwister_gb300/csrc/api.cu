@@ -274,8 +274,10 @@ int charges_on(const mtg_ctx* c) {
     return 0;
 }
 
-int grow_vlist(mtg_ctx* c, int needed) {
-    const int cap = ((needed + needed / 4 + 32) + 31) / 32 * 32;
+// Verlet list capacity per slot: a multiple of 32 (rows start on 128-byte boundaries), with 25 %
+// headroom over `needed` unless `exact` asks for the smallest multiple of 32 holding it.
+int grow_vlist(mtg_ctx* c, int needed, bool exact = false) {
+    const int cap = exact ? (std::max(needed, 1) + 31) / 32 * 32 : ((needed + needed / 4 + 32) + 31) / 32 * 32;
     if(c->vlist_buf) cudaFree(c->vlist_buf);
     c->vlist_buf = nullptr;
     void* p;
@@ -300,8 +302,14 @@ StepScalars read_scalars(mtg_ctx* c) {
 }
 
 void clear_overflow(mtg_ctx* c) {
-    // zero overflow, needed, nonfinite (contiguous int32 fields)
+    // zero overflow, needed, nonfinite (contiguous int32 fields) and the timeout flags (the
+    // system's and, in a batch, each replica's): each chunk reports its own
     cudaMemsetAsync(&c->d.sc->overflow, 0, 3 * sizeof(int32_t), c->stream);
+    cudaMemsetAsync(&c->d.sc->timeout, 0, sizeof(int32_t), c->stream);
+    if(c->P.nrep) {
+        cudaMemset2DAsync(&c->d.rsc[0].timeout, sizeof(StepScalars), 0, sizeof(int32_t), c->P.nrep, c->stream);
+        cudaMemset2DAsync(&c->d.rsc[0].nonfinite, sizeof(StepScalars), 0, sizeof(int32_t), c->P.nrep, c->stream);
+    }
 }
 
 bool is_reference(const mtg_ctx* c) { return c->P.precision == MTG_PREC_REFERENCE; }
@@ -811,6 +819,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     P.nresp = cfg->temperature_respa;
     P.fcut = cfg->cutoff_force;
     P.lj_shift = cfg->lj_shift;
+    P.wait_polls = 1 << 22;
     if(P.ensemble == MTG_NPT) {
         // SimulationBox.cpp:58-76: NH_P_ shares T; W = kT tauP^2, P_ = pressure / Conv_press, V0 = Lx Ly Lz
         const double tauP = cfg->pressure_relax / kConvt;
@@ -1060,6 +1069,18 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         d.bptr = up(L.bptr); d.bj = up(L.bj); d.bt = up(L.bt);
         d.aptr = up(L.aptr); d.ai = up(L.ai); d.aj = up(L.aj); d.at = up(L.at); d.acen = up(L.acen);
         d.dptr = up(L.dptr); d.di = up(L.di); d.dj = up(L.dj); d.dl = up(L.dl); d.dt = up(L.dt); d.dcen = up(L.dcen);
+        {
+            std::vector<int> loc(n, 0);
+            for(int k = 0; k < n; k++) {
+                const int mk = mol[k];
+                bool ok = mk >= 0;
+                for(int e = L.bptr[k]; ok && e < L.bptr[k + 1]; e++) ok = mol[L.bj[e]] == mk;
+                for(int e = L.aptr[k]; ok && e < L.aptr[k + 1]; e++) ok = L.acen[e] || mol[L.aj[e]] == mk;
+                for(int e = L.dptr[k]; ok && e < L.dptr[k + 1]; e++) ok = L.dcen[e] || mol[L.dl[e]] == mk;
+                loc[k] = ok ? 1 : 0;
+            }
+            d.excl_local = up(loc);
+        }
         rc = rc || dalloc(C, &d.atom_cell, (size_t)3 * n);
         rc = rc || dalloc(C, &d.cell_first, (size_t)c->ncell_ref);
         rc = rc || dalloc(C, &d.cell_count, (size_t)c->ncell_ref);
@@ -1188,11 +1209,18 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         // the reference list is used every step only in reference mode; elsewhere (parity hooks)
         // it starts small and grows on demand
         int est = P.precision == MTG_PREC_REFERENCE ? (int)(1.3 * rho * 4.18879 * rc3) + 32 : 16;
-        rc = grow_neighbors(c.get(), std::min(est, n));
-        if(rc) return fail(nullptr, rc, c->err);
         double rl = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
         int vest = (int)(1.2 * rho * 4.18879 * rl * rl * rl) + 32;
-        rc = grow_vlist(c.get(), std::min(vest, n));
+        if(cfg->initial_max_neighbours > 0) {
+            // the caller's first capacity (the reference starts at 10): lists grow on overflow
+            rc = grow_neighbors(c.get(), std::max(0, cfg->initial_max_neighbours - 10));
+            if(rc) return fail(nullptr, rc, c->err);
+            rc = grow_vlist(c.get(), cfg->initial_max_neighbours, true);
+        } else {
+            rc = grow_neighbors(c.get(), std::min(est, n));
+            if(rc) return fail(nullptr, rc, c->err);
+            rc = grow_vlist(c.get(), std::min(vest, n));
+        }
         if(rc) return fail(nullptr, rc, c->err);
     }
     if(is_mixed(c.get())) launch_prod_sync(d, P, kSyncFromMaster, c->stream);
@@ -1380,8 +1408,8 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             total_ms += ms;
-            if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite momenta during the run");
             if(s.timeout) return fail(c, MTG_E_TIMEOUT, "a bounded wait in the thermostat gave up");
+            if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite kinetic energy or thermostat scale during the run");
             c->stats.list_builds = s.builds - builds0;
             if(output) {
                 double rec[8];
@@ -1610,6 +1638,14 @@ int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
     }
     for(int q = 0; q < 5; q++) phase_ms[q] = acc[q] / steps;
     return settle_state(c);
+}
+
+int mtg_set_wait_limit(mtg_ctx* c, int32_t polls) {
+    if(!c) return MTG_E_INVALID;
+    if(polls < 0) return fail(c, MTG_E_INVALID, "wait limit must be non-negative");
+    c->P.wait_polls = polls;
+    drop_graphs(c);   // captured launches carry the parameters by value
+    return MTG_OK;
 }
 
 int mtg_get_run_stats(mtg_ctx* c, mtg_run_stats* st) {

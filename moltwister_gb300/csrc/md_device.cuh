@@ -225,11 +225,12 @@ struct NhExchange {
     DF dpe0, dke, dpe_m2, detop;            // the same slots of the double-float chain
     volatile int f_pe0, f_ke, f_pe_m2, f_etop;
     int timeout;
+    int polls;                              // wait limit (Params::wait_polls)
 };
 
 // Bounded wait for a flag of another warp of the block: spins on shared memory for the first
 // 4096 polls (the partner is normally a few hundred cycles away), then backs off; gives up after
-// 2^22 polls and records a timeout.
+// the context's limit (Params::wait_polls, 2^22 by default) and records a timeout.
 // Flag hand-over between warps of a block with release / acquire ordering at CTA scope: the
 // posting lane's earlier shared-memory stores (the value) are visible to a waiter once it observes
 // the flag, without a full block fence on either side.
@@ -246,8 +247,8 @@ __device__ __forceinline__ void st_release_cta(volatile int* p, int v) {
                  : "memory");
 }
 
-__device__ __forceinline__ void nh_wait(volatile int* flag, int seq, int* timeout) {
-    for(int it = 0; it < (1 << 22); it++) {
+__device__ __forceinline__ void nh_wait(volatile int* flag, int seq, int* timeout, int polls) {
+    for(int it = 0; it < polls; it++) {
         if(ld_acquire_cta(flag) >= seq) return;
         if(it >= 4096) __nanosleep(32);
     }
@@ -326,7 +327,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                 for(int j = 0; j < top; j++) {
                     double c, x;
                     if(j == top - 1) {
-                        nh_wait(&X.f_etop, seq + s + 1, tmo);      // exponential of p_eta[M-1] (warp 2)
+                        nh_wait(&X.f_etop, seq + s + 1, tmo, X.polls);      // exponential of p_eta[M-1] (warp 2)
                         etop = X.etop;
                         c = etop;
                         x = 0.0;
@@ -374,7 +375,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                     }
                     double t;
                     if(j == 0) {
-                        nh_wait(&X.f_ke, seq + s + 1, tmo);    // kinetic term after step 1.4 (warp 1)
+                        nh_wait(&X.f_ke, seq + s + 1, tmo, X.polls);    // kinetic term after step 1.4 (warp 1)
                         KE2 = X.ke;
                         t = fma(KE2, d4, -B0);
                     } else {
@@ -405,7 +406,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         for(int mu = 0; mu < 3; mu++) {
             const double d2 = (w[mu] * dt / double(nresp)) / 2.0;
             for(int it = 0; it < nresp; it++, s++) {
-                nh_wait(&X.f_pe0, seq + s + 1, tmo);
+                nh_wait(&X.f_pe0, seq + s + 1, tmo, X.polls);
                 const double c = cmt_exp_bits(-(d2 * (X.pe0 * iQ0)), fixed);
                 scale *= c;
                 KE2 *= c * c;
@@ -431,7 +432,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
             for(int it = 0; it < nresp; it++, s++) {
                 if(s > 0) {
                     // 1.6 of the previous substep, with that substep's Dt
-                    nh_wait(&X.f_pe_m2, seq + s, tmo);
+                    nh_wait(&X.f_pe_m2, seq + s, tmo, X.polls);
                     pm = X.pe_m2;
                     const double d4p = (w[(s - 1) / nresp] * dt / double(nresp)) / 4.0;
                     pt += d4p * (pm * pm * iQm - kT);
@@ -443,7 +444,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                 eta_t += d2 * (pt * iQt);                   // 1.3 for the top element
             }
         }
-        nh_wait(&X.f_pe_m2, seq + nsub, tmo);             // 1.6 of the last substep
+        nh_wait(&X.f_pe_m2, seq + nsub, tmo, X.polls);             // 1.6 of the last substep
         pm = X.pe_m2;
         pt += ((w[2] * dt / double(nresp)) / 4.0) * (pm * pm * iQm - kT);
         if(lane == 0) {
@@ -550,7 +551,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
                 for(int j = 0; j < top; j++) {
                     DF c, x;
                     if(j == top - 1) {
-                        nh_wait(&X.f_etop, seq + s + 1, tmo);      // exponential of p_eta[M-1] (warp 2)
+                        nh_wait(&X.f_etop, seq + s + 1, tmo, X.polls);      // exponential of p_eta[M-1] (warp 2)
                         etop = X.detop;
                         c = etop;
                         x = DF{0.0f, 0.0f};
@@ -597,7 +598,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
                     }
                     DF t;
                     if(j == 0) {
-                        nh_wait(&X.f_ke, seq + s + 1, tmo);    // kinetic term after step 1.4 (warp 1)
+                        nh_wait(&X.f_ke, seq + s + 1, tmo, X.polls);    // kinetic term after step 1.4 (warp 1)
                         KE2 = X.dke;
                         t = df_fma(KE2, d4D, nB0);
                     } else {
@@ -630,7 +631,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
         for(int mu = 0; mu < 3; mu++) {
             const DF D1 = D1W[mu == 1 ? 1 : 0];
             for(int it = 0; it < nresp; it++, s++) {
-                nh_wait(&X.f_pe0, seq + s + 1, tmo);
+                nh_wait(&X.f_pe0, seq + s + 1, tmo, X.polls);
                 const DF c = df_exp_chain(df_mul(X.dpe0, D1));
                 scale = df_mul(scale, c);
                 KE2 = df_mul(KE2, df_mul(c, c));
@@ -658,7 +659,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
             for(int it = 0; it < nresp; it++, s++) {
                 if(s > 0) {
                     // 1.6 of the previous substep, with that substep's Dt
-                    nh_wait(&X.f_pe_m2, seq + s, tmo);
+                    nh_wait(&X.f_pe_m2, seq + s, tmo, X.polls);
                     pm = X.dpe_m2;
                     pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
                 }
@@ -670,7 +671,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
                 d4prev = d4;
             }
         }
-        nh_wait(&X.f_pe_m2, seq + nsub, tmo);             // 1.6 of the last substep
+        nh_wait(&X.f_pe_m2, seq + nsub, tmo, X.polls);             // 1.6 of the last substep
         pm = X.dpe_m2;
         pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
         if(lane == 0) {
@@ -777,6 +778,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
             X.scale = 1.0;
             X.f_pe0 = X.f_ke = X.f_pe_m2 = X.f_etop = 0;
             X.timeout = 0;
+            X.polls = P.wait_polls;
         }
         bar96();
         int seq = 0;
@@ -846,6 +848,7 @@ __device__ inline void end_of_step(const Params& P, StepScalars* sc, ThermoDev* 
     double c2 = 1.0, c1 = 1.0;
     if(P.ensemble == MTG_NVT || P.ensemble == MTG_NPT) thermostat<DFLOAT>(P, sc, th, th_saved, KE2, true, &c2, &c1);
     if(threadIdx.x == 0) {
+        if(!isfinite(KE2) || !isfinite(c2 * c1)) sc->nonfinite = 1;
         sc->c2 = c2;
         sc->S = c2 * c1;
         sc->KE2 = KE2;

@@ -307,6 +307,7 @@ __device__ __forceinline__ void step_end(const DevSys& d, const Params& P, const
         for(int a = 0; a < 3; a++) Q.box[a] = sv.box[a];
         end_of_step<DFLOAT>(Q, sv.sc, sv.th, sv.th_saved, tot[0], tot[2], tot[1], output, sv.rec);
         if(threadIdx.x == 0 && sv.sc->timeout) d.sc->timeout = 1;
+        if(threadIdx.x == 0 && sv.sc->nonfinite) d.sc->nonfinite = 1;
     } else {
         end_of_step<DFLOAT>(P, d.sc, d.th, d.th_saved, tot[0], tot[2], tot[1], output, d.rec);
     }

@@ -112,6 +112,7 @@ struct Params {
     double Pext;          // pressure / Conv_press
     double W;             // barostat mass kT tauP^2
     double V0;            // LmaxX LmaxY LmaxZ
+    int wait_polls;       // limit of the bounded device waits (thermostat hand-overs)
 };
 
 
@@ -157,6 +158,9 @@ struct DevSys {
     const int *bptr, *bj, *bt;
     const int *aptr, *ai, *aj, *at, *acen;
     const int *dptr, *di, *dj, *dl, *dt, *dcen;
+    // 1 when every partner an exclusion could name (bonded, 1-3 and 1-4 lists) shares the atom's
+    // molecule index (>= 0): a pair of different molecules then has no exclusion
+    const int* excl_local;
     // reference cell & neighbour lists
     int* atom_cell;       // [3n]
     int* cell_first;      // [ncell]

@@ -202,6 +202,9 @@ __global__ void k_cell_assign(DevSys d, Params P) {
     d.atom_cell[3 * i + 1] = iy;
     d.atom_cell[3 * i + 2] = iz;
     atomicAdd(&d.cell_count[ix + Nx * (iy + iz * Ny)], 1);
+    // FP32 copy of the positions for the neighbour-list prefilter (absent in the context-free
+    // neighbour list, which then decides every candidate in FP64)
+    if(d.rb4) d.rb4[i] = make_float4((float)d.r[3 * i], (float)d.r[3 * i + 1], (float)d.r[3 * i + 2], 0.0f);
 }
 
 // Exclusive scan of the cell counts in one block; empty cells get first = -1 (CListPointer default).
@@ -264,10 +267,15 @@ __global__ void k_cell_rank(DevSys d, int ncell, const int* tmp) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Full neighbour list in the reference order (CFunctorGenNeighList::operator())
+// Full neighbour list in the reference order (CFunctorGenNeighList::operator()), one warp per
+// atom: the 27 cells in the reference's loop order, each cell's atoms 32 at a time, accepted ones
+// compacted in order with a ballot.  The distance test is first made in FP32 from the FP32 copy
+// of the positions; only a candidate whose FP32 squared distance lies within 0.4 % of rc^2 (the
+// FP32 error is below 0.01 % for boxes up to a few hundred A) is decided by the reference's FP64
+// arithmetic, so the accepted set is exactly the reference's.
 // ---------------------------------------------------------------------------------------------
 __global__ void k_neigh(DevSys d, Params P, float rc) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(k >= P.n) return;
     float rc2f = rc;
     rc2f *= rc2f;
@@ -275,8 +283,13 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
     const float Bx = box_f(d, P, 0), By = box_f(d, P, 1), Bz = box_f(d, P, 2);
     const float lx = -Bx / 2.0f, ly = -By / 2.0f, lz = -Bz / 2.0f;
     const double w[3] = {double(lx + Bx) - double(lx), double(ly + By) - double(ly), double(lz + Bz) - double(lz)};
+    const float wf[3] = {(float)w[0], (float)w[1], (float)w[2]};
+    const float hf[3] = {0.5f * wf[0], 0.5f * wf[1], 0.5f * wf[2]};
+    const float lo2 = (float)(rc2 * 0.996), hi2 = (float)(rc2 * 1.004);
     const int Nx = P.nx, Ny = P.ny, Nz = P.nz;
     const double x0 = d.r[3 * k], y0 = d.r[3 * k + 1], z0 = d.r[3 * k + 2];
+    const bool pre = d.rb4 != nullptr;
+    const float4 rk = pre ? d.rb4[k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int cx = d.atom_cell[3 * k], cy = d.atom_cell[3 * k + 1], cz = d.atom_cell[3 * k + 2];
     int c = 0;
     int* out = d.nbr_list + (size_t)k * d.nbr_max;
@@ -288,184 +301,268 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
                 const int Iz = (iz >= 0) ? ((iz < Nz) ? iz : 0) : Nz - 1;
                 const int cell = Ix + Nx * (Iy + Iz * Ny);
                 const int cnt = d.cell_count[cell], first = d.cell_first[cell];
-                for(int e = 0; e < cnt; e++) {
-                    const int j = d.cell_list[first + e];
-                    double dX = x0 - d.r[3 * j], dY = y0 - d.r[3 * j + 1], dZ = z0 - d.r[3 * j + 2];
-                    dX = (dX < 0.0) ? -dX : dX;
-                    dY = (dY < 0.0) ? -dY : dY;
-                    dZ = (dZ < 0.0) ? -dZ : dZ;
-                    if(dX > (w[0] / 2.0)) dX = w[0] - dX;
-                    if(dY > (w[1] / 2.0)) dY = w[1] - dY;
-                    if(dZ > (w[2] / 2.0)) dZ = w[2] - dZ;
-                    const double d2 = dX * dX + dY * dY + dZ * dZ;
-                    if(d2 < rc2 && j != k) {
-                        if(c < d.nbr_max) out[c] = j;
-                        c++;
+                for(int base = 0; base < cnt; base += 32) {
+                    bool take = false;
+                    int j = 0;
+                    if(base + lane < cnt) {
+                        j = d.cell_list[first + base + lane];
+                        float f2 = 0.5f * (lo2 + hi2);   // without the FP32 copy: always the FP64 test
+                        if(pre) {
+                            const float4 rj = d.rb4[j];
+                            float fX = fabsf(rk.x - rj.x), fY = fabsf(rk.y - rj.y), fZ = fabsf(rk.z - rj.z);
+                            if(fX > hf[0]) fX = wf[0] - fX;
+                            if(fY > hf[1]) fY = wf[1] - fY;
+                            if(fZ > hf[2]) fZ = wf[2] - fZ;
+                            f2 = fX * fX + fY * fY + fZ * fZ;
+                        }
+                        if(f2 < lo2) {
+                            take = true;
+                        } else if(f2 <= hi2) {
+                            double dX = x0 - d.r[3 * j], dY = y0 - d.r[3 * j + 1], dZ = z0 - d.r[3 * j + 2];
+                            dX = (dX < 0.0) ? -dX : dX;
+                            dY = (dY < 0.0) ? -dY : dY;
+                            dZ = (dZ < 0.0) ? -dZ : dZ;
+                            if(dX > (w[0] / 2.0)) dX = w[0] - dX;
+                            if(dY > (w[1] / 2.0)) dY = w[1] - dY;
+                            if(dZ > (w[2] / 2.0)) dZ = w[2] - dZ;
+                            take = (dX * dX + dY * dY + dZ * dZ) < rc2;
+                        }
+                        take = take && (j != k);
                     }
+                    const unsigned ball = __ballot_sync(0xffffffffu, take);
+                    if(take) {
+                        const int slot = c + __popc(ball & ((1u << lane) - 1u));
+                        if(slot < d.nbr_max) out[slot] = j;
+                    }
+                    c += __popc(ball);
                 }
             }
         }
     }
-    d.nbr_count[k] = c;
-    if(c > d.nbr_max) {
-        d.sc->overflow = 1;
-        atomicMax(&d.sc->needed, c);
+    if(lane == 0) {
+        d.nbr_count[k] = c;
+        if(c > d.nbr_max) {
+            d.sc->overflow = 1;
+            atomicMax(&d.sc->needed, c);
+        }
     }
 }
 
 // ---------------------------------------------------------------------------------------------
 // Per-atom force/energy gather, table mode (CFunctorCalcForce::operator())
 // ---------------------------------------------------------------------------------------------
-__global__ void k_force(DevSys d, Params P) {
+// Coulomb term of the pair (k, i) (FunctorCalcForce.cpp:258-278, 514-535) in the reference's
+// arithmetic: float R from the FP64 minimum-image separation, FP64 K / R^3, the pair energy on
+// the lower index, the exclusion scaling.
+__device__ __forceinline__ void coulomb_pair(const DevSys& d, const Params& P, int k, int i, const D3& rk, D3 ri,
+                                             float qk, float qi, int molk, int moli, bool local, const double* w,
+                                             D3& f, float& u) {
+    u = 0.0f;
+    same_side(rk, ri, w);
+    const D3 rv = sub(rk, ri);
+    const float R = (float)nrm(rv);
+    const double R3 = double(R * R * R);
+    const double K = double(kCoulombKf * qk * qi);
+    if((i > k) && (R != 0.0f)) u += float(K) / R;
+    f = (R3 != 0.0) ? scl(rv, K / R3) : d3(0, 0, 0);
+    // pairs of different molecules have no exclusion when none of k's partners lies outside its
+    // molecule; otherwise the reference's search
+    float sc;
+    if(!(local && moli != molk) && exclusion(d, P, k, i, sc)) {
+        f = scl(f, (double)sc);
+        u *= sc;
+    }
+}
+
+constexpr int kRefTile = 128;   // atoms per shared-memory tile of the all-pairs Coulomb loop
+
+// One thread per atom (the per-atom sum runs in the reference's order, i = 0 .. N-1); the block's
+// threads stage each tile of positions, charges and molecule indices in shared memory.  A pair
+// whose charge product K is zero adds exactly +-0 to every sum and is skipped (the whole loop when
+// the atom's own charge is zero), which leaves every sum bit-identical.
+__global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
+    __shared__ double tx[kRefTile], ty[kRefTile], tz[kRefTile];
+    __shared__ float tq[kRefTile];
+    __shared__ int tm[kRefTile];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if(k >= P.n) return;
     const float Lf[3] = {box_f(d, P, 0), box_f(d, P, 1), box_f(d, P, 2)};
     const double w[3] = {double(Lf[0]) / 2.0 - (-double(Lf[0]) / 2.0), double(Lf[1]) / 2.0 - (-double(Lf[1]) / 2.0),
                          double(Lf[2]) / 2.0 - (-double(Lf[2]) / 2.0)};
     if(d.sc->overflow) return;   // neighbour list incomplete: the step is redone after growing it
+    const bool act = k < P.n;
+    const bool live = act && d.mobile[k];
     double Fx = 0.0, Fy = 0.0, Fz = 0.0;
     float Uk = 0.0f;
-    if(!d.mobile[k]) {
-        d.F[3 * k] = d.F[3 * k + 1] = d.F[3 * k + 2] = 0.0;
-        d.U[k] = 0.0;
-        return;
-    }
-    const D3 rk = load3(d.r, k);
-    // bonds
-    for(int e = d.bptr[k]; e < d.bptr[k + 1]; e++) {
-        const int i = d.bj[e];
-        D3 ri = load3(d.r, i);
-        same_side(rk, ri, w);
-        const float* tab = d.bond_tab + (size_t)d.bt[e] * kNpts * 3;
-        const float rr = (float)nrm(sub(rk, ri));
-        const int idx = tindex(rr, tab);
-        float md = 0.0f;
-        if(idx >= 0 && idx < kNpts - 1) {
-            const float* p1 = tab + 3 * idx;
-            const float* p2 = p1 + 3;
-            md += interp(rr, p1[0], p1[1], p2[0], p2[1]);
-            if(i > k) Uk += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+    const D3 rk = live ? load3(d.r, k) : d3(0, 0, 0);
+    if(live) {
+        // bonds
+        for(int e = d.bptr[k]; e < d.bptr[k + 1]; e++) {
+            const int i = d.bj[e];
+            D3 ri = load3(d.r, i);
+            same_side(rk, ri, w);
+            const float* tab = d.bond_tab + (size_t)d.bt[e] * kNpts * 3;
+            const float rr = (float)nrm(sub(rk, ri));
+            const int idx = tindex(rr, tab);
+            float md = 0.0f;
+            if(idx >= 0 && idx < kNpts - 1) {
+                const float* p1 = tab + 3 * idx;
+                const float* p2 = p1 + 3;
+                md += interp(rr, p1[0], p1[1], p2[0], p2[1]);
+                if(i > k) Uk += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+            }
+            const D3 f = scl(coeff12(ri, rk), (double)md);
+            Fx += f.x; Fy += f.y; Fz += f.z;
         }
-        const D3 f = scl(coeff12(ri, rk), (double)md);
-        Fx += f.x; Fy += f.y; Fz += f.z;
-    }
-    // angles
-    for(int e = d.aptr[k]; e < d.aptr[k + 1]; e++) {
-        D3 ri = load3(d.r, d.ai[e]), rj = load3(d.r, d.aj[e]);
-        same_side(rk, ri, w);
-        same_side(rk, rj, w);
-        const float* tab = d.angle_tab + (size_t)d.at[e] * kNpts * 3;
-        D3 f;
-        if(d.acen[e]) {
-            const float th = calc_angle(ri, rk, rj);
-            const int idx = tindex(th, tab);
-            float md = 0.0f;
-            if(idx >= 0 && idx < kNpts - 1) {
-                const float* p1 = tab + 3 * idx;
-                const float* p2 = p1 + 3;
-                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
-                Uk += interp(th, p1[0], p1[2], p2[0], p2[2]);
-            }
-            f = scl(coeff_ang2(rj, rk, ri), (double)md);
-        } else {
-            const float th = calc_angle(rk, ri, rj);
-            const int idx = tindex(th, tab);
-            float md = 0.0f;
-            if(idx >= 0 && idx < kNpts - 1) {
-                const float* p1 = tab + 3 * idx;
-                const float* p2 = p1 + 3;
-                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
-            }
-            f = scl(coeff_ang13(rj, ri, rk), (double)md);
-        }
-        Fx += f.x; Fy += f.y; Fz += f.z;
-    }
-    // dihedrals
-    for(int e = d.dptr[k]; e < d.dptr[k + 1]; e++) {
-        D3 ri = load3(d.r, d.di[e]), rj = load3(d.r, d.dj[e]), rl = load3(d.r, d.dl[e]);
-        same_side(rk, ri, w);
-        same_side(rk, rj, w);
-        same_side(rk, rl, w);
-        const float* tab = d.dih_tab + (size_t)d.dt[e] * kNpts * 3;
-        D3 f;
-        if(d.dcen[e]) {
-            const float th = calc_dihedral(ri, rk, rj, rl);
-            const int idx = tindex(th, tab);
-            float md = 0.0f;
-            if(idx >= 0 && idx < kNpts - 1) {
-                const float* p1 = tab + 3 * idx;
-                const float* p2 = p1 + 3;
-                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
-                Uk += 0.5f * interp(th, p1[0], p1[2], p2[0], p2[2]);
-            }
-            f = scl(coeff_dih23(rl, rj, rk, ri), (double)md);
-        } else {
-            const float th = calc_dihedral(rk, ri, rj, rl);
-            const int idx = tindex(th, tab);
-            float md = 0.0f;
-            if(idx >= 0 && idx < kNpts - 1) {
-                const float* p1 = tab + 3 * idx;
-                const float* p2 = p1 + 3;
-                md += interp(th, p1[0], p1[1], p2[0], p2[1]);
-            }
-            f = scl(coeff_dih14(rl, rj, ri, rk), (double)md);
-        }
-        Fx += f.x; Fy += f.y; Fz += f.z;
-    }
-    // short range, neighbour-list order
-    const int T = P.T;
-    const int nn = min(d.nbr_count[k], d.nbr_max);
-    const int* nl = d.nbr_list + (size_t)k * d.nbr_max;
-    for(int e = 0; e < nn; e++) {
-        const int i = nl[e];
-        float u = 0.0f;
-        D3 ri = load3(d.r, i);
-        same_side(rk, ri, w);
-        D3 f = d3(0, 0, 0);
-        const float rr = (float)nrm(sub(rk, ri));
-        if(!(rr < 1E-3f)) {
-            float sum = 0.0f;
-            const int pair = d.type[k] * T + d.type[i];
-            const int cnt = d.nb_cnt[pair];
-            for(int ff = 0; ff < cnt; ff++) {
-                const float* tab = d.nb_tab + ((size_t)pair * kMaxFF + ff) * kNpts * 3;
-                const int idx = tindex(rr, tab);
+        // angles
+        for(int e = d.aptr[k]; e < d.aptr[k + 1]; e++) {
+            D3 ri = load3(d.r, d.ai[e]), rj = load3(d.r, d.aj[e]);
+            same_side(rk, ri, w);
+            same_side(rk, rj, w);
+            const float* tab = d.angle_tab + (size_t)d.at[e] * kNpts * 3;
+            D3 f;
+            if(d.acen[e]) {
+                const float th = calc_angle(ri, rk, rj);
+                const int idx = tindex(th, tab);
+                float md = 0.0f;
                 if(idx >= 0 && idx < kNpts - 1) {
                     const float* p1 = tab + 3 * idx;
                     const float* p2 = p1 + 3;
-                    sum += interp(rr, p1[0], p1[1], p2[0], p2[1]);
-                    if(i > k) u += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+                    md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+                    Uk += interp(th, p1[0], p1[2], p2[0], p2[2]);
                 }
+                f = scl(coeff_ang2(rj, rk, ri), (double)md);
+            } else {
+                const float th = calc_angle(rk, ri, rj);
+                const int idx = tindex(th, tab);
+                float md = 0.0f;
+                if(idx >= 0 && idx < kNpts - 1) {
+                    const float* p1 = tab + 3 * idx;
+                    const float* p2 = p1 + 3;
+                    md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+                }
+                f = scl(coeff_ang13(rj, ri, rk), (double)md);
             }
-            f = scl(coeff12(ri, rk), (double)sum);
+            Fx += f.x; Fy += f.y; Fz += f.z;
         }
-        float sc;
-        if(exclusion(d, P, k, i, sc)) { f = scl(f, (double)sc); u *= sc; }
-        Fx += f.x; Fy += f.y; Fz += f.z;
-        Uk += u;
+        // dihedrals
+        for(int e = d.dptr[k]; e < d.dptr[k + 1]; e++) {
+            D3 ri = load3(d.r, d.di[e]), rj = load3(d.r, d.dj[e]), rl = load3(d.r, d.dl[e]);
+            same_side(rk, ri, w);
+            same_side(rk, rj, w);
+            same_side(rk, rl, w);
+            const float* tab = d.dih_tab + (size_t)d.dt[e] * kNpts * 3;
+            D3 f;
+            if(d.dcen[e]) {
+                const float th = calc_dihedral(ri, rk, rj, rl);
+                const int idx = tindex(th, tab);
+                float md = 0.0f;
+                if(idx >= 0 && idx < kNpts - 1) {
+                    const float* p1 = tab + 3 * idx;
+                    const float* p2 = p1 + 3;
+                    md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+                    Uk += 0.5f * interp(th, p1[0], p1[2], p2[0], p2[2]);
+                }
+                f = scl(coeff_dih23(rl, rj, rk, ri), (double)md);
+            } else {
+                const float th = calc_dihedral(rk, ri, rj, rl);
+                const int idx = tindex(th, tab);
+                float md = 0.0f;
+                if(idx >= 0 && idx < kNpts - 1) {
+                    const float* p1 = tab + 3 * idx;
+                    const float* p2 = p1 + 3;
+                    md += interp(th, p1[0], p1[1], p2[0], p2[1]);
+                }
+                f = scl(coeff_dih14(rl, rj, ri, rk), (double)md);
+            }
+            Fx += f.x; Fy += f.y; Fz += f.z;
+        }
+        // short range, neighbour-list order
+        const int T = P.T;
+        const int nn = min(d.nbr_count[k], d.nbr_max);
+        const int* nl = d.nbr_list + (size_t)k * d.nbr_max;
+        for(int e = 0; e < nn; e++) {
+            const int i = nl[e];
+            float u = 0.0f;
+            D3 ri = load3(d.r, i);
+            same_side(rk, ri, w);
+            D3 f = d3(0, 0, 0);
+            const float rr = (float)nrm(sub(rk, ri));
+            if(!(rr < 1E-3f)) {
+                float sum = 0.0f;
+                const int pair = d.type[k] * T + d.type[i];
+                const int cnt = d.nb_cnt[pair];
+                for(int ff = 0; ff < cnt; ff++) {
+                    const float* tab = d.nb_tab + ((size_t)pair * kMaxFF + ff) * kNpts * 3;
+                    const int idx = tindex(rr, tab);
+                    if(idx >= 0 && idx < kNpts - 1) {
+                        const float* p1 = tab + 3 * idx;
+                        const float* p2 = p1 + 3;
+                        sum += interp(rr, p1[0], p1[1], p2[0], p2[1]);
+                        if(i > k) u += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+                    }
+                }
+                f = scl(coeff12(ri, rk), (double)sum);
+            }
+            float sc;
+            if(!(d.excl_local[k] && d.mol[i] != d.mol[k]) && exclusion(d, P, k, i, sc)) {
+                f = scl(f, (double)sc);
+                u *= sc;
+            }
+            Fx += f.x; Fy += f.y; Fz += f.z;
+            Uk += u;
+        }
     }
     // Coulomb over all atoms, minimum image, no cutoff (FunctorCalcForce.cpp:258-278, 514-535)
-    const float qk = d.qf[k];
-    for(int i = 0; i < P.n; i++) {
-        float u = 0.0f;
-        D3 ri = load3(d.r, i);
-        same_side(rk, ri, w);
-        const D3 rv = sub(rk, ri);
-        const float qi = d.qf[i];
-        const float R = (float)nrm(rv);
-        const double R3 = double(R * R * R);
-        const double K = double(kCoulombKf * qk * qi);
-        if((i > k) && (R != 0.0f)) u += float(K) / R;
-        D3 f = (R3 != 0.0) ? scl(rv, K / R3) : d3(0, 0, 0);
-        float sc;
-        if(exclusion(d, P, k, i, sc)) { f = scl(f, (double)sc); u *= sc; }
-        Fx += f.x; Fy += f.y; Fz += f.z;
-        Uk += u;
+    const float qk = live ? d.qf[k] : 0.0f;
+    const int molk = live ? d.mol[k] : -1;
+    const bool local = live && d.excl_local[k] != 0;
+    if(__syncthreads_or(qk != 0.0f)) {
+        for(int base = 0; base < P.n; base += kRefTile) {
+            __syncthreads();
+            const int j = base + (int)threadIdx.x;
+            if(j < P.n) {
+                tx[threadIdx.x] = d.r[3 * j];
+                ty[threadIdx.x] = d.r[3 * j + 1];
+                tz[threadIdx.x] = d.r[3 * j + 2];
+                tq[threadIdx.x] = d.qf[j];
+                tm[threadIdx.x] = d.mol[j];
+            }
+            __syncthreads();
+            if(qk == 0.0f) continue;
+            const int m = min(kRefTile, P.n - base);
+            int t = 0;
+            // two pairs in flight: their terms are independent; they are added in order
+            for(; t + 1 < m; t += 2) {
+                const bool z0 = (kCoulombKf * qk * tq[t]) == 0.0f, z1 = (kCoulombKf * qk * tq[t + 1]) == 0.0f;
+                D3 f0 = d3(0, 0, 0), f1 = d3(0, 0, 0);
+                float u0 = 0.0f, u1 = 0.0f;
+                if(!z0) coulomb_pair(d, P, k, base + t, rk, d3(tx[t], ty[t], tz[t]), qk, tq[t], molk, tm[t], local, w, f0, u0);
+                if(!z1)
+                    coulomb_pair(d, P, k, base + t + 1, rk, d3(tx[t + 1], ty[t + 1], tz[t + 1]), qk, tq[t + 1], molk, tm[t + 1],
+                                 local, w, f1, u1);
+                if(!z0) {
+                    Fx += f0.x; Fy += f0.y; Fz += f0.z;
+                    Uk += u0;
+                }
+                if(!z1) {
+                    Fx += f1.x; Fy += f1.y; Fz += f1.z;
+                    Uk += u1;
+                }
+            }
+            if(t < m && (kCoulombKf * qk * tq[t]) != 0.0f) {
+                D3 f0;
+                float u0;
+                coulomb_pair(d, P, k, base + t, rk, d3(tx[t], ty[t], tz[t]), qk, tq[t], molk, tm[t], local, w, f0, u0);
+                Fx += f0.x; Fy += f0.y; Fz += f0.z;
+                Uk += u0;
+            }
+        }
     }
+    if(!act) return;
     d.F[3 * k] = Fx;
     d.F[3 * k + 1] = Fy;
     d.F[3 * k + 2] = Fz;
-    d.U[k] = (double)Uk;
+    d.U[k] = live ? (double)Uk : 0.0;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -628,11 +725,11 @@ void launch_ref_cells(const DevSys& d, const Params& P, cudaStream_t s) {
 }
 
 void launch_ref_neigh(const DevSys& d, const Params& P, cudaStream_t s) {
-    k_neigh<<<nblk(P.n, 128), 128, 0, s>>>(d, P, P.rc);
+    k_neigh<<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P, P.rc);
 }
 
 void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s) {
-    k_force<<<nblk(P.n, 64), 64, 0, s>>>(d, P);
+    k_force<<<nblk(P.n, kRefTile), kRefTile, 0, s>>>(d, P);
 }
 
 void launch_ref_kick_drift(const DevSys& d, const Params& P, cudaStream_t s) {

@@ -65,7 +65,7 @@ class ConfigDesc(C.Structure):
                 ("scale12", C.c_double), ("scale13", C.c_double), ("scale14", C.c_double), ("scale1N", C.c_double),
                 ("coulomb_cutoff", C.c_double), ("list_skin", C.c_double),
                 ("opt_learning_rate", C.c_double), ("opt_accuracy", C.c_double), ("opt_max_steps", C.c_int32),
-                ("device", C.c_int32), ("lj_shift", C.c_int32), ("reserved", C.c_int32)]
+                ("device", C.c_int32), ("lj_shift", C.c_int32), ("initial_max_neighbours", C.c_int32)]
 
 
 class ThermoState(C.Structure):
@@ -139,6 +139,7 @@ def load_library(path: str = LIB_PATH):
         "mtg_get_neighbors": ([P, C.c_int32, P, P, P], C.c_int),
         "mtg_get_run_stats": ([P, C.POINTER(RunStats)], C.c_int),
         "mtg_profile_phases": ([P, C.c_int, P], C.c_int),
+        "mtg_set_wait_limit": ([P, C.c_int32], C.c_int),
         "mtg_neighbors_noalloc": ([P, C.c_int32, P, C.c_double, C.c_double, C.c_int32, P, P, P, P], C.c_int),
         "mtg_batch_create": ([P, C.c_int32, C.POINTER(ConfigDesc), P, P, C.POINTER(P)], C.c_int),
         "mtg_batch_info": ([P, P, P], C.c_int),
@@ -289,6 +290,7 @@ def config_desc(c: MDConfig, device: int = 0) -> ConfigDesc:
     cf.opt_learning_rate, cf.opt_accuracy, cf.opt_max_steps = c.optlearningrate, c.optaccuracy, c.optmaxsteps
     cf.device = device
     cf.lj_shift = int(c.ljshift)
+    cf.initial_max_neighbours = int(getattr(c, "initialmaxneighbours", 0))
     return cf
 
 
@@ -450,6 +452,10 @@ class Engine:
         return {"device_ms": st.device_ms, "steps": st.steps, "list_builds": st.list_builds,
                 "kernel_launches": st.kernel_launches, "graph_steps": st.graph_steps,
                 "force_team": st.force_team}
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Poll limit of the bounded device waits (C ABI mtg_set_wait_limit); 0 = give up at once."""
+        self._check(self.lib.mtg_set_wait_limit(self.h, int(polls)))
 
     def profile_phases(self, steps: int) -> dict:
         """Mean device ms per step of each phase (C ABI mtg_profile_phases)."""

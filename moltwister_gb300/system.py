@@ -127,6 +127,9 @@ class MDConfig:
       ljshift       : production modes, LJ at each term's cutoff: 0 truncated (the reference),
                       1 energy shifted to zero (forces unchanged), 2 force shifted (force and
                       energy continuous: smooth trajectories for gradients).
+      initialmaxneighbours : first capacity of the neighbour lists per atom (the reference starts
+                      at 10, MDFFMatrices.cpp:246); 0 sizes them from the density.  Lists that
+                      overflow grow and the step is redone.
     """
     timestep: float = 1.0
     timesteps: int = 50000
@@ -157,6 +160,7 @@ class MDConfig:
     listskin: float = 1.0
     clipforces: bool = True
     ljshift: int = 0
+    initialmaxneighbours: int = 0
 
     REFERENCE_KEYS = ("timestep", "timesteps", "outstride", "temperature", "temperaturerelax",
                       "temperaturenhlen", "temperaturerespa", "pressure", "pressurerelax",
