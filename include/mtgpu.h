@@ -261,6 +261,29 @@ typedef struct mtg_run_stats {
 } mtg_run_stats;
 int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
 
+/* Initial momenta and Nose-Hoover / barostat state.
+ *
+ * MTG_INIT_REFERENCE: what CSimulationBox::initSystem draws (SimulationBox.cpp:53-96): chain
+ * positions (NHChain.cpp:126-133), momenta uniform in [-1, 1) per component with 0 replaced by 1,
+ * immobile atoms at rest, scaled to the temperature (SimulationBox.cpp:98-133), chain momenta
+ * (NHChain.cpp:135-143) and the barostat momentum (VelVerlet.cpp:176-182), in that order, from the C
+ * library's rand() seeded with `seed` (the reference draws in the CSimulationBox constructor,
+ * before CMDLoop::runSimulation seeds rand() from the clock, MDLoop.cpp:118: a fresh MolTwister
+ * process draws with seed 1).  As in the reference the momenta are scaled before the masses are
+ * copied in, that is with a mass of 1 g/mol for every atom (Particle3D.cpp:25-27).
+ * MTG_INIT_MAXWELL: seeded Maxwell-Boltzmann momenta with the real masses, the mobile atoms'
+ * centre-of-mass momentum removed, scaled to sum p^2/m / 3N = kT; chain positions uniform in
+ * [0, 1); chain and barostat momenta thermal (variance Q kT, W kT).  Not in the reference.
+ *
+ * mtg_draw_initial_state computes on the host only (p[3 n], *th) from the descriptors;
+ * mtg_init_state draws for a context and sets the momenta and chain state (mtg_set_state), the
+ * positions unchanged.  A batch returns MTG_E_UNSUPPORTED (set replicas' states one by one). */
+#define MTG_INIT_REFERENCE 0
+#define MTG_INIT_MAXWELL 1
+int mtg_draw_initial_state(const mtg_system_desc* sys, const mtg_config_desc* cfg, uint32_t seed, int32_t mode, double* p,
+                           mtg_thermo_state* th);
+int mtg_init_state(mtg_ctx* ctx, uint32_t seed, int32_t mode);
+
 /* Limit of every bounded device wait of this context (the thermostat chain's hand-overs between
  * warps), in polls of the flag; the default is 2^22.  A wait that runs out ends its kernel with
  * the values it has and the run returns MTG_E_TIMEOUT; the context stays usable after

@@ -31,6 +31,7 @@ UNITS = [
     ("adjoint.cu", []),
     ("tables.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("writers.cpp", []),
+    ("init_state.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

@@ -63,6 +63,8 @@ struct mtg_ctx {
     std::vector<double> h_bond_par, h_angle_par, h_dih_par;   // device layouts
     std::vector<int> h_bond_kind, h_angle_kind, h_dih_kind;
     std::vector<double> h_charge;
+    std::vector<uint8_t> h_mobile;
+    mtg_config_desc h_cfg{};
     bool has_tables = false;
     // buffers
     std::vector<void*> bufs;         // owned device allocations
@@ -992,6 +994,9 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         invm[i] = (float)(1.0 / sys->mass[i]);
     }
     c->h_mass.assign(sys->mass, sys->mass + n);
+    c->h_mobile.resize(n);
+    for(int i = 0; i < n; i++) c->h_mobile[i] = (uint8_t)mob[i];
+    c->h_cfg = *cfg;
     c->h_type = type;
     c->h_nb_terms.assign(sys->nb_terms, sys->nb_terms + TT * kMaxFF);
     c->h_nb_count.assign(sys->nb_count, sys->nb_count + TT);
@@ -1638,6 +1643,31 @@ int mtg_profile_phases(mtg_ctx* c, int steps, double* phase_ms) {
     }
     for(int q = 0; q < 5; q++) phase_ms[q] = acc[q] / steps;
     return settle_state(c);
+}
+
+int mtg_draw_initial_state(const mtg_system_desc* sys, const mtg_config_desc* cfg, uint32_t seed, int32_t mode, double* p,
+                           mtg_thermo_state* th) {
+    g_create_error.clear();
+    if(!sys || !cfg || !p || !th || sys->n_atoms <= 0 || !sys->mass)
+        return fail(nullptr, MTG_E_INVALID, "mtg_draw_initial_state: null argument or no atoms");
+    if(mode != MTG_INIT_REFERENCE && mode != MTG_INIT_MAXWELL)
+        return fail(nullptr, MTG_E_INVALID, "mtg_draw_initial_state: unknown mode");
+    const int rc = draw_initial_state(sys->n_atoms, sys->mass, sys->mobile, cfg, seed, mode, p, th);
+    if(rc) return fail(nullptr, rc, "mtg_draw_initial_state: chain lengths must lie in 0 .. MTG_MAX_NH_CHAIN");
+    return MTG_OK;
+}
+
+int mtg_init_state(mtg_ctx* c, uint32_t seed, int32_t mode) {
+    if(!c) return MTG_E_INVALID;
+    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "a batch takes per-replica states (mtg_set_state, mtg_batch_set_thermo)");
+    if(mode != MTG_INIT_REFERENCE && mode != MTG_INIT_MAXWELL) return fail(c, MTG_E_INVALID, "unknown initial-state mode");
+    const int n = c->P.n;
+    std::vector<double> p((size_t)3 * n);
+    mtg_thermo_state th{};
+    int rc = draw_initial_state(n, c->h_mass.data(), c->h_mobile.data(), &c->h_cfg, seed, mode, p.data(), &th);
+    if(rc) return fail(c, rc, "initial state: chain lengths must lie in 0 .. MTG_MAX_NH_CHAIN");
+    th.eps = 0.0;
+    return mtg_set_state(c, nullptr, p.data(), &th);
 }
 
 int mtg_set_wait_limit(mtg_ctx* c, int32_t polls) {

@@ -281,6 +281,10 @@ void launch_pair_hist(const double* pos, const int* ia, int na, const int* ib, i
 // out[0] += w * sum_k x[k] y[k] (deterministic; part holds dot_blocks(n) partials)
 void launch_dot_accum(int n, const double* x, const double* y, double w, double* part, double* out, cudaStream_t s);
 
+// Initial momenta and chain / barostat state (init_state.cpp), MTG_INIT_* modes.
+int draw_initial_state(int n, const double* mass, const uint8_t* mobile, const mtg_config_desc* cfg, uint32_t seed,
+                       int mode, double* p, mtg_thermo_state* th);
+
 // Host-side table generation (tables.cpp): out[npts*3] = (x, -dU/dx, U)
 int profile_nonbonded(int kind, const double* p, float r0, float r1, int npts, float* out);
 int profile_bond(int kind, const double* p, float r0, float r1, int npts, float* out);

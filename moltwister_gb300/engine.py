@@ -140,6 +140,9 @@ def load_library(path: str = LIB_PATH):
         "mtg_get_run_stats": ([P, C.POINTER(RunStats)], C.c_int),
         "mtg_profile_phases": ([P, C.c_int, P], C.c_int),
         "mtg_set_wait_limit": ([P, C.c_int32], C.c_int),
+        "mtg_draw_initial_state": ([C.POINTER(SystemDesc), C.POINTER(ConfigDesc), C.c_uint32, C.c_int32, P,
+                                    C.POINTER(ThermoState)], C.c_int),
+        "mtg_init_state": ([P, C.c_uint32, C.c_int32], C.c_int),
         "mtg_neighbors_noalloc": ([P, C.c_int32, P, C.c_double, C.c_double, C.c_int32, P, P, P, P], C.c_int),
         "mtg_batch_create": ([P, C.c_int32, C.POINTER(ConfigDesc), P, P, C.POINTER(P)], C.c_int),
         "mtg_batch_info": ([P, P, P], C.c_int),
@@ -453,6 +456,11 @@ class Engine:
                 "kernel_launches": st.kernel_launches, "graph_steps": st.graph_steps,
                 "force_team": st.force_team}
 
+    def init_state(self, seed: int = 1, mode: str = "reference") -> None:
+        """Draw and set the initial momenta and chain state (C ABI mtg_init_state); see
+        draw_initial_state for the modes."""
+        self._check(self.lib.mtg_init_state(self.h, int(seed) & 0xFFFFFFFF, INIT_MODES[mode]))
+
     def set_wait_limit(self, polls: int) -> None:
         """Poll limit of the bounded device waits (C ABI mtg_set_wait_limit); 0 = give up at once."""
         self._check(self.lib.mtg_set_wait_limit(self.h, int(polls)))
@@ -503,6 +511,26 @@ def _param_array(params):
             arr[k].dq = a.ctypes.data
     keep.append(arr)
     return arr, keep
+
+
+INIT_MODES = {"reference": 0, "maxwell": 1}
+
+
+def draw_initial_state(system: MDSystem, config: MDConfig, seed: int = 1, mode: str = "reference"):
+    """(p [n, 3], Thermo) as mtg_draw_initial_state draws them on the host: "reference" is the
+    state MolTwister's CSimulationBox constructor draws after srand(seed); "maxwell" a seeded
+    Maxwell-Boltzmann state."""
+    lib = load_library()
+    keep: List[object] = []
+    sd = system_desc(system, keep)
+    cd = config_desc(config)
+    p = np.zeros((system.n, 3))
+    th = ThermoState()
+    rc = lib.mtg_draw_initial_state(C.byref(sd), C.byref(cd), int(seed) & 0xFFFFFFFF, INIT_MODES[mode], _ptr(p),
+                                    C.byref(th))
+    if rc != MTG_OK:
+        raise MTGError(rc, lib.mtg_last_error(None).decode())
+    return p, thermo_tuple(th)
 
 
 def neighbors_noalloc(r_ptr: int, n: int, box, cutoff: float, shell: float, max_neigh: int,

@@ -413,11 +413,39 @@ int cmdTime(const SysIn& s, int nsteps) {
     return 0;
 }
 
+// init: the initial state the reference's CSimulationBox constructor draws (initSystem,
+// SimulationBox.cpp:53-96) after srand(seed); seed 1 is also what a fresh process draws with
+int cmdInit(const SysIn& s, const std::string& out, unsigned seed) {
+    CMolTwisterState st; buildState(s, st);
+    SMolDynConfigStruct cfg = makeCfg(s);
+    FILE* devnull = fopen("/dev/null", "w");
+    COut::setStdOut(devnull);
+    srand(seed);
+    CSimulationBox sb(&st, devnull, cfg);
+    const int N = sb.N_;
+    std::vector<double> Pm, nh, nhp, peps;
+    for(int k = 0; k < N; k++) {
+        Pm.push_back(sb.particles_[k].p_.x_); Pm.push_back(sb.particles_[k].p_.y_); Pm.push_back(sb.particles_[k].p_.z_);
+    }
+    for(int j = 0; j < sb.NH_T_.M_; j++) nh.push_back(sb.NH_T_.eta_[j]);
+    for(int j = 0; j < sb.NH_T_.M_; j++) nh.push_back(sb.NH_T_.p_eta_[j]);
+    for(int j = 0; j < sb.NH_P_.M_; j++) nhp.push_back(sb.NH_P_.eta_[j]);
+    for(int j = 0; j < sb.NH_P_.M_; j++) nhp.push_back(sb.NH_P_.p_eta_[j]);
+    peps.push_back(sb.velVerlet_.p_eps_);
+    MtbWriter w(out);
+    w.d("init_p", Pm, {(uint64_t)N, 3});
+    w.d("init_nhT", nh, {2, (uint64_t)sb.NH_T_.M_});
+    w.d("init_nhP", nhp, {2, (uint64_t)sb.NH_P_.M_});
+    w.d("init_peps", peps, {1});
+    fclose(devnull);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     if(argc < 3) {
-        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT\n");
+        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT | init SYS OUT SEED\n");
         return 1;
     }
     std::string cmd = argv[1];
@@ -426,6 +454,7 @@ int main(int argc, char** argv) {
     if(cmd == "run" && argc >= 6) return cmdRun(s, argv[3], atoi(argv[4]), atoi(argv[5]));
     if(cmd == "time" && argc >= 4) return cmdTime(s, atoi(argv[3]));
     if(cmd == "dcd" && argc >= 7) return cmdDcd(s, argv[3], atoi(argv[4]), atoi(argv[5]), atof(argv[6]));
+    if(cmd == "init" && argc >= 5) return cmdInit(s, argv[3], (unsigned)strtoul(argv[4], nullptr, 10));
     fprintf(stderr, "bad arguments\n");
     return 1;
 }

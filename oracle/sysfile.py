@@ -82,3 +82,12 @@ def harness_run(s: MDSystem, cfg: MDConfig, nsteps: int, stride: int):
         out = os.path.join(td, "o.mtb")
         run_harness(["run", out, nsteps, stride], s, cfg)
         return read_mtb(out)
+
+
+def harness_init(s: MDSystem, cfg: MDConfig, seed: int):
+    """The reference's initial state after srand(seed) (oracle/ref/harness.cpp `init`)."""
+    from .mtb import read_mtb
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.mtb")
+        run_harness(["init", out, int(seed)], s, cfg)
+        return read_mtb(out)

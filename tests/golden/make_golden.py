@@ -159,6 +159,38 @@ def make_dcd(name="water648_nvt"):
     return path
 
 
+def init_cases():
+    """(name, system, config, seed) of the initial-state fixture: mixed masses with immobile atoms,
+    one mass, and an NPT configuration (barostat chain and momentum)."""
+    out = []
+    s, c = W.chains(n_chain=27, L=24.0, seed=15, immobile_every=7)
+    out += [("chains108_seed1", s, c, 1), ("chains108_seed12345", s, c, 12345)]
+    s, c = W.argon(ncell=5, seed=11, jitter=0.05)
+    out.append(("argon500_seed1", s, c, 1))
+    s, c = W.water(n_mol=216, L=W.water_box_length(216), seed=14, rc=6.0)
+    c.ensemble = "NPT"
+    out.append(("water648_npt_seed7", s, c, 7))
+    return out
+
+
+def make_init():
+    """init_states.npz: per case the reference's drawn momenta, chains and barostat momentum, with
+    the inputs that determine them (masses, mobility, configuration)."""
+    from oracle.sysfile import harness_init
+    arrays = {}
+    for name, s, c, seed in init_cases():
+        d = harness_init(s, c, seed)
+        arrays[f"{name}__m"] = s.m
+        arrays[f"{name}__mobile"] = s.mobile.astype(np.int8)
+        arrays[f"{name}__cfg"] = np.array(json.dumps(dataclasses.asdict(c)))
+        arrays[f"{name}__seed"] = np.array(seed)
+        for k in ("init_p", "init_nhT", "init_nhP", "init_peps"):
+            arrays[f"{name}__{k}"] = d[k]
+    path = os.path.join(OUT, "init_states.npz")
+    np.savez_compressed(path, **arrays)
+    return path
+
+
 def main(only=()):
     todo = [(k, v, False) for k, v in cases().items()] + [(k, v, True) for k, v in big_cases().items()]
     for name, (s, c, steps, stride), big in todo:
@@ -171,5 +203,7 @@ def main(only=()):
 if __name__ == "__main__":
     if sys.argv[1:] == ["dcd"]:
         print(make_dcd())
+    elif sys.argv[1:] == ["init"]:
+        print(make_init())
     else:
         main(tuple(sys.argv[1:]))
