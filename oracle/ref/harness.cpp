@@ -39,6 +39,7 @@
 #include "Cmd/MolTwisterCmdMolDyn/Config/MolDynConfig.h"
 #include "Cmd/Tools/MolTwisterStateTools.h"
 #include "Utilities/DCDFile.h"
+#include "Cmd/MolTwisterCmdCalculate/CmdPairCorrelation.h"
 #include <functional>
 #include <tuple>
 
@@ -413,6 +414,50 @@ int cmdTime(const SysIn& s, int nsteps) {
     return 0;
 }
 
+// paircorr: `calculate paircorrelation` (Cmd/MolTwisterCmdCalculate/CmdPairCorrelation.cpp) on a
+// DCD file of nframes frames (frame f: the input positions shifted by f * shift on every axis),
+// written through the reference's CDCDFile with the box truncated to integers as the MD loop
+// writes it (MDLoop.cpp:248-258).  The command's table goes to OUT; the PBC widths it used for
+// each frame (CDCDFile::getCurrentPBC) are appended as "pbc <f> <wx> <wy> <wz>" lines.
+int cmdPairCorr(const SysIn& s, const std::string& out, int nframes, double shift, const std::vector<std::string>& args) {
+    CMolTwisterState st; buildState(s, st);
+    const int N = (int)s.atoms.size();
+    const std::string dcd = out + ".dcd";
+    remove(dcd.c_str());
+    for(int f = 0; f < nframes; f++) {
+        const double sh = shift * f;
+        std::function<std::tuple<double, double, double>(const int&)> pos = [&s, sh](const int& i) -> std::tuple<double, double, double> {
+            const AtomIn& a = s.atoms[i];
+            return std::tuple<double, double, double>(a.x + sh, a.y + sh, a.z + sh);
+        };
+        CDCDFile::createDCDFileIfNotExists(dcd, nframes, 1, 1.0, N);
+        CDCDFile::appendToDCDFile(dcd, N, {(int)s.L[0], (int)s.L[1], (int)s.L[2]}, pos);
+    }
+    FILE* fo = fopen(out.c_str(), "w");
+    FILE* devnull = fopen("/dev/null", "w");
+    COut::setStdOut(devnull);
+    CCmdPairCorrelation cmd(&st, fo);
+    std::vector<std::string> a = {dcd, "0", std::to_string(nframes)};
+    a.insert(a.end(), args.begin(), args.end());
+    const std::string err = cmd.execute(a);
+    CDCDFile file;
+    if(file.open(dcd)) {
+        for(int f = 0; f < nframes; f++) {
+            file.gotoRecord(f);
+            const C3DRect pbc = file.getCurrentPBC();
+            fprintf(fo, "pbc %d %.17g %.17g %.17g\n", f, pbc.getWidthX(), pbc.getWidthY(), pbc.getWidthZ());
+        }
+    }
+    fclose(fo);
+    fclose(devnull);
+    remove(dcd.c_str());
+    if(!err.empty()) {
+        fprintf(stderr, "%s\n", err.c_str());
+        return 1;
+    }
+    return 0;
+}
+
 // init: the initial state the reference's CSimulationBox constructor draws (initSystem,
 // SimulationBox.cpp:53-96) after srand(seed); seed 1 is also what a fresh process draws with
 int cmdInit(const SysIn& s, const std::string& out, unsigned seed) {
@@ -445,7 +490,7 @@ int cmdInit(const SysIn& s, const std::string& out, unsigned seed) {
 
 int main(int argc, char** argv) {
     if(argc < 3) {
-        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT | init SYS OUT SEED\n");
+        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT | init SYS OUT SEED | paircorr SYS OUT NFRAMES SHIFT ARGS...\n");
         return 1;
     }
     std::string cmd = argv[1];
@@ -455,6 +500,10 @@ int main(int argc, char** argv) {
     if(cmd == "time" && argc >= 4) return cmdTime(s, atoi(argv[3]));
     if(cmd == "dcd" && argc >= 7) return cmdDcd(s, argv[3], atoi(argv[4]), atoi(argv[5]), atof(argv[6]));
     if(cmd == "init" && argc >= 5) return cmdInit(s, argv[3], (unsigned)strtoul(argv[4], nullptr, 10));
+    if(cmd == "paircorr" && argc >= 6) {
+        std::vector<std::string> rest(argv + 6, argv + argc);
+        return cmdPairCorr(s, argv[3], atoi(argv[4]), atof(argv[5]), rest);
+    }
     fprintf(stderr, "bad arguments\n");
     return 1;
 }

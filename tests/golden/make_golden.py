@@ -191,6 +191,34 @@ def make_init():
     return path
 
 
+PAIRCORR_CASES = [("Ow_Hw", ["Ow", "Hw", "120", "0.0", "9.0"]),
+                  ("Ow_Ow_ignore", ["Ow", "Ow", "90", "0.0", "9.0", "ignoredistbelow", "2.5"]),
+                  ("Hw_Hw_nopbc", ["Hw", "Hw", "60", "0.5", "12.0", "ignorepbc"])]
+
+
+def make_paircorr(name="water648_nvt", nframes=3, shift=0.37):
+    """paircorr_<name>.npz: the reference's `calculate paircorrelation` table (counts and its
+    PairCorr / RDF columns) over a DCD of nframes frames, frame f = the case's positions + f shift,
+    for the argument lists of PAIRCORR_CASES, with the PBC widths the command read."""
+    import tempfile
+    from oracle.analysis import read_pair_correlation
+    from oracle.sysfile import run_harness
+    from tests.golden_cases import load
+    s, c, _ = load(name)
+    arrays = {"nframes": np.array(nframes), "shift": np.array(shift)}
+    with tempfile.TemporaryDirectory() as td:
+        for key, args in PAIRCORR_CASES:
+            out = os.path.join(td, key + ".txt")
+            run_harness(["paircorr", out, nframes, shift] + args, s, c)
+            table, pbc = read_pair_correlation(out)
+            arrays[key + "__args"] = np.array(json.dumps(args))
+            arrays[key + "__table"] = table
+            arrays[key + "__pbc"] = pbc
+    path = os.path.join(OUT, f"paircorr_{name}.npz")
+    np.savez_compressed(path, **arrays)
+    return path
+
+
 def main(only=()):
     todo = [(k, v, False) for k, v in cases().items()] + [(k, v, True) for k, v in big_cases().items()]
     for name, (s, c, steps, stride), big in todo:
@@ -205,5 +233,7 @@ if __name__ == "__main__":
         print(make_dcd())
     elif sys.argv[1:] == ["init"]:
         print(make_init())
+    elif sys.argv[1:] == ["paircorr"]:
+        print(make_paircorr())
     else:
         main(tuple(sys.argv[1:]))

@@ -48,9 +48,9 @@ def neighbours_match(d, cnt: np.ndarray, lst: np.ndarray) -> bool:
 
 
 def names():
-    # every fixture but the initial-state one (init_states.npz) is a system with its reference run
+    # every fixture but the initial-state and pair-correlation ones is a system with its reference run
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("init_"))
+                  if not os.path.basename(p).startswith(("init_", "paircorr_")))
 
 
 def load(name: str) -> Tuple[MDSystem, MDConfig, Dict[str, np.ndarray]]:
