@@ -85,6 +85,31 @@ __device__ __forceinline__ SysView sys_view(const DevSys& d, const Params& P, in
 __device__ __forceinline__ int rep_of_atom(const DevSys& d, const Params& P, int i) { return P.nrep ? d.rep_of[i] : -1; }
 __device__ __forceinline__ int rep_of_block(const DevSys& d, const Params& P) { return P.nrep ? d.blk_rep[blockIdx.x] : -1; }
 
+// List rebuilds.  StepScalars::rebuild of the system: 0 none due, -1 every list (a forced
+// rebuild), 1 due somewhere; in a batch each replica's own flag then says whether its lists are
+// rebuilt, so a replica rebuilds exactly when it would alone (its atoms moved half the skin).
+__device__ __forceinline__ bool rebuild_due(const DevSys& d, const Params& P, int r) {
+    const int g = d.sc->rebuild;
+    if(g == 0) return false;
+    if(g < 0 || !P.nrep || r < 0) return true;
+    return d.rsc[r].rebuild != 0;
+}
+__device__ __forceinline__ void flag_rebuild(const DevSys& d, const Params& P, const SysView& v) {
+    if(P.nrep) v.sc->rebuild = 1;
+    if(d.sc->rebuild == 0) d.sc->rebuild = 1;   // a forced rebuild (-1) stays forced
+}
+// Replica of production cell c (cells are numbered replica by replica from cbase).
+__device__ __forceinline__ int rep_of_cell(const DevSys& d, const Params& P, int c) {
+    if(!P.nrep) return -1;
+    int lo = 0, hi = P.nrep - 1;
+    while(lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if(d.reps[mid].cbase <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 
 // Totals of one system's block partials (blocks b0 .. b0+nb-1, four doubles each), summed by the
 // whole last block: thread t adds blocks t, t + blockDim, ... in order, then the fixed shuffle
@@ -285,7 +310,7 @@ __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, cons
     const double by = minimg_d(y - d.r_build[3 * k + 1], v.box[1], v.fconv[1] * 0x1p-32);
     const double bz = minimg_d(z - d.r_build[3 * k + 2], v.box[2], v.fconv[2] * 0x1p-32);
     const double h = 0.5 * double(v.skin);
-    if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
+    if(bx * bx + by * by + bz * bz > h * h) flag_rebuild(d, P, v);
 }
 
 __device__ __forceinline__ double wrap_coord(double x, double Lm) {
@@ -426,7 +451,7 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
         const uint4 qk = make_uint4(q[0], q[1], q[2], (unsigned int)__float_as_int(l.w));
         d.pq[k] = qk;
         d.pqs[d.slot_of[k]] = qk;   // the force gather reads positions in cell (slot) order
-        if(d2 > K.h2) d.sc->rebuild = 1;
+        if(d2 > K.h2) flag_rebuild(d, P, v);
     }
     if(cond) {
         // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
@@ -528,7 +553,7 @@ __global__ void __launch_bounds__(96, 1) k_mstep_end(DevSys d, Params P) {
 template<bool MIXED>
 __global__ void k_pcell_assign(DevSys d, Params P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= P.n || !d.sc->rebuild) return;
+    if(i >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     double x, y, z;
     load_pos(d, i, x, y, z, MIXED);
     d.r_build[3 * i] = x;
@@ -547,16 +572,22 @@ __global__ void k_pcell_assign(DevSys d, Params P) {
     atomicAdd(&d.pcell_count[c], 1);
 }
 
-__global__ void k_pcell_scan(DevSys d, int ncell) {
-    if(!d.sc->rebuild) return;
+// Exclusive scan of one system's cell counts (one block per replica of a batch): the replica's
+// cells map onto its own slot range, so replicas rebuild independently.
+__global__ void k_pcell_scan(DevSys d, Params P) {
+    const int r = P.nrep ? (int)blockIdx.x : -1;
+    if(!rebuild_due(d, P, r)) return;
+    const int cbase = P.nrep ? d.reps[r].cbase : 0;
+    const int ncell = P.nrep ? d.reps[r].pnx * d.reps[r].pny * d.reps[r].pnz : P.pnx * P.pny * P.pnz;
+    const int slot0 = P.nrep ? d.reps[r].off : 0;
     __shared__ int warp_tot[32];
     __shared__ int carry;
-    if(threadIdx.x == 0) carry = 0;
+    if(threadIdx.x == 0) carry = slot0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for(int base = 0; base < ncell; base += blockDim.x) {
         const int c = base + threadIdx.x;
-        const int v = (c < ncell) ? d.pcell_count[c] : 0;
+        const int v = (c < ncell) ? d.pcell_count[cbase + c] : 0;
         int x = v;
         for(int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -575,8 +606,8 @@ __global__ void k_pcell_scan(DevSys d, int ncell) {
         __syncthreads();
         const int excl = carry + (warp ? warp_tot[warp - 1] : 0) + x - v;
         if(c < ncell) {
-            d.pcell_first[c] = excl;
-            d.pcell_cursor[c] = 0;
+            d.pcell_first[cbase + c] = excl;
+            d.pcell_cursor[cbase + c] = 0;
         }
         __syncthreads();
         if(threadIdx.x == blockDim.x - 1) carry = excl + v;
@@ -586,7 +617,7 @@ __global__ void k_pcell_scan(DevSys d, int ncell) {
 
 __global__ void k_pcell_scatter(DevSys d, Params P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= P.n || !d.sc->rebuild) return;
+    if(i >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     const int c = d.pcell_of[i];
     const int slot = atomicAdd(&d.pcell_cursor[c], 1);
     d.vcount[d.pcell_first[c] + slot] = i;   // vcount doubles as scratch until the list kernel
@@ -596,10 +627,9 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
 // cell order is the atom's slot: the Verlet list is kept per slot with partners named by slot,
 // and the positions the force gather reads are copied into slot order, so the partners of the
 // atoms a block works on lie in a compact, cache-resident range.
-__global__ void k_pcell_rank(DevSys d, int ncell, bool mixed) {
-    if(!d.sc->rebuild) return;
+__global__ void k_pcell_rank(DevSys d, Params P, int ncell, bool mixed) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if(warp >= ncell) return;
+    if(warp >= ncell || !rebuild_due(d, P, rep_of_cell(d, P, warp))) return;
     const int cnt = d.pcell_count[warp], first = d.pcell_first[warp];
     const int* tmp = d.vcount;
     for(int a = lane; a < cnt; a += 32) {
@@ -630,6 +660,7 @@ __global__ void k_vlist(DevSys d, Params P) {
     const int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(si >= P.n) return;
     const int i = d.pcell_list[si];
+    if(!rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
     const float rfull = fmaxf(v.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? v.rcoul : 0.0f);
     // FP32 distances: rounding (~1e-6 A) is far inside the skin margin
@@ -1268,8 +1299,11 @@ __global__ void k_forces_to_double(DevSys d, Params P) {
     d.F[3 * i + 2] = double(d.Fz[i]) * (1.0 / kFixScale);
 }
 
-__global__ void k_clear_rebuild(DevSys d) {
-    if(threadIdx.x == 0 && blockIdx.x == 0 && d.sc->rebuild) {
+__global__ void k_clear_rebuild(DevSys d, Params P) {
+    if(!d.sc->rebuild) return;
+    for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) d.rsc[r].rebuild = 0;
+    __syncthreads();
+    if(threadIdx.x == 0) {
         d.sc->rebuild = 0;
         d.sc->builds += 1;
     }
@@ -1306,7 +1340,7 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
             const double by = minimg_d(r[1] - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
             const double bz = minimg_d(r[2] - d.r_build[3 * k + 2], P.box[2], 1.0 / P.box[2]);
             const double h = 0.5 * double(P.skin);
-            if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = 1;
+            if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = -1;
         }
         v[0] = d.U[k];
         v[1] = p2 / d.m[k];
@@ -1361,12 +1395,12 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     cudaMemsetAsync(d.pcell_count, 0, sizeof(int) * ncell, s);
     if(P.precision == MTG_PREC_MIXED) k_pcell_assign<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    k_pcell_scan<<<1, 1024, 0, s>>>(d, ncell);
+    k_pcell_scan<<<P.nrep ? P.nrep : 1, 1024, 0, s>>>(d, P);
     k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, ncell, P.precision == MTG_PREC_MIXED);
+    k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, P, ncell, P.precision == MTG_PREC_MIXED);
     if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
-    k_clear_rebuild<<<1, 32, 0, s>>>(d);
+    k_clear_rebuild<<<1, 256, 0, s>>>(d, P);
 }
 
 template<bool MIXED, bool ENERGY>
