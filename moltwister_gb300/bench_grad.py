@@ -51,10 +51,12 @@ def main(argv=None):
     loss.target = e.loss_grad(loss, params, with_grad=False)[2]
     e.set_params(params, base)
     e.loss_grad(loss, params)                          # warm-up
-    t0 = time.perf_counter()
-    for _ in range(args.reps):
-        L, g, _ = e.loss_grad(loss, params)
-    dt = (time.perf_counter() - t0) / args.reps
+    from .clocks import ClockSampler
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            L, g, _ = e.loss_grad(loss, params)
+        dt = (time.perf_counter() - t0) / args.reps
     t0 = time.perf_counter()
     for _ in range(args.reps):
         e.loss_grad(loss, params, with_grad=False)
@@ -83,7 +85,7 @@ def main(argv=None):
     Lm_, gm, _ = em.loss_grad(loss, params)
     out = {"metric": "grads/s", "value": 1.0 / dt, "unit": "loss+gradient evaluations/s", "device": device_name(0),
            "workload": f"water{3 * args.n_mol}_rdf_loss", "steps": args.steps, "checkpoint_every": args.checkpoint,
-           "seconds_per_grad": dt, "seconds_per_loss": dt_fwd, "loss": L,
+           "seconds_per_grad": dt, "seconds_per_loss": dt_fwd, "loss": L, "clocks": clk.summary(),
            "params": dict(zip(names, base.tolist())), "grad": dict(zip(names, g.tolist())),
            "fd": dict(zip(names, fd.tolist())), "rel_diff_vs_fd": dict(zip(names, rel.tolist())),
            "max_rel_diff_vs_fd": float(rel.max()),

@@ -94,8 +94,10 @@ def main(argv=None):
     setup_s = time.perf_counter() - t0
 
     # mixed: throughput and NVE drift from the relaxed start
+    from .clocks import ClockSampler
     em.run(100)                                 # warm-up: graph capture, autotuner
-    ms_m, recs_m = _timed_run(em, args.steps)
+    with ClockSampler(0) as clk_m:
+        ms_m, recs_m = _timed_run(em, args.steps)
 
     # FP64 on the same final state: force error on that (equilibrated) configuration, then its
     # own throughput and drift over a shorter run from there
@@ -113,7 +115,8 @@ def main(argv=None):
     mx = float(np.abs(dF).max() / np.abs(F64).max())
     rms_atom = float(np.sqrt((dF ** 2).sum(1).mean()))
     e64.run(20)
-    ms_64, recs_64 = _timed_run(e64, args.fp64_steps)
+    with ClockSampler(0) as clk_64:
+        ms_64, recs_64 = _timed_run(e64, args.fp64_steps)
     rate_m = n * args.steps / (ms_m * 1e-3)
     rate_64 = n * args.fp64_steps / (ms_64 * 1e-3)
     builds_m = em.stats()["list_builds"]
@@ -135,6 +138,7 @@ def main(argv=None):
         "fp64": {"value": rate_64, "steps": args.fp64_steps, "ms_per_step": ms_64 / args.fp64_steps,
                  "nve_drift_kT_per_atom_per_ns": drift_64, "nve_drift_stderr": se_64, "nve_noise_kT_per_atom": noise_64},
         "speedup_mixed_over_fp64": rate_m / rate_64,
+        "clocks": {"mixed": clk_m.summary(), "fp64": clk_64.summary()},
         "force_error_mixed_vs_fp64": {"rel_rms": rms, "max_rel_to_max_force": mx, "rms_abs_kJ_mol_A": rms_atom,
                                       "configuration": f"after the {args.steps}-step mixed NVE run"},
         "config": {"rho_star": 1.2, "T_star": 0.75, "dt_fs": cfg.timestep, "cutoff": "2.5 sigma_ab per pair, shifted",

@@ -77,14 +77,16 @@ def main(argv=None):
     b = BatchEngine(systems, cfg, temperatures=temps, cutoffs=cutoffs)
     ntot = b.n
     b.run_batch(100, out_stride=100)                 # warm-up: graph capture
+    from .clocks import ClockSampler
     ms = 0.0
     done = 0
     recs = []
-    while done < args.steps:
-        k = min(100, args.steps - done)
-        recs += b.run_batch(k, out_stride=100)
-        ms += b.stats()["device_ms"]
-        done += k
+    with ClockSampler(0) as clk:
+        while done < args.steps:
+            k = min(100, args.steps - done)
+            recs += b.run_batch(k, out_stride=100)
+            ms += b.stats()["device_ms"]
+            done += k
     st = b.stats()
     rate = ntot * args.steps / (ms * 1e-3)
     last = recs[-1][1]
@@ -111,7 +113,7 @@ def main(argv=None):
     out = {"metric": "atom-steps/s", "workload": f"replicas_{args.nrep}", "replicas": args.nrep, "atoms": ntot,
            "device": device_name(0), "value": rate, "steps": args.steps, "ms_per_step": ms / args.steps,
            "serial": {"value": serial_rate, "sample": int(len(sample)), "ms_per_step": serial_ms_per_step},
-           "speedup_batch_over_serial": rate / serial_rate,
+           "speedup_batch_over_serial": rate / serial_rate, "clocks": clk.summary(),
            "graph_steps": st["graph_steps"], "force_team": st["force_team"], "list_builds": st["list_builds"],
            "final_T_K": {"min": float(T_K.min()), "max": float(T_K.max())}, "finite": finite,
            "config": {"argon": "rho* 0.8, LJ 2.5 sigma", "water": "1.0 g/cm3, 10 A, shifted Coulomb",
