@@ -86,6 +86,11 @@ struct mtg_ctx {
     mtg_run_stats stats{};
     // output staging
     std::vector<double> h_r, h_p;
+    // pinned double buffer of the output callback: the copies of output step k land in buffer
+    // k % 2 while the next chunk is already queued, and the callback reads them while it runs
+    double* pin_r[2] = {nullptr, nullptr};
+    double* pin_p[2] = {nullptr, nullptr};
+    cudaEvent_t ev_out[2] = {nullptr, nullptr};
     // batch of replicas (P.nrep > 0)
     std::vector<int> rep_off;          // nrep + 1 atom offsets
     std::vector<double> h_rep_box;     // 3 per replica
@@ -100,6 +105,11 @@ struct mtg_ctx {
         if(vlist_buf) cudaFree(vlist_buf);
         if(ev0) cudaEventDestroy(ev0);
         if(ev1) cudaEventDestroy(ev1);
+        for(int b = 0; b < 2; b++) {
+            if(pin_r[b]) cudaFreeHost(pin_r[b]);
+            if(pin_p[b]) cudaFreeHost(pin_p[b]);
+            if(ev_out[b]) cudaEventDestroy(ev_out[b]);
+        }
         if(stream) cudaStreamDestroy(stream);
     }
 };
@@ -559,6 +569,62 @@ void scale_momenta(mtg_ctx* c, std::vector<double>& p, const std::vector<double>
     for(int r = 0; r < c->P.nrep; r++)
         if(c2[r] != 1.0)
             for(size_t i = (size_t)3 * c->rep_off[r]; i < (size_t)3 * c->rep_off[r + 1]; i++) p[i] *= c2[r];
+}
+
+// One output step whose positions and momenta are on their way into pinned buffer `buf`.
+struct PendingOutput {
+    bool live = false;
+    int buf = 0;
+    int64_t step = 0;
+    double rec[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<double> c2;
+};
+
+// Queues the copies of r and p (with the pending thermostat scales read now) into pinned buffer
+// `buf`; the caller delivers them once the next chunk is queued.
+int queue_output(mtg_ctx* c, int buf, double c2, PendingOutput& out) {
+    const size_t n3 = (size_t)c->P.n * 3;
+    if(!c->pin_r[buf]) {
+        CUDA_TRY(c, cudaMallocHost((void**)&c->pin_r[buf], n3 * sizeof(double)));
+        CUDA_TRY(c, cudaMallocHost((void**)&c->pin_p[buf], n3 * sizeof(double)));
+        CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_out[buf], cudaEventDisableTiming));
+    }
+    out.c2.assign(1, c2);
+    if(c->P.nrep) {
+        int rc = replica_c2(c, out.c2);
+        if(rc) return rc;
+    }
+    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(c->pin_r[buf], c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->pin_p[buf], c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaEventRecord(c->ev_out[buf], c->stream));
+    out.buf = buf;
+    out.live = true;
+    return MTG_OK;
+}
+
+// Waits for a queued output step's copies and calls the callback; *stop is its request to stop.
+int deliver_output(mtg_ctx* c, PendingOutput& o, mtg_output_cb cb, void* user, bool* stop) {
+    *stop = false;
+    if(!o.live) return MTG_OK;
+    o.live = false;
+    CUDA_TRY(c, cudaEventSynchronize(c->ev_out[o.buf]));
+    const size_t n3 = (size_t)c->P.n * 3;
+    std::vector<double> pv(c->pin_p[o.buf], c->pin_p[o.buf] + n3);
+    scale_momenta(c, pv, o.c2);
+    std::memcpy(c->pin_p[o.buf], pv.data(), n3 * sizeof(double));
+    mtg_output out{};
+    out.step = o.step;
+    out.U = o.rec[0];
+    out.K = o.rec[1];
+    out.T = o.rec[2];
+    out.P = o.rec[3];
+    out.V = o.rec[4];
+    out.E = o.rec[0] + o.rec[1];
+    out.r = c->pin_r[o.buf];
+    out.p = c->pin_p[o.buf];
+    *stop = cb(&out, user) != 0;
+    return MTG_OK;
 }
 
 int fetch_rp(mtg_ctx* c, double c2) {
@@ -1377,6 +1443,9 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     float total_ms = 0.0f;
     int t = 0;
     int gen_seen = c->generation;
+    PendingOutput pend;       // the previous output step, delivered while the next chunk runs
+    int nout = 0;
+    int64_t last_done = -1;   // last step of the chunk before the one in flight
     while(t < nsteps) {
         // chunk: up to the next output step (t % out_stride == 0) inclusive
         int next_out = (t % out_stride == 0) ? t : (t / out_stride + 1) * out_stride;
@@ -1397,6 +1466,20 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
             CUDA_TRY(c, cudaGraphLaunch(ge, c->stream));
             CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+            // the previous output step's callback runs on the host while this chunk runs
+            if(pend.live) {
+                bool stop = false;
+                rc = deliver_output(c, pend, cb, user, &stop);
+                if(rc) return rc;
+                if(stop) {
+                    // undo the chunk in flight: back to the state after the delivered step
+                    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+                    restore_snapshot(c);
+                    c->stats.steps = last_done + 1;
+                    c->stats.device_ms = total_ms;
+                    return settle_state(c);
+                }
+            }
             StepScalars s = read_scalars(c);
             CUDA_TRY(c, cudaGetLastError());
             if(s.overflow) {
@@ -1422,30 +1505,23 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
                 if(rrc) return rrc;
                 if(!std::isfinite(rec[0]) || !std::isfinite(rec[1])) return fail(c, MTG_E_NONFINITE, "non-finite energy during the run");
                 if(cb) {
-                    int frc = fetch_rp(c, s.c2);
+                    int frc = queue_output(c, nout & 1, s.c2, pend);
                     if(frc) return frc;
-                    mtg_output o{};
-                    o.step = end;
-                    o.U = rec[0];
-                    o.K = rec[1];
-                    o.T = rec[2];
-                    o.P = rec[3];
-                    o.V = rec[4];
-                    o.E = rec[0] + rec[1];
-                    o.r = c->h_r.data();
-                    o.p = c->h_p.data();
-                    if(cb(&o, user)) {
-                        t = end + 1;
-                        c->stats.steps = t;
-                        c->stats.device_ms = total_ms;
-                        return settle_state(c);
-                    }
+                    pend.step = end;
+                    std::memcpy(pend.rec, rec, sizeof rec);
+                    nout++;
                 }
             }
             break;
         }
+        last_done = end;
         t = end + 1;
         c->stats.graph_steps = steps;
+    }
+    if(pend.live) {
+        bool stop = false;
+        int rc = deliver_output(c, pend, cb, user, &stop);
+        if(rc) return rc;
     }
     c->stats.steps = nsteps;
     c->stats.device_ms = total_ms;

@@ -94,3 +94,25 @@ def test_non_finite_kinetic_energy_is_reported_at_the_step_end(prec, big):
     with pytest.raises(MTGError) as ei:
         e.run(50, out_stride=1000)          # no output step inside the run
     assert ei.value.code == NONFINITE
+
+
+@pytest.mark.parametrize("prec", ["reference", "mixed"])
+def test_output_stream_and_early_stop(prec):
+    """Output steps stream through the pinned double buffer while the next chunk runs: the records
+    carry the positions and momenta of their own step (equal to a run that ends there), and a
+    callback that asks to stop leaves the state after its step even though the next chunk had
+    already been queued."""
+    from moltwister_gb300 import workloads as W
+    s, cfg = W.argon(ncell=5, seed=11, jitter=0.05)
+    cfg.precision = prec
+    e1 = engine(s, cfg)
+    recs = e1.run(100, out_stride=10, callback=lambda rec: rec.step >= 50)
+    assert [r.step for r in recs] == [0, 10, 20, 30, 40, 50]
+    r1, p1, _ = e1.get_state()
+    e2 = engine(s, cfg)
+    recs2 = e2.run(51, out_stride=10)
+    r2, p2, _ = e2.get_state()
+    assert np.array_equal(r1, r2) and np.array_equal(p1, p2)
+    for a, b in zip(recs, recs2):
+        assert a.step == b.step and np.array_equal(a.r, b.r) and np.array_equal(a.p, b.p) and a.U == b.U
+    assert np.array_equal(recs[-1].r, r2) and np.array_equal(recs[-1].p, p2)
