@@ -329,6 +329,10 @@ int mtg_get_params(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, doubl
 int mtg_set_params(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, const double* values);
 /* Total potential energy at the current positions and its derivatives d U / d theta_k. */
 int mtg_energy_grad(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, double* U, double* grad);
+/* A batch's per-replica energies U[nrep] and derivatives grad[r * nparams + k] = d U_r / d theta_k
+ * of the shared force-field parameters, from one force-tangent pass per parameter over all
+ * replicas and deterministic per-replica sums.  The single-system form above refuses batches. */
+int mtg_batch_energy_grad(mtg_ctx* ctx, int32_t nparams, const mtg_param* params, double* U, double* grad);
 
 /* Short-trajectory loss: from the current state, `nsteps` plain velocity-Verlet steps (NVE, no
  * force clipping, whatever the context's ensemble), and the squared deviation

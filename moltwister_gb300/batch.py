@@ -131,6 +131,16 @@ class BatchEngine(Engine):
             raise ValueError("a batch sets chain states per replica (set_thermo)")
         Engine.set_state(self, r, p)
 
+    def energy_grad(self, params):
+        """(U [nrep], dU/dtheta [nrep, nparams]) of every replica at the current positions
+        (C ABI mtg_batch_energy_grad); parameters name the shared force field (self.systems)."""
+        from .engine import _param_array
+        arr, keep = _param_array(params)
+        U = np.zeros(self.nrep)
+        g = np.zeros((self.nrep, len(params)))
+        self._check(self.lib.mtg_batch_energy_grad(self.h, len(params), C.cast(arr, C.c_void_p), _ptr(U), _ptr(g)))
+        return U, g
+
     def replica(self, a: np.ndarray, rep: int) -> np.ndarray:
         return a[self.offsets[rep]:self.offsets[rep + 1]]
 

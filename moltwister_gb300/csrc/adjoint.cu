@@ -431,6 +431,17 @@ __global__ void k_accum_partials(const double* part, int nb, double w, double* o
     out[0] += w * s;
 }
 
+// out[s] = sum of x[off[s] .. off[s+1]) in a fixed order (one block per segment: strided thread
+// sums, then the fixed shuffle tree of block_sum): per-replica totals of a batch.
+__global__ void k_segment_sums(const double* x, const int* off, double* out) {
+    __shared__ double smem[32];
+    const int a = off[blockIdx.x], b = off[blockIdx.x + 1];
+    double v[1] = {0.0};
+    for(int k = a + (int)threadIdx.x; k < b; k += blockDim.x) v[0] += x[k];
+    block_sum<1>(v, smem);
+    if(threadIdx.x == 0) out[blockIdx.x] = v[0];
+}
+
 __global__ void k_inv_mass(int n, const double* m, double* im) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if(k < n) im[k] = 1.0 / m[k];
@@ -513,6 +524,10 @@ int dot_blocks(int n) { return nblk(n, 256); }
 
 void launch_dot_blocks(int n, const double* x, const double* y, double* out, cudaStream_t s) {
     k_dot_blocks<<<nblk(n, 256), 256, 0, s>>>(n, x, y, out);
+}
+
+void launch_segment_sums(const double* x, const int* off, int nseg, double* out, cudaStream_t s) {
+    k_segment_sums<<<nseg, 256, 0, s>>>(x, off, out);
 }
 
 void launch_inv_mass(int n, const double* m, double* im, cudaStream_t s) { k_inv_mass<<<nblk(n, 256), 256, 0, s>>>(n, m, im); }

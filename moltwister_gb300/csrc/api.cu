@@ -2198,9 +2198,10 @@ int dot(mtg_ctx* c, int n, const double* x, const double* y, DBuf& part, double*
     return MTG_OK;
 }
 
-int grad_preflight(mtg_ctx* c, int32_t np, const mtg_param* params) {
+int grad_preflight(mtg_ctx* c, int32_t np, const mtg_param* params, bool batch = false) {
     if(is_reference(c)) return fail(c, MTG_E_UNSUPPORTED, "gradients use the analytic terms of the fp64 / mixed modes");
-    if(c->P.nrep) return fail(c, MTG_E_UNSUPPORTED, "gradients are taken per system, not for batches");
+    if(c->P.nrep && !batch) return fail(c, MTG_E_UNSUPPORTED, "a batch takes its gradients per replica (mtg_batch_energy_grad)");
+    if(!c->P.nrep && batch) return fail(c, MTG_E_INVALID, "not a batch");
     if(c->has_tables) return fail(c, MTG_E_UNSUPPORTED, "tabulated terms have no derivative");
     if(np < 0 || (np > 0 && !params)) return MTG_E_INVALID;
     for(int k = 0; k < np; k++) {
@@ -2269,6 +2270,43 @@ int mtg_energy_grad(mtg_ctx* c, int32_t np, const mtg_param* params, double* U, 
         CUDA_TRY(c, cudaGetLastError());
         rc = dot(c, n, Ut.as<double>(), nullptr, part, &grad[k]);
         if(rc) return rc;
+    }
+    return MTG_OK;
+}
+
+int mtg_batch_energy_grad(mtg_ctx* c, int32_t np, const mtg_param* params, double* U, double* grad) {
+    if(!c || (np > 0 && !grad)) return MTG_E_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = grad_preflight(c, np, params, true);
+    if(rc) return rc;
+    rc = settle_state(c);
+    if(rc) return rc;
+    const int n = c->P.n, nr = c->P.nrep;
+    positions_to_r(c);
+    place_positions(c, c->d.r);
+    launch_prod_force(c->d, c->P, true, c->stream);
+    if(is_mixed(c)) launch_prod_forces_to_double(c->d, c->P, c->stream);
+    DBuf Ft, Ut, off, sums;
+    if((rc = dbuf(c, Ft, sizeof(double) * 3 * n)) || (rc = dbuf(c, Ut, sizeof(double) * n)) ||
+       (rc = dbuf(c, off, sizeof(int) * (nr + 1))) || (rc = dbuf(c, sums, sizeof(double) * nr * (np + 1))))
+        return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(off.p, c->rep_off.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice, c->stream));
+    double* sm = sums.as<double>();
+    launch_segment_sums(c->d.U, off.as<int>(), nr, sm, c->stream);
+    for(int k = 0; k < np; k++) {
+        TangentSet ts;
+        rc = make_tangents(c, params[k], ts);
+        if(rc) return rc;
+        launch_force_tangent(c->d, c->P, c->d.r, ts.t, Ft.as<double>(), Ut.as<double>(), c->stream);
+        launch_segment_sums(Ut.as<double>(), off.as<int>(), nr, sm + (size_t)nr * (k + 1), c->stream);
+        CUDA_TRY(c, cudaGetLastError());
+    }
+    std::vector<double> h((size_t)nr * (np + 1));
+    CUDA_TRY(c, cudaMemcpyAsync(h.data(), sm, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    for(int r = 0; r < nr; r++) {
+        if(U) U[r] = h[r];
+        for(int k = 0; k < np; k++) grad[(size_t)r * np + k] = h[(size_t)nr * (k + 1) + r];
     }
     return MTG_OK;
 }

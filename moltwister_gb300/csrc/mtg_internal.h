@@ -276,6 +276,8 @@ void launch_axpy(int n3, double a, const double* x, const double* scale, double*
 int dot_blocks(int n);
 void launch_dot_blocks(int n, const double* x, const double* y, double* out, cudaStream_t s);
 void launch_inv_mass(int n, const double* m, double* im, cudaStream_t s);
+// out[s] = sum x[off[s] .. off[s+1]) for s < nseg, fixed order
+void launch_segment_sums(const double* x, const int* off, int nseg, double* out, cudaStream_t s);
 void launch_pair_hist(const double* pos, const int* ia, int na, const int* ib, int nb, const double* box, double rmin,
                       double rmax, int nbins, double ignore_below, unsigned long long* prof, cudaStream_t s);
 // out[0] += w * sum_k x[k] y[k] (deterministic; part holds dot_blocks(n) partials)

@@ -152,6 +152,7 @@ def load_library(path: str = LIB_PATH):
         "mtg_get_params": ([P, C.c_int32, P, P], C.c_int),
         "mtg_set_params": ([P, C.c_int32, P, P], C.c_int),
         "mtg_energy_grad": ([P, C.c_int32, P, P, P], C.c_int),
+        "mtg_batch_energy_grad": ([P, C.c_int32, P, P, P], C.c_int),
         "mtg_loss_grad": ([P, C.POINTER(LossDesc), C.c_int32, P, P, P, P], C.c_int),
         "mtg_pair_histogram": ([P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, P], C.c_int),
         "mtg_dcd_append": ([C.c_char_p, C.c_int32, P, P, C.c_int32, C.c_int32, C.c_double], C.c_int),

@@ -68,3 +68,31 @@ def test_batch_thermostats_hold_their_temperatures():
     outs = b.run_batch(3000, out_stride=100)
     T_K = np.array([o[1][:, 0] for o in outs[-10:]]) * 120.272    # kJ/mol -> K, last 1,000 steps
     assert np.allclose(T_K.mean(0), temps, rtol=0.15), T_K.mean(0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_energy_gradients_match_single_systems(prec):
+    """mtg_batch_energy_grad: every replica's energy and its derivatives with respect to shared
+    force-field parameters (LJ sigma and epsilon of both species, the water charge scale, bond k)
+    equal those of the same replica alone (the fixed-point forces and the per-atom tangents are
+    summed in a fixed order per replica; FP64 tangents)."""
+    from moltwister_gb300 import grad as Gr
+    from moltwister_gb300.batch import BatchEngine, shared_force_field
+    from moltwister_gb300.engine import Engine
+    systems, temps = replica_systems()
+    cfg = shared_config(300.0)
+    cfg.precision = prec
+    b = BatchEngine(systems, cfg, temperatures=temps)
+    ff = b.systems
+    s0 = ff[1]                                  # the water replica names every type of the union
+    params = [Gr.lj_sigma(s0, "Ar", "Ar"), Gr.lj_eps(s0, "Ow", "Ow"), Gr.bond_k(s0, 0)]
+    U, g = b.energy_grad(params)
+    for k, sk in enumerate(shared_force_field(systems)):
+        ck = shared_config(temps[k])
+        ck.precision = prec
+        e = Engine(sk, ck)
+        Uk, gk = e.energy_grad(params)
+        assert abs(U[k] - Uk) <= 1e-12 * max(1.0, abs(Uk)), (k, U[k], Uk)
+        assert np.allclose(g[k], gk, rtol=1e-11, atol=1e-9 * np.abs(gk).max()), (k, g[k], gk)
+        e.close()
