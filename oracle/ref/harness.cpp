@@ -40,6 +40,7 @@
 #include "Cmd/Tools/MolTwisterStateTools.h"
 #include "Utilities/DCDFile.h"
 #include "Cmd/MolTwisterCmdCalculate/CmdPairCorrelation.h"
+#include "adapter.h"
 #include <functional>
 #include <tuple>
 
@@ -458,6 +459,49 @@ int cmdPairCorr(const SysIn& s, const std::string& out, int nframes, double shif
     return 0;
 }
 
+// desc: the descriptors the adapter (adapter.cpp) builds from the reference's objects
+int cmdDesc(const SysIn& s, const std::string& out) {
+    CMolTwisterState st; buildState(s, st);
+    SMolDynConfigStruct cfg = makeCfg(s);
+    FILE* devnull = fopen("/dev/null", "w");
+    COut::setStdOut(devnull);
+    mtgpu_adapter::Descriptors d;
+    std::string err;
+    if(!mtgpu_adapter::build(&st, cfg, d, err)) {
+        fprintf(stderr, "%s\n", err.c_str());
+        return 1;
+    }
+    auto terms = [](const std::vector<mtg_term>& v, std::vector<int32_t>& kind, std::vector<double>& p) {
+        for(const mtg_term& t : v) {
+            kind.push_back(t.kind);
+            for(int k = 0; k < 4; k++) p.push_back(t.p[k]);
+        }
+    };
+    std::vector<int32_t> nk, bk, ak, dk;
+    std::vector<double> np_, bp, ap, dp;
+    terms(d.nb_terms, nk, np_);
+    terms(d.bond_terms, bk, bp);
+    terms(d.angle_terms, ak, ap);
+    terms(d.dih_terms, dk, dp);
+    std::vector<int32_t> mob(d.mobile.begin(), d.mobile.end());
+    const mtg_config_desc& c = d.cfg;
+    std::vector<double> cfgv = {(double)c.ensemble, (double)c.temperature_nh_len, (double)c.temperature_respa,
+                                (double)c.pressure_nh_len, (double)c.pressure_respa, c.timestep, c.temperature,
+                                c.temperature_relax, c.pressure, c.pressure_relax, c.cutoff_radius, c.neigh_shell,
+                                c.cutoff_force, c.scale12, c.scale13, c.scale14, c.scale1N};
+    MtbWriter w(out);
+    w.d("r", d.r); w.d("mass", d.mass); w.d("charge", d.charge); w.i("type", d.type); w.i("mol", d.mol); w.i("mobile", mob);
+    w.d("box", {d.sys.box[0], d.sys.box[1], d.sys.box[2]});
+    w.i("nb_count", d.nb_count); w.i("nb_kind", nk); w.d("nb_p", np_); w.f("nb_tables", d.nb_tables);
+    w.i("bond_kind", bk); w.d("bond_p", bp); w.f("bond_tables", d.bond_tables);
+    w.i("angle_kind", ak); w.d("angle_p", ap); w.f("angle_tables", d.angle_tables);
+    w.i("dih_kind", dk); w.d("dih_p", dp); w.f("dih_tables", d.dih_tables);
+    w.i("bonds", d.bonds); w.i("angles", d.angles); w.i("dihedrals", d.dihedrals);
+    w.d("cfg", cfgv);
+    fclose(devnull);
+    return 0;
+}
+
 // init: the initial state the reference's CSimulationBox constructor draws (initSystem,
 // SimulationBox.cpp:53-96) after srand(seed); seed 1 is also what a fresh process draws with
 int cmdInit(const SysIn& s, const std::string& out, unsigned seed) {
@@ -490,7 +534,7 @@ int cmdInit(const SysIn& s, const std::string& out, unsigned seed) {
 
 int main(int argc, char** argv) {
     if(argc < 3) {
-        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT | init SYS OUT SEED | paircorr SYS OUT NFRAMES SHIFT ARGS...\n");
+        fprintf(stderr, "usage: mtref static SYS OUT | run SYS OUT NSTEPS STRIDE | time SYS NSTEPS | dcd SYS OUT NSTEPS STRIDE DT | init SYS OUT SEED | paircorr SYS OUT NFRAMES SHIFT ARGS... | desc SYS OUT\n");
         return 1;
     }
     std::string cmd = argv[1];
@@ -500,6 +544,7 @@ int main(int argc, char** argv) {
     if(cmd == "time" && argc >= 4) return cmdTime(s, atoi(argv[3]));
     if(cmd == "dcd" && argc >= 7) return cmdDcd(s, argv[3], atoi(argv[4]), atoi(argv[5]), atof(argv[6]));
     if(cmd == "init" && argc >= 5) return cmdInit(s, argv[3], (unsigned)strtoul(argv[4], nullptr, 10));
+    if(cmd == "desc" && argc >= 4) return cmdDesc(s, argv[3]);
     if(cmd == "paircorr" && argc >= 6) {
         std::vector<std::string> rest(argv + 6, argv + argc);
         return cmdPairCorr(s, argv[3], atoi(argv[4]), atof(argv[5]), rest);
