@@ -27,7 +27,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE
 UNITS = [
     ("ref_kernels.cu", ["-fmad=false"]),
     ("md_kernels.cu", ["-Xptxas", "-v"] if os.environ.get("MTG_PTXAS_VERBOSE") else []),
-    ("api.cu", []),
+    ("api.cu", ["-Xcompiler", "-ffp-contract=off"]),
     ("adjoint.cu", []),
     ("tables.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("writers.cpp", []),

@@ -131,13 +131,22 @@ int fail(mtg_ctx* c, int code, const std::string& msg) {
         }                                                                                          \
     } while(0)
 
+// A copy ordered after the work already queued on the context's stream and complete when it
+// returns.  The stream is non-blocking, so a plain cudaMemcpy (legacy default stream) would
+// neither wait for that work nor be waited for by it.
+cudaError_t copy_now(mtg_ctx* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, c->stream);
+    if(e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e;
+}
+
 template<class T>
 int dalloc(mtg_ctx* c, T** out, size_t count) {
     void* p = nullptr;
     size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
     cudaError_t e = cudaMalloc(&p, bytes);
     if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    cudaMemset(p, 0, bytes);
+    cudaMemsetAsync(p, 0, bytes, c->stream);
     c->bufs.push_back(p);
     *out = (T*)p;
     return MTG_OK;
@@ -147,7 +156,7 @@ template<class T>
 int upload(mtg_ctx* c, T** out, const T* host, size_t count) {
     int rc = dalloc(c, out, count);
     if(rc) return rc;
-    if(count && host) CUDA_TRY(c, cudaMemcpy(*out, host, count * sizeof(T), cudaMemcpyHostToDevice));
+    if(count && host) CUDA_TRY(c, copy_now(c, *out, host, count * sizeof(T), cudaMemcpyHostToDevice));
     return MTG_OK;
 }
 
@@ -554,21 +563,33 @@ int replica_c2(mtg_ctx* c, std::vector<double>& c2) {
         return MTG_OK;
     }
     std::vector<StepScalars> rs(c->P.nrep);
-    CUDA_TRY(c, cudaMemcpy(rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, copy_now(c, rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
     c2.resize(rs.size());
     for(size_t r = 0; r < rs.size(); r++) c2[r] = rs[r].c2;
     return MTG_OK;
 }
 
+// A double rounded to the nearest double-float pair (hi = float(x), lo = float(x - hi)) and back,
+// as the mixed mode stores a momentum the host scaled (k_sync, then the FP64 master from hi + lo).
+double round_df(double x) {
+    const float h = (float)x;
+    return (double)h + (double)(float)(x - (double)h);
+}
+
+// Momenta times the pending thermostat scale c2 of their system; in the mixed mode the result is
+// rounded as the device stores it, so an output record's momenta equal the state a run that ends
+// at that step leaves.
 void scale_momenta(mtg_ctx* c, std::vector<double>& p, const std::vector<double>& c2) {
+    const bool df = is_mixed(c);
     if(!c->P.nrep) {
         if(c2[0] != 1.0)
-            for(double& v : p) v *= c2[0];
+            for(double& v : p) v = df ? round_df(v * c2[0]) : v * c2[0];
         return;
     }
     for(int r = 0; r < c->P.nrep; r++)
         if(c2[r] != 1.0)
-            for(size_t i = (size_t)3 * c->rep_off[r]; i < (size_t)3 * c->rep_off[r + 1]; i++) p[i] *= c2[r];
+            for(size_t i = (size_t)3 * c->rep_off[r]; i < (size_t)3 * c->rep_off[r + 1]; i++)
+                p[i] = df ? round_df(p[i] * c2[r]) : p[i] * c2[r];
 }
 
 // One output step whose positions and momenta are on their way into pinned buffer `buf`.
@@ -695,12 +716,12 @@ BaroDev baro_at(const Params& P, double p_eps, double eps) {
 // atoms, P the mean of the replicas' pressures.
 int read_records(mtg_ctx* c, double* rec) {
     if(!c->P.nrep) {
-        CUDA_TRY(c, cudaMemcpy(rec, c->d.rec, sizeof(double) * 8, cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, rec, c->d.rec, sizeof(double) * 8, cudaMemcpyDeviceToHost));
         return MTG_OK;
     }
     const int nr = c->P.nrep;
     c->h_rrec.resize((size_t)nr * 8);
-    CUDA_TRY(c, cudaMemcpy(c->h_rrec.data(), c->d.rrec, sizeof(double) * 8 * nr, cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, copy_now(c, c->h_rrec.data(), c->d.rrec, sizeof(double) * 8 * nr, cudaMemcpyDeviceToHost));
     for(int q = 0; q < 8; q++) rec[q] = 0.0;
     for(int r = 0; r < nr; r++) {
         const double* x = &c->h_rrec[(size_t)8 * r];
@@ -720,19 +741,19 @@ int settle_state(mtg_ctx* c) {
     if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
     if(c->P.ensemble == MTG_NPT) {
         BaroDev b{};
-        CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, &b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
         b.p_eps = b.p_eps_saved;
         b.eps = b.eps_saved;
         for(int a = 0; a < 3; a++) {
             b.L[a] = b.L_saved[a];
             b.Lf[a] = (float)b.L[a];
         }
-        CUDA_TRY(c, cudaMemcpy(c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
-        CUDA_TRY(c, cudaMemcpy(c->d.thp, c->d.thp_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.thp, c->d.thp_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
     }
     if(c->P.nrep) {
         std::vector<StepScalars> rs(c->P.nrep);
-        CUDA_TRY(c, cudaMemcpy(rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
         std::vector<double> c2(rs.size());
         bool any = false;
         for(size_t r = 0; r < rs.size(); r++) {
@@ -741,30 +762,30 @@ int settle_state(mtg_ctx* c) {
         }
         if(any) {
             std::vector<double> p((size_t)c->P.n * 3);
-            CUDA_TRY(c, cudaMemcpy(p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            CUDA_TRY(c, copy_now(c, p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
             scale_momenta(c, p, c2);
-            CUDA_TRY(c, cudaMemcpy(c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, copy_now(c, c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
             if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
-            CUDA_TRY(c, cudaMemcpy(c->d.ths, c->d.ths_saved, sizeof(ThermoDev) * rs.size(), cudaMemcpyDeviceToDevice));
+            CUDA_TRY(c, copy_now(c, c->d.ths, c->d.ths_saved, sizeof(ThermoDev) * rs.size(), cudaMemcpyDeviceToDevice));
             for(auto& x : rs) {
                 x.c2 = 1.0;
                 x.S = 1.0;
             }
-            CUDA_TRY(c, cudaMemcpy(c->d.rsc, rs.data(), sizeof(StepScalars) * rs.size(), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, copy_now(c, c->d.rsc, rs.data(), sizeof(StepScalars) * rs.size(), cudaMemcpyHostToDevice));
         }
         return MTG_OK;
     }
     StepScalars s = read_scalars(c);
     if(s.c2 != 1.0 || s.S != 1.0) {
         std::vector<double> p((size_t)c->P.n * 3);
-        CUDA_TRY(c, cudaMemcpy(p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        for(double& v : p) v *= s.c2;
-        CUDA_TRY(c, cudaMemcpy(c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        scale_momenta(c, p, std::vector<double>(1, s.c2));
+        CUDA_TRY(c, copy_now(c, c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
         if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
-        CUDA_TRY(c, cudaMemcpy(c->d.th, c->d.th_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.th, c->d.th_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
         s.c2 = 1.0;
         s.S = 1.0;
-        CUDA_TRY(c, cudaMemcpy(c->d.sc, &s, sizeof(s), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.sc, &s, sizeof(s), cudaMemcpyHostToDevice));
     }
     return MTG_OK;
 }
@@ -1253,22 +1274,22 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             for(int j = 1; j < P.M; j++) th.Q[j] = P.kT * P.tau * P.tau;
         }
         for(int j = 0; j < kMaxChain; j++) th.iQ[j] = 1.0 / th.Q[j];
-        cudaMemcpy(d.th, &th, sizeof(th), cudaMemcpyHostToDevice);
-        cudaMemcpy(d.th_saved, &th, sizeof(th), cudaMemcpyHostToDevice);
+        copy_now(c.get(), d.th, &th, sizeof(th), cudaMemcpyHostToDevice);
+        copy_now(c.get(), d.th_saved, &th, sizeof(th), cudaMemcpyHostToDevice);
         StepScalars s{};
         s.S = 1.0;
         s.c2 = 1.0;
-        cudaMemcpy(d.sc, &s, sizeof(s), cudaMemcpyHostToDevice);
+        copy_now(c.get(), d.sc, &s, sizeof(s), cudaMemcpyHostToDevice);
         // barostat chain: prepareArrays(1, 1) gives Q0 = kT tauP^2 as well (NHChain.cpp:115-124)
         ThermoDev tp{};
         for(int j = 0; j < kMaxChain; j++) tp.Q[j] = 1.0;
         if(P.ensemble == MTG_NPT)
             for(int j = 0; j < P.MP; j++) tp.Q[j] = P.W;
         for(int j = 0; j < kMaxChain; j++) tp.iQ[j] = 1.0 / tp.Q[j];
-        cudaMemcpy(d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice);
-        cudaMemcpy(d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice);
+        copy_now(c.get(), d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice);
+        copy_now(c.get(), d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice);
         BaroDev b = baro_at(P, 0.0, 0.0);
-        cudaMemcpy(d.baro, &b, sizeof(b), cudaMemcpyHostToDevice);
+        copy_now(c.get(), d.baro, &b, sizeof(b), cudaMemcpyHostToDevice);
     }
     // list capacities: start from a density estimate, grown on demand
     {
@@ -1351,37 +1372,37 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
     if(rc) return rc;
     if(r) {
         if(!finite_all(r, n3)) return fail(c, MTG_E_NONFINITE, "non-finite positions");
-        CUDA_TRY(c, cudaMemcpy(c->d.r, r, n3 * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.r, r, n3 * sizeof(double), cudaMemcpyHostToDevice));
     }
     if(p) {
         if(!finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
-        CUDA_TRY(c, cudaMemcpy(c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
     }
     if((r || p) && is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
     if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch sets chain states per replica (mtg_batch_set_thermo)");
     if(th) {
         ThermoDev t{};
-        CUDA_TRY(c, cudaMemcpy(&t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, &t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
         const int M = std::min<int>(th->M, kMaxChain);
         for(int j = 0; j < M; j++) {
             t.eta[j] = th->eta[j];
             t.peta[j] = th->p_eta[j];
         }
-        CUDA_TRY(c, cudaMemcpy(c->d.th, &t, sizeof(t), cudaMemcpyHostToDevice));
-        CUDA_TRY(c, cudaMemcpy(c->d.th_saved, &t, sizeof(t), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.th, &t, sizeof(t), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, c->d.th_saved, &t, sizeof(t), cudaMemcpyHostToDevice));
         if(c->P.ensemble == MTG_NPT) {
             if(!std::isfinite(th->p_eps) || !std::isfinite(th->eps)) return fail(c, MTG_E_NONFINITE, "non-finite barostat state");
             ThermoDev tp{};
-            CUDA_TRY(c, cudaMemcpy(&tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
+            CUDA_TRY(c, copy_now(c, &tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
             const int MP = std::min<int>(th->MP, kMaxChain);
             for(int j = 0; j < MP; j++) {
                 tp.eta[j] = th->etaP[j];
                 tp.peta[j] = th->p_etaP[j];
             }
-            CUDA_TRY(c, cudaMemcpy(c->d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice));
-            CUDA_TRY(c, cudaMemcpy(c->d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, copy_now(c, c->d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, copy_now(c, c->d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice));
             BaroDev b = baro_at(c->P, th->p_eps, th->eps);
-            CUDA_TRY(c, cudaMemcpy(c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, copy_now(c, c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
             if(!r) return compute_forces_now(c, true);   // the box may have changed
         }
     }
@@ -1404,7 +1425,7 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
     if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch reads chain states per replica (mtg_batch_get_thermo)");
     if(th) {
         ThermoDev t{};
-        CUDA_TRY(c, cudaMemcpy(&t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, &t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
         std::memset(th, 0, sizeof(*th));
         th->M = c->P.M;
         for(int j = 0; j < c->P.M; j++) {
@@ -1415,8 +1436,8 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
         if(c->P.ensemble == MTG_NPT) {
             ThermoDev tp{};
             BaroDev b{};
-            CUDA_TRY(c, cudaMemcpy(&tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
-            CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+            CUDA_TRY(c, copy_now(c, &tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
+            CUDA_TRY(c, copy_now(c, &b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
             th->MP = c->P.MP;
             for(int j = 0; j < c->P.MP; j++) {
                 th->etaP[j] = tp.eta[j];
@@ -1587,7 +1608,7 @@ int mtg_get_neighbors(mtg_ctx* c, int32_t max_neigh, int32_t* count, int32_t* li
     }
     const int n = c->P.n;
     std::vector<int> cnt(n);
-    CUDA_TRY(c, cudaMemcpy(cnt.data(), c->d.nbr_count, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, copy_now(c, cnt.data(), c->d.nbr_count, sizeof(int) * n, cudaMemcpyDeviceToHost));
     int mx = 0;
     for(int v : cnt) mx = std::max(mx, v);
     if(needed) *needed = mx;
@@ -1595,7 +1616,7 @@ int mtg_get_neighbors(mtg_ctx* c, int32_t max_neigh, int32_t* count, int32_t* li
     if(list) {
         if(max_neigh < mx) return fail(c, MTG_E_INVALID, "max_neigh smaller than the longest list");
         std::vector<int> tmp((size_t)n * c->d.nbr_max);
-        CUDA_TRY(c, cudaMemcpy(tmp.data(), c->d.nbr_list, tmp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, tmp.data(), c->d.nbr_list, tmp.size() * sizeof(int), cudaMemcpyDeviceToHost));
         for(int k = 0; k < n; k++)
             for(int e = 0; e < max_neigh; e++) list[(size_t)k * max_neigh + e] = e < cnt[k] ? tmp[(size_t)k * c->d.nbr_max + e] : -1;
     }
@@ -1617,7 +1638,7 @@ int mtg_optimize(mtg_ctx* c, double accuracy, int max_steps, int out_stride, mtg
         rc = compute_forces_now(c, true);
         if(rc) return rc;
         std::vector<double> U(c->P.n);
-        CUDA_TRY(c, cudaMemcpy(U.data(), c->d.U, sizeof(double) * c->P.n, cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, U.data(), c->d.U, sizeof(double) * c->P.n, cudaMemcpyDeviceToHost));
         for(double u : U) U_n += u;
     }
     c->stats = mtg_run_stats{};
@@ -1909,14 +1930,14 @@ int mtg_batch_set_thermo(mtg_ctx* c, int32_t rep, const mtg_thermo_state* th) {
     int rc = settle_state(c);
     if(rc) return rc;
     ThermoDev t{};
-    CUDA_TRY(c, cudaMemcpy(&t, c->d.ths + rep, sizeof(t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, copy_now(c, &t, c->d.ths + rep, sizeof(t), cudaMemcpyDeviceToHost));
     const int M = std::min<int>(th->M, kMaxChain);
     for(int j = 0; j < M; j++) {
         t.eta[j] = th->eta[j];
         t.peta[j] = th->p_eta[j];
     }
-    CUDA_TRY(c, cudaMemcpy(c->d.ths + rep, &t, sizeof(t), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy(c->d.ths_saved + rep, &t, sizeof(t), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, c->d.ths + rep, &t, sizeof(t), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, c->d.ths_saved + rep, &t, sizeof(t), cudaMemcpyHostToDevice));
     return MTG_OK;
 }
 
@@ -1927,7 +1948,7 @@ int mtg_batch_get_thermo(mtg_ctx* c, int32_t rep, mtg_thermo_state* th) {
     int rc = settle_state(c);
     if(rc) return rc;
     ThermoDev t{};
-    CUDA_TRY(c, cudaMemcpy(&t, c->d.ths + rep, sizeof(t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, copy_now(c, &t, c->d.ths + rep, sizeof(t), cudaMemcpyDeviceToHost));
     std::memset(th, 0, sizeof(*th));
     th->M = c->P.M;
     for(int j = 0; j < c->P.M; j++) {
@@ -2051,15 +2072,15 @@ int push_params(mtg_ctx* c) {
     DevSys& d = c->d;
     const int n = c->P.n;
     std::vector<float> f(c->h_nb_coef.begin(), c->h_nb_coef.end());
-    CUDA_TRY(c, cudaMemcpy((void*)d.nb_par, c->h_nb_coef.data(), c->h_nb_coef.size() * sizeof(double), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy((void*)d.nb_parf, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, (void*)d.nb_par, c->h_nb_coef.data(), c->h_nb_coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, (void*)d.nb_parf, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
     std::vector<float> fsf(c->h_nb_fs.begin(), c->h_nb_fs.end());
-    CUDA_TRY(c, cudaMemcpy((void*)d.nb_fs, c->h_nb_fs.data(), c->h_nb_fs.size() * sizeof(double), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy((void*)d.nb_fsf, fsf.data(), fsf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, (void*)d.nb_fs, c->h_nb_fs.data(), c->h_nb_fs.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, (void*)d.nb_fsf, fsf.data(), fsf.size() * sizeof(float), cudaMemcpyHostToDevice));
     auto push = [&](const std::vector<double>& h, const double* dd, const float* df) -> int {
         std::vector<float> hf(h.begin(), h.end());
-        CUDA_TRY(c, cudaMemcpy((void*)dd, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
-        CUDA_TRY(c, cudaMemcpy((void*)df, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, (void*)dd, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, (void*)df, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
         return MTG_OK;
     };
     int rc = push(c->h_bond_par, d.bond_par, d.bond_parf);
@@ -2067,8 +2088,8 @@ int push_params(mtg_ctx* c) {
     if(rc) return rc;
     std::vector<float> qf(n);
     for(int i = 0; i < n; i++) qf[i] = (float)c->h_charge[i];
-    CUDA_TRY(c, cudaMemcpy(d.qd, c->h_charge.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy(d.qf, qf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, d.qd, c->h_charge.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, d.qf, qf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     // per-type charge table (and whether it describes every atom)
     const int T = c->P.T;
     std::vector<float> qt(std::max(T, 1), 0.0f);
@@ -2079,7 +2100,7 @@ int push_params(mtg_ctx* c) {
         if(!seen[t]) { seen[t] = 1; qt[t] = qf[i]; }
         else if(qt[t] != qf[i]) uniform = false;
     }
-    CUDA_TRY(c, cudaMemcpy((void*)d.qtype, qt.data(), sizeof(float) * qt.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, (void*)d.qtype, qt.data(), sizeof(float) * qt.size(), cudaMemcpyHostToDevice));
     if((uniform ? 1 : 0) != c->P.qtype) {
         c->P.qtype = uniform ? 1 : 0;
         c->generation++;   // captured graphs hold the old flag
@@ -2134,8 +2155,8 @@ int make_tangents(mtg_ctx* c, const mtg_param& p, TangentSet& ts) {
         int rc = dbuf(c, ts.nb, nt.size() * sizeof(double));
         if(!rc) rc = dbuf(c, ts.fs, ft.size() * sizeof(double));
         if(rc) return rc;
-        CUDA_TRY(c, cudaMemcpy(ts.nb.p, nt.data(), nt.size() * sizeof(double), cudaMemcpyHostToDevice));
-        CUDA_TRY(c, cudaMemcpy(ts.fs.p, ft.data(), ft.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, ts.nb.p, nt.data(), nt.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, ts.fs.p, ft.data(), ft.size() * sizeof(double), cudaMemcpyHostToDevice));
         ts.t.nb_par_t = ts.nb.as<double>();
         ts.t.nb_fs_t = ts.fs.as<double>();
         return MTG_OK;
@@ -2143,7 +2164,7 @@ int make_tangents(mtg_ctx* c, const mtg_param& p, TangentSet& ts) {
     case MTG_P_CHARGE: {
         int rc = dbuf(c, ts.q, sizeof(double) * n);
         if(rc) return rc;
-        CUDA_TRY(c, cudaMemcpy(ts.q.p, p.dq, sizeof(double) * n, cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, ts.q.p, p.dq, sizeof(double) * n, cudaMemcpyHostToDevice));
         ts.t.q_t = ts.q.as<double>();
         return MTG_OK;
     }
@@ -2153,7 +2174,7 @@ int make_tangents(mtg_ctx* c, const mtg_param& p, TangentSet& ts) {
         bt[4 * p.index + (p.kind == MTG_P_BOND_K ? 0 : 1)] = 1.0;
         int rc = dbuf(c, ts.bond, bt.size() * sizeof(double));
         if(rc) return rc;
-        CUDA_TRY(c, cudaMemcpy(ts.bond.p, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, ts.bond.p, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice));
         ts.t.bond_par_t = ts.bond.as<double>();
         return MTG_OK;
     }
@@ -2164,7 +2185,7 @@ int make_tangents(mtg_ctx* c, const mtg_param& p, TangentSet& ts) {
         else at[4 * p.index + 1] = c->h_angle_par[4 * p.index + 2];   // d(theta0 rad)/d(theta0 deg)
         int rc = dbuf(c, ts.angle, at.size() * sizeof(double));
         if(rc) return rc;
-        CUDA_TRY(c, cudaMemcpy(ts.angle.p, at.data(), at.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, ts.angle.p, at.data(), at.size() * sizeof(double), cudaMemcpyHostToDevice));
         ts.t.angle_par_t = ts.angle.as<double>();
         return MTG_OK;
     }
@@ -2359,9 +2380,9 @@ int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_para
         // 1/m for mobile atoms, 0 for immobile ones (their positions never change)
         std::vector<double> im(n);
         std::vector<int> mob(n);
-        CUDA_TRY(c, cudaMemcpy(mob.data(), c->d.mobile, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, mob.data(), c->d.mobile, sizeof(int) * n, cudaMemcpyDeviceToHost));
         for(int i = 0; i < n; i++) im[i] = mob[i] ? 1.0 / c->h_mass[i] : 0.0;
-        CUDA_TRY(c, cudaMemcpy(invm.p, im.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        CUDA_TRY(c, copy_now(c, invm.p, im.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     }
     AdjRdf rs{L->type_a, L->type_b, L->nbins, L->rmax, L->width};
     const double dt = c->P.dt;
@@ -2412,7 +2433,7 @@ int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_para
     }
     // ---- loss ----
     std::vector<double> h(L->nbins), norm(L->nbins), gbar(L->nbins), w(L->nbins);
-    CUDA_TRY(c, cudaMemcpy(h.data(), hist.p, sizeof(double) * L->nbins, cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, copy_now(c, h.data(), hist.p, sizeof(double) * L->nbins, cudaMemcpyDeviceToHost));
     long long na = 0, nb = 0;
     for(int i = 0; i < n; i++) {
         na += (c->h_type[i] == L->type_a);
@@ -2432,7 +2453,7 @@ int mtg_loss_grad(mtg_ctx* c, const mtg_loss_desc* L, int32_t np, const mtg_para
     }
     if(loss) *loss = Lval;
     if(rdf) std::memcpy(rdf, gbar.data(), sizeof(double) * L->nbins);
-    CUDA_TRY(c, cudaMemcpy(cb.p, w.data(), sizeof(double) * L->nbins, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, copy_now(c, cb.p, w.data(), sizeof(double) * L->nbins, cudaMemcpyHostToDevice));
     if(np == 0 || !grad) {
         rc = restore_state(r0.as<double>(), p0.as<double>());
         if(rc) return rc;
@@ -2518,7 +2539,7 @@ int mtg_pair_histogram(mtg_ctx* c, int32_t type_a, int32_t type_b, int32_t nbins
     double box[3] = {c->P.box[0], c->P.box[1], c->P.box[2]};
     if(c->P.ensemble == MTG_NPT) {
         BaroDev b{};
-        CUDA_TRY(c, cudaMemcpy(&b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, copy_now(c, &b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
         for(int a = 0; a < 3; a++) box[a] = b.L[a];
     }
     launch_pair_hist(c->d.r, dia.as<int>(), (int)ia.size(), dib.as<int>(), (int)ib.size(), box, rmin, rmax, nbins, ignore_below,
