@@ -84,7 +84,15 @@ extern "C" {
 #define MTG_COULOMB_SHIFTED 2  /* shifted force, zero force and energy at coulomb_cutoff (new option):
                                   F = K qi qj (1/r^2 - 1/rc^2), U = K qi qj (1/r - 1/rc + (r - rc)/rc^2) */
 
-/* Ensembles (SMolDynConfigStruct::Ensemble, MolDynConfigStruct.h:24) */
+/* Ensembles (SMolDynConfigStruct::Ensemble, MolDynConfigStruct.h:24).  NPT runs the reference's
+ * MTK barostat and barostat chain (VelVerlet.cpp:57-71, 124-211, MDLoop.cpp:62-83) in every
+ * precision mode; a batch refuses it.  The reference precision mode reproduces the reference's
+ * arithmetic (barostat mass kT tauP^2, driven by sum F.r over wrapped positions).  The fp64 and
+ * mixed modes drive the barostat with the pair virial (every pair's r_ij . F_ij plus the bonded
+ * terms' virial), give it the MTK mass 3 (N + 1) kT tauP^2, and keep their Verlet list valid as
+ * the box changes (the displacement test scales the build positions with the box; the cell grid
+ * follows the box).  A box that shrinks until a cutoff reaches half its width ends the run with
+ * MTG_E_UNSUPPORTED. */
 #define MTG_NVT 0
 #define MTG_NPT 1
 #define MTG_NVE 2

@@ -326,7 +326,7 @@ void clear_overflow(mtg_ctx* c) {
     // zero overflow, needed, nonfinite (contiguous int32 fields) and the timeout flags (the
     // system's and, in a batch, each replica's): each chunk reports its own
     cudaMemsetAsync(&c->d.sc->overflow, 0, 3 * sizeof(int32_t), c->stream);
-    cudaMemsetAsync(&c->d.sc->timeout, 0, sizeof(int32_t), c->stream);
+    cudaMemsetAsync(&c->d.sc->timeout, 0, 2 * sizeof(int32_t), c->stream);   // timeout, boxerr
     if(c->P.nrep) {
         cudaMemset2DAsync(&c->d.rsc[0].timeout, sizeof(StepScalars), 0, sizeof(int32_t), c->P.nrep, c->stream);
         cudaMemset2DAsync(&c->d.rsc[0].nonfinite, sizeof(StepScalars), 0, sizeof(int32_t), c->P.nrep, c->stream);
@@ -552,6 +552,9 @@ void take_snapshot(mtg_ctx* c) {
 
 void restore_snapshot(mtg_ctx* c) {
     for(auto& s : c->snaps) cudaMemcpyAsync((void*)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice, c->stream);
+    // production NPT: the restored barostat state holds the box of an earlier list build than the
+    // list in place, so the next step rebuilds it
+    if(c->P.ensemble == MTG_NPT && !is_reference(c)) cudaMemsetAsync(&c->d.sc->rebuild, 0xff, sizeof(int32_t), c->stream);
 }
 
 // Host copies of r and p after a step; p carries the pending scale c2 of the last second
@@ -696,7 +699,12 @@ struct BatchSpec {
 
 // Barostat state with momentum p_eps and strain eps: box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax
 // (VelVerlet.cpp:192-211); the saved copy equals the live one (no step pending).
-BaroDev baro_at(const Params& P, double p_eps, double eps) {
+// Barostat state at strain eps (box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax, VelVerlet.cpp:198-211).
+// `box`, when given, is that box as a previous get_state returned it: used as is when it agrees
+// with eps to rounding, so that a state written back continues bit for bit.  The production modes
+// also derive the box fields their kernels read, with the list counted as built in this box (the
+// caller rebuilds it).  Returns false when a cutoff reaches half the box.
+bool baro_at(const Params& P, double p_eps, double eps, BaroDev* out, const double* box = nullptr) {
     BaroDev b{};
     b.p_eps = b.p_eps_saved = p_eps;
     b.eps = b.eps_saved = eps;
@@ -704,11 +712,19 @@ BaroDev baro_at(const Params& P, double p_eps, double eps) {
     double ec = (P.V0 * std::exp(3.0 * eps)) / Vmax;
     ec = std::pow(ec, 1.0 / 3.0);
     for(int a = 0; a < 3; a++) {
-        b.L[a] = b.L_saved[a] = (eps == 0.0) ? P.box[a] : ec * P.box[a];
+        b.L[a] = (eps == 0.0) ? P.box[a] : ec * P.box[a];
+        if(box && std::fabs(box[a] - b.L[a]) <= 1e-12 * b.L[a]) b.L[a] = box[a];
+        b.L_saved[a] = b.L[a];
         b.Lf[a] = (float)b.L[a];
     }
     b.ap = b.ar = 1.0;
-    return b;
+    bool ok = true;
+    if(P.precision != MTG_PREC_REFERENCE) {
+        for(int a = 0; a < 3; a++) b.Lb[a] = b.L[a];
+        ok = baro_box_fields(P, b);
+    }
+    *out = b;
+    return ok;
 }
 
 // Output record of the last output step: U, K, T, P, V.  For a batch the per-replica records go
@@ -748,6 +764,9 @@ int settle_state(mtg_ctx* c) {
             b.L[a] = b.L_saved[a];
             b.Lf[a] = (float)b.L[a];
         }
+        // production: the box fields the kernels read, for the completed step's box (the list in
+        // place was built in b.Lb)
+        if(!is_reference(c)) baro_box_fields(c->P, b);
         CUDA_TRY(c, copy_now(c, c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
         CUDA_TRY(c, copy_now(c, c->d.thp, c->d.thp_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
     }
@@ -846,8 +865,6 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     if(cfg->lj_shift < 0 || cfg->lj_shift > 2) return fail(nullptr, MTG_E_INVALID, "lj_shift must be 0, 1 or 2");
     if(cfg->precision == MTG_PREC_REFERENCE && cfg->coulomb != MTG_COULOMB_ALLPAIRS)
         return fail(nullptr, MTG_E_INVALID, "the reference precision mode has all-pairs Coulomb only");
-    if(cfg->ensemble == MTG_NPT && cfg->precision != MTG_PREC_REFERENCE)
-        return fail(nullptr, MTG_E_UNSUPPORTED, "NPT (MTK barostat) is available in the reference precision mode");
     if(cfg->ensemble == MTG_NPT && (cfg->pressure_nh_len < 1 || cfg->pressure_nh_len > MTG_MAX_NH_CHAIN ||
                                     cfg->pressure_respa < 1 || !(cfg->pressure_relax > 0.0)))
         return fail(nullptr, MTG_E_INVALID, "NPT needs 1 <= pressure_nh_len <= MTG_MAX_NH_CHAIN, pressure_respa >= 1, pressure_relax > 0");
@@ -915,7 +932,11 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         P.MP = cfg->pressure_nh_len;
         P.nrespP = cfg->pressure_respa;
         P.Pext = cfg->pressure / kConvPress;
-        P.W = P.kT * tauP * tauP;
+        P.QP = P.kT * tauP * tauP;
+        // the production modes give the barostat the MTK mass (N_f + 3) kT tauP^2 (N_f = 3N), so
+        // that tauP is its period; the reference's mass kT tauP^2 makes the volume of a system of
+        // N atoms oscillate about sqrt(3N) times faster
+        P.W = P.precision == MTG_PREC_REFERENCE ? P.QP : 3.0 * (double(sys->n_atoms) + 1.0) * P.QP;
         P.V0 = sys->box[0] * sys->box[1] * sys->box[2];
         P.clip = 0;   // the NPT branch does not clip forces (VelVerlet.cpp:57-71)
     }
@@ -1110,6 +1131,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         rc = rc || upload(C, &d.p, p0.data(), (size_t)3 * n);
         rc = rc || dalloc(C, &d.F, (size_t)3 * n);
         rc = rc || dalloc(C, &d.U, (size_t)n);
+        if(P.precision != MTG_PREC_REFERENCE) rc = rc || dalloc(C, &d.W, (size_t)n);
         rc = rc || upload(C, &d.m, sys->mass, (size_t)n);
         rc = rc || upload(C, &d.qd, sys->charge, (size_t)n);
         rc = rc || upload(C, &d.qf, qf.data(), (size_t)n);
@@ -1284,11 +1306,12 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         ThermoDev tp{};
         for(int j = 0; j < kMaxChain; j++) tp.Q[j] = 1.0;
         if(P.ensemble == MTG_NPT)
-            for(int j = 0; j < P.MP; j++) tp.Q[j] = P.W;
+            for(int j = 0; j < P.MP; j++) tp.Q[j] = P.QP;
         for(int j = 0; j < kMaxChain; j++) tp.iQ[j] = 1.0 / tp.Q[j];
         copy_now(c.get(), d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice);
         copy_now(c.get(), d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice);
-        BaroDev b = baro_at(P, 0.0, 0.0);
+        BaroDev b{};
+        baro_at(P, 0.0, 0.0, &b);
         copy_now(c.get(), d.baro, &b, sizeof(b), cudaMemcpyHostToDevice);
     }
     // list capacities: start from a density estimate, grown on demand
@@ -1335,6 +1358,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             rc = rc || add_snap(C, d.baro, sizeof(BaroDev));
             rc = rc || add_snap(C, d.thp, sizeof(ThermoDev));
             rc = rc || add_snap(C, d.thp_saved, sizeof(ThermoDev));
+            if(P.precision != MTG_PREC_REFERENCE) rc = rc || add_snap(C, d.W, sizeof(double) * n);
         }
         if(is_mixed(C)) {
             rc = rc || add_snap(C, d.hi, sizeof(float4) * n);
@@ -1378,8 +1402,8 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
         if(!finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
         CUDA_TRY(c, copy_now(c, c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
     }
-    if((r || p) && is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
     if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch sets chain states per replica (mtg_batch_set_thermo)");
+    const bool box_changes = th && c->P.ensemble == MTG_NPT;
     if(th) {
         ThermoDev t{};
         CUDA_TRY(c, copy_now(c, &t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
@@ -1401,12 +1425,18 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
             }
             CUDA_TRY(c, copy_now(c, c->d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice));
             CUDA_TRY(c, copy_now(c, c->d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice));
-            BaroDev b = baro_at(c->P, th->p_eps, th->eps);
+            BaroDev b{};
+            if(!baro_at(c->P, th->p_eps, th->eps, &b, th->box))
+                return fail(c, MTG_E_UNSUPPORTED, "the barostat state's box is narrower than twice the cutoff");
             CUDA_TRY(c, copy_now(c, c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
-            if(!r) return compute_forces_now(c, true);   // the box may have changed
         }
     }
-    if(r) return compute_forces_now(c, true);
+    // mixed: the double-float mirrors and the box fractions, in the box just set
+    if(is_mixed(c)) {
+        if(r || p) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
+        else if(box_changes) launch_prod_sync(c->d, c->P, kSyncPositionsFromMaster, c->stream);
+    }
+    if(r || box_changes) return compute_forces_now(c, true);
     return MTG_OK;
 }
 
@@ -1518,6 +1548,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             total_ms += ms;
             if(s.timeout) return fail(c, MTG_E_TIMEOUT, "a bounded wait in the thermostat gave up");
+            if(s.boxerr) return fail(c, MTG_E_UNSUPPORTED, "NPT: the box shrank until a cutoff reached half its width");
             if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite kinetic energy or thermostat scale during the run");
             c->stats.list_builds = s.builds - builds0;
             if(output) {
@@ -2222,6 +2253,7 @@ int dot(mtg_ctx* c, int n, const double* x, const double* y, DBuf& part, double*
 int grad_preflight(mtg_ctx* c, int32_t np, const mtg_param* params, bool batch = false) {
     if(is_reference(c)) return fail(c, MTG_E_UNSUPPORTED, "gradients use the analytic terms of the fp64 / mixed modes");
     if(c->P.nrep && !batch) return fail(c, MTG_E_UNSUPPORTED, "a batch takes its gradients per replica (mtg_batch_energy_grad)");
+    if(c->P.ensemble == MTG_NPT) return fail(c, MTG_E_UNSUPPORTED, "gradients are taken at a fixed box (NVT or NVE)");
     if(!c->P.nrep && batch) return fail(c, MTG_E_INVALID, "not a batch");
     if(c->has_tables) return fail(c, MTG_E_UNSUPPORTED, "tabulated terms have no derivative");
     if(np < 0 || (np > 0 && !params)) return MTG_E_INVALID;

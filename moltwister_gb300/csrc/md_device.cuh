@@ -887,12 +887,18 @@ __device__ inline double sinhx_over_x(double x) {
 //   3.1  p_eps += dt/2 G_eps(p after NH_T, F, wrapped r) of the next step
 //   prop_p / prop_r coefficients, 3.4 eps += dt p_eps / W, and the next box getSimBox().
 // G_eps = (1 + 1/N) sum p^2/m + sum F.r - 3 P V (VelVerlet.cpp:160-174).
+// The production modes pass the pair virial (sum over pairs of r_ij . F_ij plus the bonded terms'
+// virial) as both virials, use the exponential itself for the coefficients (and the chains'
+// published Suzuki-Yoshida weights, as their NVT does), run the particle chain in double-float
+// in the mixed mode (DFLOAT), and derive the box fields the production kernels read.
+template<bool DFLOAT>
 __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2, double vir_unw, double vir_wr,
                                    double U, bool second_half, bool output) {
     __shared__ double sh_kep;
     const int tid = threadIdx.x;
     BaroDev* b = d.baro;
     const double dt = P.dt;
+    const bool prod = P.precision != MTG_PREC_REFERENCE;
     const double alpha = (1.0 + 1.0 / double(P.n));
     if(second_half && tid == 0) {
         const double V = P.V0 * exp(3.0 * b->eps);
@@ -900,7 +906,7 @@ __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2,
     }
     bar96();
     double c2 = 1.0, c1 = 1.0, KEf = KE2;
-    thermostat_chain<false>(P, d.sc, d.th, d.th_saved, KE2, second_half, &c2, &c1, double(3 * P.n), P.M, P.nresp, &KEf);
+    thermostat_chain<DFLOAT>(P, d.sc, d.th, d.th_saved, KE2, second_half, &c2, &c1, double(3 * P.n), P.M, P.nresp, &KEf);
     bar96();
     if(tid == 0) sh_kep = b->p_eps * b->p_eps / P.W;
     bar96();
@@ -931,11 +937,11 @@ __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2,
         b->p_eps = pe;
         const double u = pe / P.W;
         double parm = alpha * u * dt / 4.0;
-        double co = cmt_exp(-parm);
+        double co = prod ? exp(-parm) : cmt_exp(-parm);
         b->ap = co * co;
         b->bp = (dt / 2.0) * co * sinhx_over_x(parm);
         parm = u * dt / 2.0;
-        co = cmt_exp(parm);
+        co = prod ? exp(parm) : cmt_exp(parm);
         b->ar = co * co;
         b->br = dt * (sinhx_over_x(parm) * co);
         b->eps += (dt * pe / P.W);                                          // 3.4
@@ -946,6 +952,8 @@ __device__ inline void npt_scalars(const Params& P, const DevSys& d, double KE2,
             b->L[a] = ec * P.box[a];
             b->Lf[a] = (float)b->L[a];
         }
+        if(prod && !baro_box_fields(P, *b)) sc->boxerr = 1;
+        if(!isfinite(KE2) || !isfinite(pe) || !isfinite(c2 * c1)) sc->nonfinite = 1;
     }
 }
 

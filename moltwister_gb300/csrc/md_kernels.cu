@@ -59,11 +59,22 @@ __device__ __forceinline__ SysView sys_view(const DevSys& d, const Params& P, in
     SysView v;
     if(r < 0) {
         v.off = 0; v.n = P.n; v.bbase = 0; v.nb = (P.n + 255) / 256;
-        v.cbase = 0; v.pnx = P.pnx; v.pny = P.pny; v.pnz = P.pnz;
-        for(int a = 0; a < 3; a++) {
-            v.box[a] = P.box[a];
-            v.fconv[a] = P.fconv[a];
-            v.fscale[a] = P.fscale[a];
+        if(P.ensemble == MTG_NPT && P.precision != MTG_PREC_REFERENCE) {
+            // the box changes every step: the barostat state holds it and its derived fields
+            const BaroDev* b = d.baro;
+            v.cbase = 0; v.pnx = b->pn[0]; v.pny = b->pn[1]; v.pnz = b->pn[2];
+            for(int a = 0; a < 3; a++) {
+                v.box[a] = b->L[a];
+                v.fconv[a] = b->conv[a];
+                v.fscale[a] = b->fscale[a];
+            }
+        } else {
+            v.cbase = 0; v.pnx = P.pnx; v.pny = P.pny; v.pnz = P.pnz;
+            for(int a = 0; a < 3; a++) {
+                v.box[a] = P.box[a];
+                v.fconv[a] = P.fconv[a];
+                v.fscale[a] = P.fscale[a];
+            }
         }
         v.rc = P.rc; v.rcoul = P.rcoul; v.skin = P.skin; v.kT = P.kT;
         v.sc = d.sc; v.th = d.th; v.th_saved = d.th_saved; v.rec = d.rec;
@@ -161,7 +172,9 @@ __global__ void k_prologue(DevSys d, Params P) {
         }
         v[0] = (px * px + py * py + pz * pz) / d.m[k];
         if(P.ensemble == MTG_NPT)
-            v[1] = d.F[3 * k] * d.r[3 * k] + d.F[3 * k + 1] * d.r[3 * k + 1] + d.F[3 * k + 2] * d.r[3 * k + 2];
+            v[1] = P.precision == MTG_PREC_REFERENCE
+                       ? d.F[3 * k] * d.r[3 * k] + d.F[3 * k + 1] * d.r[3 * k + 1] + d.F[3 * k + 2] * d.r[3 * k + 2]
+                       : d.W[k];
     }
     block_sum<2>(v, smem);
     if(threadIdx.x == 0) {
@@ -185,7 +198,7 @@ __global__ void k_prologue(DevSys d, Params P) {
         }
         __syncthreads();
         if(P.ensemble == MTG_NPT) {
-            if(threadIdx.x < 96) npt_scalars(P, d, tot, 0.0, tot_fr, 0.0, false, false);
+            if(threadIdx.x < 96) npt_scalars<DFLOAT>(P, d, tot, 0.0, tot_fr, 0.0, false, false);
             if(threadIdx.x == 0) d.sc->c2 = 1.0;
             return;
         }
@@ -289,28 +302,49 @@ __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
 
 __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, const SysView& v, int k) {
     const double S = v.sc->S;
-    const double dt_2 = P.dt / 2.0;
-    const double dm = P.dt / d.m[k];
+    const bool npt = P.ensemble == MTG_NPT;
     double fx, fy, fz, x, y, z;
     load_force(d, k, fx, fy, fz, false);
     load_pos(d, k, x, y, z, false);
-    double px = d.p[3 * k] * S + fx * dt_2;
-    double py = d.p[3 * k + 1] * S + fy * dt_2;
-    double pz = d.p[3 * k + 2] * S + fz * dt_2;
+    double px, py, pz;
+    double sb = 1.0, h2;
+    if(npt) {
+        // prop_p then prop_r with the coefficients of this step's barostat momentum
+        // (VelVerlet.cpp:57-71, 124-150); the momenta carry the pending thermostat scale
+        const BaroDev* b = d.baro;
+        const double ap = b->ap, bp = b->bp, ar = b->ar, br = b->br;
+        const double im = 1.0 / d.m[k];
+        px = (d.p[3 * k] * S) * ap + fx * bp;
+        py = (d.p[3 * k + 1] * S) * ap + fy * bp;
+        pz = (d.p[3 * k + 2] * S) * ap + fz * bp;
+        x = x * ar + (px * im) * br;
+        y = y * ar + (py * im) * br;
+        z = z * ar + (pz * im) * br;
+        sb = (double)b->sb;
+        h2 = (double)b->h2;
+    } else {
+        const double dt_2 = P.dt / 2.0;
+        const double dm = P.dt / d.m[k];
+        px = d.p[3 * k] * S + fx * dt_2;
+        py = d.p[3 * k + 1] * S + fy * dt_2;
+        pz = d.p[3 * k + 2] * S + fz * dt_2;
+        x += px * dm;
+        y += py * dm;
+        z += pz * dm;
+        const double h = 0.5 * double(v.skin);
+        h2 = h * h;
+    }
     d.p[3 * k] = px;
     d.p[3 * k + 1] = py;
     d.p[3 * k + 2] = pz;
-    x += px * dm;
-    y += py * dm;
-    z += pz * dm;
     store_pos(d, v.fconv, k, x, y, z, false);
-    // displacement since the last list build (minimum image: wrapping is not a displacement);
-    // fconv 2^-32 = 1/L rounded, without a division
-    const double bx = minimg_d(x - d.r_build[3 * k], v.box[0], v.fconv[0] * 0x1p-32);
-    const double by = minimg_d(y - d.r_build[3 * k + 1], v.box[1], v.fconv[1] * 0x1p-32);
-    const double bz = minimg_d(z - d.r_build[3 * k + 2], v.box[2], v.fconv[2] * 0x1p-32);
-    const double h = 0.5 * double(v.skin);
-    if(bx * bx + by * by + bz * bz > h * h) flag_rebuild(d, P, v);
+    // displacement since the last list build (minimum image: wrapping is not a displacement),
+    // against the build positions scaled with the box under NPT; fconv 2^-32 = 1/L rounded,
+    // without a division
+    const double bx = minimg_d(x - d.r_build[3 * k] * sb, v.box[0], v.fconv[0] * 0x1p-32);
+    const double by = minimg_d(y - d.r_build[3 * k + 1] * sb, v.box[1], v.fconv[1] * 0x1p-32);
+    const double bz = minimg_d(z - d.r_build[3 * k + 2] * sb, v.box[2], v.fconv[2] * 0x1p-32);
+    if(bx * bx + by * by + bz * bz > h2) flag_rebuild(d, P, v);
 }
 
 __device__ __forceinline__ double wrap_coord(double x, double Lm) {
@@ -345,30 +379,42 @@ __global__ void k_pkick2(DevSys d, Params P) {
     const SysView sv = sys_view(d, P, rep_of_block(d, P));
     const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
+    const bool npt = P.ensemble == MTG_NPT;
     if(k < sv.off + sv.n) {
         const double dt_2 = P.dt / 2.0;
         double f[3], r[3];
         load_force(d, k, f[0], f[1], f[2], false);
         load_pos(d, k, r[0], r[1], r[2], false);
         double p2 = 0.0, fr = 0.0;
+        if(npt) {
+            // 3.5 prop_p with the new forces (no clipping in the NPT branch, VelVerlet.cpp:57-71)
+            const double ap = d.baro->ap, bp = d.baro->bp;
 #pragma unroll
-        for(int a = 0; a < 3; a++) {
-            if(P.clip && P.fcut > 0.0 && fabs(f[a]) > P.fcut) {
-                f[a] = ((f[a] >= 0.0) ? 1.0 : -1.0) * P.fcut;
-                d.F[3 * k + a] = f[a];
+            for(int a = 0; a < 3; a++) {
+                const double p = d.p[3 * k + a] * ap + f[a] * bp;
+                d.p[3 * k + a] = p;
+                r[a] = wrap_coord(r[a], sv.box[a]);
+                p2 += p * p;
             }
-            const double p = d.p[3 * k + a] + f[a] * dt_2;
-            d.p[3 * k + a] = p;
-            r[a] = wrap_coord(r[a], sv.box[a]);
-            p2 += p * p;
-            fr += f[a] * r[a];
+        } else {
+#pragma unroll
+            for(int a = 0; a < 3; a++) {
+                if(P.clip && P.fcut > 0.0 && fabs(f[a]) > P.fcut) {
+                    f[a] = ((f[a] >= 0.0) ? 1.0 : -1.0) * P.fcut;
+                    d.F[3 * k + a] = f[a];
+                }
+                const double p = d.p[3 * k + a] + f[a] * dt_2;
+                d.p[3 * k + a] = p;
+                r[a] = wrap_coord(r[a], sv.box[a]);
+                p2 += p * p;
+                fr += f[a] * r[a];
+            }
         }
         store_pos(d, sv.fconv, k, r[0], r[1], r[2], false);
         v[0] = p2 / d.m[k];
-        if(OUTPUT) {
-            v[1] = fr;
-            v[2] = d.U[k];
-        }
+        if(npt) v[1] = d.W[k];   // pair virial: every step drives the barostat
+        else if(OUTPUT) v[1] = fr;
+        if(OUTPUT) v[2] = d.U[k];
     }
     block_sum<3>(v, smem);
     if(threadIdx.x == 0) {
@@ -385,7 +431,10 @@ __global__ void k_pkick2(DevSys d, Params P) {
             sv.sc->done_blocks = 0;
         }
         __syncthreads();
-        if(threadIdx.x < 96) step_end<false>(d, P, sv, tot, OUTPUT);
+        if(threadIdx.x < 96) {
+            if(npt) npt_scalars<false>(P, d, tot[0], tot[1], tot[1], tot[2], true, OUTPUT);
+            else step_end<false>(d, P, sv, tot, OUTPUT);
+        }
     }
 }
 
@@ -462,6 +511,117 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
                 cudaGraphSetConditional(cond, d.sc->rebuild ? 1u : 0u);
             }
         }
+    }
+}
+
+// NPT, mixed mode: 3.2 prop_p and 3.3 prop_r (VelVerlet.cpp:57-71, 124-150) in double-float with
+// the coefficients of this step's barostat momentum (the momenta carry the pending thermostat
+// scale), box fractions in this step's box, and the displacement test against the build positions
+// scaled with the box (baro_box_fields).
+__global__ void k_mkick_drift_npt(DevSys d, Params P, cudaGraphConditionalHandle cond) {
+    __shared__ MixK K;
+    __shared__ DF ap, bp, ar, br;
+    __shared__ float sb, h2;
+    const SysView v = sys_view(d, P, -1);
+    if(threadIdx.x == 0) {
+        mix_consts(v, P, K);
+        const BaroDev* b = d.baro;
+        ap = df_of(b->ap);
+        bp = df_of(b->bp);
+        ar = df_of(b->ar);
+        br = df_of(b->br);
+        sb = b->sb;
+        h2 = b->h2;
+    }
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k < P.n) {
+        const float4 h = d.hi[k], l = d.lo[k], ph = d.ph[k], pl = d.pl[k], rb = d.rb4[k];
+        const DF im{ph.w, pl.w};
+        const long long fq[3] = {d.Fx[k], d.Fy[k], d.Fz[k]};
+        DF p[3] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}};
+        DF x[3] = {{h.x, l.x}, {h.y, l.y}, {h.z, l.z}};
+        const float rbv[3] = {rb.x, rb.y, rb.z};
+        unsigned int q[3];
+        float d2 = 0.0f;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            p[a] = df_add(df_mul(df_mul(p[a], K.S), ap), df_mul(df_fix(fq[a]), bp));
+            x[a] = df_add(df_mul(x[a], ar), df_mul(df_mul(p[a], im), br));
+            q[a] = frac32_df(x[a], K.conv[a]);
+            const float dd = minimg_f(__fsub_rn(x[a].h, __fmul_rn(rbv[a], sb)) + x[a].l, K.Lf[a], K.iLf[a]);
+            d2 += dd * dd;
+        }
+        d.ph[k] = make_float4(p[0].h, p[1].h, p[2].h, ph.w);
+        d.pl[k] = make_float4(p[0].l, p[1].l, p[2].l, pl.w);
+        d.hi[k] = make_float4(x[0].h, x[1].h, x[2].h, h.w);
+        d.lo[k] = make_float4(x[0].l, x[1].l, x[2].l, l.w);
+        const uint4 qk = make_uint4(q[0], q[1], q[2], (unsigned int)__float_as_int(l.w));
+        d.pq[k] = qk;
+        d.pqs[d.slot_of[k]] = qk;
+        if(d2 > h2) flag_rebuild(d, P, v);
+    }
+    if(cond) {
+        if(last_block(&d.sc->done_blocks)) {
+            if(threadIdx.x == 0) {
+                d.sc->done_blocks = 0;
+                cudaGraphSetConditional(cond, d.sc->rebuild ? 1u : 0u);
+            }
+        }
+    }
+}
+
+// NPT, mixed mode: 3.5 prop_p with the new forces (no clipping in the NPT branch), wrap into the
+// current box, block sums of p^2/m, of the pair virial and (output steps) of U.
+template<bool OUTPUT>
+__global__ void k_mkick2_npt(DevSys d, Params P) {
+    __shared__ MixK K;
+    __shared__ DF ap, bp;
+    __shared__ double smem[32 * 3];
+    const SysView sv = sys_view(d, P, -1);
+    if(threadIdx.x == 0) {
+        mix_consts(sv, P, K);
+        ap = df_of(d.baro->ap);
+        bp = df_of(d.baro->bp);
+    }
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    DF ke{0.0f, 0.0f};
+    double v[3] = {0.0, 0.0, 0.0};
+    if(k < P.n) {
+        float4 h = d.hi[k], l = d.lo[k];
+        const float4 ph = d.ph[k], pl = d.pl[k];
+        const long long fq[3] = {d.Fx[k], d.Fy[k], d.Fz[k]};
+        DF p[3] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}};
+        DF x[3] = {{h.x, l.x}, {h.y, l.y}, {h.z, l.z}};
+        DF p2{0.0f, 0.0f};
+        bool wrapped = false;
+#pragma unroll
+        for(int a = 0; a < 3; a++) {
+            p[a] = df_add(df_mul(p[a], ap), df_mul(df_fix(fq[a]), bp));
+            if(x[a].h >= K.L2f[a] || x[a].h < -K.L2f[a]) {
+                const float m = floorf(__fmul_rn(__fadd_rn(x[a].h, K.L2f[a]), K.iLf[a]));
+                x[a] = df_add(x[a], df_mul_f(K.L[a], -m));
+                wrapped = true;
+            }
+            p2 = df_add(p2, df_mul(p[a], p[a]));
+        }
+        d.ph[k] = make_float4(p[0].h, p[1].h, p[2].h, ph.w);
+        d.pl[k] = make_float4(p[0].l, p[1].l, p[2].l, pl.w);
+        if(wrapped) {
+            d.hi[k] = make_float4(x[0].h, x[1].h, x[2].h, h.w);
+            d.lo[k] = make_float4(x[0].l, x[1].l, x[2].l, l.w);
+        }
+        ke = df_mul(p2, DF{ph.w, pl.w});
+        v[1] = d.W[k];
+        if(OUTPUT) v[2] = d.U[k];
+    }
+    const double ke_blk = block_sum_df(ke, smem);
+    block_sum<3>(v, smem);
+    if(threadIdx.x == 0) {
+        d.partial[blockIdx.x * 4 + 0] = ke_blk;
+        d.partial[blockIdx.x * 4 + 1] = v[1];
+        d.partial[blockIdx.x * 4 + 2] = v[2];
     }
 }
 
@@ -546,6 +706,21 @@ __global__ void __launch_bounds__(96, 1) k_mstep_end(DevSys d, Params P) {
     step_end<true>(d, P, sv, tot, OUTPUT);
 }
 
+// NPT, mixed mode: the system's totals (the pair virial drives the barostat every step), then the
+// barostat and chain half-steps, the output record and the next step's box (npt_scalars).
+template<bool OUTPUT>
+__global__ void __launch_bounds__(96, 1) k_mstep_end_npt(DevSys d, Params P) {
+    __shared__ double smem[32 * 3];
+    __shared__ double tot[3];
+    const SysView sv = sys_view(d, P, -1);
+    double s3[3];
+    system_totals<3>(d.partial, sv.bbase, sv.nb, s3, smem);
+    if(threadIdx.x == 0)
+        for(int q = 0; q < 3; q++) tot[q] = s3[q];
+    __syncthreads();
+    npt_scalars<true>(P, d, tot[0], tot[1], tot[1], tot[2], true, OUTPUT);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Verlet list build: cell grid with edge >= rlist (or one cell for small boxes), counting sort
 // with a per-cell rank pass (deterministic order), then one warp per atom scanning the 27 cells.
@@ -554,6 +729,15 @@ template<bool MIXED>
 __global__ void k_pcell_assign(DevSys d, Params P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, i))) return;
+    if(P.ensemble == MTG_NPT && i == 0) {
+        // the list is built in the current box: displacements count from here (the box fields
+        // the rest of this build reads do not change)
+        BaroDev* b = d.baro;
+        for(int a = 0; a < 3; a++) b->Lb[a] = b->L[a];
+        const float hs = 0.5f * P.skin;
+        b->sb = 1.0f;
+        b->h2 = hs * hs;
+    }
     double x, y, z;
     load_pos(d, i, x, y, z, MIXED);
     d.r_build[3 * i] = x;
@@ -577,8 +761,9 @@ __global__ void k_pcell_assign(DevSys d, Params P) {
 __global__ void k_pcell_scan(DevSys d, Params P) {
     const int r = P.nrep ? (int)blockIdx.x : -1;
     if(!rebuild_due(d, P, r)) return;
-    const int cbase = P.nrep ? d.reps[r].cbase : 0;
-    const int ncell = P.nrep ? d.reps[r].pnx * d.reps[r].pny * d.reps[r].pnz : P.pnx * P.pny * P.pnz;
+    const SysView v = sys_view(d, P, r);   // cell counts of the current box (NPT: of this build)
+    const int cbase = v.cbase;
+    const int ncell = v.pnx * v.pny * v.pnz;
     const int slot0 = P.nrep ? d.reps[r].off : 0;
     __shared__ int warp_tot[32];
     __shared__ int carry;
@@ -864,8 +1049,13 @@ __device__ __forceinline__ void load_par(const double* pd, const float* pf, int 
 
 // Bonded contribution of entry `e` (global bonded-entry index space: bonds, then angles, then
 // dihedrals of atom k) to the force on k, and to k's energy (reference bookkeeping).
+// With `energy` it also adds atom k's share of the term's virial, (r_k - r_X) . F_k with X a
+// fixed atom of the term (a bond's or a dihedral's lowest-index atom, an angle's centre): summed
+// over the term's atoms this is the term's virial sum_a r_a . F_a, because its forces sum to
+// zero.  The relative vectors are the minimum-image ones the force uses.
 template<bool MIXED, class R>
-__device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& fx, R& fy, R& fz, R& u, bool energy) {
+__device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& fx, R& fy, R& fz, R& u, R& w,
+                             bool energy) {
     const int nb = d.bptr[k + 1] - d.bptr[k];
     const int na = d.aptr[k + 1] - d.aptr[k];
     if(e < nb) {
@@ -904,6 +1094,7 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
         const R s = md / r;
         fx += s * dx; fy += s * dy; fz += s * dz;
         if(energy && i > k) u += uu;
+        if(energy && k > i) w += s * (dx * dx + dy * dy + dz * dz);   // (r_k - r_i) . F_k
         return;
     }
     e -= nb;
@@ -955,6 +1146,7 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
             if(energy) u += uu;
         } else {
             fx -= dU * g1x; fy -= dU * g1y; fz -= dU * g1z;
+            if(energy) w -= dU * (ux * g1x + uy * g1y + uz * g1z);   // (r_k - r_centre) . F_k
         }
         return;
     }
@@ -1005,7 +1197,30 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
         } else {
             gx = ga * mx; gy = ga * my; gz = ga * mz;
         }
-        fx -= dV * sgn * gx; fy -= dV * sgn * gy; fz -= dV * sgn * gz;
+        const R Fx = -dV * sgn * gx, Fy = -dV * sgn * gy, Fz = -dV * sgn * gz;
+        fx += Fx; fy += Fy; fz += Fz;
+        if(energy) {
+            // r_k - r_X along the chain a-b-c-dd (k is a, or b for a centre entry), X the
+            // lowest-index atom of the four
+            int X = a;
+            if(b < X) X = b;
+            if(c < X) X = c;
+            if(dd < X) X = dd;
+            const bool kb = d.dcen[q] != 0;
+            R rx = 0, ry = 0, rz = 0;                       // r_k - r_X
+            if(X == a) {
+                if(kb) { rx = b1x; ry = b1y; rz = b1z; }
+            } else if(X == b) {
+                if(!kb) { rx = -b1x; ry = -b1y; rz = -b1z; }
+            } else if(X == c) {
+                rx = -b2x; ry = -b2y; rz = -b2z;
+                if(!kb) { rx -= b1x; ry -= b1y; rz -= b1z; }
+            } else {
+                rx = -b2x - b3x; ry = -b2y - b3y; rz = -b2z - b3z;
+                if(!kb) { rx -= b1x; ry -= b1y; rz -= b1z; }
+            }
+            w += rx * Fx + ry * Fy + rz * Fz;
+        }
     }
 }
 
@@ -1064,7 +1279,7 @@ template<bool ENERGY>
 __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int si, uint32_t ent, int ti, float qi,
                                            float rc2, float rq2, float irc, float gmax, const PairCoef* pc,
                                            const float* us, const float* qt, uint4 qi4, const float (&fs)[3], Fix& fx,
-                                           Fix& fy, Fix& fz, Fix& fu) {
+                                           Fix& fy, Fix& fz, Fix& fu, Fix& fw) {
     const int sj = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
     const uint4 qj4 = d.pqs[sj];
@@ -1112,11 +1327,15 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
         g *= sc;
         u *= sc;
     }
-    const float g16 = __fmul_rn(fminf(fmaxf(g, -gmax), gmax), 16.0f);
+    const float gc = fminf(fmaxf(g, -gmax), gmax);
+    const float g16 = __fmul_rn(gc, 16.0f);
     fix_add16(fx, __fmul_rn(g16, dx));
     fix_add16(fy, __fmul_rn(g16, dy));
     fix_add16(fz, __fmul_rn(g16, dz));
-    if(ENERGY && sj > si) fix_add_clamped(fu, u);
+    if(ENERGY && sj > si) {
+        fix_add_clamped(fu, u);
+        fix_add_clamped(fw, gc * r2);   // the pair's virial (r_i - r_j) . F_i, once per pair
+    }
 }
 
 // Force gather: TEAM lanes per atom (8, 16 or 32; chosen per system by the autotuner), atoms taken
@@ -1159,8 +1378,8 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
     const bool active = si < P.n;
     const int i = active ? d.pcell_list[si] : 0;
     const bool mob = active && d.mobile[i] != 0;
-    Fix fx{0, 0}, fy{0, 0}, fz{0, 0}, fu{0, 0};   // mixed: exact fixed point
-    double bx = 0, by = 0, bz = 0, bu = 0;        // fp64
+    Fix fx{0, 0}, fy{0, 0}, fz{0, 0}, fu{0, 0}, fw{0, 0};   // mixed: exact fixed point
+    double bx = 0, by = 0, bz = 0, bu = 0, bw = 0;          // fp64
     if(mob) {
         const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
         const R rc2 = (R)v.rc * (R)v.rc;
@@ -1181,10 +1400,10 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
                 for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
 #pragma unroll
                 for(int q = 0; q < 4; q++)
-                    pair_mixed<ENERGY>(d, P, si, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
+                    pair_mixed<ENERGY>(d, P, si, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
             }
             for(; e < cnt; e += TEAM)
-                pair_mixed<ENERGY>(d, P, si, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu);
+                pair_mixed<ENERGY>(d, P, si, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
         } else {
             const int ti = d.type[i];
             const double qi = d.qd[i];
@@ -1202,59 +1421,85 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
                     double dx, dy, dz, g, u;
                     pair_entry_d<ENERGY>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
                     bx += g * dx; by += g * dy; bz += g * dz;
-                    if(ENERGY) bu += u;
+                    if(ENERGY) {
+                        bu += u;
+                        if((int)(ent[q] & kIdxMask) > i) bw += g * (dx * dx + dy * dy + dz * dz);
+                    }
                 }
             }
             for(; e < cnt; e += TEAM) {
                 double dx, dy, dz, g, u;
-                pair_entry_d<ENERGY>(d, P, i, atom_entry(__ldg(lst + e)), ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
+                const uint32_t ent = atom_entry(__ldg(lst + e));
+                pair_entry_d<ENERGY>(d, P, i, ent, ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
                 bx += g * dx; by += g * dy; bz += g * dz;
-                if(ENERGY) bu += u;
+                if(ENERGY) {
+                    bu += u;
+                    if((int)(ent & kIdxMask) > i) bw += g * (dx * dx + dy * dy + dz * dz);
+                }
             }
         }
         // bonded terms of atom i, one entry per lane
         const int nbd = (d.bptr[i + 1] - d.bptr[i]) + (d.aptr[i + 1] - d.aptr[i]) + (d.dptr[i + 1] - d.dptr[i]);
         for(int b = lane; b < nbd; b += TEAM) {
-            R gx = 0, gy = 0, gz = 0, gu = 0;
-            bonded_entry<MIXED, R>(d, P, i, b, gx, gy, gz, gu, ENERGY);
+            R gx = 0, gy = 0, gz = 0, gu = 0, gw = 0;
+            bonded_entry<MIXED, R>(d, P, i, b, gx, gy, gz, gu, gw, ENERGY);
             if(MIXED) {
                 fix_add_clamped(fx, (float)gx);
                 fix_add_clamped(fy, (float)gy);
                 fix_add_clamped(fz, (float)gz);
-                if(ENERGY) fix_add_clamped(fu, (float)gu);
+                if(ENERGY) {
+                    fix_add_clamped(fu, (float)gu);
+                    fix_add_clamped(fw, (float)gw);
+                }
             } else {
                 bx += (double)gx; by += (double)gy; bz += (double)gz;
-                if(ENERGY) bu += (double)gu;
+                if(ENERGY) {
+                    bu += (double)gu;
+                    bw += (double)gw;
+                }
             }
         }
     }
     // team reduction (integer: exact; FP64: fixed tree); teams are aligned within the warp
     if(MIXED) {
         long long ax = fix_total(fx), ay = fix_total(fy), az = fix_total(fz), au = ENERGY ? fix_total(fu) : 0;
+        long long aw = ENERGY ? fix_total(fw) : 0;
         for(int o = TEAM / 2; o > 0; o >>= 1) {
             ax += __shfl_xor_sync(0xffffffffu, ax, o);
             ay += __shfl_xor_sync(0xffffffffu, ay, o);
             az += __shfl_xor_sync(0xffffffffu, az, o);
-            if(ENERGY) au += __shfl_xor_sync(0xffffffffu, au, o);
+            if(ENERGY) {
+                au += __shfl_xor_sync(0xffffffffu, au, o);
+                aw += __shfl_xor_sync(0xffffffffu, aw, o);
+            }
         }
         if(active && lane == 0) {
             d.Fx[i] = ax;
             d.Fy[i] = ay;
             d.Fz[i] = az;
-            if(ENERGY) d.U[i] = double(au) * (1.0 / kFixScale);
+            if(ENERGY) {
+                d.U[i] = double(au) * (1.0 / kFixScale);
+                d.W[i] = double(aw) * (1.0 / kFixScale);
+            }
         }
     } else {
         for(int o = TEAM / 2; o > 0; o >>= 1) {
             bx += __shfl_xor_sync(0xffffffffu, bx, o);
             by += __shfl_xor_sync(0xffffffffu, by, o);
             bz += __shfl_xor_sync(0xffffffffu, bz, o);
-            if(ENERGY) bu += __shfl_xor_sync(0xffffffffu, bu, o);
+            if(ENERGY) {
+                bu += __shfl_xor_sync(0xffffffffu, bu, o);
+                bw += __shfl_xor_sync(0xffffffffu, bw, o);
+            }
         }
         if(active && lane == 0) {
             d.F[3 * i] = bx;
             d.F[3 * i + 1] = by;
             d.F[3 * i + 2] = bz;
-            if(ENERGY) d.U[i] = bu;
+            if(ENERGY) {
+                d.U[i] = bu;
+                d.W[i] = bw;
+            }
         }
     }
 }
@@ -1316,6 +1561,7 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
     __shared__ double smem[32 * 3];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
+    const SysView sv = sys_view(d, P, -1);   // the current box (it changes under NPT)
     if(k < P.n) {
         const bool mixed = (mode == MTG_PREC_MIXED);
         double f[3], r[3];
@@ -1334,13 +1580,16 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
             fr += f[a] * r[a];
             p2 += pk[a] * pk[a];
         }
-        store_pos(d, P.fconv, k, r[0], r[1], r[2], mixed);
+        store_pos(d, sv.fconv, k, r[0], r[1], r[2], mixed);
         if(mode != MTG_PREC_REFERENCE) {
-            const double bx = minimg_d(r[0] - d.r_build[3 * k], P.box[0], 1.0 / P.box[0]);
-            const double by = minimg_d(r[1] - d.r_build[3 * k + 1], P.box[1], 1.0 / P.box[1]);
-            const double bz = minimg_d(r[2] - d.r_build[3 * k + 2], P.box[2], 1.0 / P.box[2]);
+            const bool npt = P.ensemble == MTG_NPT;
+            const double sb = npt ? (double)d.baro->sb : 1.0;
             const double h = 0.5 * double(P.skin);
-            if(bx * bx + by * by + bz * bz > h * h) d.sc->rebuild = -1;
+            const double h2 = npt ? (double)d.baro->h2 : h * h;
+            const double bx = minimg_d(r[0] - d.r_build[3 * k] * sb, sv.box[0], 1.0 / sv.box[0]);
+            const double by = minimg_d(r[1] - d.r_build[3 * k + 1] * sb, sv.box[1], 1.0 / sv.box[1]);
+            const double bz = minimg_d(r[2] - d.r_build[3 * k + 2] * sb, sv.box[2], 1.0 / sv.box[2]);
+            if(bx * bx + by * by + bz * bz > h2) d.sc->rebuild = -1;
         }
         v[0] = d.U[k];
         v[1] = p2 / d.m[k];
@@ -1357,7 +1606,7 @@ __global__ void k_gd_step(DevSys d, Params P, double lr, int mode) {
             double sum[3] = {0.0, 0.0, 0.0};
             for(int b = 0; b < (int)gridDim.x; b++)
                 for(int q = 0; q < 3; q++) sum[q] += d.partial[b * 4 + q];
-            const double V = P.box[0] * P.box[1] * P.box[2];
+            const double V = sv.box[0] * sv.box[1] * sv.box[2];
             d.rec[0] = sum[0];
             d.rec[1] = 0.5 * sum[1];
             d.rec[2] = sum[1] / (3.0 * double(P.n));
@@ -1384,7 +1633,8 @@ void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
 
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {
     const int nb = integration_blocks(P);
-    if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
+    if(P.precision == MTG_PREC_MIXED && P.ensemble == MTG_NPT) k_mkick_drift_npt<<<nb, 256, 0, s>>>(d, P, cond);
+    else if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
     else k_pkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
 }
 
@@ -1413,6 +1663,7 @@ static void force_team(const DevSys& d, const Params& P, cudaStream_t s) {
 }
 
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s) {
+    energy = energy || P.ensemble == MTG_NPT;   // the energy variant also sums the virial
     if(P.precision == MTG_PREC_MIXED) {
         if(energy) force_team<true, true>(d, P, s);
         else force_team<true, false>(d, P, s);
@@ -1426,11 +1677,17 @@ void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream
     const int nb = integration_blocks(P);
     if(P.precision == MTG_PREC_MIXED) {
         const int nsys = P.nrep ? P.nrep : 1;
-        if(parts & kKick2Atoms) {
+        if((parts & kKick2Atoms) && P.ensemble == MTG_NPT) {
+            if(output) k_mkick2_npt<true><<<nb, 256, 0, s>>>(d, P);
+            else k_mkick2_npt<false><<<nb, 256, 0, s>>>(d, P);
+        } else if(parts & kKick2Atoms) {
             if(output) k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
             else k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
         }
-        if(parts & kKick2StepEnd) {
+        if((parts & kKick2StepEnd) && P.ensemble == MTG_NPT) {
+            if(output) k_mstep_end_npt<true><<<1, 96, 0, s>>>(d, P);
+            else k_mstep_end_npt<false><<<1, 96, 0, s>>>(d, P);
+        } else if(parts & kKick2StepEnd) {
             if(output) k_mstep_end<true><<<nsys, 96, 0, s>>>(d, P);
             else k_mstep_end<false><<<nsys, 96, 0, s>>>(d, P);
         }

@@ -48,6 +48,14 @@ struct BaroDev {
     double ar, br;        // prop_r: r = r ar + (p (1/m)) br (VelVerlet.cpp:138-150)
     double p_eps_saved, eps_saved;
     double L_saved[3];
+    // production modes: the current box as the production kernels read it (in place of the
+    // Params fields), and what the Verlet list needs when the box changes between rebuilds
+    double conv[3];       // 2^32 / L: box fractions of the mixed mode
+    float fscale[3];      // L / 2^32
+    float sb;             // L / Lb: scale of the box since the last list build
+    double Lb[3];         // box at the last list build
+    float h2;             // squared displacement that triggers a rebuild in the current box
+    int pn[3];            // production cell counts for the current box (at most the allocated grid)
 };
 
 // One replica of a batch (several independent systems advanced by the same launches): its atom
@@ -78,7 +86,7 @@ struct StepScalars {
     uint32_t done_blocks; // last-block counter of the reduction kernels
     int32_t builds;       // neighbour-list rebuilds performed
     int32_t timeout;      // a bounded device wait gave up
-    int32_t pad;
+    int32_t boxerr;       // NPT (production): the box shrank until a cutoff reached half its width
 };
 
 struct Params {
@@ -110,12 +118,44 @@ struct Params {
     // NPT
     int MP, nrespP;       // barostat chain length and RESPA steps
     double Pext;          // pressure / Conv_press
-    double W;             // barostat mass kT tauP^2
+    double W;             // barostat mass: kT tauP^2 (reference), 3 (N + 1) kT tauP^2 (production)
+    double QP;            // barostat chain masses kT tauP^2
     double V0;            // LmaxX LmaxY LmaxZ
     int wait_polls;       // limit of the bounded device waits (thermostat hand-overs)
 };
 
 
+
+// Production NPT: the fields of b derived from its box b.L and the box b.Lb of the last list
+// build, computed by the same code on the host (state set, creation) and on the device (end of
+// every step).  A pair left out of the list at the build was at least rlist = r + skin apart in
+// box fractions times Lb; after the box scales by s = L / Lb and two atoms moved by at most
+// delta in the current box it is at least s rlist - 2 delta apart, so the list stays valid while
+// delta <= (skin s + r (s - 1)) / 2 for every pair radius r <= rfull (the smallest margin is at
+// r = rfull when s < 1 and at r = 0 when s > 1).  The kernels compare the displacement from the
+// build positions scaled by s.  Cell counts follow the box, at most the allocated grid; one cell
+// when fewer than three fit.  Returns false when a cutoff reaches half the box.
+__host__ __device__ inline bool baro_box_fields(const Params& P, BaroDev& b) {
+    const double rfull = (double)fmaxf(P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? P.rcoul : 0.0f);
+    const double rlist = rfull + (double)P.skin;
+    const int cap[3] = {P.pnx, P.pny, P.pnz};
+    bool ok = true;
+    for(int a = 0; a < 3; a++) {
+        b.Lf[a] = (float)b.L[a];
+        b.conv[a] = 4294967296.0 / b.L[a];
+        b.fscale[a] = (float)(b.L[a] / 4294967296.0);
+        int pn = (int)floor(b.L[a] / rlist);
+        if(pn > cap[a]) pn = cap[a];
+        if(pn < 3) pn = 1;
+        b.pn[a] = pn;
+        if(2.0 * rfull >= b.L[a] || (pn > 1 && 2.0 * rlist > b.L[a])) ok = false;
+    }
+    const double sb = b.L[0] / b.Lb[0];
+    const double margin = (double)P.skin * sb + rfull * (sb < 1.0 ? sb - 1.0 : 0.0);
+    b.sb = (float)sb;
+    b.h2 = margin > 0.0 ? (float)(0.25 * margin * margin) : -1.0f;
+    return ok;
+}
 
 // Everything a force/integration kernel reads, as raw device pointers.
 struct DevSys {
@@ -125,6 +165,7 @@ struct DevSys {
     double* p;            // [3n]
     double* F;            // [3n]  FP64 forces (reference, fp64)
     double* U;            // [n]   per-atom energies
+    double* W;            // [n]   per-atom virial (production modes: pair r.F once per pair, bonded terms)
     double* m;            // [n]
     double* qd;           // [n]   charges (double)
     float* qf;            // [n]   charges as float (CMDFFMatrices::CAtom::q_)

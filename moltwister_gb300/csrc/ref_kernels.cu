@@ -703,7 +703,7 @@ __global__ void k_kick2_npt(DevSys d, Params P) {
             d.sc->done_blocks = 0;
         }
         __syncthreads();
-        if(threadIdx.x < 96) npt_scalars(P, d, tot[0], tot[1], tot[2], tot[3], true, OUTPUT);
+        if(threadIdx.x < 96) npt_scalars<false>(P, d, tot[0], tot[1], tot[2], tot[3], true, OUTPUT);
     }
 }
 

@@ -219,6 +219,9 @@ def thermo_struct(thermo) -> ThermoState:
         for j in range(th.MP):
             th.etaP[j] = float(thermo.etaP[j])
             th.p_etaP[j] = float(thermo.petaP[j])
+    if thermo.box is not None:
+        for a in range(3):
+            th.box[a] = float(thermo.box[a])
     return th
 
 

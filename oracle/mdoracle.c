@@ -769,16 +769,29 @@ static void nb_analytic(int kind, const double* p, double R, double rglob, int s
     } else { *u = 0.0; *mdUdr = 0.0; }
 }
 
-int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
+/* FP64 analytic forces and per-atom energies; with W also each atom's share of the virial
+ * sum_a r_a . F_a: (r_i - r_j) . F_i once per pair (on the lower index), and for every bonded term
+ * (r_k - r_X) . F_k with X the term's lowest-index atom (bonds, dihedrals) or its centre (angles),
+ * which sums over the term's atoms to the term's virial because its forces sum to zero. */
+static int forces_fp64(const orc_sys* s, double rcut, double* F, double* U, double* W);
+
+int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) { return forces_fp64(s, rcut, F, U, NULL); }
+
+int orc_forces_fp64_vir(const orc_sys* s, double rcut, double* F, double* U, double* W) {
+    return forces_fp64(s, rcut, F, U, W);
+}
+
+static int forces_fp64(const orc_sys* s, double rcut, double* F, double* U, double* W) {
     const double* L = s->box;
     const int T = s->ntypes;
     const double rc2 = rcut * rcut;
     const double crc2 = s->coulomb_rc * s->coulomb_rc;
 #pragma omp parallel for schedule(dynamic, 16)
     for(int k = 0; k < s->n; k++) {
-        double fx = 0, fy = 0, fz = 0, uk = 0;
+        double fx = 0, fy = 0, fz = 0, uk = 0, wk = 0;
         F[3 * k] = F[3 * k + 1] = F[3 * k + 2] = 0.0;
         U[k] = 0.0;
+        if(W) W[k] = 0.0;
         if(!s->mobile[k]) continue;
         v3 rk = mk(s->r[3 * k], s->r[3 * k + 1], s->r[3 * k + 2]);
         for(int e = s->bptr[k]; e < s->bptr[k + 1]; e++) {
@@ -792,6 +805,7 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
             else if(kind == K_BOND_MORSE) { double E = exp(-p[1] * (R - p[2])); md = -2.0 * p[0] * p[1] * E * (1.0 - E); u = p[0] * (1.0 - E) * (1.0 - E); }
             fx += md * d.x / R; fy += md * d.y / R; fz += md * d.z / R;
             if(i > k) uk += u;
+            if(k > i) wk += md * R;
         }
         for(int e = s->aptr[k]; e < s->aptr[k + 1]; e++) {
             /* theta at the centre; gradient of theta wrt each atom */
@@ -815,7 +829,10 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
             v3 g3 = scl(sub(scl(u1, 1.0 / (n1 * n3)), scl(u3, cs / (n3 * n3))), -1.0 / sn);
             v3 g;
             if(s->acen[e]) { g = mk(-g1.x - g3.x, -g1.y - g3.y, -g1.z - g3.z); uk += u; }
-            else g = g1;
+            else {
+                g = g1;
+                wk -= dU * dot(u1, g1);      /* (r_k - r_centre) . F_k */
+            }
             fx -= dU * g.x; fy -= dU * g.y; fz -= dU * g.z;
         }
         for(int e = s->dptr[k]; e < s->dptr[k + 1]; e++) {
@@ -852,6 +869,20 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
             v3 g = s->dcen[e] ? gb : ga;
             fx -= dV * sgn * g.x; fy -= dV * sgn * g.y; fz -= dV * sgn * g.z;
             if(s->dcen[e]) uk += 0.5 * V;
+            {
+                /* r_k - r_X along a-b-c-d, X the lowest-index atom of the four */
+                int X = a;
+                if(b < X) X = b;
+                if(c < X) X = c;
+                if(d < X) X = d;
+                v3 rel = mk(0.0, 0.0, 0.0);
+                v3 r_a = mk(0.0, 0.0, 0.0), r_b = b1, r_c = mk(b1.x + b2.x, b1.y + b2.y, b1.z + b2.z);
+                v3 r_d = mk(r_c.x + b3.x, r_c.y + b3.y, r_c.z + b3.z);   /* unwrapped chain from a */
+                v3 rk_ = s->dcen[e] ? r_b : r_a;
+                v3 rX = (X == a) ? r_a : (X == b) ? r_b : (X == c) ? r_c : r_d;
+                rel = sub(rk_, rX);
+                wk += -dV * sgn * dot(rel, g);
+            }
         }
         /* non-bonded + Coulomb over all atoms (within cutoffs), in index order */
         const double qk = s->qd[k];
@@ -886,10 +917,14 @@ int orc_forces_fp64(const orc_sys* s, double rcut, double* F, double* U) {
             float sc = exclusion_scale(s, k, i, &ap);
             double scd = ap ? (double)sc : 1.0;
             fx += scd * md * d.x / R; fy += scd * md * d.y / R; fz += scd * md * d.z / R;
-            if(i > k) uk += scd * u;
+            if(i > k) {
+                uk += scd * u;
+                wk += scd * md * R;
+            }
         }
         F[3 * k] = fx; F[3 * k + 1] = fy; F[3 * k + 2] = fz;
         U[k] = uk;
+        if(W) W[k] = wk;
     }
     return 0;
 }

@@ -55,6 +55,7 @@ def lib():
         _lib.orc_neigh_list.restype = C.c_int
         _lib.orc_forces_ref.argtypes = [P, P, P, C.c_int, P, P]
         _lib.orc_forces_fp64.argtypes = [P, C.c_double, P, P]
+        _lib.orc_forces_fp64_vir.argtypes = [P, C.c_double, P, P, P]
         _lib.orc_run_ref.argtypes = [P, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P]
         _lib.orc_run_ref.restype = C.c_int
     return _lib
