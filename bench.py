@@ -184,7 +184,7 @@ def timed_device(e, steps: int, chunk: int = CHUNK):
     launches = 0
     while done < steps:
         n = min(chunk, steps - done)
-        e.run(n)
+        e.run(n, out_stride=chunk, copy_coords=False)   # one output step (energies, record) per chunk
         st = e.stats()
         total += st["device_ms"]
         builds += st["list_builds"]

@@ -236,7 +236,8 @@ int mtg_get_state(mtg_ctx* ctx, double* r, double* p, mtg_thermo_state* th);
 
 /* Runs nsteps of the reference step sequence NH_P, NH_T, velocity-Verlet, NH_T, NH_P, pbcWrap
  * (MDLoop.cpp:128-133).  Every out_stride steps (step % out_stride == 0, as MDLoop.cpp:388) the
- * callback receives the output scalars and host copies of r and p; cb may be NULL. */
+ * callback receives the output scalars and host copies of r and p; cb may be NULL.  out_stride
+ * <= 0: no output steps (read the state with mtg_get_state). */
 int mtg_run(mtg_ctx* ctx, int nsteps, int out_stride, mtg_output_cb cb, void* user);
 
 /* Gradient-descent energy minimisation, CMDLoop::runOptimization (MDLoop.cpp:143-173). */

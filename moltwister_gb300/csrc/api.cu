@@ -753,59 +753,10 @@ int read_records(mtg_ctx* c, double* rec) {
 // Applies the pending c2 to the device momenta and rewinds the thermostat (and, under NPT, the
 // barostat) to the state after the last completed step (end of a run).
 int settle_state(mtg_ctx* c) {
-    // mixed: the kernels advance the double-float mirrors; bring the FP64 masters up to date
-    if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
-    if(c->P.ensemble == MTG_NPT) {
-        BaroDev b{};
-        CUDA_TRY(c, copy_now(c, &b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
-        b.p_eps = b.p_eps_saved;
-        b.eps = b.eps_saved;
-        for(int a = 0; a < 3; a++) {
-            b.L[a] = b.L_saved[a];
-            b.Lf[a] = (float)b.L[a];
-        }
-        // production: the box fields the kernels read, for the completed step's box (the list in
-        // place was built in b.Lb)
-        if(!is_reference(c)) baro_box_fields(c->P, b);
-        CUDA_TRY(c, copy_now(c, c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
-        CUDA_TRY(c, copy_now(c, c->d.thp, c->d.thp_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
-    }
-    if(c->P.nrep) {
-        std::vector<StepScalars> rs(c->P.nrep);
-        CUDA_TRY(c, copy_now(c, rs.data(), c->d.rsc, sizeof(StepScalars) * rs.size(), cudaMemcpyDeviceToHost));
-        std::vector<double> c2(rs.size());
-        bool any = false;
-        for(size_t r = 0; r < rs.size(); r++) {
-            c2[r] = rs[r].c2;
-            any |= (rs[r].c2 != 1.0 || rs[r].S != 1.0);
-        }
-        if(any) {
-            std::vector<double> p((size_t)c->P.n * 3);
-            CUDA_TRY(c, copy_now(c, p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
-            scale_momenta(c, p, c2);
-            CUDA_TRY(c, copy_now(c, c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
-            if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
-            CUDA_TRY(c, copy_now(c, c->d.ths, c->d.ths_saved, sizeof(ThermoDev) * rs.size(), cudaMemcpyDeviceToDevice));
-            for(auto& x : rs) {
-                x.c2 = 1.0;
-                x.S = 1.0;
-            }
-            CUDA_TRY(c, copy_now(c, c->d.rsc, rs.data(), sizeof(StepScalars) * rs.size(), cudaMemcpyHostToDevice));
-        }
-        return MTG_OK;
-    }
-    StepScalars s = read_scalars(c);
-    if(s.c2 != 1.0 || s.S != 1.0) {
-        std::vector<double> p((size_t)c->P.n * 3);
-        CUDA_TRY(c, copy_now(c, p.data(), c->d.p, p.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        scale_momenta(c, p, std::vector<double>(1, s.c2));
-        CUDA_TRY(c, copy_now(c, c->d.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice));
-        if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
-        CUDA_TRY(c, copy_now(c, c->d.th, c->d.th_saved, sizeof(ThermoDev), cudaMemcpyDeviceToDevice));
-        s.c2 = 1.0;
-        s.S = 1.0;
-        CUDA_TRY(c, copy_now(c, c->d.sc, &s, sizeof(s), cudaMemcpyHostToDevice));
-    }
+    // the kernels advance the double-float mirrors (mixed) and scale momenta lazily: bring the FP64
+    // masters, the chains and the barostat to the completed step, on the device
+    launch_settle(c->d, c->P, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
     return MTG_OK;
 }
 
@@ -1217,6 +1168,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             d.slot_of = q;
         }
         rc = rc || dalloc(C, &d.vcount, (size_t)n);
+        rc = rc || dalloc(C, &d.vsr, (size_t)n);
         rc = rc || dalloc(C, &d.r_build, (size_t)3 * n);
         rc = rc || dalloc(C, &d.rb4, (size_t)n);
         rc = rc || dalloc(C, &d.rb4s, (size_t)n);
@@ -1394,42 +1346,35 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = settle_state(c);
     if(rc) return rc;
-    if(r) {
-        if(!finite_all(r, n3)) return fail(c, MTG_E_NONFINITE, "non-finite positions");
-        CUDA_TRY(c, copy_now(c, c->d.r, r, n3 * sizeof(double), cudaMemcpyHostToDevice));
-    }
-    if(p) {
-        if(!finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
-        CUDA_TRY(c, copy_now(c, c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice));
-    }
+    if(r && !finite_all(r, n3)) return fail(c, MTG_E_NONFINITE, "non-finite positions");
+    if(p && !finite_all(p, n3)) return fail(c, MTG_E_NONFINITE, "non-finite momenta");
+    // stream-ordered uploads; the force evaluation below synchronises once (from pageable memory
+    // the copy has left the caller's buffer when cudaMemcpyAsync returns)
+    if(r) CUDA_TRY(c, cudaMemcpyAsync(c->d.r, r, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if(p) CUDA_TRY(c, cudaMemcpyAsync(c->d.p, p, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch sets chain states per replica (mtg_batch_set_thermo)");
     const bool box_changes = th && c->P.ensemble == MTG_NPT;
     if(th) {
-        ThermoDev t{};
-        CUDA_TRY(c, copy_now(c, &t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
-        const int M = std::min<int>(th->M, kMaxChain);
-        for(int j = 0; j < M; j++) {
-            t.eta[j] = th->eta[j];
-            t.peta[j] = th->p_eta[j];
+        // chain and barostat values go to the device as kernel arguments (no synchronous copy)
+        ChainSet cs{};
+        cs.M = std::max(0, std::min<int>(th->M, kMaxChain));
+        for(int j = 0; j < cs.M; j++) {
+            cs.eta[j] = th->eta[j];
+            cs.peta[j] = th->p_eta[j];
         }
-        CUDA_TRY(c, copy_now(c, c->d.th, &t, sizeof(t), cudaMemcpyHostToDevice));
-        CUDA_TRY(c, copy_now(c, c->d.th_saved, &t, sizeof(t), cudaMemcpyHostToDevice));
         if(c->P.ensemble == MTG_NPT) {
             if(!std::isfinite(th->p_eps) || !std::isfinite(th->eps)) return fail(c, MTG_E_NONFINITE, "non-finite barostat state");
-            ThermoDev tp{};
-            CUDA_TRY(c, copy_now(c, &tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
-            const int MP = std::min<int>(th->MP, kMaxChain);
-            for(int j = 0; j < MP; j++) {
-                tp.eta[j] = th->etaP[j];
-                tp.peta[j] = th->p_etaP[j];
+            cs.MP = std::max(0, std::min<int>(th->MP, kMaxChain));
+            for(int j = 0; j < cs.MP; j++) {
+                cs.etaP[j] = th->etaP[j];
+                cs.petaP[j] = th->p_etaP[j];
             }
-            CUDA_TRY(c, copy_now(c, c->d.thp, &tp, sizeof(tp), cudaMemcpyHostToDevice));
-            CUDA_TRY(c, copy_now(c, c->d.thp_saved, &tp, sizeof(tp), cudaMemcpyHostToDevice));
-            BaroDev b{};
-            if(!baro_at(c->P, th->p_eps, th->eps, &b, th->box))
+            if(!baro_at(c->P, th->p_eps, th->eps, &cs.baro, th->box))
                 return fail(c, MTG_E_UNSUPPORTED, "the barostat state's box is narrower than twice the cutoff");
-            CUDA_TRY(c, copy_now(c, c->d.baro, &b, sizeof(b), cudaMemcpyHostToDevice));
+            cs.set_baro = 1;
         }
+        launch_set_chains(c->d, cs, c->stream);
+        CUDA_TRY(c, cudaGetLastError());
     }
     // mixed: the double-float mirrors and the box fractions, in the box just set
     if(is_mixed(c)) {
@@ -1481,11 +1426,15 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
     return MTG_OK;
 }
 
+// Longest chunk of steps in one step graph (a run without output steps is cut into chunks of this
+// length: each chunk is one graph launch, a snapshot for the overflow redo and one host check).
+constexpr int kMaxChunk = 100;
+
 int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user) {
     if(!c || nsteps < 0) return MTG_E_INVALID;
     if(nsteps == 0) return MTG_OK;
     CUDA_TRY(c, cudaSetDevice(c->device));
-    if(out_stride <= 0) out_stride = nsteps + 1;
+    if(out_stride < 0) out_stride = 0;   // 0: no output steps
     c->stats = mtg_run_stats{};
     const int builds0 = read_scalars(c).builds;
     // thermostat first half-step of step 0 from the current momenta
@@ -1498,10 +1447,11 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     int nout = 0;
     int64_t last_done = -1;   // last step of the chunk before the one in flight
     while(t < nsteps) {
-        // chunk: up to the next output step (t % out_stride == 0) inclusive
-        int next_out = (t % out_stride == 0) ? t : (t / out_stride + 1) * out_stride;
-        int end = std::min(nsteps - 1, next_out);
-        const bool output = (end % out_stride == 0);
+        // chunk: up to the next output step (t % out_stride == 0) inclusive, at most kMaxChunk steps
+        int end = nsteps - 1;
+        if(out_stride > 0) end = std::min(end, (t % out_stride == 0) ? t : (t / out_stride + 1) * out_stride);
+        end = std::min(end, t + kMaxChunk - 1);
+        const bool output = out_stride > 0 && end % out_stride == 0;
         const int steps = end - t + 1;
         int attempt = 0;
         for(;;) {

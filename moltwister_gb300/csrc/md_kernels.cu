@@ -865,8 +865,12 @@ __global__ void k_vlist(DevSys d, Params P) {
     const int ci = d.pcell_of[i] - v.cbase;
     const int cx = ci % v.pnx, cy = (ci / v.pnx) % v.pny, cz = ci / (v.pnx * v.pny);
     const int sx = v.pnx >= 3 ? 3 : 1, sy = v.pny >= 3 ? 3 : 1, sz = v.pnz >= 3 ? 3 : 1;
+    // pairs with short-range terms fill the row from the front, Coulomb-only pairs from the back;
+    // the back segment then moves behind the front one, so the force gather runs the short-range
+    // arithmetic only where it applies
     uint32_t* out = d.vlist + (size_t)si * d.vmax;
-    int cnt = 0;
+    int cnt = 0, cq = 0;
+    const int* nbc = d.nb_cnt + ti * P.T;
     for(int oz = 0; oz < sz; oz++) {
         const int z = sz == 1 ? 0 : (cz + oz - 1 + v.pnz) % v.pnz;
         for(int oy = 0; oy < sy; oy++) {
@@ -876,7 +880,7 @@ __global__ void k_vlist(DevSys d, Params P) {
                 const int c = v.cbase + x + v.pnx * (y + v.pny * z);
                 const int first = d.pcell_first[c], n = d.pcell_count[c];
                 for(int base = 0; base < n; base += 32) {
-                    bool take = false;
+                    bool take = false, sr = false;
                     uint32_t entry = 0;
                     if(base + lane < n) {
                         const int sj = first + base + lane;
@@ -885,30 +889,52 @@ __global__ void k_vlist(DevSys d, Params P) {
                             const float dx = minimg_f(ri.x - rj.x, Lx, iLx);
                             const float dy = minimg_f(ri.y - rj.y, Ly, iLy);
                             const float dz = minimg_f(ri.z - rj.z, Lz, iLz);
-                            if(dx * dx + dy * dy + dz * dz < list_r2(__float_as_int(rj.w))) {
+                            const int tj = __float_as_int(rj.w);
+                            if(dx * dx + dy * dy + dz * dz < list_r2(tj)) {
                                 const int cls = excl_class(d, i, d.pcell_list[sj]);
                                 if(P.scale[cls] != 0.0f) {
                                     take = true;
+                                    sr = nbc[tj] > 0;
                                     entry = (uint32_t)sj | ((uint32_t)cls << kClassShift);
                                 }
                             }
                         }
                     }
-                    const unsigned ball = __ballot_sync(0xffffffffu, take);
-                    if(take) {
-                        const int slot = cnt + __popc(ball & ((1u << lane) - 1u));
+                    const unsigned below = (1u << lane) - 1u;
+                    const unsigned bsr = __ballot_sync(0xffffffffu, take && sr);
+                    const unsigned bq = __ballot_sync(0xffffffffu, take && !sr);
+                    if(take && sr) {
+                        const int slot = cnt + __popc(bsr & below);
                         if(slot < d.vmax) out[slot] = entry;
+                    } else if(take) {
+                        const int slot = d.vmax - 1 - (cq + __popc(bq & below));
+                        if(slot >= 0) out[slot] = entry;
                     }
-                    cnt += __popc(ball);
+                    cnt += __popc(bsr);
+                    cq += __popc(bq);
                 }
             }
         }
     }
+    const int total = cnt + cq;
+    if(total <= d.vmax) {
+        // move the Coulomb-only entries [vmax - cq, vmax) to [cnt, cnt + cq): the destination lies
+        // below the source, so copying upwards in warp-wide chunks (each read before it is
+        // written) never reads an overwritten entry
+        for(int b = 0; b < cq; b += 32) {
+            uint32_t v = 0;
+            if(b + lane < cq) v = out[d.vmax - cq + b + lane];
+            __syncwarp();
+            if(b + lane < cq) out[cnt + b + lane] = v;
+            __syncwarp();
+        }
+    }
     if(lane == 0) {
-        d.vcount[si] = cnt;
-        if(cnt > d.vmax) {
+        d.vcount[si] = total;
+        d.vsr[si] = cnt;
+        if(total > d.vmax) {
             d.sc->overflow = 1;
-            atomicMax(&d.sc->needed, cnt);
+            atomicMax(&d.sc->needed, total);
         }
     }
 }
@@ -1275,7 +1301,8 @@ constexpr int kSmemPairs = 64;   // type pairs staged (T <= 8)
 // how its row is split over lanes.  The cutoff tests select instead of branching: out-of-range
 // entries, about a quarter of a list with a skin, would otherwise split the warp.  g is clamped
 // to gmax so that |g d| < 2^18.
-template<bool ENERGY>
+// SR = false: a pair without short-range terms (the row's Coulomb-only segment), Coulomb alone.
+template<bool ENERGY, bool SR>
 __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int si, uint32_t ent, int ti, float qi,
                                            float rc2, float rq2, float irc, float gmax, const PairCoef* pc,
                                            const float* us, const float* qt, uint4 qi4, const float (&fs)[3], Fix& fx,
@@ -1292,21 +1319,23 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
     const float ir2 = ir * ir;
     const bool live = r2 >= 1e-6f;
     float g = 0.0f, u = 0.0f;
-    const int pr = ti * P.T + tj;
-    if(pc) {
-        const PairCoef c = pc[pr];
-        if(c.own2 < 0.0f) {
-            if(live && r2 < rc2) pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
-        } else {
-            const bool in = live && r2 < fminf(rc2, c.own2);
-            const float ir6 = ir2 * ir2 * ir2;
-            const float t12 = c.a * ir6 * ir6, t6 = c.b * ir6;
-            const float gl = (12.0f * t12 - 6.0f * t6) * ir2 - c.fs * ir;
-            g = in ? gl : 0.0f;
-            if(ENERGY) u = in ? t12 - t6 - us[pr] + r2 * ir * c.fs : 0.0f;
+    if(SR) {
+        const int pr = ti * P.T + tj;
+        if(pc) {
+            const PairCoef c = pc[pr];
+            if(c.own2 < 0.0f) {
+                if(live && r2 < rc2) pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
+            } else {
+                const bool in = live && r2 < fminf(rc2, c.own2);
+                const float ir6 = ir2 * ir2 * ir2;
+                const float t12 = c.a * ir6 * ir6, t6 = c.b * ir6;
+                const float gl = (12.0f * t12 - 6.0f * t6) * ir2 - c.fs * ir;
+                g = in ? gl : 0.0f;
+                if(ENERGY) u = in ? t12 - t6 - us[pr] + r2 * ir * c.fs : 0.0f;
+            }
+        } else if(live && r2 < rc2) {
+            pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
         }
-    } else if(live && r2 < rc2) {
-        pair_terms<float>(d, pr, r2, ir, ir2, g, u, ENERGY, P.lj_shift);
     }
     if(P.qon) {
         const float qq = kCoulombKf * qi * (qt ? qt[tj] : d.qf[d.pcell_list[sj]]);
@@ -1393,17 +1422,32 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
             const uint4 qi4 = d.pqs[si];
             const int ti = (int)qi4.w;
             const float qi = d.qf[i];
+            const int nsr = min(d.vsr[si], cnt);
+            // the row's pairs with short-range terms, then (with charges on) its Coulomb-only pairs
             int e = lane;
-            for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
+            for(; e + 3 * TEAM < nsr; e += 4 * TEAM) {
                 uint32_t ent[4];
 #pragma unroll
                 for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
 #pragma unroll
                 for(int q = 0; q < 4; q++)
-                    pair_mixed<ENERGY>(d, P, si, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
+                    pair_mixed<ENERGY, true>(d, P, si, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
             }
-            for(; e < cnt; e += TEAM)
-                pair_mixed<ENERGY>(d, P, si, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
+            for(; e < nsr; e += TEAM)
+                pair_mixed<ENERGY, true>(d, P, si, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
+            if(P.qon) {
+                e = nsr + lane;
+                for(; e + 3 * TEAM < cnt; e += 4 * TEAM) {
+                    uint32_t ent[4];
+#pragma unroll
+                    for(int q = 0; q < 4; q++) ent[q] = __ldg(lst + e + q * TEAM);
+#pragma unroll
+                    for(int q = 0; q < 4; q++)
+                        pair_mixed<ENERGY, false>(d, P, si, ent[q], ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
+                }
+                for(; e < cnt; e += TEAM)
+                    pair_mixed<ENERGY, false>(d, P, si, __ldg(lst + e), ti, qi, rc2, rq2, irc, gmax, pc, us_s, qt, qi4, fs, fx, fy, fz, fu, fw);
+            }
         } else {
             const int ti = d.type[i];
             const double qi = d.qd[i];
@@ -1542,6 +1586,80 @@ __global__ void k_forces_to_double(DevSys d, Params P) {
     d.F[3 * i] = double(d.Fx[i]) * (1.0 / kFixScale);
     d.F[3 * i + 1] = double(d.Fy[i]) * (1.0 / kFixScale);
     d.F[3 * i + 2] = double(d.Fz[i]) * (1.0 / kFixScale);
+}
+
+// State after the completed step, on the device (no host round trip).  The kernels apply the
+// thermostat's second-half scale c2 of a step lazily at the next kick; these bring the momenta up
+// to it (mixed: the FP64 master is (hi + lo) c2 rounded to the nearest double-float, which the
+// mirrors then hold), rewind the chains to their state after the second half-step and, under NPT,
+// the barostat to the completed step (its box fields recomputed for that box).
+__global__ void k_settle_momenta(DevSys d, Params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= P.n) return;
+    const double c2 = P.nrep ? d.rsc[d.rep_of[i]].c2 : d.sc->c2;
+    if(c2 == 1.0) return;
+    if(P.precision == MTG_PREC_MIXED) {
+        const float4 ph = d.ph[i], pl = d.pl[i];
+        const DF x = df_of(((double)ph.x + (double)pl.x) * c2);
+        const DF y = df_of(((double)ph.y + (double)pl.y) * c2);
+        const DF z = df_of(((double)ph.z + (double)pl.z) * c2);
+        d.ph[i] = make_float4(x.h, y.h, z.h, ph.w);
+        d.pl[i] = make_float4(x.l, y.l, z.l, pl.w);
+        d.p[3 * i] = (double)x.h + (double)x.l;
+        d.p[3 * i + 1] = (double)y.h + (double)y.l;
+        d.p[3 * i + 2] = (double)z.h + (double)z.l;
+    } else {
+        d.p[3 * i] *= c2;
+        d.p[3 * i + 1] *= c2;
+        d.p[3 * i + 2] *= c2;
+    }
+}
+
+__global__ void k_settle_scalars(DevSys d, Params P) {
+    if(P.nrep) {
+        for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) {
+            StepScalars& s = d.rsc[r];
+            if(s.c2 != 1.0 || s.S != 1.0) {
+                d.ths[r] = d.ths_saved[r];
+                s.c2 = 1.0;
+                s.S = 1.0;
+            }
+        }
+        return;
+    }
+    if(threadIdx.x != 0) return;
+    StepScalars* s = d.sc;
+    if(s->c2 != 1.0 || s->S != 1.0) {
+        *d.th = *d.th_saved;
+        s->c2 = 1.0;
+        s->S = 1.0;
+    }
+    if(P.ensemble == MTG_NPT) {
+        BaroDev& b = *d.baro;
+        b.p_eps = b.p_eps_saved;
+        b.eps = b.eps_saved;
+        for(int a = 0; a < 3; a++) {
+            b.L[a] = b.L_saved[a];
+            b.Lf[a] = (float)b.L[a];
+        }
+        if(P.precision != MTG_PREC_REFERENCE) baro_box_fields(P, b);
+        *d.thp = *d.thp_saved;
+    }
+}
+
+__global__ void k_set_chains(DevSys d, ChainSet cs) {
+    if(threadIdx.x != 0) return;
+    for(int j = 0; j < cs.M; j++) {
+        d.th->eta[j] = d.th_saved->eta[j] = cs.eta[j];
+        d.th->peta[j] = d.th_saved->peta[j] = cs.peta[j];
+    }
+    if(cs.set_baro) {
+        for(int j = 0; j < cs.MP; j++) {
+            d.thp->eta[j] = d.thp_saved->eta[j] = cs.etaP[j];
+            d.thp->peta[j] = d.thp_saved->peta[j] = cs.petaP[j];
+        }
+        *d.baro = cs.baro;
+    }
 }
 
 __global__ void k_clear_rebuild(DevSys d, Params P) {
@@ -1696,6 +1814,14 @@ void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream
         else k_pkick2<false><<<nb, 256, 0, s>>>(d, P);
     }
 }
+
+void launch_settle(const DevSys& d, const Params& P, cudaStream_t s) {
+    if(P.precision == MTG_PREC_MIXED) k_sync<<<nblk(P.n, 256), 256, 0, s>>>(d, P, (int)kSyncToMaster);
+    k_settle_momenta<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
+    k_settle_scalars<<<1, 256, 0, s>>>(d, P);
+}
+
+void launch_set_chains(const DevSys& d, const ChainSet& cs, cudaStream_t s) { k_set_chains<<<1, 32, 0, s>>>(d, cs); }
 
 void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s) {
     k_sync<<<nblk(P.n, 256), 256, 0, s>>>(d, P, (int)mode);

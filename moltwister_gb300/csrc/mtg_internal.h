@@ -220,6 +220,8 @@ struct DevSys {
     int* slot_of;         // [n] atom -> slot (inverse of pcell_list)
     uint32_t* vlist;      // [n * vmax] one row per slot; entries are slots of the partners
     int* vcount;          // [n] per slot
+    int* vsr;             // [n] per slot: the row's first vsr entries are pairs with short-range
+                          //     terms, the rest pairs with Coulomb only
     int vmax;
     double* r_build;      // [3n] positions at the last build (displacement check)
     float4* rb4;          // [n]  the same in FP32 (displacement test), per atom
@@ -287,6 +289,17 @@ void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream
 // fractions pq; the FP64 arrays r and p are the masters the host reads and writes.
 enum SyncMode { kSyncToMaster = 0, kSyncFromMaster = 1, kSyncPositionsFromMaster = 2 };
 void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s);
+void launch_settle(const DevSys& d, const Params& P, cudaStream_t s);   // state after the completed step
+// Chain (and, with set_baro, barostat) state written by a kernel from its arguments, so that a
+// state write-back needs no synchronous copy.
+struct ChainSet {
+    double eta[kMaxChain], peta[kMaxChain];     // particle chain, M entries
+    double etaP[kMaxChain], petaP[kMaxChain];   // barostat chain, MP entries
+    int M, MP;
+    int set_baro;
+    BaroDev baro;
+};
+void launch_set_chains(const DevSys& d, const ChainSet& cs, cudaStream_t s);
 void launch_prod_forces_to_double(const DevSys& d, const Params& P, cudaStream_t s);
 void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s);
 int reduction_blocks(int n);
