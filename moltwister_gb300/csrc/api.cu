@@ -78,11 +78,21 @@ struct mtg_ctx {
     };
     std::vector<Snap> snaps;
     std::vector<void*> snap_bufs;
-    // graphs keyed by (steps, output_at_end)
+    // graphs keyed by (steps, output_at_end + 2 * form)
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
     int generation = 0;
     bool forces_valid = false;
-    bool conditional = true;          // production list builds sit under graph IF nodes
+    // Step graph form of the production modes: 0 = plain capture (the list-build kernels run every
+    // step and return at once when no rebuild is due), 1 = the list build under a conditional IF
+    // node.  Which is faster depends on the system (on GB300 the IF node costs more than the
+    // early-exit kernels of a 9,000-atom system), so the first two chunks of at least
+    // kTuneSteps steps run one form each, timed, and the faster is kept.  Both forms run the
+    // same kernels on the same data: the trajectory does not depend on the choice.
+    bool conditional = true;          // IF nodes accepted by this driver
+    int graph_form = -1;              // chosen form, -1 while measuring
+    double form_us[2] = {0.0, 0.0};   // device time per step of each form
+    bool form_seen[2] = {false, false};
+    int last_form = 0;
     mtg_run_stats stats{};
     // output staging
     std::vector<double> h_r, h_p;
@@ -433,7 +443,28 @@ int enqueue_step(mtg_ctx* c, bool output) {
 // Kernels per step when no list rebuild is due (reference mode rebuilds every step).
 int kernels_per_step(const mtg_ctx* c) {
     // mixed mode ends a step with a second kernel (k_mstep_end)
-    return ((is_reference(c) || !c->conditional) ? 9 : 3) + (is_mixed(c) ? 1 : 0);
+    return ((is_reference(c) || c->last_form == 0) ? 9 : 3) + (is_mixed(c) ? 1 : 0);
+}
+
+constexpr int kTuneSteps = 20;
+
+// Step graph form for the next chunk (see mtg_ctx::graph_form).
+int choose_form(mtg_ctx* c, int steps) {
+    if(is_reference(c) || !c->conditional) return 0;
+    if(c->graph_form >= 0) return c->graph_form;
+    if(steps < kTuneSteps) return 0;
+    return c->form_seen[1] ? 0 : 1;
+}
+
+void record_form(mtg_ctx* c, int form, int steps, float ms) {
+    if(c->graph_form >= 0 || steps < kTuneSteps || is_reference(c)) return;
+    if(!c->conditional) {
+        c->graph_form = 0;
+        return;
+    }
+    c->form_us[form] = 1000.0 * ms / steps;
+    c->form_seen[form] = true;
+    if(c->form_seen[0] && c->form_seen[1]) c->graph_form = (c->form_us[1] < c->form_us[0]) ? 1 : 0;
 }
 
 template<class F>
@@ -452,20 +483,12 @@ int capture_segment(mtg_ctx* c, cudaGraph_t* out, F&& body) {
 //   child(kick+drift, sets the condition) -> IF(rebuild){ child(list build) } -> child(force, kick+reduce)
 // assembled explicitly from captured segments.  Returns non-zero if the driver refuses.
 int build_conditional_graph(mtg_ctx* c, int steps, bool output, cudaGraph_t* out) {
-    cudaGraph_t G = nullptr, gA = nullptr, gB = nullptr, gC = nullptr, gCo = nullptr;
+    cudaGraph_t G = nullptr, gC = nullptr, gCo = nullptr;
     int rc = MTG_OK;
     auto cleanup = [&]() {
-        for(cudaGraph_t x : {gA, gB, gC, gCo}) if(x) cudaGraphDestroy(x);
+        for(cudaGraph_t x : {gC, gCo}) if(x) cudaGraphDestroy(x);
     };
     CUDA_TRY(c, cudaGraphCreate(&G, 0));
-    cudaGraphConditionalHandle cond;
-    if(cudaGraphConditionalHandleCreate(&cond, G, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
-        (void)cudaGetLastError();
-        cudaGraphDestroy(G);
-        return fail(c, MTG_E_UNSUPPORTED, "conditional graph handles unavailable");
-    }
-    rc = rc || capture_segment(c, &gA, [&] { launch_prod_kick_drift(c->d, c->P, c->stream, cond); });
-    rc = rc || capture_segment(c, &gB, [&] { launch_prod_build(c->d, c->P, false, c->stream); });
     rc = rc || capture_segment(c, &gC, [&] {
         launch_prod_force(c->d, c->P, false, c->stream);
         launch_prod_kick2(c->d, c->P, false, c->stream);
@@ -481,19 +504,46 @@ int build_conditional_graph(mtg_ctx* c, int steps, bool output, cudaGraph_t* out
     }
     cudaGraphNode_t prev = nullptr;
     for(int s = 0; s < steps && !rc; s++) {
-        cudaGraphNode_t nA, nB, nC, nBody;
-        cudaError_t e = cudaGraphAddChildGraphNode(&nA, G, prev ? &prev : nullptr, prev ? 1 : 0, gA);
+        // a conditional handle belongs to one IF node: each step has its own, set by its own
+        // kick-drift kernel
+        cudaGraphConditionalHandle cond;
+        const char* where = "conditional handle";
+        cudaError_t e = cudaGraphConditionalHandleCreate(&cond, G, 0, cudaGraphCondAssignDefault);
+        cudaGraph_t gA = nullptr;
+        if(e == cudaSuccess) {
+            where = "kick-drift node";
+            if(capture_segment(c, &gA, [&] { launch_prod_kick_drift(c->d, c->P, c->stream, cond, true); }) != MTG_OK)
+                e = cudaErrorUnknown;
+        }
+        cudaGraphNode_t nA, nB, nC;
+        if(e == cudaSuccess) e = cudaGraphAddChildGraphNode(&nA, G, prev ? &prev : nullptr, prev ? 1 : 0, gA);
+        if(gA) cudaGraphDestroy(gA);
         cudaGraphNodeParams np{};
         np.type = cudaGraphNodeTypeConditional;
         np.conditional.handle = cond;
         np.conditional.type = cudaGraphCondTypeIf;
         np.conditional.size = 1;
-        if(e == cudaSuccess) e = cudaGraphAddNode(&nB, G, &nA, nullptr, 1, &np);
-        if(e == cudaSuccess) e = cudaGraphAddChildGraphNode(&nBody, np.conditional.phGraph_out[0], nullptr, 0, gB);
-        if(e == cudaSuccess) e = cudaGraphAddChildGraphNode(&nC, G, &nB, 1, (output && s == steps - 1) ? gCo : gC);
+        if(e == cudaSuccess) {
+            where = "IF node";
+            e = cudaGraphAddNode(&nB, G, &nA, nullptr, 1, &np);
+        }
+        if(e == cudaSuccess) {
+            // the list build is captured straight into the IF node's body graph
+            where = "list build in the IF body";
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if(e == cudaSuccess) {
+                launch_prod_build(c->d, c->P, false, c->stream);
+                e = cudaStreamEndCapture(c->stream, &body);
+            }
+        }
+        if(e == cudaSuccess) {
+            where = "force node";
+            e = cudaGraphAddChildGraphNode(&nC, G, &nB, 1, (output && s == steps - 1) ? gCo : gC);
+        }
         if(e != cudaSuccess) {
             (void)cudaGetLastError();
-            rc = fail(c, MTG_E_UNSUPPORTED, std::string("conditional step graph: ") + cudaGetErrorString(e));
+            rc = fail(c, MTG_E_UNSUPPORTED, std::string("conditional step graph (") + where + "): " + cudaGetErrorString(e));
         }
         prev = nC;
     }
@@ -506,28 +556,44 @@ int build_conditional_graph(mtg_ctx* c, int steps, bool output, cudaGraph_t* out
     return MTG_OK;
 }
 
-int get_graph(mtg_ctx* c, int steps, bool output, cudaGraphExec_t* out) {
-    auto key = std::make_pair(steps, output ? 1 : 0);
+int get_graph(mtg_ctx* c, int steps, bool output, int form, cudaGraphExec_t* out) {
+    if(form == 1 && !c->conditional) form = 0;
+    auto key = std::make_pair(steps, (output ? 1 : 0) + 2 * form);
     auto it = c->graphs.find(key);
     if(it != c->graphs.end()) {
         *out = it->second;
+        c->last_form = form;
         return MTG_OK;
     }
     cudaGraph_t g = nullptr;
-    bool built = false;
-    if(!is_reference(c) && c->conditional) {
-        if(build_conditional_graph(c, steps, output, &g) == MTG_OK) built = true;
-        else c->conditional = false;   // this driver refuses IF nodes: plain capture from now on
+    c->last_form = 0;
+    if(form == 1 && !is_reference(c)) {
+        if(build_conditional_graph(c, steps, output, &g) == MTG_OK) {
+            cudaGraphExec_t ge;
+            const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            g = nullptr;
+            if(e == cudaSuccess) {
+                cudaGraphUpload(ge, c->stream);   // not on the first timed launch
+                c->graphs[key] = ge;
+                *out = ge;
+                c->last_form = 1;
+                return MTG_OK;
+            }
+            (void)cudaGetLastError();
+            c->err = std::string("conditional step graph (instantiation): ") + cudaGetErrorString(e);
+        }
+        c->conditional = false;   // IF nodes refused: plain capture (early-exit build kernels) from now on
+        key = std::make_pair(steps, output ? 1 : 0);
     }
-    if(!built) {
-        CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        for(int s = 0; s < steps; s++) enqueue_step(c, output && s == steps - 1);
-        CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
-    }
+    CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    for(int s = 0; s < steps; s++) enqueue_step(c, output && s == steps - 1);
+    CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
     cudaGraphExec_t ge;
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if(e != cudaSuccess) return fail(c, MTG_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    cudaGraphUpload(ge, c->stream);
     c->graphs[key] = ge;
     *out = ge;
     return MTG_OK;
@@ -699,6 +765,33 @@ struct BatchSpec {
 
 // Barostat state with momentum p_eps and strain eps: box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax
 // (VelVerlet.cpp:192-211); the saved copy equals the live one (no step pending).
+DF host_df(double x) {
+    DF r;
+    r.h = (float)x;
+    r.l = (float)(x - (double)r.h);
+    return r;
+}
+
+// The mixed integrator's constants for a box, converted as the device's df_of would.
+MixConst mix_const_for(const Params& P, const double* box, const double* fconv, float skin) {
+    MixConst m{};
+    m.dt = host_df(P.dt);
+    m.dt2 = host_df(P.dt / 2.0);
+    for(int a = 0; a < 3; a++) {
+        m.conv[a] = host_df(fconv[a]);
+        m.L[a] = host_df(box[a]);
+        m.Lf[a] = (float)box[a];
+        m.iLf[a] = (float)(1.0 / box[a]);
+        m.L2f[a] = (float)(0.5 * box[a]);
+    }
+    const float hs = 0.5f * skin;
+    m.h2 = hs * hs;
+    m.fcut = host_df(P.fcut);
+    m.fcutf = (float)P.fcut;
+    m.fcut_q = (long long)(P.fcut * kFixScale);
+    return m;
+}
+
 // Barostat state at strain eps (box L = (V0 e^{3 eps} / Vmax)^{1/3} Lmax, VelVerlet.cpp:198-211).
 // `box`, when given, is that box as a previous get_state returned it: used as is when it agrees
 // with eps to rounding, so that a state written back continues bit for bit.  The production modes
@@ -1169,6 +1262,16 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         }
         rc = rc || dalloc(C, &d.vcount, (size_t)n);
         rc = rc || dalloc(C, &d.vsr, (size_t)n);
+        {
+            std::vector<MixConst> mk;
+            if(bs)
+                for(const RepDev& R : reps) mk.push_back(mix_const_for(P, R.box, R.fconv, R.skin));
+            else
+                mk.push_back(mix_const_for(P, P.box, P.fconv, P.skin));
+            MixConst* q = nullptr;
+            rc = rc || upload(C, &q, mk.data(), mk.size());
+            d.mixk = q;
+        }
         rc = rc || dalloc(C, &d.r_build, (size_t)3 * n);
         rc = rc || dalloc(C, &d.rb4, (size_t)n);
         rc = rc || dalloc(C, &d.rb4s, (size_t)n);
@@ -1462,8 +1565,9 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             take_snapshot(c);
             clear_overflow(c);
             cudaGraphExec_t ge;
-            int rc = get_graph(c, steps, output, &ge);
+            int rc = get_graph(c, steps, output, choose_form(c, steps), &ge);
             if(rc) return rc;
+            const int form = c->last_form;
             CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
             CUDA_TRY(c, cudaGraphLaunch(ge, c->stream));
             CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -1497,6 +1601,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             total_ms += ms;
+            record_form(c, form, steps, ms);
             if(s.timeout) return fail(c, MTG_E_TIMEOUT, "a bounded wait in the thermostat gave up");
             if(s.boxerr) return fail(c, MTG_E_UNSUPPORTED, "NPT: the box shrank until a cutoff reached half its width");
             if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite kinetic energy or thermostat scale during the run");

@@ -149,9 +149,6 @@ __device__ inline double nh_chain_half(ThermoDev& th, double& KE2, double g, dou
 // transformations below are Knuth's two-sum, Dekker's fast two-sum and the FMA-based exact
 // product.  The _rn intrinsics keep the compiler from contracting or reordering them.
 // ---------------------------------------------------------------------------------------------
-struct DF {
-    float h, l;
-};
 __device__ __forceinline__ DF two_sum(float a, float b) {
     const float s = __fadd_rn(a, b);
     const float bb = __fsub_rn(s, a);

@@ -280,11 +280,11 @@ __device__ __forceinline__ void load_force(const DevSys& d, int i, double& fx, d
 __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, const SysView& v, int k);
 
 // FP64 mode.  One 256-atom block per launch block; a batch maps blocks to replicas (blk_rep).
-__global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond) {
+__global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond, int use_cond) {
     const SysView v = sys_view(d, P, rep_of_block(d, P));
     const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
     const bool mine = k < v.off + v.n;
-    if(cond) {
+    if(use_cond) {
         // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
         // graph's IF node that wraps the list build
         if(mine) kick_drift_atom(d, P, v, k);
@@ -468,12 +468,33 @@ __device__ __forceinline__ void mix_consts(const SysView& v, const Params& P, Mi
     K.fcut_q = (long long)(P.fcut * kFixScale);
 }
 
+// The same from the constants converted once on the host (MixConst): only the pending scale S
+// changes from step to step.
+__device__ __forceinline__ void mix_load(const DevSys& d, const SysView& v, int rep, MixK& K) {
+    const MixConst& m = d.mixk[rep < 0 ? 0 : rep];
+    K.S = df_of(v.sc->S);
+    K.dt = m.dt;
+    K.dt2 = m.dt2;
+    for(int a = 0; a < 3; a++) {
+        K.conv[a] = m.conv[a];
+        K.L[a] = m.L[a];
+        K.Lf[a] = m.Lf[a];
+        K.iLf[a] = m.iLf[a];
+        K.L2f[a] = m.L2f[a];
+    }
+    K.h2 = m.h2;
+    K.fcut = m.fcut;
+    K.fcutf = m.fcutf;
+    K.fcut_q = m.fcut_q;
+}
+
 // p <- S p + dt/2 F, r <- r + dt p / m (VelVerlet.cpp:74-93 with the pending thermostat scale),
 // box fractions, and the half-skin displacement test against the positions of the last list build.
-__global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond) {
+__global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond, int use_cond) {
     __shared__ MixK K;
-    const SysView v = sys_view(d, P, rep_of_block(d, P));
-    if(threadIdx.x == 0) mix_consts(v, P, K);
+    const int rep = rep_of_block(d, P);
+    const SysView v = sys_view(d, P, rep);
+    if(threadIdx.x == 0) mix_load(d, v, rep, K);
     __syncthreads();
     const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
     if(k < v.off + v.n) {
@@ -502,7 +523,7 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
         d.pqs[d.slot_of[k]] = qk;   // the force gather reads positions in cell (slot) order
         if(d2 > K.h2) flag_rebuild(d, P, v);
     }
-    if(cond) {
+    if(use_cond) {
         // inside a captured step graph: the last block hands the grid-wide rebuild decision to the
         // graph's IF node that wraps the list build
         if(last_block(&d.sc->done_blocks)) {
@@ -518,7 +539,7 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
 // the coefficients of this step's barostat momentum (the momenta carry the pending thermostat
 // scale), box fractions in this step's box, and the displacement test against the build positions
 // scaled with the box (baro_box_fields).
-__global__ void k_mkick_drift_npt(DevSys d, Params P, cudaGraphConditionalHandle cond) {
+__global__ void k_mkick_drift_npt(DevSys d, Params P, cudaGraphConditionalHandle cond, int use_cond) {
     __shared__ MixK K;
     __shared__ DF ap, bp, ar, br;
     __shared__ float sb, h2;
@@ -561,7 +582,7 @@ __global__ void k_mkick_drift_npt(DevSys d, Params P, cudaGraphConditionalHandle
         d.pqs[d.slot_of[k]] = qk;
         if(d2 > h2) flag_rebuild(d, P, v);
     }
-    if(cond) {
+    if(use_cond) {
         if(last_block(&d.sc->done_blocks)) {
             if(threadIdx.x == 0) {
                 d.sc->done_blocks = 0;
@@ -633,8 +654,9 @@ template<bool OUTPUT>
 __global__ void k_mkick2(DevSys d, Params P) {
     __shared__ MixK K;
     __shared__ double smem[32 * 3];
-    const SysView sv = sys_view(d, P, rep_of_block(d, P));
-    if(threadIdx.x == 0) mix_consts(sv, P, K);
+    const int rep = rep_of_block(d, P);
+    const SysView sv = sys_view(d, P, rep);
+    if(threadIdx.x == 0) mix_load(d, sv, rep, K);
     __syncthreads();
     const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
     DF ke{0.0f, 0.0f};
@@ -1662,6 +1684,11 @@ __global__ void k_set_chains(DevSys d, ChainSet cs) {
     }
 }
 
+__global__ void k_clear_cell_counts(DevSys d, int ncell) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if(c < ncell && d.sc->rebuild) d.pcell_count[c] = 0;
+}
+
 __global__ void k_clear_rebuild(DevSys d, Params P) {
     if(!d.sc->rebuild) return;
     for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) d.rsc[r].rebuild = 0;
@@ -1749,18 +1776,20 @@ void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
     else k_prologue<false><<<integration_blocks(P), 256, 0, s>>>(d, P);
 }
 
-void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond) {
+void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond, bool use_cond) {
     const int nb = integration_blocks(P);
-    if(P.precision == MTG_PREC_MIXED && P.ensemble == MTG_NPT) k_mkick_drift_npt<<<nb, 256, 0, s>>>(d, P, cond);
-    else if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
-    else k_pkick_drift<<<nb, 256, 0, s>>>(d, P, cond);
+    const int u = use_cond ? 1 : 0;
+    if(P.precision == MTG_PREC_MIXED && P.ensemble == MTG_NPT) k_mkick_drift_npt<<<nb, 256, 0, s>>>(d, P, cond, u);
+    else if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond, u);
+    else k_pkick_drift<<<nb, 256, 0, s>>>(d, P, cond, u);
 }
 
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
     const int ncell = P.nrep ? P.ncell_total : P.pnx * P.pny * P.pnz;
     if(force) cudaMemsetAsync(&d.sc->rebuild, 0xff, sizeof(int32_t), s);
-    // counts are cleared unconditionally; the kernels below return early when no rebuild is due
-    cudaMemsetAsync(d.pcell_count, 0, sizeof(int) * ncell, s);
+    // counts are cleared by a kernel (a graph's conditional body holds kernel nodes) and only
+    // when a rebuild is due; the kernels below return early otherwise
+    k_clear_cell_counts<<<nblk(ncell, 256), 256, 0, s>>>(d, ncell);
     if(P.precision == MTG_PREC_MIXED) k_pcell_assign<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     k_pcell_scan<<<P.nrep ? P.nrep : 1, 1024, 0, s>>>(d, P);

@@ -26,6 +26,22 @@ constexpr uint32_t kIdxMask = 0x1FFFFFFFu;
 constexpr int kClassShift = 29;
 // Exclusion classes (FunctorCalcForce.cpp:95-157): 0 none, 1 1-2, 2 1-3, 3 1-4, 4 same molecule.
 
+// A double-float value hi + lo (two FP32 numbers, |lo| <= ulp(hi)/2): about 48 bits of mantissa
+// from FP32 arithmetic.
+struct DF {
+    float h, l;
+};
+
+// Constants of the mixed-precision integration kernels for one system's box (NVT/NVE: fixed for
+// the context's life), converted from FP64 once on the host instead of by every block.
+struct MixConst {
+    DF dt, dt2, fcut;
+    DF conv[3], L[3];          // 2^32 / L, L
+    float Lf[3], iLf[3], L2f[3];
+    float h2, fcutf;           // (skin / 2)^2; cutoff force
+    long long fcut_q;          // cutoff force in fixed point
+};
+
 // Device-side thermostat state.  `th` is the live chain; `saved` is the chain right after the
 // second half-step of the last completed step (what the reference holds between steps).
 struct ThermoDev {
@@ -220,6 +236,7 @@ struct DevSys {
     int* slot_of;         // [n] atom -> slot (inverse of pcell_list)
     uint32_t* vlist;      // [n * vmax] one row per slot; entries are slots of the partners
     int* vcount;          // [n] per slot
+    const MixConst* mixk; // [1] or [nrep]: the mixed integrator's constants per system
     int* vsr;             // [n] per slot: the row's first vsr entries are pairs with short-range
                           //     terms, the rest pairs with Coulomb only
     int vmax;
@@ -277,7 +294,9 @@ void launch_ref_kick2(const DevSys& d, const Params& P, bool output, cudaStream_
 // Shared
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s);
 // Production modes
-void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond = 0);
+// use_cond: inside a conditional step graph, the last block sets `cond` to the rebuild decision
+void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond = 0,
+                            bool use_cond = false);
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s);
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s);
 // Second half of the step: the per-atom kick and block sums (kKick2Atoms) and, in mixed mode, the
