@@ -970,6 +970,11 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
     P.fcut = cfg->cutoff_force;
     P.lj_shift = cfg->lj_shift;
     P.wait_polls = 1 << 22;
+    {
+        const double w0 = 1.0 / (2.0 - std::cbrt(2.0));
+        P.chain_stage[0] = w0 * P.dt / double(P.nresp > 0 ? P.nresp : 1);
+        P.chain_stage[1] = (1.0 - 2.0 * w0) * P.dt / double(P.nresp > 0 ? P.nresp : 1);
+    }
     if(P.ensemble == MTG_NPT) {
         // SimulationBox.cpp:58-76: NH_P_ shares T; W = kT tauP^2, P_ = pressure / Conv_press, V0 = Lx Ly Lz
         const double tauP = cfg->pressure_relax / kConvt;

@@ -499,31 +499,38 @@ __device__ __forceinline__ DF df_exp_tiny(DF x) {
 }
 
 template<int MM>
-__device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, double dt, int M_rt, int nresp, int seq) {
+__device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, const double* stage, int M_rt, int nresp,
+                                          int seq) {
     constexpr int CAP = MM > 0 ? MM : kMaxChain;
     const int M = MM > 0 ? MM : M_rt;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const double w0 = sy_w0(true);
-    const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
-    const double gkT = g * kT;
+    const unsigned full = 0xffffffffu;
     const int top = M - 1;
     const int nsub = 3 * nresp;
     int* tmo = &X.timeout;
     const float tiny = 0.0009765625f;   // 2^-10
+    // FP64 -> double-float conversions run one value per lane: an FP64 instruction costs the
+    // same for one lane as for 32 on this GPU, so a warp converts its inputs in one pass and
+    // hands them out by shuffles.  Lanes 0..15 take one table, lanes 16..31 another.
+    auto from = [&](const DF& mine, int l) { return DF{__shfl_sync(full, mine.h, l), __shfl_sync(full, mine.l, l)}; };
     if(warp == 0) {
         // ---------------- main: p_eta[0..M-2], steps 1.2 and 1.5 ----------------
-        // FP64 -> double-float once per call; every per-stage constant is then a double-float
-        // product (the Suzuki-Yoshida stages have two distinct weights)
+        // every per-stage constant is then a double-float product (the Suzuki-Yoshida stages have
+        // two distinct lengths, stage[0] and stage[1])
         DF pe[CAP], iQ[CAP], cprev[CAP], xprev[CAP];
+        const int l16 = lane & 15;
+        double v1 = (lane < 16) ? X.pe[l16 < M ? l16 : 0] : X.iQ[l16 < M ? l16 : 0];
+        double v2 = (lane == 0) ? X.KE2 : (lane == 1) ? kT : (lane == 2) ? g * kT : (lane == 3) ? stage[0] : stage[1];
+        const DF c1 = df_of(v1), c2 = df_of(v2);
 #pragma unroll
         for(int j = 0; j < M; j++) {
-            pe[j] = df_of(X.pe[j]);
-            iQ[j] = df_of(X.iQ[j]);
+            pe[j] = from(c1, j);
+            iQ[j] = from(c1, 16 + j);
         }
-        DF KE2 = df_of(X.KE2);
+        DF KE2 = from(c2, 0);
         DF eta_mine = df_of((lane < top) ? X.eta[lane] : 0.0);
-        const DF kTD = df_of(kT), gkTD = df_of(gkT);
-        const DF DtW[2] = {df_of(w[0] * dt / double(nresp)), df_of(w[1] * dt / double(nresp))};
+        const DF kTD = from(c2, 1), gkTD = from(c2, 2);
+        const DF DtW[2] = {from(c2, 3), from(c2, 4)};
         DF iQl{0.0f, 0.0f};
 #pragma unroll
         for(int j = 0; j < top; j++)
@@ -610,20 +617,27 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
             }
         }
         __syncwarp();
-        if(lane < top) {
+        {
+            // lanes 0..top-1 return p_eta, lanes 16..16+top-1 eta, in one conversion pass
+            const int l16 = lane & 15;
             DF v{0.0f, 0.0f};
 #pragma unroll
             for(int j = 0; j < top; j++)
-                if(j == lane) v = pe[j];
-            X.pe[lane] = df_val(v);
-            X.eta[lane] = df_val(eta_mine);
+                if(j == l16) v = pe[j];
+            const DF e = from(eta_mine, l16);
+            const double o = df_val(lane < 16 ? v : e);
+            if(l16 < top) {
+                if(lane < 16) X.pe[l16] = o;
+                else X.eta[l16] = o;
+            }
         }
     } else if(warp == 1) {
         // ---------------- warp 1: step 1.4, kinetic term, momentum scale ----------------
-        const DF iQ0 = df_of(X.iQ[0]);
-        DF KE2 = df_of(X.KE2), scale{1.0f, 0.0f};
-        const DF D1W[2] = {df_neg(df_mul(df_of(w[0] * dt / double(nresp)), df_scale(iQ0, 0.5f))),
-                           df_neg(df_mul(df_of(w[1] * dt / double(nresp)), df_scale(iQ0, 0.5f)))};
+        const double v = (lane == 0) ? X.iQ[0] : (lane == 1) ? X.KE2 : (lane == 2) ? stage[0] : stage[1];
+        const DF cv = df_of(v);
+        const DF iQ0 = from(cv, 0);
+        DF KE2 = from(cv, 1), scale{1.0f, 0.0f};
+        const DF D1W[2] = {df_neg(df_mul(from(cv, 2), df_scale(iQ0, 0.5f))), df_neg(df_mul(from(cv, 3), df_scale(iQ0, 0.5f)))};
         int s = 0;
         for(int mu = 0; mu < 3; mu++) {
             const DF D1 = D1W[mu == 1 ? 1 : 0];
@@ -636,18 +650,22 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
                 nh_post(&X.f_ke, seq + s + 1);
             }
         }
-        if(lane == 0) {
-            X.KE2 = df_val(KE2);
-            X.scale = df_val(scale);
-        }
+        const DF out = (lane == 0) ? KE2 : scale;
+        const double o = df_val(out);   // both in one pass
+        if(lane == 0) X.KE2 = o;
+        if(lane == 1) X.scale = o;
     } else if(warp == 2) {
         // ---------------- warp 2: p_eta[M-1] (steps 1.1, 1.6), its exponential, eta[M-1] ----------------
-        const DF iQt = df_of(X.iQ[top]);
-        const DF iQm = df_of(X.iQ[top - 1]), nkT = df_of(-kT);
-        const DF DtW[2] = {df_of(w[0] * dt / double(nresp)), df_of(w[1] * dt / double(nresp))};
-        DF pt = df_of(X.pe[top]);
-        DF eta_t = df_of(X.eta[top]);
-        DF pm = df_of(X.pe[top - 1]);
+        const double v = (lane == 0) ? X.iQ[top] : (lane == 1) ? X.iQ[top - 1] : (lane == 2) ? -kT
+                         : (lane == 3) ? stage[0] : (lane == 4) ? stage[1] : (lane == 5) ? X.pe[top]
+                         : (lane == 6) ? X.eta[top] : X.pe[top - 1];
+        const DF cv = df_of(v);
+        const DF iQt = from(cv, 0);
+        const DF iQm = from(cv, 1), nkT = from(cv, 2);
+        const DF DtW[2] = {from(cv, 3), from(cv, 4)};
+        DF pt = from(cv, 5);
+        DF eta_t = from(cv, 6);
+        DF pm = from(cv, 7);
         DF d4prev{0.0f, 0.0f};
         int s = 0;
         for(int mu = 0; mu < 3; mu++) {
@@ -671,10 +689,9 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, do
         nh_wait(&X.f_pe_m2, seq + nsub, tmo, X.polls);             // 1.6 of the last substep
         pm = X.dpe_m2;
         pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
-        if(lane == 0) {
-            X.pe[top] = df_val(pt);
-            X.eta[top] = df_val(eta_t);
-        }
+        const double o = df_val((lane == 0) ? pt : eta_t);   // both in one pass
+        if(lane == 0) X.pe[top] = o;
+        if(lane == 1) X.eta[top] = o;
     }
     return seq + nsub;
 }
@@ -736,10 +753,10 @@ __device__ inline bool last_block(unsigned int* counter) {
 // for any other.
 template<bool DFLOAT>
 __device__ __forceinline__ int nh_chain_half_3w(NhExchange& X, double g, double kT, double dt, int M, int nresp, int seq,
-                                                bool fixed) {
+                                                bool fixed, const double* stage) {
     if constexpr(DFLOAT) {
-        if(M == 4) return nh_chain_half_3w_df<4>(X, g, kT, dt, M, nresp, seq);
-        return nh_chain_half_3w_df<0>(X, g, kT, dt, M, nresp, seq);
+        if(M == 4) return nh_chain_half_3w_df<4>(X, g, kT, stage, M, nresp, seq);
+        return nh_chain_half_3w_df<0>(X, g, kT, stage, M, nresp, seq);
     } else {
         if(M == 4) return nh_chain_half_3w_t<4>(X, g, kT, dt, M, nresp, seq, fixed);
         return nh_chain_half_3w_t<0>(X, g, kT, dt, M, nresp, seq, fixed);
@@ -780,7 +797,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         bar96();
         int seq = 0;
         if(second_half) {
-            seq = nh_chain_half_3w<DFLOAT>(X, g, P.kT, P.dt, M, nresp, seq, fixed);
+            seq = nh_chain_half_3w<DFLOAT>(X, g, P.kT, P.dt, M, nresp, seq, fixed, P.chain_stage);
             bar96();
             c2 = X.scale;
             if(tid < M) {
@@ -798,7 +815,7 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
         }
         const double KE_after2 = X.KE2;
         bar96();
-        seq = nh_chain_half_3w<DFLOAT>(X, g, P.kT, P.dt, M, nresp, seq, fixed);
+        seq = nh_chain_half_3w<DFLOAT>(X, g, P.kT, P.dt, M, nresp, seq, fixed, P.chain_stage);
         bar96();
         c1 = X.scale;
         KEf = X.KE2;

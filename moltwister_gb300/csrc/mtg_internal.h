@@ -138,6 +138,8 @@ struct Params {
     double QP;            // barostat chain masses kT tauP^2
     double V0;            // LmaxX LmaxY LmaxZ
     int wait_polls;       // limit of the bounded device waits (thermostat hand-overs)
+    double chain_stage[2];// production particle chain: the Suzuki-Yoshida stage lengths w0 dt / nresp
+                          // and (1 - 2 w0) dt / nresp, w0 = 1 / (2 - 2^(1/3))
 };
 
 
