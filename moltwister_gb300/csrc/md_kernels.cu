@@ -1684,18 +1684,21 @@ __global__ void k_set_chains(DevSys d, ChainSet cs) {
     }
 }
 
-__global__ void k_clear_cell_counts(DevSys d, int ncell) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if(c < ncell && d.sc->rebuild) d.pcell_count[c] = 0;
-}
-
-__global__ void k_clear_rebuild(DevSys d, Params P) {
+// End of a list build: the cell counts go back to zero for the next build (they start at zero
+// when allocated), and the last block clears the rebuild flags and counts the build.  Every block
+// passes the early-exit test before the last one clears the flag it tests.
+__global__ void k_finish_build(DevSys d, Params P, int ncell) {
     if(!d.sc->rebuild) return;
-    for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) d.rsc[r].rebuild = 0;
-    __syncthreads();
-    if(threadIdx.x == 0) {
-        d.sc->rebuild = 0;
-        d.sc->builds += 1;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if(c < ncell) d.pcell_count[c] = 0;
+    if(last_block(&d.sc->done_blocks)) {
+        for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) d.rsc[r].rebuild = 0;
+        __syncthreads();
+        if(threadIdx.x == 0) {
+            d.sc->done_blocks = 0;
+            d.sc->rebuild = 0;
+            d.sc->builds += 1;
+        }
     }
 }
 
@@ -1787,9 +1790,8 @@ void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cu
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
     const int ncell = P.nrep ? P.ncell_total : P.pnx * P.pny * P.pnz;
     if(force) cudaMemsetAsync(&d.sc->rebuild, 0xff, sizeof(int32_t), s);
-    // counts are cleared by a kernel (a graph's conditional body holds kernel nodes) and only
-    // when a rebuild is due; the kernels below return early otherwise
-    k_clear_cell_counts<<<nblk(ncell, 256), 256, 0, s>>>(d, ncell);
+    // the cell counts are zero here (k_finish_build); every kernel returns at once when no
+    // rebuild is due
     if(P.precision == MTG_PREC_MIXED) k_pcell_assign<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     k_pcell_scan<<<P.nrep ? P.nrep : 1, 1024, 0, s>>>(d, P);
@@ -1797,7 +1799,7 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, P, ncell, P.precision == MTG_PREC_MIXED);
     if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
-    k_clear_rebuild<<<1, 256, 0, s>>>(d, P);
+    k_finish_build<<<nblk(ncell, 256), 256, 0, s>>>(d, P, ncell);
 }
 
 template<bool MIXED, bool ENERGY>
