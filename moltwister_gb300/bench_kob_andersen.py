@@ -5,8 +5,9 @@
 System: the Kob-Andersen 80:20 binary LJ mixture at reduced density 1.2 (workloads.kob_andersen;
 ncell = 64 gives 1,048,576 atoms), cutoff 2.5 sigma_ab per pair with energies shifted to zero at
 the cutoffs, LJ reduced units mapped to sigma = 1 A, eps = 1 kJ/mol, m = 1 g/mol (T* = 0.75 is
-90.2 K, dt* = 0.005 is 0.5 fs).  Seeded FCC sites with a random A/B assignment and jitter, relaxed by
-gradient descent, then Maxwell-Boltzmann momenta at T*.
+90.2 K, dt* = 0.005 is 0.5 fs).  Atoms placed uniformly at random (seeded; --placement lattice:
+jittered FCC sites) with a random A/B assignment, relaxed by gradient descent in stages of growing
+learning rate (workloads.relax_random) and --relax more steps, then Maxwell-Boltzmann momenta at T*.
 
 Reported (one JSON line):
   - atom-steps/s of the mixed and the FP64 path (CUDA events around the step graphs), and their ratio;
@@ -75,16 +76,19 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--drift-steps", type=int, default=80000)
     ap.add_argument("--drift-stride", type=int, default=20)
+    ap.add_argument("--placement", choices=("random", "lattice"), default="random")
     args = ap.parse_args(argv)
 
     from moltwister_gb300 import workloads as W
     from moltwister_gb300.build import build
     from moltwister_gb300.engine import Engine, device_name
     build()
-    s, cfg = W.kob_andersen(ncell=args.ncell, seed=args.seed)
+    s, cfg = W.kob_andersen(ncell=args.ncell, seed=args.seed, placement=args.placement)
     n = s.n
     kT = cfg.temperature / W.CONV_T
     t0 = time.perf_counter()
+    if args.placement == "random":
+        s.r = W.relax_random(s, cfg)
     em = Engine(s, cfg)
     em.optimize(args.relax)
     r, _, _ = em.get_state()
@@ -142,8 +146,12 @@ def main(argv=None):
         "force_error_mixed_vs_fp64": {"rel_rms": rms, "max_rel_to_max_force": mx, "rms_abs_kJ_mol_A": rms_atom,
                                       "configuration": f"after the {args.steps}-step mixed NVE run"},
         "config": {"rho_star": 1.2, "T_star": 0.75, "dt_fs": cfg.timestep, "cutoff": "2.5 sigma_ab per pair, shifted",
-                   "skin_A": cfg.listskin, "relax": f"{args.relax} gradient-descent steps", "setup_s": setup_s,
-                   "data": "synthetic (seeded FCC sites, random A/B, jitter 0.05)"},
+                   "skin_A": cfg.listskin,
+                   "relax": (f"{sum(k for _, k in W.RANDOM_RELAX_STAGES)} staged gradient-descent steps (learning rates "
+                             f"{', '.join(str(lr) for lr, _ in W.RANDOM_RELAX_STAGES)}) + " if args.placement == "random" else "")
+                            + f"{args.relax} gradient-descent steps", "setup_s": setup_s,
+                   "data": ("synthetic (seeded uniform random placement, random A/B)" if args.placement == "random"
+                            else "synthetic (seeded FCC sites, random A/B, jitter 0.05)")},
     }
     print(json.dumps(out))
     em.close()

@@ -125,17 +125,24 @@ KA_PAIRS = {("A", "A"): (1.0, 1.0), ("A", "B"): (1.5, 0.8), ("B", "B"): (0.5, 0.
 
 def kob_andersen(ncell: int = 64, seed: int = 3, T_star: float = 0.75, rho_star: float = 1.2,
                  frac_a: float = 0.8, jitter: float = 0.05, per_pair_cutoff: bool = True,
-                 dt_fs: float = 0.5) -> Tuple[MDSystem, MDConfig]:
+                 dt_fs: float = 0.5, placement: str = "lattice") -> Tuple[MDSystem, MDConfig]:
     """Kob-Andersen 80:20 mixture, N = 4 ncell^3 (ncell = 64: 1,048,576 atoms) at reduced
-    density rho_star: FCC sites with a seeded random A/B assignment and seeded jitter (the caller
-    relaxes it with Engine.optimize), eps/sigma AA 1/1, AB 1.5/0.8, BB 0.5/0.88, cutoff 2.5
-    sigma_ab per pair (with per_pair_cutoff; else 2.5 for every pair, the only form the reference can
-    express), energies shifted to zero at the cutoffs, Maxwell-Boltzmann momenta at T*, NVE."""
+    density rho_star, with a seeded random A/B assignment: placement "lattice" puts the atoms on
+    FCC sites with seeded jitter, "random" uniformly at random in the box (seeded; overlapping
+    atoms then need relax_random before dynamics).  eps/sigma AA 1/1, AB 1.5/0.8, BB 0.5/0.88,
+    cutoff 2.5 sigma_ab per pair (with per_pair_cutoff; else 2.5 for every pair, the only form the
+    reference can express), energies shifted to zero at the cutoffs, Maxwell-Boltzmann momenta at
+    T*, NVE."""
     rng = np.random.default_rng(seed)
     a = (4.0 / rho_star) ** (1.0 / 3.0)
     r = fcc_positions(ncell, a)
     N = r.shape[0]
-    if jitter > 0:
+    if placement == "random":
+        L = ncell * a
+        r = rng.uniform(-0.5 * L, 0.5 * L, (N, 3))
+    elif placement != "lattice":
+        raise ValueError(placement)
+    elif jitter > 0:
         r = r + rng.uniform(-jitter, jitter, r.shape)
     nb = int(round((1.0 - frac_a) * N))
     ids = np.array(["A"] * N, dtype=object)
@@ -153,6 +160,31 @@ def kob_andersen(ncell: int = 64, seed: int = 3, T_star: float = 0.75, rho_star:
                    cutoffradius=2.5, neighshell=0.3, listskin=0.3, coulomb="cutoff", coulombcutoff=2.5,
                    precision="mixed", ljshift=True, clipforces=False, optlearningrate=1e-4)
     return sys_, cfg
+
+
+# Learning-rate stages of relax_random: the mixed force gather caps every pair force at about
+# 2.6e5 (its fixed-point range), so the first stages move overlapping atoms by at most a few
+# hundredths of sigma per step while they separate; the later ones relax the structure.
+RANDOM_RELAX_STAGES = ((1e-7, 100), (1e-6, 100), (1e-5, 200), (1e-4, 200))
+
+
+def relax_random(s: "MDSystem", cfg: "MDConfig", stages=RANDOM_RELAX_STAGES, device: int = 0) -> np.ndarray:
+    """Gradient descent (Engine.optimize, the reference's optimizeenergy) from a random placement,
+    in stages of growing learning rate, in the mixed mode; returns the relaxed positions."""
+    from .engine import Engine
+    from .system import MDConfig as _C
+    r = np.array(s.r, np.float64)
+    for lr, steps in stages:
+        c = _C(**{k: getattr(cfg, k) for k in cfg.__dataclass_fields__})
+        c.precision = "mixed"
+        c.optlearningrate = lr
+        si = s.copy()
+        si.r = r
+        e = Engine(si, c, device=device)
+        e.optimize(steps)
+        r = e.get_state()[0]
+        e.close()
+    return r
 
 
 # ------------------------------------------------------------------------------------------------
