@@ -66,7 +66,7 @@ def cases():
 
 
 def big_cases():
-    """The two BASELINE-sized parity cases.  Their neighbour lists are stored as one 64-bit hash
+    """The two full-size parity cases (4,000-atom argon, 9,000-atom water).  Their neighbour lists are stored as one 64-bit hash
     per atom (golden_cases.neighbour_hash) and their trajectories without forces, which keeps the
     fixtures near a megabyte each."""
     out = {}

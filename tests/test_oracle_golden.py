@@ -49,7 +49,7 @@ def test_forces_bit_exact(name):
 def test_trajectory_bit_exact(name):
     s, cfg, d = G.load(name)
     if "prefix_steps" in d:
-        # the BASELINE-sized cases: the oracle replays the reference's short prefix run (the
+        # the full-size cases (4,000-atom argon, 9,000-atom water): the oracle replays the reference's short prefix run (the
         # 100-step trajectory is checked against the GPU, which the oracle is pinned to here)
         k = int(d["prefix_steps"])
         o = O.Oracle(s, cfg).run_ref(k, k)
