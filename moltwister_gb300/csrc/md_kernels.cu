@@ -830,7 +830,7 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
     d.vcount[d.pcell_first[c] + slot] = i;   // vcount doubles as scratch until the list kernel
 }
 
-// Atoms of a cell ordered by index (a rank pass, deterministic).  The position in the resulting
+// Atoms of a cell ordered by type and index (a rank pass, deterministic).  The position in the resulting
 // cell order is the atom's slot: the Verlet list is kept per slot with partners named by slot,
 // and the positions the force gather reads are copied into slot order, so the partners of the
 // atoms a block works on lie in a compact, cache-resident range.
@@ -840,9 +840,16 @@ __global__ void k_pcell_rank(DevSys d, Params P, int ncell, bool mixed) {
     const int cnt = d.pcell_count[warp], first = d.pcell_first[warp];
     const int* tmp = d.vcount;
     for(int a = lane; a < cnt; a += 32) {
+        // order within the cell: by type, then by index (deterministic); atoms of one type sit
+        // together, so the atoms a warp's force gather takes have alike rows (same split into
+        // short-range and Coulomb-only pairs, similar lengths)
         const int v = tmp[first + a];
+        const long long kv = ((long long)d.type[v] << 32) | (unsigned)v;
         int rank = 0;
-        for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < v);
+        for(int b = 0; b < cnt; b++) {
+            const int u = tmp[first + b];
+            rank += ((((long long)d.type[u] << 32) | (unsigned)u) < kv);
+        }
         const int slot = first + rank;
         d.pcell_list[slot] = v;
         d.slot_of[v] = slot;
