@@ -830,10 +830,10 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
     d.vcount[d.pcell_first[c] + slot] = i;   // vcount doubles as scratch until the list kernel
 }
 
-// Atoms of a cell ordered by type and index (a rank pass, deterministic).  The position in the resulting
-// cell order is the atom's slot: the Verlet list is kept per slot with partners named by slot,
-// and the positions the force gather reads are copied into slot order, so the partners of the
-// atoms a block works on lie in a compact, cache-resident range.
+// Atoms of a cell ordered by type and index (a rank pass, deterministic).  The position in the
+// resulting cell order is the atom's slot: the Verlet list is kept per slot with partners named by
+// slot, and the positions the force gather reads are copied into slot order, so the partners of
+// the atoms a block works on lie in a compact, cache-resident range.
 __global__ void k_pcell_rank(DevSys d, Params P, int ncell, bool mixed) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(warp >= ncell || !rebuild_due(d, P, rep_of_cell(d, P, warp))) return;
