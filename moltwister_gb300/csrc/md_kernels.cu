@@ -494,13 +494,27 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
     __shared__ MixK K;
     const int rep = rep_of_block(d, P);
     const SysView v = sys_view(d, P, rep);
+    // the atom's loads are issued before the block waits for the constants
+    const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
+    const bool mine = k < v.off + v.n;
+    float4 h, l, ph, pl, rb;
+    long long fq[3];
+    int slot = 0;
+    if(mine) {
+        h = d.hi[k];
+        l = d.lo[k];
+        ph = d.ph[k];
+        pl = d.pl[k];
+        rb = d.rb4[k];
+        fq[0] = d.Fx[k];
+        fq[1] = d.Fy[k];
+        fq[2] = d.Fz[k];
+        slot = d.slot_of[k];
+    }
     if(threadIdx.x == 0) mix_load(d, v, rep, K);
     __syncthreads();
-    const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
-    if(k < v.off + v.n) {
-        const float4 h = d.hi[k], l = d.lo[k], ph = d.ph[k], pl = d.pl[k], rb = d.rb4[k];
+    if(mine) {
         const DF dtm = df_mul(K.dt, DF{ph.w, pl.w});
-        const long long fq[3] = {d.Fx[k], d.Fy[k], d.Fz[k]};
         DF p[3] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}};
         DF x[3] = {{h.x, l.x}, {h.y, l.y}, {h.z, l.z}};
         const float rbv[3] = {rb.x, rb.y, rb.z};
@@ -520,7 +534,7 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
         d.lo[k] = make_float4(x[0].l, x[1].l, x[2].l, l.w);
         const uint4 qk = make_uint4(q[0], q[1], q[2], (unsigned int)__float_as_int(l.w));
         d.pq[k] = qk;
-        d.pqs[d.slot_of[k]] = qk;   // the force gather reads positions in cell (slot) order
+        d.pqs[slot] = qk;   // the force gather reads positions in cell (slot) order
         if(d2 > K.h2) flag_rebuild(d, P, v);
     }
     if(use_cond) {
@@ -656,15 +670,27 @@ __global__ void k_mkick2(DevSys d, Params P) {
     __shared__ double smem[32 * 3];
     const int rep = rep_of_block(d, P);
     const SysView sv = sys_view(d, P, rep);
+    // the atom's loads are issued before the block waits for the constants
+    const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
+    const bool mine = k < sv.off + sv.n;
+    float4 h, l, ph, pl;
+    long long fq[3];
+    double uk = 0.0;
+    if(mine) {
+        h = d.hi[k];
+        l = d.lo[k];
+        ph = d.ph[k];
+        pl = d.pl[k];
+        fq[0] = d.Fx[k];
+        fq[1] = d.Fy[k];
+        fq[2] = d.Fz[k];
+        if(OUTPUT) uk = d.U[k];
+    }
     if(threadIdx.x == 0) mix_load(d, sv, rep, K);
     __syncthreads();
-    const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
     DF ke{0.0f, 0.0f};
     double v[3] = {0.0, 0.0, 0.0};
-    if(k < sv.off + sv.n) {
-        float4 h = d.hi[k], l = d.lo[k];
-        const float4 ph = d.ph[k], pl = d.pl[k];
-        long long fq[3] = {d.Fx[k], d.Fy[k], d.Fz[k]};
+    if(mine) {
         DF p[3] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}};
         DF x[3] = {{h.x, l.x}, {h.y, l.y}, {h.z, l.z}};
         DF p2{0.0f, 0.0f};
@@ -697,7 +723,7 @@ __global__ void k_mkick2(DevSys d, Params P) {
         ke = df_mul(p2, DF{ph.w, pl.w});
         if(OUTPUT) {
             v[1] = fr;
-            v[2] = d.U[k];
+            v[2] = uk;
         }
     }
     const double ke_blk = block_sum_df(ke, smem);
@@ -827,7 +853,9 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
     if(i >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     const int c = d.pcell_of[i];
     const int slot = atomicAdd(&d.pcell_cursor[c], 1);
-    d.vcount[d.pcell_first[c] + slot] = i;   // vcount doubles as scratch until the list kernel
+    // vcount doubles as scratch until the list kernel: the atom's sort key, its type above its
+    // index (index alone with more than 8 types)
+    d.vcount[d.pcell_first[c] + slot] = (int)(P.T <= 8 ? ((unsigned)d.type[i] << kClassShift) | (unsigned)i : (unsigned)i);
 }
 
 // Atoms of a cell ordered by type and index (a rank pass, deterministic).  The position in the
@@ -838,18 +866,15 @@ __global__ void k_pcell_rank(DevSys d, Params P, int ncell, bool mixed) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(warp >= ncell || !rebuild_due(d, P, rep_of_cell(d, P, warp))) return;
     const int cnt = d.pcell_count[warp], first = d.pcell_first[warp];
-    const int* tmp = d.vcount;
+    const unsigned* tmp = reinterpret_cast<const unsigned*>(d.vcount);
     for(int a = lane; a < cnt; a += 32) {
-        // order within the cell: by type, then by index (deterministic); atoms of one type sit
-        // together, so the atoms a warp's force gather takes have alike rows (same split into
-        // short-range and Coulomb-only pairs, similar lengths)
-        const int v = tmp[first + a];
-        const long long kv = ((long long)d.type[v] << 32) | (unsigned)v;
+        // order within the cell: by type, then by index (the keys k_pcell_scatter wrote;
+        // deterministic); atoms of one type sit together, so the atoms a warp's force gather takes
+        // have alike rows (same split into short-range and Coulomb-only pairs, similar lengths)
+        const unsigned kv = tmp[first + a];
+        const int v = (int)(kv & kIdxMask);
         int rank = 0;
-        for(int b = 0; b < cnt; b++) {
-            const int u = tmp[first + b];
-            rank += ((((long long)d.type[u] << 32) | (unsigned)u) < kv);
-        }
+        for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < kv);
         const int slot = first + rank;
         d.pcell_list[slot] = v;
         d.slot_of[v] = slot;
