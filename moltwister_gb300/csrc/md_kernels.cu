@@ -109,17 +109,6 @@ __device__ __forceinline__ void flag_rebuild(const DevSys& d, const Params& P, c
     if(P.nrep) v.sc->rebuild = 1;
     if(d.sc->rebuild == 0) d.sc->rebuild = 1;   // a forced rebuild (-1) stays forced
 }
-// Replica of production cell c (cells are numbered replica by replica from cbase).
-__device__ __forceinline__ int rep_of_cell(const DevSys& d, const Params& P, int c) {
-    if(!P.nrep) return -1;
-    int lo = 0, hi = P.nrep - 1;
-    while(lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if(d.reps[mid].cbase <= c) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
 
 
 // Totals of one system's block partials (blocks b0 .. b0+nb-1, four doubles each), summed by the
@@ -862,25 +851,26 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
 // resulting cell order is the atom's slot: the Verlet list is kept per slot with partners named by
 // slot, and the positions the force gather reads are copied into slot order, so the partners of
 // the atoms a block works on lie in a compact, cache-resident range.
-__global__ void k_pcell_rank(DevSys d, Params P, int ncell, bool mixed) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if(warp >= ncell || !rebuild_due(d, P, rep_of_cell(d, P, warp))) return;
-    const int cnt = d.pcell_count[warp], first = d.pcell_first[warp];
+__global__ void k_pcell_rank(DevSys d, Params P, bool mixed) {
+    // one thread per position of the scratch array (positions are grouped by cell; a replica's
+    // positions are its own atom range): the rank of its key among its cell's keys is its slot
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if(t >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, t))) return;
     const unsigned* tmp = reinterpret_cast<const unsigned*>(d.vcount);
-    for(int a = lane; a < cnt; a += 32) {
-        // order within the cell: by type, then by index (the keys k_pcell_scatter wrote;
-        // deterministic); atoms of one type sit together, so the atoms a warp's force gather takes
-        // have alike rows (same split into short-range and Coulomb-only pairs, similar lengths)
-        const unsigned kv = tmp[first + a];
-        const int v = (int)(kv & kIdxMask);
-        int rank = 0;
-        for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < kv);
-        const int slot = first + rank;
-        d.pcell_list[slot] = v;
-        d.slot_of[v] = slot;
-        d.rb4s[slot] = d.rb4[v];
-        if(mixed) d.pqs[slot] = d.pq[v];
-    }
+    // order within the cell: by type, then by index (the keys k_pcell_scatter wrote;
+    // deterministic); atoms of one type sit together, so the atoms a warp's force gather takes
+    // have alike rows (same split into short-range and Coulomb-only pairs, similar lengths)
+    const unsigned kv = tmp[t];
+    const int v = (int)(kv & kIdxMask);
+    const int c = d.pcell_of[v];
+    const int cnt = d.pcell_count[c], first = d.pcell_first[c];
+    int rank = 0;
+    for(int b = 0; b < cnt; b++) rank += (tmp[first + b] < kv);
+    const int slot = first + rank;
+    d.pcell_list[slot] = v;
+    d.slot_of[v] = slot;
+    d.rb4s[slot] = d.rb4[v];
+    if(mixed) d.pqs[slot] = d.pq[v];
 }
 
 // Exclusion class of the pair (k, i) from k's bonded lists and molecule indices.
@@ -1828,7 +1818,7 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
     k_pcell_scan<<<P.nrep ? P.nrep : 1, 1024, 0, s>>>(d, P);
     k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    k_pcell_rank<<<nblk(ncell * 32, 256), 256, 0, s>>>(d, P, ncell, P.precision == MTG_PREC_MIXED);
+    k_pcell_rank<<<nblk(P.n, 256), 256, 0, s>>>(d, P, P.precision == MTG_PREC_MIXED);
     if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
     k_finish_build<<<nblk(ncell, 256), 256, 0, s>>>(d, P, ncell);
