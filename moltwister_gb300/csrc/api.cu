@@ -347,7 +347,9 @@ bool is_reference(const mtg_ctx* c) { return c->P.precision == MTG_PREC_REFERENC
 bool is_mixed(const mtg_ctx* c) { return c->P.precision == MTG_PREC_MIXED; }
 
 // Forces at the current positions, growing lists as needed.  Host-synchronous.
-int compute_forces_now(mtg_ctx* c, bool energy) {
+// keep_list: the production Verlet list is rebuilt only if an atom moved more than half the skin
+// since the last build (positions written from the host; the box unchanged), else always.
+int compute_forces_now(mtg_ctx* c, bool energy, bool keep_list = false) {
     for(int attempt = 0; attempt < 64; attempt++) {
         clear_overflow(c);
         if(is_reference(c)) {
@@ -355,7 +357,11 @@ int compute_forces_now(mtg_ctx* c, bool energy) {
             launch_ref_neigh(c->d, c->P, c->stream);
             launch_ref_force(c->d, c->P, c->stream);
         } else {
-            launch_prod_build(c->d, c->P, true, c->stream);
+            // a redo after an overflow rebuilds whatever the test said (the failed build moved the
+            // build positions)
+            const bool test = keep_list && attempt == 0;
+            if(test) launch_prod_check_list(c->d, c->P, c->stream);
+            launch_prod_build(c->d, c->P, !test, c->stream);
             launch_prod_force(c->d, c->P, energy, c->stream);
         }
         CUDA_TRY(c, cudaGetLastError());
@@ -1489,7 +1495,7 @@ int mtg_set_state(mtg_ctx* c, const double* r, const double* p, const mtg_thermo
         if(r || p) launch_prod_sync(c->d, c->P, kSyncFromMaster, c->stream);
         else if(box_changes) launch_prod_sync(c->d, c->P, kSyncPositionsFromMaster, c->stream);
     }
-    if(r || box_changes) return compute_forces_now(c, true);
+    if(r || box_changes) return compute_forces_now(c, true, !box_changes);
     return MTG_OK;
 }
 

@@ -1706,6 +1706,23 @@ __global__ void k_set_chains(DevSys d, ChainSet cs) {
     }
 }
 
+// Positions written from the host (FP64 masters; mixed mode has synced its mirrors): flags a list
+// rebuild when an atom lies more than half the skin from its position at the last build, the
+// test the kick-drift applies every step (the box does not change here).
+__global__ void k_check_list(DevSys d, Params P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= P.n) return;
+    const SysView v = sys_view(d, P, rep_of_atom(d, P, k));
+    const double h = 0.5 * double(v.skin);
+    double d2 = 0.0;
+#pragma unroll
+    for(int a = 0; a < 3; a++) {
+        const double x = minimg_d(d.r[3 * k + a] - d.r_build[3 * k + a], v.box[a], 1.0 / v.box[a]);
+        d2 += x * x;
+    }
+    if(d2 > h * h) flag_rebuild(d, P, v);
+}
+
 // End of a list build: the cell counts go back to zero for the next build (they start at zero
 // when allocated), and the last block clears the rebuild flags and counts the build.  Every block
 // passes the early-exit test before the last one clears the flag it tests.
@@ -1807,6 +1824,10 @@ void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cu
     if(P.precision == MTG_PREC_MIXED && P.ensemble == MTG_NPT) k_mkick_drift_npt<<<nb, 256, 0, s>>>(d, P, cond, u);
     else if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond, u);
     else k_pkick_drift<<<nb, 256, 0, s>>>(d, P, cond, u);
+}
+
+void launch_prod_check_list(const DevSys& d, const Params& P, cudaStream_t s) {
+    k_check_list<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
 }
 
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {

@@ -310,6 +310,7 @@ void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream
 // fractions pq; the FP64 arrays r and p are the masters the host reads and writes.
 enum SyncMode { kSyncToMaster = 0, kSyncFromMaster = 1, kSyncPositionsFromMaster = 2 };
 void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s);
+void launch_prod_check_list(const DevSys& d, const Params& P, cudaStream_t s);   // flags a rebuild if positions moved
 void launch_settle(const DevSys& d, const Params& P, cudaStream_t s);   // state after the completed step
 // Chain (and, with set_baro, barostat) state written by a kernel from its arguments, so that a
 // state write-back needs no synchronous copy.
