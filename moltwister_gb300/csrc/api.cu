@@ -618,12 +618,31 @@ int add_snap(mtg_ctx* c, const void* src, size_t bytes) {
     return MTG_OK;
 }
 
-void take_snapshot(mtg_ctx* c) {
-    for(auto& s : c->snaps) cudaMemcpyAsync(s.dst, s.src, s.bytes, cudaMemcpyDeviceToDevice, c->stream);
+// The snapshot copies as one launch (the copies of a chunk's snapshot would otherwise cost a
+// host call each before the chunk's graph can be queued); any copy that is not a whole number of
+// 8-byte words goes through cudaMemcpyAsync.
+void copy_snaps(mtg_ctx* c, bool take) {
+    CopyTable t{};
+    for(auto& s : c->snaps) {
+        void* to = take ? s.dst : (void*)s.src;
+        const void* from = take ? s.src : s.dst;
+        const bool words = s.bytes % 8 == 0 && (reinterpret_cast<uintptr_t>(to) | reinterpret_cast<uintptr_t>(from)) % 8 == 0;
+        if(!words || t.n == kCopyMax) {
+            cudaMemcpyAsync(to, from, s.bytes, cudaMemcpyDeviceToDevice, c->stream);
+            continue;
+        }
+        t.src[t.n] = static_cast<const unsigned long long*>(from);
+        t.dst[t.n] = static_cast<unsigned long long*>(to);
+        t.words[t.n] = s.bytes / 8;
+        t.n++;
+    }
+    launch_copy_table(t, c->stream);
 }
 
+void take_snapshot(mtg_ctx* c) { copy_snaps(c, true); }
+
 void restore_snapshot(mtg_ctx* c) {
-    for(auto& s : c->snaps) cudaMemcpyAsync((void*)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice, c->stream);
+    copy_snaps(c, false);
     // production NPT: the restored barostat state holds the box of an earlier list build than the
     // list in place, so the next step rebuilds it
     if(c->P.ensemble == MTG_NPT && !is_reference(c)) cudaMemsetAsync(&c->d.sc->rebuild, 0xff, sizeof(int32_t), c->stream);
@@ -1550,7 +1569,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     CUDA_TRY(c, cudaSetDevice(c->device));
     if(out_stride < 0) out_stride = 0;   // 0: no output steps
     c->stats = mtg_run_stats{};
-    const int builds0 = read_scalars(c).builds;
+    cudaMemsetAsync(&c->d.sc->builds_run, 0, sizeof(int32_t), c->stream);
     // thermostat first half-step of step 0 from the current momenta
     launch_prologue(c->d, c->P, c->stream);
     CUDA_TRY(c, cudaGetLastError());
@@ -1616,7 +1635,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
             if(s.timeout) return fail(c, MTG_E_TIMEOUT, "a bounded wait in the thermostat gave up");
             if(s.boxerr) return fail(c, MTG_E_UNSUPPORTED, "NPT: the box shrank until a cutoff reached half its width");
             if(s.nonfinite) return fail(c, MTG_E_NONFINITE, "non-finite kinetic energy or thermostat scale during the run");
-            c->stats.list_builds = s.builds - builds0;
+            c->stats.list_builds = s.builds_run;
             if(output) {
                 double rec[8];
                 int rrc = read_records(c, rec);

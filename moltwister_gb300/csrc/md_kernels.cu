@@ -1737,6 +1737,7 @@ __global__ void k_finish_build(DevSys d, Params P, int ncell) {
             d.sc->done_blocks = 0;
             d.sc->rebuild = 0;
             d.sc->builds += 1;
+            d.sc->builds_run += 1;
         }
     }
 }
@@ -1896,6 +1897,25 @@ void launch_settle(const DevSys& d, const Params& P, cudaStream_t s) {
 }
 
 void launch_set_chains(const DevSys& d, const ChainSet& cs, cudaStream_t s) { k_set_chains<<<1, 32, 0, s>>>(d, cs); }
+
+__global__ void k_copy_table(CopyTable t) {
+    // block y = copy, blocks x stride over its words
+    const int q = blockIdx.y;
+    if(q >= t.n) return;
+    const unsigned long long* src = t.src[q];
+    unsigned long long* dst = t.dst[q];
+    for(unsigned long long w = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; w < t.words[q];
+        w += (unsigned long long)gridDim.x * blockDim.x)
+        dst[w] = src[w];
+}
+
+void launch_copy_table(const CopyTable& t, cudaStream_t s) {
+    if(t.n <= 0) return;
+    unsigned long long most = 0;
+    for(int q = 0; q < t.n; q++) most = t.words[q] > most ? t.words[q] : most;
+    const int bx = (int)((most + 255) / 256 < 304 ? (most + 255) / 256 : 304);
+    k_copy_table<<<dim3(bx > 0 ? bx : 1, t.n), 256, 0, s>>>(t);
+}
 
 void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s) {
     k_sync<<<nblk(P.n, 256), 256, 0, s>>>(d, P, (int)mode);

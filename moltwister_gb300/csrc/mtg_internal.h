@@ -103,6 +103,7 @@ struct StepScalars {
     int32_t builds;       // neighbour-list rebuilds performed
     int32_t timeout;      // a bounded device wait gave up
     int32_t boxerr;       // NPT (production): the box shrank until a cutoff reached half its width
+    int32_t builds_run;   // production list builds since the start of the current run
 };
 
 struct Params {
@@ -312,6 +313,16 @@ enum SyncMode { kSyncToMaster = 0, kSyncFromMaster = 1, kSyncPositionsFromMaster
 void launch_prod_sync(const DevSys& d, const Params& P, SyncMode mode, cudaStream_t s);
 void launch_prod_check_list(const DevSys& d, const Params& P, cudaStream_t s);   // flags a rebuild if positions moved
 void launch_settle(const DevSys& d, const Params& P, cudaStream_t s);   // state after the completed step
+// Up to kCopyMax device-to-device copies (8-byte multiples at 8-byte aligned addresses) in one
+// launch: the chunk snapshot of the run loop and its rollback.
+constexpr int kCopyMax = 32;
+struct CopyTable {
+    const unsigned long long* src[kCopyMax];
+    unsigned long long* dst[kCopyMax];
+    unsigned long long words[kCopyMax];
+    int n;
+};
+void launch_copy_table(const CopyTable& t, cudaStream_t s);
 // Chain (and, with set_baro, barostat) state written by a kernel from its arguments, so that a
 // state write-back needs no synchronous copy.
 struct ChainSet {
