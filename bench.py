@@ -37,6 +37,20 @@ from moltwister_gb300.clocks import ClockSampler  # noqa: E402
 WORKLOAD = "water9000_nvt"
 METRIC = "atom-steps/s"
 CHUNK = 100
+# DRAM bytes of one force-gather launch on this workload (10 A Coulomb cutoff), from a committed
+# ncu capture that names its command
+PFORCE_DRAM_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                                "k_pforce_water9000_mixed_dram.json")
+
+
+def pforce_traffic(coulomb: str):
+    """dram__bytes_read.sum + dram__bytes_write.sum per force-gather launch (None when no capture
+    of this workload is committed)."""
+    if coulomb != "cutoff" or not os.path.exists(PFORCE_DRAM_FILE):
+        return None
+    with open(PFORCE_DRAM_FILE) as f:
+        d = json.load(f)
+    return float(d["dram__bytes_read.sum"] + d["dram__bytes_write.sum"])
 SIGMA_O, EPS_O = 3.166, 0.650
 
 
@@ -269,7 +283,9 @@ def our_arm(args):
            "device": device_name(local),
            "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d / args.steps,
                    "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s,
-                   "path": "Engine.set_state / run / get_state (C ABI), pinned host buffers, after one untimed pass"},
+                   "path": "Engine.set_state / run / get_state (C ABI), pinned host buffers, after one untimed pass; "
+                           "one run of all steps with no L2 flush (the device-timed value flushes L2 before every "
+                           f"chunk of {CHUNK} steps)"},
            "gpu_launches": int(launches),
            "list_builds": int(builds),
            "phase_ms": phases}
@@ -321,8 +337,11 @@ def our_arm(args):
                            "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                            "peak_source": f"FP32 SIMT peak {props.multi_processor_count} SM x 128 lanes x 2 x "
                                           f"{sm_max:.0f} MHz (sm_max_mhz {kind} in MEASURED_PEAKS.json)",
-                           "algorithmic_flop_per_launch": flops, "launch_ms": fms, "traffic": None,
-                           "traffic_note": "DRAM bytes per launch come from an ncu capture, not from this run"}
+                           "algorithmic_flop_per_launch": flops, "launch_ms": fms,
+                           "traffic": pforce_traffic(args.coulomb),
+                           "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one k_pforce launch "
+                                           "(step loop, no energy) of this workload, from a committed ncu "
+                                           "capture (not measured in this run): the Verlet list read once"}
         # integrator: HBM-bound per-atom kernels (kick-drift and second kick, without the step end)
         kd = phases["kick_drift"] + phases["kick_reduce"]
         out["roofline_integrator"] = {"bound": "hbm", "kernels": "k_mkick_drift + k_mkick2",
@@ -344,7 +363,7 @@ def our_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--coulomb", default="cutoff", choices=["cutoff", "shifted"])

@@ -101,6 +101,13 @@ struct mtg_ctx {
     double* pin_r[2] = {nullptr, nullptr};
     double* pin_p[2] = {nullptr, nullptr};
     cudaEvent_t ev_out[2] = {nullptr, nullptr};
+    // pinned staging of the chain and barostat state a state read returns (queued with the
+    // position and momentum copies, one synchronisation for all)
+    struct ThermoStage {
+        ThermoDev th, thp;
+        BaroDev baro;
+    };
+    ThermoStage* pin_th = nullptr;
     // batch of replicas (P.nrep > 0)
     std::vector<int> rep_off;          // nrep + 1 atom offsets
     std::vector<double> h_rep_box;     // 3 per replica
@@ -120,6 +127,7 @@ struct mtg_ctx {
             if(pin_p[b]) cudaFreeHost(pin_p[b]);
             if(ev_out[b]) cudaEventDestroy(ev_out[b]);
         }
+        if(pin_th) cudaFreeHost(pin_th);
         if(stream) cudaStreamDestroy(stream);
     }
 };
@@ -1524,16 +1532,22 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
     int rc = settle_state(c);
     if(rc) return rc;
     const size_t n3 = (size_t)c->P.n * 3;
-    if(r) {
-        if(is_mixed(c)) launch_prod_sync(c->d, c->P, kSyncToMaster, c->stream);
-        CUDA_TRY(c, cudaMemcpyAsync(r, c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    }
-    if(p) CUDA_TRY(c, cudaMemcpyAsync(p, c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if(th && c->P.nrep) return fail(c, MTG_E_INVALID, "a batch reads chain states per replica (mtg_batch_get_thermo)");
+    // settle_state has brought the FP64 masters up to date (mixed: from the double-float mirrors)
+    if(r) CUDA_TRY(c, cudaMemcpyAsync(r, c->d.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if(p) CUDA_TRY(c, cudaMemcpyAsync(p, c->d.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    const bool npt = c->P.ensemble == MTG_NPT;
     if(th) {
-        ThermoDev t{};
-        CUDA_TRY(c, copy_now(c, &t, c->d.th, sizeof(t), cudaMemcpyDeviceToHost));
+        if(!c->pin_th) CUDA_TRY(c, cudaMallocHost((void**)&c->pin_th, sizeof(mtg_ctx::ThermoStage)));
+        CUDA_TRY(c, cudaMemcpyAsync(&c->pin_th->th, c->d.th, sizeof(ThermoDev), cudaMemcpyDeviceToHost, c->stream));
+        if(npt) {
+            CUDA_TRY(c, cudaMemcpyAsync(&c->pin_th->thp, c->d.thp, sizeof(ThermoDev), cudaMemcpyDeviceToHost, c->stream));
+            CUDA_TRY(c, cudaMemcpyAsync(&c->pin_th->baro, c->d.baro, sizeof(BaroDev), cudaMemcpyDeviceToHost, c->stream));
+        }
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if(th) {
+        const ThermoDev& t = c->pin_th->th;
         std::memset(th, 0, sizeof(*th));
         th->M = c->P.M;
         for(int j = 0; j < c->P.M; j++) {
@@ -1541,11 +1555,9 @@ int mtg_get_state(mtg_ctx* c, double* r, double* p, mtg_thermo_state* th) {
             th->p_eta[j] = t.peta[j];
         }
         for(int a = 0; a < 3; a++) th->box[a] = c->P.box[a];
-        if(c->P.ensemble == MTG_NPT) {
-            ThermoDev tp{};
-            BaroDev b{};
-            CUDA_TRY(c, copy_now(c, &tp, c->d.thp, sizeof(tp), cudaMemcpyDeviceToHost));
-            CUDA_TRY(c, copy_now(c, &b, c->d.baro, sizeof(b), cudaMemcpyDeviceToHost));
+        if(npt) {
+            const ThermoDev& tp = c->pin_th->thp;
+            const BaroDev& b = c->pin_th->baro;
             th->MP = c->P.MP;
             for(int j = 0; j < c->P.MP; j++) {
                 th->etaP[j] = tp.eta[j];
