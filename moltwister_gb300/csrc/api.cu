@@ -306,11 +306,15 @@ int upload_pair_cuts(mtg_ctx* c, int full_a, int full_b) {
 }
 
 // 1 when the production kernels have Coulomb work: a cutoff mode and some nonzero charge.
-int charges_on(const mtg_ctx* c) {
-    if(c->P.coulomb == MTG_COULOMB_ALLPAIRS) return 0;
+int any_charge(const mtg_ctx* c) {
     for(double q : c->h_charge)
         if(q != 0.0) return 1;
     return 0;
+}
+
+int charges_on(const mtg_ctx* c) {
+    if(c->P.coulomb == MTG_COULOMB_ALLPAIRS) return 0;
+    return any_charge(c);
 }
 
 // Verlet list capacity per slot: a multiple of 32 (rows start on 128-byte boundaries), with 25 %
@@ -1238,6 +1242,7 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
             const std::vector<float> pcut = pair_cuts(c.get(), -1, -1);
             rc = rc || upload(C, &f, pcut.data(), pcut.size()); d.pair_cut = f;
             P.qon = charges_on(c.get());
+            P.qany = any_charge(c.get());
         }
         // angle parameters on the device: (k, theta0 in radians, toRad, 0)
         for(size_t t = 0; t < akind.size(); t++) apar[4 * t + 1] = apar[4 * t + 1] * apar[4 * t + 2];
@@ -2232,6 +2237,11 @@ int push_params(mtg_ctx* c) {
     if((uniform ? 1 : 0) != c->P.qtype) {
         c->P.qtype = uniform ? 1 : 0;
         c->generation++;   // captured graphs hold the old flag
+    }
+    const int qany = any_charge(c);
+    if(qany != c->P.qany) {
+        c->P.qany = qany;
+        c->generation++;
     }
     const int qon = charges_on(c);
     if(qon != c->P.qon) {

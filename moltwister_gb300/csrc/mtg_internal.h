@@ -128,6 +128,7 @@ struct Params {
     double fconv[3];      // 2^32 / L
     int qtype;            // 1: charges are a function of the type (qtype table)
     int qon;              // 1: cutoff Coulomb with some charge nonzero (production); 0: no Coulomb work
+    int qany;             // 1: some charge nonzero (reference precision: the all-pairs Coulomb kernel runs)
     int lj_shift;         // 0 truncated LJ, 1 energy shifted at the cutoff, 2 force shifted
     int nrep;             // 0: one system; > 0: a batch of nrep replicas (RepDev table)
     int ncell_total;      // batch: production cells of all replicas

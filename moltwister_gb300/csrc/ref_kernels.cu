@@ -351,39 +351,213 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
 // ---------------------------------------------------------------------------------------------
 // Per-atom force/energy gather, table mode (CFunctorCalcForce::operator())
 // ---------------------------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------------
+// Exact FP64 results with little FP64 work, for the all-pairs Coulomb loop.  On this GPU an FP64
+// instruction occupies the FP64 pipe for a whole warp, and that pipe bounds the loop.  The pair's
+// float distance R and its FP64 quotient K / R^3 are therefore reached with FP32 and integer
+// instructions, bit-identical to the reference's FP64 arithmetic: each result is decided with a
+// margin far above the error of its FP32 evaluation, and the rare operands too close to a
+// rounding boundary (or outside the ranges the argument covers) take the FP64 operations.
+// ---------------------------------------------------------------------------------------------
+
+// The FP64 operations themselves.  Not inlined: a call is a branch that warps skip when no lane
+// needs it, where inlined code could be predicated and would then occupy the FP64 pipe on every
+// pass.
+__device__ __noinline__ float dist_fp64(double x, double y, double z) { return (float)sqrt(x * x + y * y + z * z); }
+__device__ __noinline__ double quot_fp64(float K, float R) { return (double)K / (double)R; }
+
+// x = hi + lo with hi the float of x's leading 24 bits (exact) and lo the float of the remaining
+// 29 (rounded); false when x is neither zero nor in [2^-60, 2^60].
+__device__ __forceinline__ bool split_df(double x, float& hi, float& lo) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if((b & 0x7fffffffffffffffLL) == 0) {
+        hi = lo = 0.0f;
+        return true;
+    }
+    if(ex < 1023 - 60 || ex > 1023 + 60) return false;
+    const uint32_t sgn = (uint32_t)((unsigned long long)b >> 63) << 31;
+    hi = __uint_as_float(sgn | ((uint32_t)(ex - 1023 + 127) << 23) | (uint32_t)((b >> 29) & 0x7fffff));
+    const float l = __fmul_rn(__uint2float_rn((uint32_t)(b & 0x1fffffff)), __uint_as_float((uint32_t)(ex - 1075 + 127) << 23));
+    lo = __uint_as_float(__float_as_uint(l) | sgn);
+    return true;
+}
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& t) {
+    const float ss = __fadd_rn(a, b), bb = __fsub_rn(ss, a);
+    s = ss;
+    t = __fadd_rn(__fsub_rn(a, __fsub_rn(ss, bb)), __fsub_rn(b, bb));
+}
+
+// R = (float)sqrt(x*x + y*y + z*z) as the reference evaluates it in FP64 (its norm, then the
+// conversion), bit for bit.  S = x^2 + y^2 + z^2 is formed as a float pair Sh + Sl from the
+// components' hi/lo splits (hi^2 exactly by fma, the cross and lo terms in FP32) to about 2^-44
+// relative, which covers the reference's own FP64 roundings of S (about 2^-52).  For the candidate
+// a = RN(sqrt(Sh)) the residual S - a^2 = fma(-a, a, Sh) + Sl places sqrt(S) against a's rounding
+// interval (a - D/2, a + U/2), D and U the float spacings below and above a: in residual terms
+// -(a D - D^2/4) < S - a^2 < a U + U^2/4.  A residual inside by a relative margin of 2^-12 decides
+// R = a; one step to a neighbouring float is decided the same way; the rest (including any S
+// within 2^-52 of a midpoint square, where the FP64 rounding of the root could land on the
+// midpoint) takes the FP64 evaluation.
+__device__ __forceinline__ float dist_to_float(double x, double y, double z) {
+    float xh, xl, yh, yl, zh, zl;
+    if(!split_df(x, xh, xl) || !split_df(y, yh, yl) || !split_df(z, zh, zl)) return dist_fp64(x, y, z);
+    const float px = __fmul_rn(xh, xh), ex = __fmaf_rn(xh, xh, -px);
+    const float py = __fmul_rn(yh, yh), ey = __fmaf_rn(yh, yh, -py);
+    const float pz = __fmul_rn(zh, zh), ez = __fmaf_rn(zh, zh, -pz);
+    float s1, t1, s2, t2;
+    two_sum_f(px, py, s1, t1);
+    two_sum_f(s1, pz, s2, t2);
+    const float cross = __fadd_rn(__fadd_rn(__fmul_rn(xh, xl), __fmul_rn(yh, yl)), __fmul_rn(zh, zl));
+    const float low = __fadd_rn(__fadd_rn(__fmul_rn(xl, xl), __fmul_rn(yl, yl)), __fmul_rn(zl, zl));
+    const float c = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), __fadd_rn(__fadd_rn(ex, ey), ez)),
+                                        __fmul_rn(2.0f, cross)), low);
+    const float Sh = __fadd_rn(s2, c), Sl = __fsub_rn(c, __fsub_rn(Sh, s2));
+    if(!(Sh >= 0x1p-100f)) {
+        if(x == 0.0 && y == 0.0 && z == 0.0) return 0.0f;
+        return dist_fp64(x, y, z);
+    }
+    const float lo = 1.0f - 0x1p-12f, hi = 1.0f + 0x1p-12f;
+    const float a = __fsqrt_rn(Sh);
+    const float Er = __fadd_rn(__fmaf_rn(-a, a, Sh), Sl);
+    const uint32_t ab = __float_as_uint(a);
+    const float U = __uint_as_float((ab & 0x7f800000u) - (23u << 23));
+    const float D = ((ab & 0x7fffffu) == 0) ? 0.5f * U : U;
+    const float tu = __fmul_rn(a, U), td = __fmul_rn(a, D);
+    if(Er < tu * lo && Er > -td * lo) return a;
+    if(Er > tu * hi || Er < -td * hi) {
+        const bool up = Er > 0.0f;
+        const float a1 = __uint_as_float(up ? ab + 1u : ab - 1u);
+        const uint32_t b1 = __float_as_uint(a1);
+        const float U1 = __uint_as_float((b1 & 0x7f800000u) - (23u << 23));
+        const float D1 = ((b1 & 0x7fffffu) == 0) ? 0.5f * U1 : U1;
+        const float Er1 = up ? __fsub_rn(Er, 2.0f * tu) : __fadd_rn(Er, 2.0f * td);   // S - a1^2, up to U^2 or D^2
+        if(Er1 < __fmul_rn(a1, U1) * lo && Er1 > -__fmul_rn(a1, D1) * lo) return a1;
+    }
+    return dist_fp64(x, y, z);
+}
+
+// (double)K / (double)R3 for floats, the correctly rounded FP64 quotient, bit for bit.  On |K|:
+// q1 = RN(K / R3) and q2 = RN(r1 / R3) are correctly rounded FP32 quotients, so the remainders
+// r1 = K - R3 q1 and r2 = r1 - R3 q2 are exact as fused multiply-adds (with the operand ranges
+// below none of them underflows), and q3 = r2 (1 / R3) has relative error <= 2^-23.  The sum
+// q1 + q2 + q3 is assembled in a 128-bit integer with 72 bits below q1's last bit, where the
+// truncations and q3's error stay below 8 units; rounded to 53 bits it is the FP64 quotient unless
+// its rounding bits lie within 16 units of the half-way point, which then takes the FP64 division.
+// (A quotient of two floats is never an FP64 midpoint, so no tie arises.)
+__device__ __forceinline__ double quot_ff(float K, float R) {
+    const uint32_t kb = __float_as_uint(K), rb = __float_as_uint(R);
+    const int ke = (int)((kb >> 23) & 0xff), re = (int)((rb >> 23) & 0xff);
+    if(ke < 127 - 60 || ke > 127 + 60 || re < 127 - 60 || re > 127 + 60 || ke - re < -40 || ke - re > 40 || (rb >> 31))
+        return quot_fp64(K, R);
+    const float Ka = __uint_as_float(kb & 0x7fffffffu);
+    const float q1 = __fdiv_rn(Ka, R);
+    const float r1 = __fmaf_rn(-R, q1, Ka);
+    const float q2 = __fdiv_rn(r1, R);
+    const float r2 = __fmaf_rn(-R, q2, r1);
+    const float q3 = __fmul_rn(r2, __frcp_rn(R));
+    const uint32_t b1 = __float_as_uint(q1);
+    const int e1 = (int)(b1 >> 23);
+    unsigned __int128 V = (unsigned __int128)((b1 & 0x7fffffu) | 0x800000u) << 72;
+#pragma unroll
+    for(int i = 0; i < 2; i++) {
+        const uint32_t bf = __float_as_uint(i == 0 ? q2 : q3);
+        if((bf & 0x7fffffffu) == 0) continue;
+        const int ef = (int)((bf >> 23) & 0xff);
+        const unsigned __int128 M = (unsigned __int128)((bf & 0x7fffffu) | 0x800000u);
+        const int sh = ef - e1 + 72;
+        const unsigned __int128 c = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> (-sh)) : (unsigned __int128)0);
+        if(bf >> 31) V -= c;
+        else V += c;
+    }
+    if(!(V >> 94)) return quot_fp64(K, R);
+    const int msb = (V >> 95) ? 95 : 94;
+    const int drop = msb - 52;
+    unsigned long long sig = (unsigned long long)(V >> drop);
+    const unsigned __int128 rem = V & (((unsigned __int128)1 << drop) - 1);
+    const unsigned __int128 half = (unsigned __int128)1 << (drop - 1);
+    if(rem + 16 >= half && rem <= half + 16) return quot_fp64(K, R);
+    if(rem > half) sig++;
+    const unsigned long long bits = ((unsigned long long)(msb + e1 - 222 + 1023) << 52) + sig - (1ULL << 52);
+    return __longlong_as_double((long long)(bits | ((unsigned long long)(kb >> 31) << 63)));
+}
+
+// Box widths of the minimum image: w, -w, w/2 (bits, and rounded to float) per axis.  Kept in
+// shared memory by the Coulomb kernel, so that the loop reads them instead of recomputing them
+// with FP64 operations when registers run short.
+struct BoxImage {
+    double w[3], nw[3];
+    long long hw[3];
+    float hwf[3];
+};
+
+// x truncated to a float (relative error < 2^-23; |x| < 2^-126 gives 0, larger than the float
+// range or NaN gives NaN, on which every comparison below is false).
+__device__ __forceinline__ float trunc_f(double x) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    const uint32_t sgn = (uint32_t)((unsigned long long)b >> 63) << 31;
+    if(ex <= 0) return __uint_as_float(sgn);
+    if(ex >= 255) return __uint_as_float(sgn | 0x7fc00000u);
+    return __uint_as_float(sgn | ((uint32_t)ex << 23) | (uint32_t)((b >> 29) & 0x7fffff));
+}
+
+// The image shift of moveToSameSideOfPBCAsThis from the FP64 test itself: |c - v| > w/2 compared
+// as bit patterns, the direction from the sign of c - v.
+__device__ __noinline__ double image_shift_fp64(double c, double v, const BoxImage& bx, int a) {
+    const long long db = __double_as_longlong(c - v);
+    if((db & 0x7fffffffffffffffLL) > bx.hw[a]) return (db >= 0) ? bx.w[a] : bx.nw[a];
+    return -0.0;
+}
+
+// One axis of moveToSameSideOfPBCAsThis (Utilities/3DVector.cpp:133-165) followed by the
+// separation c - v.  The test |c - v| > w/2 runs on the float truncations cf, vf: their
+// difference is within 1.5 2^-23 (|cf| + |vf|) of c - v, so a margin of 2^-20 (|cf| + |vf| + w/2)
+// decides it, and only separations within the margin of w/2 take the FP64 test.  The shift is
+// then one FP64 addition for every lane: v + (-0.0) is v for every v, signed zeros included.
+__device__ __forceinline__ double image_sep(double c, double v, float cf, float vf, const BoxImage& bx, int a) {
+    const float d = fabsf(__fsub_rn(cf, vf));
+    const float m = __fmul_rn(0x1p-20f, __fadd_rn(__fadd_rn(fabsf(cf), fabsf(vf)), bx.hwf[a]));
+    double ws;
+    if(d > __fadd_rn(bx.hwf[a], m)) ws = (cf > vf) ? bx.w[a] : bx.nw[a];
+    else if(d < __fsub_rn(bx.hwf[a], m)) ws = -0.0;
+    else ws = image_shift_fp64(c, v, bx, a);
+    return c - (v + ws);
+}
+
+// The exclusion scaling of a pair's force (rare: bonded partners and same-molecule pairs), out of
+// line for the same reason as the FP64 fallbacks above.
+__device__ __noinline__ D3 scale_fp64(D3 f, float sc) { return scl(f, (double)sc); }
+
 // Coulomb term of the pair (k, i) (FunctorCalcForce.cpp:258-278, 514-535) in the reference's
 // arithmetic: float R from the FP64 minimum-image separation, FP64 K / R^3, the pair energy on
 // the lower index, the exclusion scaling.
 __device__ __forceinline__ void coulomb_pair(const DevSys& d, const Params& P, int k, int i, const D3& rk, D3 ri,
-                                             float qk, float qi, int molk, int moli, bool local, const double* w,
-                                             D3& f, float& u) {
+                                             const float* rkf, const float* rif, float qk, float qi, int molk,
+                                             int moli, bool local, const BoxImage& bx, D3& f, float& u) {
     u = 0.0f;
-    same_side(rk, ri, w);
-    const D3 rv = sub(rk, ri);
-    const float R = (float)nrm(rv);
-    const double R3 = double(R * R * R);
-    const double K = double(kCoulombKf * qk * qi);
-    if((i > k) && (R != 0.0f)) u += float(K) / R;
-    f = (R3 != 0.0) ? scl(rv, K / R3) : d3(0, 0, 0);
+    const D3 rv = d3(image_sep(rk.x, ri.x, rkf[0], rif[0], bx, 0), image_sep(rk.y, ri.y, rkf[1], rif[1], bx, 1),
+                     image_sep(rk.z, ri.z, rkf[2], rif[2], bx, 2));
+    const float R = dist_to_float(rv.x, rv.y, rv.z);
+    const float R3 = R * R * R;
+    const float K = kCoulombKf * qk * qi;
+    if((i > k) && (R != 0.0f)) u += K / R;
+    f = (R3 != 0.0f) ? scl(rv, quot_ff(K, R3)) : d3(0, 0, 0);
     // pairs of different molecules have no exclusion when none of k's partners lies outside its
     // molecule; otherwise the reference's search
     float sc;
     if(!(local && moli != molk) && exclusion(d, P, k, i, sc)) {
-        f = scl(f, (double)sc);
+        f = scale_fp64(f, sc);
         u *= sc;
     }
 }
 
-constexpr int kRefTile = 128;   // atoms per shared-memory tile of the all-pairs Coulomb loop
+constexpr int kRefTile = 64;    // threads per block of the bonded and short-range gather (spread over every SM)
 
-// One thread per atom (the per-atom sum runs in the reference's order, i = 0 .. N-1); the block's
-// threads stage each tile of positions, charges and molecule indices in shared memory.  A pair
-// whose charge product K is zero adds exactly +-0 to every sum and is skipped (the whole loop when
-// the atom's own charge is zero), which leaves every sum bit-identical.
+// Bonded and short-range terms, one thread per atom, each sum in the reference's order (bonds,
+// angles, dihedrals, then the neighbour list).  The sums are stored in F and U; the all-pairs
+// Coulomb kernel continues them.
 __global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
-    __shared__ double tx[kRefTile], ty[kRefTile], tz[kRefTile];
-    __shared__ float tq[kRefTile];
-    __shared__ int tm[kRefTile];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const float Lf[3] = {box_f(d, P, 0), box_f(d, P, 1), box_f(d, P, 2)};
     const double w[3] = {double(Lf[0]) / 2.0 - (-double(Lf[0]) / 2.0), double(Lf[1]) / 2.0 - (-double(Lf[1]) / 2.0),
@@ -512,57 +686,155 @@ __global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
             Uk += u;
         }
     }
-    // Coulomb over all atoms, minimum image, no cutoff (FunctorCalcForce.cpp:258-278, 514-535)
-    const float qk = live ? d.qf[k] : 0.0f;
-    const int molk = live ? d.mol[k] : -1;
-    const bool local = live && d.excl_local[k] != 0;
-    if(__syncthreads_or(qk != 0.0f)) {
-        for(int base = 0; base < P.n; base += kRefTile) {
-            __syncthreads();
-            const int j = base + (int)threadIdx.x;
-            if(j < P.n) {
-                tx[threadIdx.x] = d.r[3 * j];
-                ty[threadIdx.x] = d.r[3 * j + 1];
-                tz[threadIdx.x] = d.r[3 * j + 2];
-                tq[threadIdx.x] = d.qf[j];
-                tm[threadIdx.x] = d.mol[j];
-            }
-            __syncthreads();
-            if(qk == 0.0f) continue;
-            const int m = min(kRefTile, P.n - base);
-            int t = 0;
-            // two pairs in flight: their terms are independent; they are added in order
-            for(; t + 1 < m; t += 2) {
-                const bool z0 = (kCoulombKf * qk * tq[t]) == 0.0f, z1 = (kCoulombKf * qk * tq[t + 1]) == 0.0f;
-                D3 f0 = d3(0, 0, 0), f1 = d3(0, 0, 0);
-                float u0 = 0.0f, u1 = 0.0f;
-                if(!z0) coulomb_pair(d, P, k, base + t, rk, d3(tx[t], ty[t], tz[t]), qk, tq[t], molk, tm[t], local, w, f0, u0);
-                if(!z1)
-                    coulomb_pair(d, P, k, base + t + 1, rk, d3(tx[t + 1], ty[t + 1], tz[t + 1]), qk, tq[t + 1], molk, tm[t + 1],
-                                 local, w, f1, u1);
-                if(!z0) {
-                    Fx += f0.x; Fy += f0.y; Fz += f0.z;
-                    Uk += u0;
-                }
-                if(!z1) {
-                    Fx += f1.x; Fy += f1.y; Fz += f1.z;
-                    Uk += u1;
-                }
-            }
-            if(t < m && (kCoulombKf * qk * tq[t]) != 0.0f) {
-                D3 f0;
-                float u0;
-                coulomb_pair(d, P, k, base + t, rk, d3(tx[t], ty[t], tz[t]), qk, tq[t], molk, tm[t], local, w, f0, u0);
-                Fx += f0.x; Fy += f0.y; Fz += f0.z;
-                Uk += u0;
-            }
-        }
-    }
     if(!act) return;
     d.F[3 * k] = Fx;
     d.F[3 * k + 1] = Fy;
     d.F[3 * k + 2] = Fz;
     d.U[k] = live ? (double)Uk : 0.0;
+}
+
+// All-pairs Coulomb, minimum image, no cutoff (FunctorCalcForce.cpp:258-278, 514-535), continuing
+// each atom's sums after its bonded and short-range terms.
+//
+// A block owns 32 atoms.  Its first kCoulW warps compute the pair terms of those atoms (lane =
+// atom) against a tile of kCoulJ positions, two positions per warp, and park them in shared
+// memory; the last warp adds the parked terms of the previous tile to the atoms' sums in
+// ascending j.  Every sum therefore keeps the reference's order i = 0 .. N-1 while the FP64 pair
+// arithmetic, the cost of this kernel (on this GPU an FP64 instruction occupies its pipe for the
+// whole warp), is spread over nine warps per 32 atoms and over every SM.  A pair whose charge
+// product K is zero adds exactly +-0 to every sum and is skipped (all pairs of an atom whose own
+// charge is zero), as the reference's arithmetic leaves those sums unchanged.
+constexpr int kCoulI = 32;               // atoms per block
+constexpr int kCoulJ = 16;               // positions per tile
+constexpr int kCoulW = 8;                // pair warps (kCoulJ / kCoulW positions each per tile)
+constexpr int kCoulThreads = 32 * (kCoulW + 1);
+
+__global__ void __launch_bounds__(kCoulThreads) k_coulomb_allpairs(DevSys d, Params P) {
+    __shared__ double jx[2][kCoulJ], jy[2][kCoulJ], jz[2][kCoulJ];
+    __shared__ float jf[2][kCoulJ][3];    // float truncations of the positions (image test)
+    __shared__ float jq[2][kCoulJ];
+    __shared__ int jm[2][kCoulJ];
+    __shared__ double tfx[2][kCoulJ][kCoulI], tfy[2][kCoulJ][kCoulI], tfz[2][kCoulJ][kCoulI];
+    __shared__ float tu[2][kCoulJ][kCoulI];
+    __shared__ unsigned ton[2][kCoulJ];   // bit a: the term of (atom a, position jj) is added
+    if(d.sc->overflow) return;            // the step is redone after the neighbour list grows
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = P.n;
+    const int k = blockIdx.x * kCoulI + lane;
+    const bool live = k < n && d.mobile[k];
+    const float qk = live ? d.qf[k] : 0.0f;
+    if(!__syncthreads_or(qk != 0.0f)) return;
+    const bool mine = qk != 0.0f;
+    __shared__ BoxImage bx;
+    if(threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        const float Lf = box_f(d, P, a);
+        const double w = double(Lf) / 2.0 - (-double(Lf) / 2.0);
+        bx.w[a] = w;
+        bx.nw[a] = -w;
+        bx.hw[a] = __double_as_longlong(w / 2.0);
+        bx.hwf[a] = __double2float_rn(w / 2.0);
+    }
+    const int ntile = (n + kCoulJ - 1) / kCoulJ;
+    auto fetch = [&](int t, double& x, double& y, double& z, float& q, int& m) {
+        const int j = t * kCoulJ + (int)threadIdx.x;
+        if(j < n) {
+            x = d.r[3 * j];
+            y = d.r[3 * j + 1];
+            z = d.r[3 * j + 2];
+            q = d.qf[j];
+            m = d.mol[j];
+        }
+    };
+    auto park = [&](int b, double x, double y, double z, float q, int m) {
+        jx[b][threadIdx.x] = x;
+        jy[b][threadIdx.x] = y;
+        jz[b][threadIdx.x] = z;
+        jf[b][threadIdx.x][0] = trunc_f(x);
+        jf[b][threadIdx.x][1] = trunc_f(y);
+        jf[b][threadIdx.x][2] = trunc_f(z);
+        jq[b][threadIdx.x] = q;
+        jm[b][threadIdx.x] = m;
+    };
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    float sq = 0.0f;
+    int sm = -1;
+    if(threadIdx.x < kCoulJ) {
+        fetch(0, sx, sy, sz, sq, sm);
+        park(0, sx, sy, sz, sq, sm);
+    }
+    if(warp < kCoulW) {
+        // ---------------- pair warps ----------------
+        const D3 rk = mine ? load3(d.r, k) : d3(0, 0, 0);
+        const float rkf[3] = {trunc_f(rk.x), trunc_f(rk.y), trunc_f(rk.z)};
+        const int molk = mine ? d.mol[k] : -1;
+        const bool local = mine && d.excl_local[k] != 0;
+        __syncthreads();
+        for(int t = 0; t < ntile; t++) {
+            const int b = t & 1;
+            const bool stage = threadIdx.x < kCoulJ && t + 1 < ntile;
+            if(stage) fetch(t + 1, sx, sy, sz, sq, sm);
+#pragma unroll
+            for(int h = 0; h < kCoulJ / kCoulW; h++) {
+                const int jj = warp + h * kCoulW;
+                const int j = t * kCoulJ + jj;
+                bool on = false;
+                D3 f = d3(0, 0, 0);
+                float u = 0.0f;
+                if(mine && j < n) {
+                    const float qj = jq[b][jj];
+                    if((kCoulombKf * qk * qj) != 0.0f) {
+                        coulomb_pair(d, P, k, j, rk, d3(jx[b][jj], jy[b][jj], jz[b][jj]), rkf, jf[b][jj], qk, qj, molk,
+                                     jm[b][jj], local, bx, f, u);
+                        on = true;
+                    }
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, on);
+                if(on) {
+                    tfx[b][jj][lane] = f.x;
+                    tfy[b][jj][lane] = f.y;
+                    tfz[b][jj][lane] = f.z;
+                    tu[b][jj][lane] = u;
+                }
+                if(lane == 0) ton[b][jj] = m;
+            }
+            if(stage) park(b ^ 1, sx, sy, sz, sq, sm);
+            __syncthreads();
+        }
+        __syncthreads();   // the summing warp's last tile
+    } else {
+        // ---------------- summing warp: one tile behind ----------------
+        double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+        float Uk = 0.0f;
+        if(mine) {
+            Fx = d.F[3 * k];
+            Fy = d.F[3 * k + 1];
+            Fz = d.F[3 * k + 2];
+            Uk = (float)d.U[k];   // stored as double from a float: exact
+        }
+        __syncthreads();
+        for(int t = 0; t <= ntile; t++) {
+            if(t > 0) {
+                const int b = (t - 1) & 1;
+                const int m = min(kCoulJ, n - (t - 1) * kCoulJ);
+                for(int jj = 0; jj < m; jj++) {
+                    if((ton[b][jj] >> lane) & 1u) {
+                        Fx += tfx[b][jj][lane];
+                        Fy += tfy[b][jj][lane];
+                        Fz += tfz[b][jj][lane];
+                        Uk += tu[b][jj][lane];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if(mine) {
+            d.F[3 * k] = Fx;
+            d.F[3 * k + 1] = Fy;
+            d.F[3 * k + 2] = Fz;
+            d.U[k] = (double)Uk;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -730,6 +1002,7 @@ void launch_ref_neigh(const DevSys& d, const Params& P, cudaStream_t s) {
 
 void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s) {
     k_force<<<nblk(P.n, kRefTile), kRefTile, 0, s>>>(d, P);
+    if(P.qany) k_coulomb_allpairs<<<nblk(P.n, kCoulI), kCoulThreads, 0, s>>>(d, P);
 }
 
 void launch_ref_kick_drift(const DevSys& d, const Params& P, cudaStream_t s) {

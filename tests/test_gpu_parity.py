@@ -72,6 +72,31 @@ def test_reference_forces(name):
     assert np.allclose(U, d["U"].astype(np.float64), rtol=1e-5, atol=1e-5 * np.abs(d["U"]).max())
 
 
+@pytest.mark.parametrize("n_mol", [216, 1000])
+def test_reference_coulomb_bit_exact(n_mol):
+    """Charged water with its angle terms taken out (no acos on any path) and every eleventh atom
+    held fixed: reference-mode forces and per-atom energies equal the oracle's reference-order
+    restatement bit for bit.  This pins the order of each atom's sum (bonds, then short-range
+    pairs in neighbour-list order, then the all-pairs Coulomb terms in ascending j,
+    FunctorCalcForce.cpp:159-281, including the tail tiles of 648 atoms) and the FP64 square
+    root, division and minimum image of every one of the 0.4 and 9 million pairs."""
+    from moltwister_gb300 import workloads as W
+    from oracle import oracle as O
+    s, cfg = W.water(n_mol=n_mol, L=W.water_box_length(n_mol), seed=14, rc=6.0)
+    s.angles = np.zeros((0, 4), np.int32)
+    s.angle_terms = []
+    s.mobile[5::11] = False
+    assert cfg.precision == "reference" and cfg.coulomb == "allpairs"
+    orc = O.Oracle(s, cfg)
+    t = orc.tabs
+    e = engine(s, cfg, tables={"nb": t["nb"], "bond": t["bond"], "angle": t["angle"], "dih": t["dih"]})
+    F, U = e.forces()
+    Fo, Uo = orc.forces_ref()
+    assert np.abs(F).max() > 0 and np.abs(Uo).max() > 0
+    assert np.array_equal(F, Fo), np.abs(F - Fo).max()
+    assert np.array_equal(U, Uo.astype(np.float64)), np.abs(U - Uo).max()
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_reference_trajectory(name):
     s, cfg, d = G.load(name)
