@@ -69,6 +69,7 @@ struct mtg_ctx {
     // buffers
     std::vector<void*> bufs;         // owned device allocations
     void* nbr_buf = nullptr;         // reference neighbour list (growable)
+    void* nbr_nb_buf = nullptr;      // its entries with a non-bonded term (same capacity)
     void* vlist_buf = nullptr;       // production list (growable)
     // snapshot for chunk rollback
     struct Snap {
@@ -119,6 +120,7 @@ struct mtg_ctx {
         for(void* p : bufs) cudaFree(p);
         for(void* p : snap_bufs) cudaFree(p);
         if(nbr_buf) cudaFree(nbr_buf);
+        if(nbr_nb_buf) cudaFree(nbr_nb_buf);
         if(vlist_buf) cudaFree(vlist_buf);
         if(ev0) cudaEventDestroy(ev0);
         if(ev1) cudaEventDestroy(ev1);
@@ -264,12 +266,18 @@ int ref_cells(double L, double rc, double shell) {
 int grow_neighbors(mtg_ctx* c, int needed) {
     const int cap = needed + 10;     // the reference grows to need + 10 (MDFFMatrices.cpp:172-176)
     if(c->nbr_buf) cudaFree(c->nbr_buf);
-    c->nbr_buf = nullptr;
-    void* p;
+    if(c->nbr_nb_buf) cudaFree(c->nbr_nb_buf);
+    c->nbr_buf = c->nbr_nb_buf = nullptr;
+    c->d.nbr_list = c->d.nbr_list_nb = nullptr;
+    void *p, *q;
     cudaError_t e = cudaMalloc(&p, (size_t)c->P.n * cap * sizeof(int));
     if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, "neighbour list allocation failed");
     c->nbr_buf = p;
+    e = cudaMalloc(&q, (size_t)c->P.n * cap * sizeof(int));
+    if(e != cudaSuccess) return fail(c, MTG_E_NOMEM, "neighbour list allocation failed");
+    c->nbr_nb_buf = q;
     c->d.nbr_list = (int*)p;
+    c->d.nbr_list_nb = (int*)q;
     c->d.nbr_max = cap;
     c->generation++;
     return MTG_OK;
@@ -1288,6 +1296,15 @@ static int create_impl(const mtg_system_desc* sys, const mtg_config_desc* cfg, c
         rc = rc || dalloc(C, &d.cell_cursor, (size_t)c->ncell_ref);
         rc = rc || dalloc(C, &d.cell_list, (size_t)n);
         rc = rc || dalloc(C, &d.nbr_count, (size_t)n);
+        rc = rc || dalloc(C, &d.nbr_count_nb, (size_t)n);
+        {
+            // the reference-precision gather takes atoms grouped by type, so that the lanes of a
+            // warp meet the same non-bonded terms (each atom's sums keep their own order)
+            std::vector<int> order(n);
+            for(int i = 0; i < n; i++) order[i] = i;
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return type[a] < type[b]; });
+            rc = rc || upload(C, &d.force_order, order.data(), order.size());
+        }
         rc = rc || dalloc(C, &d.pcell_of, (size_t)n);
         rc = rc || dalloc(C, &d.pcell_first, (size_t)c->ncell_prod);
         rc = rc || dalloc(C, &d.pcell_count, (size_t)c->ncell_prod);

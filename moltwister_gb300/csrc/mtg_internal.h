@@ -231,6 +231,9 @@ struct DevSys {
     int* nbr_count;       // [n]
     int* nbr_list;        // [n * nbr_max]
     int nbr_max;
+    int* nbr_count_nb;    // [n]  how many entries of nbr_list have a non-bonded term (null: not kept)
+    int* nbr_list_nb;     // [n * nbr_max] those entries, in list order
+    int* force_order;     // [n]  atoms by (type, index): the reference-precision gather's thread order
     // production (Verlet) list
     int* pcell_of;        // [n] production cell of each atom
     int* pcell_first;     // [pncell]

@@ -293,6 +293,12 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
     const int cx = d.atom_cell[3 * k], cy = d.atom_cell[3 * k + 1], cz = d.atom_cell[3 * k + 2];
     int c = 0;
     int* out = d.nbr_list + (size_t)k * d.nbr_max;
+    // the entries whose type pair has a non-bonded term, in list order, for the force gather (the
+    // others add exactly zero there)
+    const bool keep_nb = d.nbr_list_nb != nullptr;
+    int c_nb = 0;
+    int* out_nb = keep_nb ? d.nbr_list_nb + (size_t)k * d.nbr_max : nullptr;
+    const int* cnt_row = keep_nb ? d.nb_cnt + d.type[k] * P.T : nullptr;
     for(int ix = cx - 1; ix <= cx + 1; ix++) {
         const int Ix = (ix >= 0) ? ((ix < Nx) ? ix : 0) : Nx - 1;
         for(int iy = cy - 1; iy <= cy + 1; iy++) {
@@ -335,12 +341,22 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
                         if(slot < d.nbr_max) out[slot] = j;
                     }
                     c += __popc(ball);
+                    if(keep_nb) {
+                        const bool nb = take && cnt_row[d.type[j]] > 0;
+                        const unsigned bnb = __ballot_sync(0xffffffffu, nb);
+                        if(nb) {
+                            const int slot = c_nb + __popc(bnb & ((1u << lane) - 1u));
+                            if(slot < d.nbr_max) out_nb[slot] = j;
+                        }
+                        c_nb += __popc(bnb);
+                    }
                 }
             }
         }
     }
     if(lane == 0) {
         d.nbr_count[k] = c;
+        if(keep_nb) d.nbr_count_nb[k] = c_nb;
         if(c > d.nbr_max) {
             d.sc->overflow = 1;
             atomicMax(&d.sc->needed, c);
@@ -558,7 +574,8 @@ constexpr int kRefTile = 64;    // threads per block of the bonded and short-ran
 // angles, dihedrals, then the neighbour list).  The sums are stored in F and U; the all-pairs
 // Coulomb kernel continues them.
 __global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (d.force_order && tid < P.n) ? d.force_order[tid] : tid;
     const float Lf[3] = {box_f(d, P, 0), box_f(d, P, 1), box_f(d, P, 2)};
     const double w[3] = {double(Lf[0]) / 2.0 - (-double(Lf[0]) / 2.0), double(Lf[1]) / 2.0 - (-double(Lf[1]) / 2.0),
                          double(Lf[2]) / 2.0 - (-double(Lf[2]) / 2.0)};
@@ -650,10 +667,13 @@ __global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
             }
             Fx += f.x; Fy += f.y; Fz += f.z;
         }
-        // short range, neighbour-list order
+        // short range, neighbour-list order.  Entries whose type pair has no non-bonded term add
+        // the force coeff12 * 0.0 = +-0 and no energy: a sum that starts at +0 is unchanged by
+        // them, so only the entries with a term are visited (the list kernel keeps them apart)
         const int T = P.T;
-        const int nn = min(d.nbr_count[k], d.nbr_max);
-        const int* nl = d.nbr_list + (size_t)k * d.nbr_max;
+        const bool nb_only = d.nbr_list_nb != nullptr;
+        const int nn = min(nb_only ? d.nbr_count_nb[k] : d.nbr_count[k], d.nbr_max);
+        const int* nl = (nb_only ? d.nbr_list_nb : d.nbr_list) + (size_t)k * d.nbr_max;
         for(int e = 0; e < nn; e++) {
             const int i = nl[e];
             float u = 0.0f;
