@@ -568,11 +568,13 @@ __device__ __forceinline__ void coulomb_pair(const DevSys& d, const Params& P, i
     }
 }
 
-constexpr int kRefTile = 64;    // threads per block of the bonded and short-range gather (spread over every SM)
+constexpr int kRefTile = 64;    // threads per block of the bonded gather (spread over every SM)
+constexpr int kSrJ = 16;         // list positions per tile of the short-range kernel
+constexpr int kSrW = 8;          // its pair warps (kSrJ / kSrW positions each per tile)
 
-// Bonded and short-range terms, one thread per atom, each sum in the reference's order (bonds,
-// angles, dihedrals, then the neighbour list).  The sums are stored in F and U; the all-pairs
-// Coulomb kernel continues them.
+// Bonded terms, one thread per atom (atoms taken by type), each sum in the reference's order
+// (bonds, angles, dihedrals).  The sums are stored in F and U; the short-range and the all-pairs
+// Coulomb kernels continue them.
 __global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int k = (d.force_order && tid < P.n) ? d.force_order[tid] : tid;
@@ -667,50 +669,144 @@ __global__ void __launch_bounds__(kRefTile) k_force(DevSys d, Params P) {
             }
             Fx += f.x; Fy += f.y; Fz += f.z;
         }
-        // short range, neighbour-list order.  Entries whose type pair has no non-bonded term add
-        // the force coeff12 * 0.0 = +-0 and no energy: a sum that starts at +0 is unchanged by
-        // them, so only the entries with a term are visited (the list kernel keeps them apart)
-        const int T = P.T;
-        const bool nb_only = d.nbr_list_nb != nullptr;
-        const int nn = min(nb_only ? d.nbr_count_nb[k] : d.nbr_count[k], d.nbr_max);
-        const int* nl = (nb_only ? d.nbr_list_nb : d.nbr_list) + (size_t)k * d.nbr_max;
-        for(int e = 0; e < nn; e++) {
-            const int i = nl[e];
-            float u = 0.0f;
-            D3 ri = load3(d.r, i);
-            same_side(rk, ri, w);
-            D3 f = d3(0, 0, 0);
-            const float rr = (float)nrm(sub(rk, ri));
-            if(!(rr < 1E-3f)) {
-                float sum = 0.0f;
-                const int pair = d.type[k] * T + d.type[i];
-                const int cnt = d.nb_cnt[pair];
-                for(int ff = 0; ff < cnt; ff++) {
-                    const float* tab = d.nb_tab + ((size_t)pair * kMaxFF + ff) * kNpts * 3;
-                    const int idx = tindex(rr, tab);
-                    if(idx >= 0 && idx < kNpts - 1) {
-                        const float* p1 = tab + 3 * idx;
-                        const float* p2 = p1 + 3;
-                        sum += interp(rr, p1[0], p1[1], p2[0], p2[1]);
-                        if(i > k) u += interp(rr, p1[0], p1[2], p2[0], p2[2]);
-                    }
-                }
-                f = scl(coeff12(ri, rk), (double)sum);
-            }
-            float sc;
-            if(!(d.excl_local[k] && d.mol[i] != d.mol[k]) && exclusion(d, P, k, i, sc)) {
-                f = scl(f, (double)sc);
-                u *= sc;
-            }
-            Fx += f.x; Fy += f.y; Fz += f.z;
-            Uk += u;
-        }
     }
     if(!act) return;
     d.F[3 * k] = Fx;
     d.F[3 * k + 1] = Fy;
     d.F[3 * k + 2] = Fz;
     d.U[k] = live ? (double)Uk : 0.0;
+}
+
+// Short-range term of the list entry (k, i) in the reference's arithmetic (FunctorCalcForce.cpp:
+// 159-256): the FP64 minimum-image separation r12 = rk - ri, the float distance of its FP64
+// norm, the tabulated terms of the pair's type, the force coeff12 (r12 / |r12|, FP64) times their
+// sum, the pair energy on the lower index, the exclusion scaling.
+__device__ __forceinline__ void sr_pair(const DevSys& d, const Params& P, int k, int i, const D3& rk, const float* rkf,
+                                        int pair_row, bool local_k, int molk, const BoxImage& bx, D3& f, float& u) {
+    u = 0.0f;
+    const D3 ri = load3(d.r, i);
+    const float rif[3] = {trunc_f(ri.x), trunc_f(ri.y), trunc_f(ri.z)};
+    const D3 rv = d3(image_sep(rk.x, ri.x, rkf[0], rif[0], bx, 0), image_sep(rk.y, ri.y, rkf[1], rif[1], bx, 1),
+                     image_sep(rk.z, ri.z, rkf[2], rif[2], bx, 2));
+    const double R = sqrt(rv.x * rv.x + rv.y * rv.y + rv.z * rv.z);
+    const float rr = (float)R;
+    f = d3(0, 0, 0);
+    if(!(rr < 1E-3f)) {
+        float sum = 0.0f;
+        const int pair = pair_row + d.type[i];
+        const int cnt = d.nb_cnt[pair];
+        for(int ff = 0; ff < cnt; ff++) {
+            const float* tab = d.nb_tab + ((size_t)pair * kMaxFF + ff) * kNpts * 3;
+            const int idx = tindex(rr, tab);
+            if(idx >= 0 && idx < kNpts - 1) {
+                const float* p1 = tab + 3 * idx;
+                const float* p2 = p1 + 3;
+                sum += interp(rr, p1[0], p1[1], p2[0], p2[1]);
+                if(i > k) u += interp(rr, p1[0], p1[2], p2[0], p2[2]);
+            }
+        }
+        f = scl(scl(rv, 1.0 / R), (double)sum);
+    }
+    float sc;
+    if(!(local_k && d.mol[i] != molk) && exclusion(d, P, k, i, sc)) {
+        f = scale_fp64(f, sc);
+        u *= sc;
+    }
+}
+
+// Short-range terms from the neighbour list (FunctorCalcForce.cpp:234-256), continuing each atom's
+// sums after its bonded terms, in list order.  Only the entries whose type pair has a non-bonded
+// term are visited: the others add the force coeff12 * 0.0 = +-0 and no energy, which leaves a sum
+// that starts at +0 unchanged.  Layout as the all-pairs Coulomb kernel below: a block owns 32
+// atoms (taken by type, so that the lanes meet the same terms); its first kCoulW warps compute
+// the terms of list positions e (lane = atom) and park them in shared memory, and the last warp
+// adds each tile's terms in ascending e one tile behind.
+__global__ void __launch_bounds__(32 * (kSrW + 1)) k_sr_parked(DevSys d, Params P) {
+    __shared__ double tfx[2][kSrJ][32], tfy[2][kSrJ][32], tfz[2][kSrJ][32];
+    __shared__ float tu[2][kSrJ][32];
+    __shared__ unsigned ton[2][kSrJ];
+    __shared__ BoxImage bx;
+    if(d.sc->overflow) return;   // the step is redone after the neighbour list grows
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = P.n;
+    const int slot = blockIdx.x * 32 + lane;
+    const int k = slot < n ? (d.force_order ? d.force_order[slot] : slot) : n;
+    const bool live = k < n && d.mobile[k];
+    const bool nb_only = d.nbr_list_nb != nullptr;
+    const int cnt = live ? min(nb_only ? d.nbr_count_nb[k] : d.nbr_count[k], d.nbr_max) : 0;
+    const int mx = __reduce_max_sync(0xffffffffu, cnt);
+    if(!__syncthreads_or(mx > 0)) return;
+    if(threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        const float Lf = box_f(d, P, a);
+        const double w = double(Lf) / 2.0 - (-double(Lf) / 2.0);
+        bx.w[a] = w;
+        bx.nw[a] = -w;
+        bx.hw[a] = __double_as_longlong(w / 2.0);
+        bx.hwf[a] = __double2float_rn(w / 2.0);
+    }
+    const int ntile = (mx + kSrJ - 1) / kSrJ;
+    if(warp < kSrW) {
+        const D3 rk = cnt > 0 ? load3(d.r, k) : d3(0, 0, 0);
+        const float rkf[3] = {trunc_f(rk.x), trunc_f(rk.y), trunc_f(rk.z)};
+        const int* nl = (nb_only ? d.nbr_list_nb : d.nbr_list) + (size_t)(k < n ? k : 0) * d.nbr_max;
+        const int pair_row = cnt > 0 ? d.type[k] * P.T : 0;
+        const bool local_k = cnt > 0 && d.excl_local[k] != 0;
+        const int molk = cnt > 0 ? d.mol[k] : -1;
+        __syncthreads();
+        for(int t = 0; t < ntile; t++) {
+            const int b = t & 1;
+#pragma unroll
+            for(int h = 0; h < kSrJ / kSrW; h++) {
+                const int jj = warp + h * kSrW;
+                const int e = t * kSrJ + jj;
+                const bool on = e < cnt;
+                D3 f = d3(0, 0, 0);
+                float u = 0.0f;
+                if(on) sr_pair(d, P, k, nl[e], rk, rkf, pair_row, local_k, molk, bx, f, u);
+                const unsigned m = __ballot_sync(0xffffffffu, on);
+                if(on) {
+                    tfx[b][jj][lane] = f.x;
+                    tfy[b][jj][lane] = f.y;
+                    tfz[b][jj][lane] = f.z;
+                    tu[b][jj][lane] = u;
+                }
+                if(lane == 0) ton[b][jj] = m;
+            }
+            __syncthreads();
+        }
+        __syncthreads();   // the summing warp's last tile
+    } else {
+        double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+        float Uk = 0.0f;
+        if(cnt > 0) {
+            Fx = d.F[3 * k];
+            Fy = d.F[3 * k + 1];
+            Fz = d.F[3 * k + 2];
+            Uk = (float)d.U[k];   // stored as double from a float: exact
+        }
+        __syncthreads();
+        for(int t = 0; t <= ntile; t++) {
+            if(t > 0) {
+                const int b = (t - 1) & 1;
+                for(int jj = 0; jj < kSrJ; jj++) {
+                    if((ton[b][jj] >> lane) & 1u) {
+                        Fx += tfx[b][jj][lane];
+                        Fy += tfy[b][jj][lane];
+                        Fz += tfz[b][jj][lane];
+                        Uk += tu[b][jj][lane];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if(cnt > 0) {
+            d.F[3 * k] = Fx;
+            d.F[3 * k + 1] = Fy;
+            d.F[3 * k + 2] = Fz;
+            d.U[k] = (double)Uk;
+        }
+    }
 }
 
 // All-pairs Coulomb, minimum image, no cutoff (FunctorCalcForce.cpp:258-278, 514-535), continuing
@@ -1022,6 +1118,7 @@ void launch_ref_neigh(const DevSys& d, const Params& P, cudaStream_t s) {
 
 void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s) {
     k_force<<<nblk(P.n, kRefTile), kRefTile, 0, s>>>(d, P);
+    k_sr_parked<<<nblk(P.n, 32), 32 * (kSrW + 1), 0, s>>>(d, P);
     if(P.qany) k_coulomb_allpairs<<<nblk(P.n, kCoulI), kCoulThreads, 0, s>>>(d, P);
 }
 
