@@ -274,18 +274,51 @@ __global__ void k_cell_rank(DevSys d, int ncell, const int* tmp) {
 // FP32 error is below 0.01 % for boxes up to a few hundred A) is decided by the reference's FP64
 // arithmetic, so the accepted set is exactly the reference's.
 // ---------------------------------------------------------------------------------------------
+// The reference's FP64 distance test of one candidate (FunctorGenNeighList.cpp:72-151), out of
+// line: warps reach it only for candidates within 0.4 % of rc^2 in FP32.
+__device__ __noinline__ bool neigh_test_fp64(double x0, double y0, double z0, const double* rj, const double* w,
+                                             double rc2) {
+    double dX = x0 - rj[0], dY = y0 - rj[1], dZ = z0 - rj[2];
+    dX = (dX < 0.0) ? -dX : dX;
+    dY = (dY < 0.0) ? -dY : dY;
+    dZ = (dZ < 0.0) ? -dZ : dZ;
+    if(dX > (w[0] / 2.0)) dX = w[0] - dX;
+    if(dY > (w[1] / 2.0)) dY = w[1] - dY;
+    if(dZ > (w[2] / 2.0)) dZ = w[2] - dZ;
+    return (dX * dX + dY * dY + dZ * dZ) < rc2;
+}
+
+// Constants of the list kernel, computed once per block into shared memory (in registers the
+// compiler recomputed them with FP64 conversions inside the candidate loop).
+struct NeighConst {
+    double w[3];
+    double rc2;
+    float wf[3], hf[3];
+    float lo2, hi2;
+};
+
 __global__ void k_neigh(DevSys d, Params P, float rc) {
+    __shared__ NeighConst nc;
+    if(threadIdx.x == 0) {
+        float rc2f = rc;
+        rc2f *= rc2f;
+        nc.rc2 = (double)rc2f;
+        const float Bx = box_f(d, P, 0), By = box_f(d, P, 1), Bz = box_f(d, P, 2);
+        const float lx = -Bx / 2.0f, ly = -By / 2.0f, lz = -Bz / 2.0f;
+        nc.w[0] = double(lx + Bx) - double(lx);
+        nc.w[1] = double(ly + By) - double(ly);
+        nc.w[2] = double(lz + Bz) - double(lz);
+        for(int a = 0; a < 3; a++) {
+            nc.wf[a] = (float)nc.w[a];
+            nc.hf[a] = 0.5f * nc.wf[a];
+        }
+        nc.lo2 = (float)(nc.rc2 * 0.996);
+        nc.hi2 = (float)(nc.rc2 * 1.004);
+    }
+    __syncthreads();
     const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(k >= P.n) return;
-    float rc2f = rc;
-    rc2f *= rc2f;
-    const double rc2 = (double)rc2f;
-    const float Bx = box_f(d, P, 0), By = box_f(d, P, 1), Bz = box_f(d, P, 2);
-    const float lx = -Bx / 2.0f, ly = -By / 2.0f, lz = -Bz / 2.0f;
-    const double w[3] = {double(lx + Bx) - double(lx), double(ly + By) - double(ly), double(lz + Bz) - double(lz)};
-    const float wf[3] = {(float)w[0], (float)w[1], (float)w[2]};
-    const float hf[3] = {0.5f * wf[0], 0.5f * wf[1], 0.5f * wf[2]};
-    const float lo2 = (float)(rc2 * 0.996), hi2 = (float)(rc2 * 1.004);
+    const float lo2 = nc.lo2, hi2 = nc.hi2;
     const int Nx = P.nx, Ny = P.ny, Nz = P.nz;
     const double x0 = d.r[3 * k], y0 = d.r[3 * k + 1], z0 = d.r[3 * k + 2];
     const bool pre = d.rb4 != nullptr;
@@ -316,22 +349,15 @@ __global__ void k_neigh(DevSys d, Params P, float rc) {
                         if(pre) {
                             const float4 rj = d.rb4[j];
                             float fX = fabsf(rk.x - rj.x), fY = fabsf(rk.y - rj.y), fZ = fabsf(rk.z - rj.z);
-                            if(fX > hf[0]) fX = wf[0] - fX;
-                            if(fY > hf[1]) fY = wf[1] - fY;
-                            if(fZ > hf[2]) fZ = wf[2] - fZ;
+                            if(fX > nc.hf[0]) fX = nc.wf[0] - fX;
+                            if(fY > nc.hf[1]) fY = nc.wf[1] - fY;
+                            if(fZ > nc.hf[2]) fZ = nc.wf[2] - fZ;
                             f2 = fX * fX + fY * fY + fZ * fZ;
                         }
                         if(f2 < lo2) {
                             take = true;
                         } else if(f2 <= hi2) {
-                            double dX = x0 - d.r[3 * j], dY = y0 - d.r[3 * j + 1], dZ = z0 - d.r[3 * j + 2];
-                            dX = (dX < 0.0) ? -dX : dX;
-                            dY = (dY < 0.0) ? -dY : dY;
-                            dZ = (dZ < 0.0) ? -dZ : dZ;
-                            if(dX > (w[0] / 2.0)) dX = w[0] - dX;
-                            if(dY > (w[1] / 2.0)) dY = w[1] - dY;
-                            if(dZ > (w[2] / 2.0)) dZ = w[2] - dZ;
-                            take = (dX * dX + dY * dY + dZ * dZ) < rc2;
+                            take = neigh_test_fp64(x0, y0, z0, d.r + 3 * j, nc.w, nc.rc2);
                         }
                         take = take && (j != k);
                     }
@@ -430,7 +456,9 @@ __device__ __forceinline__ float dist_to_float(double x, double y, double z) {
                                         __fmul_rn(2.0f, cross)), low);
     const float Sh = __fadd_rn(s2, c), Sl = __fsub_rn(c, __fsub_rn(Sh, s2));
     if(!(Sh >= 0x1p-100f)) {
-        if(x == 0.0 && y == 0.0 && z == 0.0) return 0.0f;
+        // all three components +-0 (compared as bit patterns, without FP64 instructions): R = 0
+        if(((__double_as_longlong(x) | __double_as_longlong(y) | __double_as_longlong(z)) & 0x7fffffffffffffffLL) == 0)
+            return 0.0f;
         return dist_fp64(x, y, z);
     }
     const float lo = 1.0f - 0x1p-12f, hi = 1.0f + 0x1p-12f;
@@ -570,7 +598,7 @@ __device__ __forceinline__ void coulomb_pair(const DevSys& d, const Params& P, i
 
 constexpr int kRefTile = 64;    // threads per block of the bonded gather (spread over every SM)
 constexpr int kSrJ = 16;         // list positions per tile of the short-range kernel
-constexpr int kSrW = 8;          // its pair warps (kSrJ / kSrW positions each per tile)
+constexpr int kSrW = 16;         // its pair warps (kSrJ / kSrW positions each per tile)
 
 // Bonded terms, one thread per atom (atoms taken by type), each sum in the reference's order
 // (bonds, angles, dihedrals).  The sums are stored in F and U; the short-range and the all-pairs
