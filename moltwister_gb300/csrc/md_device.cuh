@@ -13,8 +13,12 @@ namespace mtg {
 // |x| <= 2^-5, degree 11 for |x| <= 2^-3); larger ones call exp().  On this GPU an FP64
 // instruction costs about 100 cycles in the chain's warps whether or not it depends on the one
 // before, so the instruction count is what matters: Horner's scheme (one FMA per degree;
-// Estrin's shorter dependency chain needs more instructions and measured slower), and the range
-// tests compare bit patterns on the integer units.
+// Estrin's shorter dependency chain needs more instructions and measured slower), the range
+// tests compare bit patterns on the integer units, and the wider ranges sit in a function that
+// is not inlined: inlined, their instructions could be predicated off but would still occupy the
+// FP64 pipe on every call.
+static __device__ __noinline__ double nh_exp_wide(double x);
+
 __device__ __forceinline__ double nh_exp(double x) {
     const long long ax = __double_as_longlong(x) & 0x7fffffffffffffffLL;
     if(ax <= 0x3fa0000000000000LL) {            // |x| <= 2^-5
@@ -28,6 +32,11 @@ __device__ __forceinline__ double nh_exp(double x) {
         p = fma(p, x, 1.0);
         return fma(p, x, 1.0);
     }
+    return nh_exp_wide(x);
+}
+
+static __device__ __noinline__ double nh_exp_wide(double x) {
+    const long long ax = __double_as_longlong(x) & 0x7fffffffffffffffLL;
     if(ax <= 0x3fc0000000000000LL) {            // |x| <= 2^-3
         double p = 1.0 / 39916800.0;
         p = fma(p, x, 1.0 / 3628800.0);
@@ -472,22 +481,44 @@ __device__ __forceinline__ DF df_addq(DF a, DF b) {
 __device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_addq(df_mul(a, b), c); }
 __device__ __forceinline__ DF df_scale(DF a, float pow2) { return {a.h * pow2, a.l * pow2}; }   // exact
 
-// e^x, |x| <= 2^-5 in double-float; larger arguments through FP64
+// e^x for |x| > 1/2 through FP64, not inlined (see nh_exp): warps reach it only when a lane needs it
+static __device__ __noinline__ DF df_exp_wide(DF x) { return df_of(nh_exp(df_val(x))); }
+
+// e^x, |x| <= 2^-5, in double-float: 1 + x + x^2/2 + x^3/6 in double-float, the rest in FP32
+__device__ __forceinline__ DF df_exp_small(DF x) {
+    const float xf = x.h;
+    float t = fmaf(xf, 1.0f / 40320.0f, 1.0f / 5040.0f);
+    t = fmaf(t, xf, 1.0f / 720.0f);
+    t = fmaf(t, xf, 1.0f / 120.0f);
+    t = fmaf(t, xf, 1.0f / 24.0f);
+    const float x2f = xf * xf;
+    const float tail = t * (x2f * x2f);                                  // x^4/24 + ... + x^8/8!
+    const DF sixth{0x1.555556p-3f, -0x1.555556p-28f};                     // 1/6
+    const DF a = df_addq(df_mul(x, sixth), DF{0.5f, 0.0f});               // 1/2 + x/6
+    const DF b = df_addq(df_mul(df_mul(x, x), a), DF{tail, 0.0f});         // x^2/2 + x^3/6 + tail
+    return df_addq(df_addq(DF{1.0f, 0.0f}, x), b);
+}
+
+// e^x for the double-float chain.  |x| <= 2^-5 directly; |x| <= 1/2 as (e^(x/2^k))^(2^k) with k = 2
+// or 4 exact halvings and k double-float squarings (relative error about 2^k times that of one
+// product, 2^-46 for |x| <= 1/8); larger arguments through FP64.  The top chain element's argument
+// Dt/8 p_eta/Q is often above 2^-5, where the FP64 route cost about 24 FP64 instructions per call
+// on the chain's critical path.
 __device__ __forceinline__ DF df_exp_chain(DF x) {
-    if(fabsf(x.h) <= 0.03125f) {
-        const float xf = x.h;
-        float t = fmaf(xf, 1.0f / 40320.0f, 1.0f / 5040.0f);
-        t = fmaf(t, xf, 1.0f / 720.0f);
-        t = fmaf(t, xf, 1.0f / 120.0f);
-        t = fmaf(t, xf, 1.0f / 24.0f);
-        const float x2f = xf * xf;
-        const float tail = t * (x2f * x2f);                                  // x^4/24 + ... + x^8/8!
-        const DF sixth{0x1.555556p-3f, -0x1.555556p-28f};                     // 1/6
-        const DF a = df_addq(df_mul(x, sixth), DF{0.5f, 0.0f});               // 1/2 + x/6
-        const DF b = df_addq(df_mul(df_mul(x, x), a), DF{tail, 0.0f});         // x^2/2 + x^3/6 + tail
-        return df_addq(df_addq(DF{1.0f, 0.0f}, x), b);
+    const float ax = fabsf(x.h);
+    if(ax <= 0.03125f) return df_exp_small(x);
+    if(ax <= 0.5f) {
+        const bool two = ax <= 0.125f;
+        DF e = df_exp_small(df_scale(x, two ? 0.25f : 0.0625f));
+        e = df_mul(e, e);
+        e = df_mul(e, e);
+        if(!two) {
+            e = df_mul(e, e);
+            e = df_mul(e, e);
+        }
+        return e;
     }
-    return df_of(nh_exp(df_val(x)));
+    return df_exp_wide(x);
 }
 
 // e^x, |x| <= 2^-10: 1 + x + x^2/2 in double-float, x^3/6 + x^4/24 (below 2e-10) in FP32
