@@ -613,7 +613,9 @@ int get_graph(mtg_ctx* c, int steps, bool output, int form, cudaGraphExec_t* out
         key = std::make_pair(steps, output ? 1 : 0);
     }
     CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    set_pdl_launch(!is_reference(c));
     for(int s = 0; s < steps; s++) enqueue_step(c, output && s == steps - 1);
+    set_pdl_launch(false);
     CUDA_TRY(c, cudaStreamEndCapture(c->stream, &g));
     cudaGraphExec_t ge;
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);

@@ -38,6 +38,39 @@ int integration_blocks(const Params& P) { return P.nrep ? P.nblk_total : reducti
 
 namespace {
 
+// Programmatic dependent launch: a step kernel captured with the programmatic-serialization
+// attribute may be scheduled while its predecessor drains; it waits here until the predecessor
+// has completed and its writes are visible, before reading anything, and at once allows its own
+// successor to be scheduled.  Launched without the attribute both instructions return at once.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches of the step kernels: with the programmatic-serialization attribute while a plain step
+// graph is captured (set_pdl_launch), otherwise an ordinary launch.
+bool g_pdl = false;
+
+template<typename... KArgs, typename... Args>
+void launch_step_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    if(!g_pdl) {
+        kern<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
+
 // The system an atom or an integration block belongs to: the whole context (r < 0), or replica r
 // of a batch.  Gives the atom and block ranges, cell grid, box, cutoffs, temperature and the
 // per-system scalars, chains and output record.
@@ -270,6 +303,7 @@ __device__ __forceinline__ void kick_drift_atom(DevSys& d, const Params& P, cons
 
 // FP64 mode.  One 256-atom block per launch block; a batch maps blocks to replicas (blk_rep).
 __global__ void k_pkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond, int use_cond) {
+    pdl_enter();
     const SysView v = sys_view(d, P, rep_of_block(d, P));
     const int k = v.off + (blockIdx.x - v.bbase) * blockDim.x + threadIdx.x;
     const bool mine = k < v.off + v.n;
@@ -364,6 +398,7 @@ __device__ __forceinline__ void step_end(const DevSys& d, const Params& P, const
 // FP64 mode: second kick, clipping, pbcWrap, sums, end-of-step work.
 template<bool OUTPUT>
 __global__ void k_pkick2(DevSys d, Params P) {
+    pdl_enter();
     __shared__ double smem[32 * 3];
     const SysView sv = sys_view(d, P, rep_of_block(d, P));
     const int k = sv.off + (blockIdx.x - sv.bbase) * blockDim.x + threadIdx.x;
@@ -480,6 +515,7 @@ __device__ __forceinline__ void mix_load(const DevSys& d, const SysView& v, int 
 // p <- S p + dt/2 F, r <- r + dt p / m (VelVerlet.cpp:74-93 with the pending thermostat scale),
 // box fractions, and the half-skin displacement test against the positions of the last list build.
 __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle cond, int use_cond) {
+    pdl_enter();
     __shared__ MixK K;
     const int rep = rep_of_block(d, P);
     const SysView v = sys_view(d, P, rep);
@@ -543,6 +579,7 @@ __global__ void k_mkick_drift(DevSys d, Params P, cudaGraphConditionalHandle con
 // scale), box fractions in this step's box, and the displacement test against the build positions
 // scaled with the box (baro_box_fields).
 __global__ void k_mkick_drift_npt(DevSys d, Params P, cudaGraphConditionalHandle cond, int use_cond) {
+    pdl_enter();
     __shared__ MixK K;
     __shared__ DF ap, bp, ar, br;
     __shared__ float sb, h2;
@@ -599,6 +636,7 @@ __global__ void k_mkick_drift_npt(DevSys d, Params P, cudaGraphConditionalHandle
 // current box, block sums of p^2/m, of the pair virial and (output steps) of U.
 template<bool OUTPUT>
 __global__ void k_mkick2_npt(DevSys d, Params P) {
+    pdl_enter();
     __shared__ MixK K;
     __shared__ DF ap, bp;
     __shared__ double smem[32 * 3];
@@ -655,6 +693,7 @@ __global__ void k_mkick2_npt(DevSys d, Params P) {
 // chain's registers do not limit the occupancy of the per-atom pass.
 template<bool OUTPUT>
 __global__ void k_mkick2(DevSys d, Params P) {
+    pdl_enter();
     __shared__ MixK K;
     __shared__ double smem[32 * 3];
     const int rep = rep_of_block(d, P);
@@ -728,6 +767,7 @@ __global__ void k_mkick2(DevSys d, Params P) {
 // system's totals from its block partials, then the thermostat half-steps and the output record.
 template<bool OUTPUT>
 __global__ void __launch_bounds__(96, 1) k_mstep_end(DevSys d, Params P) {
+    pdl_enter();
     __shared__ double smem[32 * 3];
     __shared__ double tot[3];
     const SysView sv = sys_view(d, P, P.nrep ? (int)blockIdx.x : -1);
@@ -747,6 +787,7 @@ __global__ void __launch_bounds__(96, 1) k_mstep_end(DevSys d, Params P) {
 // barostat and chain half-steps, the output record and the next step's box (npt_scalars).
 template<bool OUTPUT>
 __global__ void __launch_bounds__(96, 1) k_mstep_end_npt(DevSys d, Params P) {
+    pdl_enter();
     __shared__ double smem[32 * 3];
     __shared__ double tot[3];
     const SysView sv = sys_view(d, P, -1);
@@ -764,6 +805,7 @@ __global__ void __launch_bounds__(96, 1) k_mstep_end_npt(DevSys d, Params P) {
 // ---------------------------------------------------------------------------------------------
 template<bool MIXED>
 __global__ void k_pcell_assign(DevSys d, Params P) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     if(P.ensemble == MTG_NPT && i == 0) {
@@ -796,6 +838,7 @@ __global__ void k_pcell_assign(DevSys d, Params P) {
 // Exclusive scan of one system's cell counts (one block per replica of a batch): the replica's
 // cells map onto its own slot range, so replicas rebuild independently.
 __global__ void k_pcell_scan(DevSys d, Params P) {
+    pdl_enter();
     const int r = P.nrep ? (int)blockIdx.x : -1;
     if(!rebuild_due(d, P, r)) return;
     const SysView v = sys_view(d, P, r);   // cell counts of the current box (NPT: of this build)
@@ -838,6 +881,7 @@ __global__ void k_pcell_scan(DevSys d, Params P) {
 }
 
 __global__ void k_pcell_scatter(DevSys d, Params P) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= P.n || !rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     const int c = d.pcell_of[i];
@@ -852,6 +896,7 @@ __global__ void k_pcell_scatter(DevSys d, Params P) {
 // slot, and the positions the force gather reads are copied into slot order, so the partners of
 // the atoms a block works on lie in a compact, cache-resident range.
 __global__ void k_pcell_rank(DevSys d, Params P, bool mixed) {
+    pdl_enter();
     // one thread per position of the scratch array (positions are grouped by cell; a replica's
     // positions are its own atom range): the rank of its key among its cell's keys is its slot
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -885,6 +930,7 @@ __device__ __forceinline__ int excl_class(const DevSys& d, int k, int i) {
 
 template<bool MIXED>
 __global__ void k_vlist(DevSys d, Params P) {
+    pdl_enter();
     if(!d.sc->rebuild) return;
     const int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if(si >= P.n) return;
@@ -1420,6 +1466,7 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
 // list entries.
 template<bool MIXED, bool ENERGY, int TEAM>
 __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
+    pdl_enter();
     using R = typename std::conditional<MIXED, float, double>::type;
     __shared__ PairCoef pc_s[kSmemPairs];
     __shared__ float us_s[kSmemPairs];   // energy shift of the staged LJ term
@@ -1727,6 +1774,7 @@ __global__ void k_check_list(DevSys d, Params P) {
 // when allocated), and the last block clears the rebuild flags and counts the build.  Every block
 // passes the early-exit test before the last one clears the flag it tests.
 __global__ void k_finish_build(DevSys d, Params P, int ncell) {
+    pdl_enter();
     if(!d.sc->rebuild) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if(c < ncell) d.pcell_count[c] = 0;
@@ -1814,6 +1862,8 @@ void launch_gd_step(const DevSys& d, const Params& P, double lr, cudaStream_t s)
     k_gd_step<<<reduction_blocks(P.n), 256, 0, s>>>(d, P, lr, P.precision);
 }
 
+void set_pdl_launch(bool on) { g_pdl = on; }
+
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
     if(P.precision == MTG_PREC_MIXED) k_prologue<true><<<integration_blocks(P), 256, 0, s>>>(d, P);
     else k_prologue<false><<<integration_blocks(P), 256, 0, s>>>(d, P);
@@ -1822,9 +1872,9 @@ void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s) {
 void launch_prod_kick_drift(const DevSys& d, const Params& P, cudaStream_t s, cudaGraphConditionalHandle cond, bool use_cond) {
     const int nb = integration_blocks(P);
     const int u = use_cond ? 1 : 0;
-    if(P.precision == MTG_PREC_MIXED && P.ensemble == MTG_NPT) k_mkick_drift_npt<<<nb, 256, 0, s>>>(d, P, cond, u);
-    else if(P.precision == MTG_PREC_MIXED) k_mkick_drift<<<nb, 256, 0, s>>>(d, P, cond, u);
-    else k_pkick_drift<<<nb, 256, 0, s>>>(d, P, cond, u);
+    if(P.precision == MTG_PREC_MIXED && P.ensemble == MTG_NPT) launch_step_kernel(k_mkick_drift_npt, nb, 256, s, d, P, cond, u);
+    else if(P.precision == MTG_PREC_MIXED) launch_step_kernel(k_mkick_drift, nb, 256, s, d, P, cond, u);
+    else launch_step_kernel(k_pkick_drift, nb, 256, s, d, P, cond, u);
 }
 
 void launch_prod_check_list(const DevSys& d, const Params& P, cudaStream_t s) {
@@ -1836,23 +1886,23 @@ void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_
     if(force) cudaMemsetAsync(&d.sc->rebuild, 0xff, sizeof(int32_t), s);
     // the cell counts are zero here (k_finish_build); every kernel returns at once when no
     // rebuild is due
-    if(P.precision == MTG_PREC_MIXED) k_pcell_assign<true><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    else k_pcell_assign<false><<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    k_pcell_scan<<<P.nrep ? P.nrep : 1, 1024, 0, s>>>(d, P);
-    k_pcell_scatter<<<nblk(P.n, 256), 256, 0, s>>>(d, P);
-    k_pcell_rank<<<nblk(P.n, 256), 256, 0, s>>>(d, P, P.precision == MTG_PREC_MIXED);
-    if(P.precision == MTG_PREC_MIXED) k_vlist<true><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
-    else k_vlist<false><<<nblk(P.n * 32, 256), 256, 0, s>>>(d, P);
-    k_finish_build<<<nblk(ncell, 256), 256, 0, s>>>(d, P, ncell);
+    if(P.precision == MTG_PREC_MIXED) launch_step_kernel(k_pcell_assign<true>, nblk(P.n, 256), 256, s, d, P);
+    else launch_step_kernel(k_pcell_assign<false>, nblk(P.n, 256), 256, s, d, P);
+    launch_step_kernel(k_pcell_scan, P.nrep ? P.nrep : 1, 1024, s, d, P);
+    launch_step_kernel(k_pcell_scatter, nblk(P.n, 256), 256, s, d, P);
+    launch_step_kernel(k_pcell_rank, nblk(P.n, 256), 256, s, d, P, P.precision == MTG_PREC_MIXED);
+    if(P.precision == MTG_PREC_MIXED) launch_step_kernel(k_vlist<true>, nblk(P.n * 32, 256), 256, s, d, P);
+    else launch_step_kernel(k_vlist<false>, nblk(P.n * 32, 256), 256, s, d, P);
+    launch_step_kernel(k_finish_build, nblk(ncell, 256), 256, s, d, P, ncell);
 }
 
 template<bool MIXED, bool ENERGY>
 static void force_team(const DevSys& d, const Params& P, cudaStream_t s) {
     const int team = P.team;
     const int nb = nblk(P.n * team, 256);
-    if(team == 8) k_pforce<MIXED, ENERGY, 8><<<nb, 256, 0, s>>>(d, P);
-    else if(team == 16) k_pforce<MIXED, ENERGY, 16><<<nb, 256, 0, s>>>(d, P);
-    else k_pforce<MIXED, ENERGY, 32><<<nb, 256, 0, s>>>(d, P);
+    if(team == 8) launch_step_kernel(k_pforce<MIXED, ENERGY, 8>, nb, 256, s, d, P);
+    else if(team == 16) launch_step_kernel(k_pforce<MIXED, ENERGY, 16>, nb, 256, s, d, P);
+    else launch_step_kernel(k_pforce<MIXED, ENERGY, 32>, nb, 256, s, d, P);
 }
 
 void launch_prod_force(const DevSys& d, const Params& P, bool energy, cudaStream_t s) {
@@ -1871,22 +1921,22 @@ void launch_prod_kick2(const DevSys& d, const Params& P, bool output, cudaStream
     if(P.precision == MTG_PREC_MIXED) {
         const int nsys = P.nrep ? P.nrep : 1;
         if((parts & kKick2Atoms) && P.ensemble == MTG_NPT) {
-            if(output) k_mkick2_npt<true><<<nb, 256, 0, s>>>(d, P);
-            else k_mkick2_npt<false><<<nb, 256, 0, s>>>(d, P);
+            if(output) launch_step_kernel(k_mkick2_npt<true>, nb, 256, s, d, P);
+            else launch_step_kernel(k_mkick2_npt<false>, nb, 256, s, d, P);
         } else if(parts & kKick2Atoms) {
-            if(output) k_mkick2<true><<<nb, 256, 0, s>>>(d, P);
-            else k_mkick2<false><<<nb, 256, 0, s>>>(d, P);
+            if(output) launch_step_kernel(k_mkick2<true>, nb, 256, s, d, P);
+            else launch_step_kernel(k_mkick2<false>, nb, 256, s, d, P);
         }
         if((parts & kKick2StepEnd) && P.ensemble == MTG_NPT) {
-            if(output) k_mstep_end_npt<true><<<1, 96, 0, s>>>(d, P);
-            else k_mstep_end_npt<false><<<1, 96, 0, s>>>(d, P);
+            if(output) launch_step_kernel(k_mstep_end_npt<true>, 1, 96, s, d, P);
+            else launch_step_kernel(k_mstep_end_npt<false>, 1, 96, s, d, P);
         } else if(parts & kKick2StepEnd) {
-            if(output) k_mstep_end<true><<<nsys, 96, 0, s>>>(d, P);
-            else k_mstep_end<false><<<nsys, 96, 0, s>>>(d, P);
+            if(output) launch_step_kernel(k_mstep_end<true>, nsys, 96, s, d, P);
+            else launch_step_kernel(k_mstep_end<false>, nsys, 96, s, d, P);
         }
     } else if(parts & kKick2Atoms) {
-        if(output) k_pkick2<true><<<nb, 256, 0, s>>>(d, P);
-        else k_pkick2<false><<<nb, 256, 0, s>>>(d, P);
+        if(output) launch_step_kernel(k_pkick2<true>, nb, 256, s, d, P);
+        else launch_step_kernel(k_pkick2<false>, nb, 256, s, d, P);
     }
 }
 

@@ -299,6 +299,8 @@ void launch_ref_force(const DevSys& d, const Params& P, cudaStream_t s);
 void launch_ref_kick_drift(const DevSys& d, const Params& P, cudaStream_t s);
 void launch_ref_kick2(const DevSys& d, const Params& P, bool output, cudaStream_t s);
 // Shared
+// step kernels launched with programmatic dependent launch while a plain step graph is captured
+void set_pdl_launch(bool on);
 void launch_prologue(const DevSys& d, const Params& P, cudaStream_t s);
 // Production modes
 // use_cond: inside a conditional step graph, the last block sets `cond` to the rebuild decision
