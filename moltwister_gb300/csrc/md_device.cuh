@@ -279,6 +279,9 @@ __device__ __forceinline__ double cmt_exp_bits(double x, bool fixed) {
     if(!fixed && __double_as_longlong(x) > 0x3ff0000000000000LL) return 2.71828 * x;
     return nh_exp(x);
 }
+// The same, not inlined: for branches that are rarely taken, whose FP64 instructions would
+// otherwise be predicated into every pass
+static __device__ __noinline__ double cmt_exp_call(double x, bool fixed) { return cmt_exp_bits(x, fixed); }
 
 // One thermostat half-step on warps 0..2; M >= 2.  X holds the chain on entry and exit; the flags
 // continue from `seq` (a counter shared by successive calls so flags only grow).  Returns the new
@@ -291,6 +294,8 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const double w0 = sy_w0(fixed);
     const double w[3] = {w0, 1.0 - 2.0 * w0, w0};
+    // the two distinct Suzuki-Yoshida stage lengths w_mu dt / nresp, each FP64 division once per call
+    const double DtS[2] = {w[0] * dt / double(nresp), w[1] * dt / double(nresp)};
     const double gkT = g * kT;
     const int top = M - 1;
     const int nsub = 3 * nresp;
@@ -310,7 +315,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         if(!fixed && pe[0] > 15.0) pe[0] = 10.0;
         int s = 0;
         for(int mu = 0; mu < 3; mu++) {
-            const double Dt = w[mu] * dt / double(nresp);
+            const double Dt = DtS[mu == 1 ? 1 : 0];
             const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
             // per-stage coefficients: d4 G_j = pe[j-1]^2 A_j - B (j >= 1), d4 G_0 = KE2 d4 - B0,
             // exponent of c_j = pe[j+1] D_j, eta step d2 pe/Q = pe E
@@ -342,7 +347,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                         x = xprev[j];
                     } else {
                         x = pe[j + 1] * D[j];
-                        c = cmt_exp_bits(x, fixed);
+                        c = cmt_exp_call(x, fixed);
                     }
                     c12[j] = c;
                     x12[j] = x;
@@ -375,7 +380,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                            __double_as_longlong(xn) <= half_bits && __double_as_longlong(x12[j]) <= half_bits)
                             c = c12[j] * exp_tiny(dx);
                         else
-                            c = cmt_exp_bits(xn, fixed);
+                            c = cmt_exp_call(xn, fixed);
                         cprev[j] = c;
                         xprev[j] = xn;
                     }
@@ -410,7 +415,7 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         double KE2 = X.KE2, scale = 1.0;
         int s = 0;
         for(int mu = 0; mu < 3; mu++) {
-            const double d2 = (w[mu] * dt / double(nresp)) / 2.0;
+            const double d2 = DtS[mu == 1 ? 1 : 0] / 2.0;
             for(int it = 0; it < nresp; it++, s++) {
                 nh_wait(&X.f_pe0, seq + s + 1, tmo, X.polls);
                 const double c = cmt_exp_bits(-(d2 * (X.pe0 * iQ0)), fixed);
@@ -432,15 +437,15 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
         double pm = X.pe[top - 1];
         if(!fixed && top - 1 == 0 && pm > 15.0) pm = 10.0;    // the guard on p_eta[0] (NHChain.cpp:61-65)
         int s = 0;
+        double d4p = 0.0;   // the previous substep's Dt/4 (the same expression as its d4)
         for(int mu = 0; mu < 3; mu++) {
-            const double Dt = w[mu] * dt / double(nresp);
+            const double Dt = DtS[mu == 1 ? 1 : 0];
             const double d8 = -(Dt / 8.0), d4 = Dt / 4.0, d2 = Dt / 2.0;
             for(int it = 0; it < nresp; it++, s++) {
                 if(s > 0) {
                     // 1.6 of the previous substep, with that substep's Dt
                     nh_wait(&X.f_pe_m2, seq + s, tmo, X.polls);
                     pm = X.pe_m2;
-                    const double d4p = (w[(s - 1) / nresp] * dt / double(nresp)) / 4.0;
                     pt += d4p * (pm * pm * iQm - kT);
                 }
                 pt += d4 * (pm * pm * iQm - kT);          // 1.1
@@ -448,11 +453,12 @@ __device__ inline int nh_chain_half_3w_t(NhExchange& X, double g, double kT, dou
                 if(lane == 0) X.etop = c;
                 nh_post(&X.f_etop, seq + s + 1);
                 eta_t += d2 * (pt * iQt);                   // 1.3 for the top element
+                d4p = d4;
             }
         }
         nh_wait(&X.f_pe_m2, seq + nsub, tmo, X.polls);             // 1.6 of the last substep
         pm = X.pe_m2;
-        pt += ((w[2] * dt / double(nresp)) / 4.0) * (pm * pm * iQm - kT);
+        pt += d4p * (pm * pm * iQm - kT);
         if(lane == 0) {
             X.pe[top] = pt;
             X.eta[top] = eta_t;
