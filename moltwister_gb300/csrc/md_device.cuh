@@ -484,7 +484,17 @@ __device__ __forceinline__ DF df_addq(DF a, DF b) {
     const DF s = two_sum(a.h, b.h);
     return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
 }
-__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_addq(df_mul(a, b), c); }
+// a b + c without renormalising the product first: the exact product p + e (e by fma), the cross
+// terms and c's low part summed in FP32 beside the exact two_sum of p and c's high part; about
+// 20 cycles shorter on a dependency chain than df_addq(df_mul(a, b), c), with the same error bound
+// (about 2^-46 of |ab| + |c|)
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = __fmaf_rn(a.h, b.h, -p);
+    const float cr = __fmaf_rn(a.l, b.h, __fmul_rn(a.h, b.l));
+    const DF s = two_sum(p, c.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(__fadd_rn(e, cr), c.l)));
+}
 __device__ __forceinline__ DF df_scale(DF a, float pow2) { return {a.h * pow2, a.l * pow2}; }   // exact
 
 // e^x for |x| > 1/2 through FP64, not inlined (see nh_exp): warps reach it only when a lane needs it
