@@ -229,6 +229,9 @@ struct NhExchange {
     double KE2, scale;
     double pe0, ke, pe_m2, etop;            // slots
     DF dpe0, dke, dpe_m2, detop;            // the same slots of the double-float chain
+    // double-float hand-over slots: each half of the value in its own 64-bit word beside the
+    // sequence number (see slot_post / slot_wait)
+    unsigned long long q_pe0[2], q_ke[2], q_pe_m2[2], q_etop[2];
     volatile int f_pe0, f_ke, f_pe_m2, f_etop;
     int timeout;
     int polls;                              // wait limit (Params::wait_polls)
@@ -259,6 +262,42 @@ __device__ __forceinline__ void nh_wait(volatile int* flag, int seq, int* timeou
         if(it >= 4096) __nanosleep(32);
     }
     *timeout = 1;
+}
+
+// Hand-over of a double-float value without acquire / release: each float travels in its own
+// aligned 64-bit word together with the sequence number, written by lane 0 with relaxed stores
+// and polled with relaxed loads.  An aligned 64-bit access is single-copy atomic, so a reader that
+// sees the expected sequence in both words has both halves of that post.  A producer never posts
+// a slot again before its consumer has read it (each post waits on a value the consumer hands
+// back after reading), so the expected sequence is the one present.  Bounded like nh_wait: after
+// `polls` reads the wait records a timeout and returns what it has.
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared((void*)p)), "l"(v)
+                 : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.cta.shared::cta.b64 %0, [%1];" : "=l"(v) : "r"((unsigned)__cvta_generic_to_shared((void*)p))
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ void slot_post(unsigned long long* q, DF v, int seq) {
+    if((threadIdx.x & 31) == 0) {
+        const unsigned long long tag = (unsigned long long)(unsigned)seq << 32;
+        st_relaxed_u64(q, tag | __float_as_uint(v.h));
+        st_relaxed_u64(q + 1, tag | __float_as_uint(v.l));
+    }
+}
+__device__ __forceinline__ DF slot_wait(const unsigned long long* q, int seq, int* timeout, int polls) {
+    unsigned long long a = 0, b = 0;
+    for(int it = 0; it < polls; it++) {
+        a = ld_relaxed_u64(q);
+        b = ld_relaxed_u64(q + 1);
+        if((int)(a >> 32) == seq && (int)(b >> 32) == seq) return DF{__uint_as_float((unsigned)a), __uint_as_float((unsigned)b)};
+        if(it >= 4096) __nanosleep(32);
+    }
+    *timeout = 1;
+    return DF{__uint_as_float((unsigned)a), __uint_as_float((unsigned)b)};
 }
 
 // Lane 0 posts; it is also the lane that stored the value being handed over.
@@ -602,8 +641,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, co
                 for(int j = 0; j < top; j++) {
                     DF c, x;
                     if(j == top - 1) {
-                        nh_wait(&X.f_etop, seq + s + 1, tmo, X.polls);      // exponential of p_eta[M-1] (warp 2)
-                        etop = X.detop;
+                        etop = slot_wait(X.q_etop, seq + s + 1, tmo, X.polls);   // exponential of p_eta[M-1] (warp 2)
                         c = etop;
                         x = DF{0.0f, 0.0f};
                     } else if(it > 0) {
@@ -618,10 +656,7 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, co
                     const DF t = (j == 0) ? df_fma(KE2, d4D, nB0) : df_fma(df_mul(pe[j - 1], pe[j - 1]), A[j], nB);
                     t12[j] = t;
                     pe[j] = df_mul(df_fma(pe[j], c, t), c);
-                    if(j == 0) {
-                        if(lane == 0) X.dpe0 = pe[0];
-                        nh_post(&X.f_pe0, seq + s + 1);
-                    }
+                    if(j == 0) slot_post(X.q_pe0, pe[0], seq + s + 1);
                 }
                 // 1.3 (this warp's elements)
                 {
@@ -649,17 +684,13 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, co
                     }
                     DF t;
                     if(j == 0) {
-                        nh_wait(&X.f_ke, seq + s + 1, tmo, X.polls);    // kinetic term after step 1.4 (warp 1)
-                        KE2 = X.dke;
+                        KE2 = slot_wait(X.q_ke, seq + s + 1, tmo, X.polls);   // kinetic term after step 1.4 (warp 1)
                         t = df_fma(KE2, d4D, nB0);
                     } else {
                         t = t12[j];
                     }
                     pe[j] = df_mul(df_fma(pe[j], c, t), c);
-                    if(j == top - 1) {
-                        if(lane == 0) X.dpe_m2 = pe[top - 1];
-                        nh_post(&X.f_pe_m2, seq + s + 1);
-                    }
+                    if(j == top - 1) slot_post(X.q_pe_m2, pe[top - 1], seq + s + 1);
                 }
             }
         }
@@ -689,12 +720,11 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, co
         for(int mu = 0; mu < 3; mu++) {
             const DF D1 = D1W[mu == 1 ? 1 : 0];
             for(int it = 0; it < nresp; it++, s++) {
-                nh_wait(&X.f_pe0, seq + s + 1, tmo, X.polls);
-                const DF c = df_exp_chain(df_mul(X.dpe0, D1));
+                const DF p0 = slot_wait(X.q_pe0, seq + s + 1, tmo, X.polls);
+                const DF c = df_exp_chain(df_mul(p0, D1));
                 scale = df_mul(scale, c);
                 KE2 = df_mul(KE2, df_mul(c, c));
-                if(lane == 0) X.dke = KE2;
-                nh_post(&X.f_ke, seq + s + 1);
+                slot_post(X.q_ke, KE2, seq + s + 1);
             }
         }
         const DF out = (lane == 0) ? KE2 : scale;
@@ -721,20 +751,17 @@ __device__ inline int nh_chain_half_3w_df(NhExchange& X, double g, double kT, co
             for(int it = 0; it < nresp; it++, s++) {
                 if(s > 0) {
                     // 1.6 of the previous substep, with that substep's Dt
-                    nh_wait(&X.f_pe_m2, seq + s, tmo, X.polls);
-                    pm = X.dpe_m2;
+                    pm = slot_wait(X.q_pe_m2, seq + s, tmo, X.polls);
                     pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
                 }
                 pt = df_fma(d4, df_fma(df_mul(pm, pm), iQm, nkT), pt);         // 1.1
                 const DF c = df_exp_chain(df_mul(pt, Dtop));
-                if(lane == 0) X.detop = c;
-                nh_post(&X.f_etop, seq + s + 1);
+                slot_post(X.q_etop, c, seq + s + 1);
                 eta_t = df_fma(pt, Etop, eta_t);                               // 1.3 for the top element
                 d4prev = d4;
             }
         }
-        nh_wait(&X.f_pe_m2, seq + nsub, tmo, X.polls);             // 1.6 of the last substep
-        pm = X.dpe_m2;
+        pm = slot_wait(X.q_pe_m2, seq + nsub, tmo, X.polls);      // 1.6 of the last substep
         pt = df_fma(d4prev, df_fma(df_mul(pm, pm), iQm, nkT), pt);
         const double o = df_val((lane == 0) ? pt : eta_t);   // both in one pass
         if(lane == 0) X.pe[top] = o;
@@ -838,6 +865,8 @@ __device__ inline void thermostat_chain(const Params& P, StepScalars* sc, Thermo
             X.KE2 = KE2;
             X.scale = 1.0;
             X.f_pe0 = X.f_ke = X.f_pe_m2 = X.f_etop = 0;
+            X.q_pe0[0] = X.q_pe0[1] = X.q_ke[0] = X.q_ke[1] = 0ULL;
+            X.q_pe_m2[0] = X.q_pe_m2[1] = X.q_etop[0] = X.q_etop[1] = 0ULL;
             X.timeout = 0;
             X.polls = P.wait_polls;
         }
