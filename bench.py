@@ -287,6 +287,7 @@ def our_arm(args):
                            "one run of all steps with no L2 flush (the device-timed value flushes L2 before every "
                            f"chunk of {CHUNK} steps)"},
            "gpu_launches": int(launches),
+           "graph_form": e.stats()["graph_form"],
            "list_builds": int(builds),
            "phase_ms": phases}
     if rank == 0:

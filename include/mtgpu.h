@@ -267,6 +267,8 @@ typedef struct mtg_run_stats {
     int64_t kernel_launches;
     int32_t graph_steps;        /* steps per captured CUDA graph (0 = not captured) */
     int32_t force_team;         /* lanes per atom chosen by the force-kernel autotuner */
+    int32_t graph_form;         /* step-graph form: 0 plain capture, 1 list build under a conditional
+                                   node, -1 not chosen yet (both are timed on the first chunks) */
 } mtg_run_stats;
 int mtg_get_run_stats(mtg_ctx* ctx, mtg_run_stats* st);
 

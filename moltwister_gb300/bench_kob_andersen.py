@@ -135,6 +135,7 @@ def main(argv=None):
     out = {
         "metric": "atom-steps/s", "workload": f"kob_andersen_{n}", "atoms": n, "device": device_name(0),
         "mixed": {"value": rate_m, "steps": args.steps, "ms_per_step": ms_m / args.steps, "list_builds": builds_m,
+                  "force_team": em.stats()["force_team"], "graph_form": em.stats()["graph_form"],
                   "nve_drift_kT_per_atom_per_ns": drift_m, "nve_drift_stderr": se_m,
                   "nve_noise_kT_per_atom": noise_m, "nve_drift_window_steps": args.drift_steps,
                   "nve_drift_stride": args.drift_stride,

@@ -90,9 +90,10 @@ struct mtg_ctx {
     // kTuneSteps steps run one form each, timed, and the faster is kept.  Both forms run the
     // same kernels on the same data: the trajectory does not depend on the choice.
     bool conditional = true;          // IF nodes accepted by this driver
+    bool team_retuned = false;        // force-gather team size re-timed at the first run
     int graph_form = -1;              // chosen form, -1 while measuring
-    double form_us[2] = {0.0, 0.0};   // device time per step of each form
-    bool form_seen[2] = {false, false};
+    double form_us[2] = {0.0, 0.0};   // best device time per step of each form so far
+    int form_n[2] = {0, 0};           // chunks timed in each form
     int last_form = 0;
     mtg_run_stats stats{};
     // output staging
@@ -409,12 +410,15 @@ struct TuneKey {
 std::map<TuneKey, int> g_tuned;
 std::mutex g_tuned_mutex;   // contexts may be created on several host threads at once
 
-int autotune_force(mtg_ctx* c) {
+// `fresh` re-times even when the class has a cached choice (the first run of a context, when the
+// configuration is the one that will run rather than an unrelaxed start) and stores the result.
+// Each team size is timed in three interleaved rounds of five launches; its fastest round counts.
+int autotune_force(mtg_ctx* c, bool fresh = false) {
     const Params& P = c->P;
     const double V = P.box[0] * P.box[1] * P.box[2];
     const double rlist = std::max((double)P.rc, P.coulomb != MTG_COULOMB_ALLPAIRS ? (double)P.rcoul : 0.0) + P.skin;
     TuneKey key{P.precision, (int)std::floor(std::log2((double)P.n)), (int)std::lround(rlist * 10.0), (int)std::lround(100.0 * P.n / V)};
-    {
+    if(!fresh) {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(key);
         if(it != g_tuned.end()) {
@@ -423,20 +427,26 @@ int autotune_force(mtg_ctx* c) {
         }
     }
     const int teams[3] = {8, 16, 32};
-    float best = 1e30f;
+    float best_of[3] = {1e30f, 1e30f, 1e30f};
+    for(int round = 0; round < 3; round++) {
+        for(int k = 0; k < 3; k++) {
+            c->P.team = teams[k];
+            launch_prod_force(c->d, c->P, false, c->stream);
+            CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+            for(int r = 0; r < 5; r++) launch_prod_force(c->d, c->P, false, c->stream);
+            CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+            CUDA_TRY(c, cudaEventSynchronize(c->ev1));
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+            best_of[k] = std::min(best_of[k], ms);
+        }
+    }
     int best_team = 32;
-    for(int t : teams) {
-        c->P.team = t;
-        launch_prod_force(c->d, c->P, false, c->stream);
-        CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-        for(int r = 0; r < 5; r++) launch_prod_force(c->d, c->P, false, c->stream);
-        CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
-        CUDA_TRY(c, cudaEventSynchronize(c->ev1));
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        if(ms < best) {
-            best = ms;
-            best_team = t;
+    float best = 1e30f;
+    for(int k = 0; k < 3; k++) {
+        if(best_of[k] < best) {
+            best = best_of[k];
+            best_team = teams[k];
         }
     }
     c->P.team = best_team;
@@ -468,18 +478,26 @@ int enqueue_step(mtg_ctx* c, bool output) {
 
 // Kernels per step when no list rebuild is due (reference mode rebuilds every step).
 int kernels_per_step(const mtg_ctx* c) {
-    // mixed mode ends a step with a second kernel (k_mstep_end)
-    return ((is_reference(c) || c->last_form == 0) ? 9 : 3) + (is_mixed(c) ? 1 : 0);
+    // reference: kick-drift, four cell-list kernels, the neighbour list, bonded and short-range
+    // force kernels (+ all-pairs Coulomb with charges), kick; production plain form: kick-drift,
+    // six list-build kernels, force, kick (+ the step end in mixed mode); conditional form: the
+    // build kernels only inside the IF node
+    if(is_reference(c)) return 9 + (c->P.qany ? 1 : 0);
+    return (c->last_form == 0 ? 9 : 3) + (is_mixed(c) ? 1 : 0);
 }
 
 constexpr int kTuneSteps = 20;
 
-// Step graph form for the next chunk (see mtg_ctx::graph_form).
+// Step graph form for the next chunk (see mtg_ctx::graph_form): the first four chunks of at least
+// kTuneSteps steps alternate the two forms (conditional, plain, conditional, plain), and the form
+// with the lower best time per step is kept.  List builds fall into the timed chunks of both forms
+// alike; taking each form's best chunk keeps an unlucky one (more builds, a slow first launch)
+// from deciding.
 int choose_form(mtg_ctx* c, int steps) {
     if(is_reference(c) || !c->conditional) return 0;
     if(c->graph_form >= 0) return c->graph_form;
     if(steps < kTuneSteps) return 0;
-    return c->form_seen[1] ? 0 : 1;
+    return ((c->form_n[0] + c->form_n[1]) % 2 == 0) ? 1 : 0;
 }
 
 void record_form(mtg_ctx* c, int form, int steps, float ms) {
@@ -488,9 +506,10 @@ void record_form(mtg_ctx* c, int form, int steps, float ms) {
         c->graph_form = 0;
         return;
     }
-    c->form_us[form] = 1000.0 * ms / steps;
-    c->form_seen[form] = true;
-    if(c->form_seen[0] && c->form_seen[1]) c->graph_form = (c->form_us[1] < c->form_us[0]) ? 1 : 0;
+    const double us = 1000.0 * ms / steps;
+    c->form_us[form] = c->form_n[form] ? std::min(c->form_us[form], us) : us;
+    c->form_n[form]++;
+    if(c->form_n[0] >= 2 && c->form_n[1] >= 2) c->graph_form = (c->form_us[1] < c->form_us[0]) ? 1 : 0;
 }
 
 template<class F>
@@ -1605,6 +1624,15 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     CUDA_TRY(c, cudaSetDevice(c->device));
     if(out_stride < 0) out_stride = 0;   // 0: no output steps
     c->stats = mtg_run_stats{};
+    if(!c->team_retuned && !is_reference(c) && c->P.nrep == 0) {
+        // the team size chosen at creation was timed on the starting configuration; re-time it
+        // once on the one that runs (forces do not depend on it: integer sums)
+        c->team_retuned = true;
+        const int before = c->P.team;
+        const int rc = autotune_force(c, true);
+        if(rc) return rc;
+        if(c->P.team != before) drop_graphs(c);   // captured graphs hold the old team size
+    }
     cudaMemsetAsync(&c->d.sc->builds_run, 0, sizeof(int32_t), c->stream);
     // thermostat first half-step of step 0 from the current momenta
     launch_prologue(c->d, c->P, c->stream);
@@ -1701,6 +1729,7 @@ int mtg_run(mtg_ctx* c, int nsteps, int out_stride, mtg_output_cb cb, void* user
     // prologue + per-step kernels + the six build kernels of every production rebuild
     c->stats.kernel_launches = (int64_t)nsteps * kernels_per_step(c) + 1 + (is_reference(c) ? 0 : 6 * c->stats.list_builds);
     c->stats.force_team = c->P.team;
+    c->stats.graph_form = is_reference(c) ? 0 : c->graph_form;
     return settle_state(c);
 }
 

@@ -929,7 +929,11 @@ __device__ __forceinline__ int excl_class(const DevSys& d, int k, int i) {
 }
 
 template<bool MIXED>
-__device__ __forceinline__ void vlist_row(const DevSys& d, const Params& P, int si, int lane) {
+__global__ void k_vlist(DevSys d, Params P) {
+    pdl_enter();
+    if(!d.sc->rebuild) return;
+    const int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if(si >= P.n) return;
     const int i = d.pcell_list[si];
     if(!rebuild_due(d, P, rep_of_atom(d, P, i))) return;
     const SysView v = sys_view(d, P, rep_of_atom(d, P, i));
@@ -1023,33 +1027,6 @@ __device__ __forceinline__ void vlist_row(const DevSys& d, const Params& P, int 
             atomicMax(&d.sc->needed, total);
         }
     }
-}
-
-// End of a list build, in the last block of the list kernel (after every row is written): the cell
-// counts cleared for the next build's counting sort, the rebuild flags reset, the build counted.
-__device__ __forceinline__ void finish_build(const DevSys& d, const Params& P, int ncell) {
-    if(last_block(&d.sc->done_blocks)) {
-        for(int c = threadIdx.x; c < ncell; c += blockDim.x) d.pcell_count[c] = 0;
-        for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) d.rsc[r].rebuild = 0;
-        __syncthreads();
-        if(threadIdx.x == 0) {
-            d.sc->done_blocks = 0;
-            d.sc->rebuild = 0;
-            d.sc->builds += 1;
-            d.sc->builds_run += 1;
-        }
-    }
-}
-
-// Verlet list rows, one warp per slot, then the end of the build (finish_build).  Returns at once
-// when no rebuild is due (the flag is set before this kernel and only its last block clears it).
-template<bool MIXED>
-__global__ void k_vlist(DevSys d, Params P, int ncell) {
-    pdl_enter();
-    if(!d.sc->rebuild) return;
-    const int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if(si < P.n) vlist_row<MIXED>(d, P, si, lane);
-    finish_build(d, P, ncell);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1489,6 +1466,7 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
 // list entries.
 template<bool MIXED, bool ENERGY, int TEAM>
 __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
+    pdl_enter();
     using R = typename std::conditional<MIXED, float, double>::type;
     __shared__ PairCoef pc_s[kSmemPairs];
     __shared__ float us_s[kSmemPairs];   // energy shift of the staged LJ term
@@ -1515,8 +1493,6 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         pc = pc_s;
         if(P.qtype) qt = qt_s;
     }
-    // the staged tables do not change within a run: staged before waiting for the predecessor
-    pdl_enter();
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int si = gt / TEAM, lane = gt % TEAM;
     const bool active = si < P.n;
@@ -1797,6 +1773,22 @@ __global__ void k_check_list(DevSys d, Params P) {
 // End of a list build: the cell counts go back to zero for the next build (they start at zero
 // when allocated), and the last block clears the rebuild flags and counts the build.  Every block
 // passes the early-exit test before the last one clears the flag it tests.
+__global__ void k_finish_build(DevSys d, Params P, int ncell) {
+    pdl_enter();
+    if(!d.sc->rebuild) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if(c < ncell) d.pcell_count[c] = 0;
+    if(last_block(&d.sc->done_blocks)) {
+        for(int r = threadIdx.x; r < P.nrep; r += blockDim.x) d.rsc[r].rebuild = 0;
+        __syncthreads();
+        if(threadIdx.x == 0) {
+            d.sc->done_blocks = 0;
+            d.sc->rebuild = 0;
+            d.sc->builds += 1;
+            d.sc->builds_run += 1;
+        }
+    }
+}
 
 // Gradient-descent step of CSimulationBox::gradientDescentStep (SimulationBox.cpp:197-208):
 // r += lr F, no clipping, no wrapping.  Also sums U, p^2/m and F.r (after the move) for the
@@ -1892,15 +1884,16 @@ void launch_prod_check_list(const DevSys& d, const Params& P, cudaStream_t s) {
 void launch_prod_build(const DevSys& d, const Params& P, bool force, cudaStream_t s) {
     const int ncell = P.nrep ? P.ncell_total : P.pnx * P.pny * P.pnz;
     if(force) cudaMemsetAsync(&d.sc->rebuild, 0xff, sizeof(int32_t), s);
-    // the cell counts are zero here (the end of the previous build); every kernel returns at once when no
+    // the cell counts are zero here (k_finish_build); every kernel returns at once when no
     // rebuild is due
     if(P.precision == MTG_PREC_MIXED) launch_step_kernel(k_pcell_assign<true>, nblk(P.n, 256), 256, s, d, P);
     else launch_step_kernel(k_pcell_assign<false>, nblk(P.n, 256), 256, s, d, P);
     launch_step_kernel(k_pcell_scan, P.nrep ? P.nrep : 1, 1024, s, d, P);
     launch_step_kernel(k_pcell_scatter, nblk(P.n, 256), 256, s, d, P);
     launch_step_kernel(k_pcell_rank, nblk(P.n, 256), 256, s, d, P, P.precision == MTG_PREC_MIXED);
-    if(P.precision == MTG_PREC_MIXED) launch_step_kernel(k_vlist<true>, nblk(P.n * 32, 256), 256, s, d, P, ncell);
-    else launch_step_kernel(k_vlist<false>, nblk(P.n * 32, 256), 256, s, d, P, ncell);
+    if(P.precision == MTG_PREC_MIXED) launch_step_kernel(k_vlist<true>, nblk(P.n * 32, 256), 256, s, d, P);
+    else launch_step_kernel(k_vlist<false>, nblk(P.n * 32, 256), 256, s, d, P);
+    launch_step_kernel(k_finish_build, nblk(ncell, 256), 256, s, d, P, ncell);
 }
 
 template<bool MIXED, bool ENERGY>

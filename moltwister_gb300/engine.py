@@ -105,7 +105,8 @@ class Output(C.Structure):
 
 class RunStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("steps", C.c_int64), ("list_builds", C.c_int64),
-                ("kernel_launches", C.c_int64), ("graph_steps", C.c_int32), ("force_team", C.c_int32)]
+                ("kernel_launches", C.c_int64), ("graph_steps", C.c_int32), ("force_team", C.c_int32),
+                ("graph_form", C.c_int32)]
 
 
 OUTPUT_CB = C.CFUNCTYPE(C.c_int, C.POINTER(Output), C.c_void_p)
@@ -458,7 +459,7 @@ class Engine:
         self._check(self.lib.mtg_get_run_stats(self.h, C.byref(st)))
         return {"device_ms": st.device_ms, "steps": st.steps, "list_builds": st.list_builds,
                 "kernel_launches": st.kernel_launches, "graph_steps": st.graph_steps,
-                "force_team": st.force_team}
+                "force_team": st.force_team, "graph_form": st.graph_form}
 
     def init_state(self, seed: int = 1, mode: str = "reference") -> None:
         """Draw and set the initial momenta and chain state (C ABI mtg_init_state); see
