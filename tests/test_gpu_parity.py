@@ -174,6 +174,27 @@ def test_mixed_mode_bit_reproducible():
     assert np.array_equal(r1, r2) and np.array_equal(p1, p2)
 
 
+def test_step_graph_form_and_team_do_not_change_results():
+    """The run picks its step-graph form from four alternating timed chunks (conditional, plain,
+    conditional, plain) and re-times the force gather's team size at its first run; the statistics
+    report both.  A 100-step run in those chunks and one in chunks too short to time (plain form
+    throughout) reach the same state bit for bit: forms, team sizes and output steps do not change
+    the arithmetic.  (Splitting a run into several runs does round differently: each run ends by
+    applying the pending thermostat scale to the momenta.)"""
+    s, cfg = analytic_case()
+    cfg.precision = "mixed"
+    e1 = engine(s, cfg)
+    e1.run(100, out_stride=20)          # chunks of 20 steps: four timed, then the chosen form
+    st = e1.stats()
+    assert st["graph_form"] in (0, 1), st
+    assert st["force_team"] in (8, 16, 32), st
+    r1, p1, _ = e1.get_state()
+    e2 = engine(s, cfg)
+    e2.run(100, out_stride=10)          # chunks of 10 steps: below the tuning length
+    r2, p2, _ = e2.get_state()
+    assert np.array_equal(r1, r2) and np.array_equal(p1, p2)
+
+
 def test_mixed_state_round_trip():
     """Mixed mode keeps positions and momenta as double-float pairs and box fractions on the
     device; the host reads and writes FP64.  Reading the state changes nothing (50 + read + 50
