@@ -526,7 +526,7 @@ int capture_segment(mtg_ctx* c, cudaGraph_t* out, F&& body) {
 
 // Production step graph with the list build under an IF node: each step is
 //   child(kick+drift, sets the condition) -> IF(rebuild){ child(list build) } -> child(force, kick+reduce)
-// assembled explicitly from captured segments.  Returns non-zero if the driver refuses.
+// assembled explicitly from captured segments.  Returns non-zero if the CUDA driver refuses conditional nodes.
 int build_conditional_graph(mtg_ctx* c, int steps, bool output, cudaGraph_t* out) {
     cudaGraph_t G = nullptr, gC = nullptr, gCo = nullptr;
     int rc = MTG_OK;
