@@ -1350,7 +1350,7 @@ __device__ __forceinline__ void pair_entry_d(const DevSys& d, const Params& P, i
     rel<false, double>(d, P, i, j, dx, dy, dz);
     const int tj = d.type[j];
     const double r2 = dx * dx + dy * dy + dz * dz;
-    const double ir = 1.0 / sqrt(r2);
+    const double ir = rsqrt(r2);   // within an ulp of 1/sqrt, without the FP64 division
     const double ir2 = ir * ir;
     g = 0;
     u = 0;
