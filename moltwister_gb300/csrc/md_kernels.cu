@@ -1342,12 +1342,17 @@ __device__ void bonded_entry(const DevSys& d, const Params& P, int k, int e, R& 
 
 // One neighbour-list entry of atom i (FP64 path): force factor g (F_i += g * d) and pair energy u.
 template<bool ENERGY>
+// ri: atom i's position; L, iL: the box and its inverse (row constants, so that no FP64 division
+// runs per pair).
 __device__ __forceinline__ void pair_entry_d(const DevSys& d, const Params& P, int i, uint32_t ent, int ti, double qi,
-                                             double rc2, double rq2, double irc, double& dx, double& dy, double& dz,
-                                             double& g, double& u) {
+                                             double rc2, double rq2, double irc, const double (&ri)[3],
+                                             const double (&L)[3], const double (&iL)[3], double& dx, double& dy,
+                                             double& dz, double& g, double& u) {
     const int j = (int)(ent & kIdxMask);
     const int cls = (int)(ent >> kClassShift);
-    rel<false, double>(d, P, i, j, dx, dy, dz);
+    dx = minimg_d(ri[0] - d.r[3 * j], L[0], iL[0]);
+    dy = minimg_d(ri[1] - d.r[3 * j + 1], L[1], iL[1]);
+    dz = minimg_d(ri[2] - d.r[3 * j + 2], L[2], iL[2]);
     const int tj = d.type[j];
     const double r2 = dx * dx + dy * dy + dz * dz;
     const double ir = rsqrt(r2);   // within an ulp of 1/sqrt, without the FP64 division
@@ -1463,9 +1468,10 @@ __device__ __forceinline__ void pair_mixed(const DevSys& d, const Params& P, int
 // so that four gathers are in flight per lane.  Bonded terms of the atom are spread over the
 // team's lanes.  Mixed: every contribution is rounded to the 2^-26 fixed-point grid and summed as
 // an integer, so forces do not depend on the team size, on the list order or on out-of-range
-// list entries.
+// list entries.  The FP64 form gets up to 80 registers (three blocks per SM): with 64 its four
+// in-flight double-precision pairs spilled about 250 bytes per thread.
 template<bool MIXED, bool ENERGY, int TEAM>
-__global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
+__global__ void __launch_bounds__(256, MIXED ? 4 : 3) k_pforce(DevSys d, Params P) {
     pdl_enter();
     using R = typename std::conditional<MIXED, float, double>::type;
     __shared__ PairCoef pc_s[kSmemPairs];
@@ -1542,6 +1548,9 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
         } else {
             const int ti = d.type[i];
             const double qi = d.qd[i];
+            const double ri[3] = {d.r[3 * i], d.r[3 * i + 1], d.r[3 * i + 2]};
+            const double L[3] = {v.box[0], v.box[1], v.box[2]};
+            const double iL[3] = {1.0 / v.box[0], 1.0 / v.box[1], 1.0 / v.box[2]};
             // list entries name slots; the FP64 path works on atom indices
             auto atom_entry = [&](uint32_t ent) -> uint32_t {
                 return (uint32_t)d.pcell_list[ent & kIdxMask] | (ent & ~kIdxMask);
@@ -1554,7 +1563,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
 #pragma unroll
                 for(int q = 0; q < 4; q++) {
                     double dx, dy, dz, g, u;
-                    pair_entry_d<ENERGY>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
+                    pair_entry_d<ENERGY>(d, P, i, ent[q], ti, qi, rc2, rq2, irc, ri, L, iL, dx, dy, dz, g, u);
                     bx += g * dx; by += g * dy; bz += g * dz;
                     if(ENERGY) {
                         bu += u;
@@ -1565,7 +1574,7 @@ __global__ void __launch_bounds__(256, 4) k_pforce(DevSys d, Params P) {
             for(; e < cnt; e += TEAM) {
                 double dx, dy, dz, g, u;
                 const uint32_t ent = atom_entry(__ldg(lst + e));
-                pair_entry_d<ENERGY>(d, P, i, ent, ti, qi, rc2, rq2, irc, dx, dy, dz, g, u);
+                pair_entry_d<ENERGY>(d, P, i, ent, ti, qi, rc2, rq2, irc, ri, L, iL, dx, dy, dz, g, u);
                 bx += g * dx; by += g * dy; bz += g * dz;
                 if(ENERGY) {
                     bu += u;
